@@ -1,0 +1,954 @@
+// C ABI of libgfcuda: problem construction, state transfer, the time-step loop and the
+// diagnostics.  The kernels live in gf_kernels.cuh (instantiated by gf_f32.cu/gf_f64.cu);
+// this file holds the host-side orchestration and the FP64 setup kernels.
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gf_fft.cuh"
+#include "gf_internal.h"
+#include "gfcuda.h"
+
+using namespace gf;
+
+static std::string g_create_error;
+
+struct gf_ctx {
+  gf_config cfg;
+  int prec = GF_F32;
+  size_t rb = 4, cb = 8;  // real / complex element bytes
+  cudaStream_t stream = nullptr;
+  Geom g{};
+  ModArgs m{};
+  int kind = SK_RK4, filtered = 0, hasL = 0, cplxL = 0, nstages = 4;
+  double t = 0;
+  int64_t step = 0;
+  bool W_valid = false;
+  double last_fscale = 0;  // forcing scale of the last calcN! (deterministic forcing)
+  double Hsum = 1, f0 = 1;
+  std::vector<double> gprime, Hl;
+  // device buffers
+  std::vector<void*> allocs;
+  void *sol = nullptr, *X = nullptr, *acc = nullptr, *s1 = nullptr, *N1 = nullptr, *R3[3] = {nullptr, nullptr, nullptr};
+  void *W = nullptr, *P = nullptr, *D = nullptr, *twid = nullptr;
+  void *Ltab = nullptr, *filt = nullptr, *etd[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  void *mult = nullptr, *eta = nullptr, *U1D = nullptr, *Qy1D = nullptr, *Qx2D = nullptr, *Qy2D = nullptr,
+       *etah = nullptr;
+  void *Fh = nullptr, *fspec = nullptr, *Fstore = nullptr, *prevsol = nullptr;
+  void *phys = nullptr;     // [4][nl][ny][nx] physical fields from updatevars!
+  void *tmp_spec = nullptr; // [nl][ny][ldk] scratch spectral array
+  void *tmp_spec2 = nullptr;
+  double *dpart = nullptr, *dout = nullptr;
+  int diag_blocks = 0;
+  int ab3_out = 0, ab3_m1 = 1, ab3_m2 = 2;
+  // kernel timing (gf_profile_enable): CUDA events around every row / column launch
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev_free;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_used;
+  double prof_ms[2] = {0, 0};
+  int64_t prof_n[2] = {0, 0};
+  int64_t launches = 0;
+  std::string err;
+};
+
+// ------------------------------------------------------------------------ FP64 setup kernels
+template <class T>
+__global__ void etd_coeffs_kernel(int n, const double* __restrict__ Lre, const double* __restrict__ Lim, double dt,
+                                  int ncirc, double rcirc, int cplx_out, T* e, T* e2, T* zeta, T* alpha, T* beta,
+                                  T* gamma, int nkr, int ldk) {
+  typedef std::complex<double> Z;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+    const double lr = Lre[idx], li = Lim ? Lim[idx] : 0.0;
+    double zr = 0, zi = 0, ar = 0, ai = 0, br = 0, bi = 0, gr = 0, gi = 0;
+    for (int q = 0; q < ncirc; ++q) {
+      double s, c;
+      sincospi(2.0 * (q + 0.5) / ncirc, &s, &c);
+      // z = dt L + r e^{i theta}
+      const double xr = dt * lr + rcirc * c, xi = dt * li + rcirc * s;
+      double es, ec;
+      sincos(xi, &es, &ec);
+      const double ea = exp(xr);
+      const double ezr = ea * ec, ezi = ea * es;  // e^z
+      sincos(0.5 * xi, &es, &ec);
+      const double eh = exp(0.5 * xr);
+      const double ehr = eh * ec, ehi = eh * es;  // e^{z/2}
+      // complex helpers
+      auto mul = [](double a, double b, double c_, double d, double* r, double* i) { *r = a * c_ - b * d; *i = a * d + b * c_; };
+      double z2r, z2i, z3r, z3i;
+      mul(xr, xi, xr, xi, &z2r, &z2i);
+      mul(z2r, z2i, xr, xi, &z3r, &z3i);
+      const double den1 = xr * xr + xi * xi, den3 = z3r * z3r + z3i * z3i;
+      double nr, ni, tr, ti;
+      // zeta: (e^{z/2} - 1) / z
+      nr = ehr - 1; ni = ehi;
+      zr += (nr * xr + ni * xi) / den1; zi += (ni * xr - nr * xi) / den1;
+      // alpha: (-4 - z + e^z (4 - 3z + z^2)) / z^3
+      mul(ezr, ezi, 4 - 3 * xr + z2r, -3 * xi + z2i, &tr, &ti);
+      nr = -4 - xr + tr; ni = -xi + ti;
+      ar += (nr * z3r + ni * z3i) / den3; ai += (ni * z3r - nr * z3i) / den3;
+      // beta: (2 + z + e^z (-2 + z)) / z^3
+      mul(ezr, ezi, -2 + xr, xi, &tr, &ti);
+      nr = 2 + xr + tr; ni = xi + ti;
+      br += (nr * z3r + ni * z3i) / den3; bi += (ni * z3r - nr * z3i) / den3;
+      // gamma: (-4 - 3z - z^2 + e^z (4 - z)) / z^3
+      mul(ezr, ezi, 4 - xr, -xi, &tr, &ti);
+      nr = -4 - 3 * xr - z2r + tr; ni = -3 * xi - z2i + ti;
+      gr += (nr * z3r + ni * z3i) / den3; gi += (ni * z3r - nr * z3i) / den3;
+    }
+    const double sc = dt / ncirc;
+    double s_, c_;
+    sincos(dt * li, &s_, &c_);
+    const double ea = exp(dt * lr);
+    sincos(0.5 * dt * li, &s_, &c_);
+    double s2, c2;
+    sincos(dt * li, &s2, &c2);
+    const double er = ea * c2, ei = ea * s2;
+    const double eh = exp(0.5 * dt * lr);
+    const double e2r = eh * c_, e2i = eh * s_;
+    const int kr = idx % nkr, j = idx / nkr;
+    const size_t o = (size_t)j * ldk + kr;
+    const double vals[12] = {er, ei, e2r, e2i, zr * sc, zi * sc, ar * sc, ai * sc, br * sc, bi * sc, gr * sc, gi * sc};
+    T* outs[6] = {e, e2, zeta, alpha, beta, gamma};
+    for (int q = 0; q < 6; ++q) {
+      if (cplx_out) { outs[q][2 * o] = (T)vals[2 * q]; outs[q][2 * o + 1] = (T)vals[2 * q + 1]; }
+      else outs[q][o] = (T)vals[2 * q];
+    }
+  }
+}
+
+__global__ void diag_finish(const double* __restrict__ partial, int nblocks, uint32_t mask, double* out) {
+  __shared__ double red[256];
+  for (int q = 0; q < NDIAG; ++q) {
+    if (!(mask & (1u << q))) { if (threadIdx.x == 0) out[q] = 0; continue; }
+    double s = 0, c = 0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+      const double x = partial[(size_t)q * nblocks + b];
+      const double t = s + x;
+      c += (fabs(s) >= fabs(x)) ? (s - t) + x : (x - t) + s;
+      s = t;
+    }
+    red[threadIdx.x] = s + c;
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+      if ((int)threadIdx.x < st) red[threadIdx.x] += red[threadIdx.x + st];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[q] = red[0];
+    __syncthreads();
+  }
+}
+
+template <class T>
+__global__ void add_scalar_kernel(T* a, size_t n, double v) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) a[i] += (T)v;
+}
+
+// ------------------------------------------------------------------------------- helpers
+#define GF_CUDA(ctx, call)                                                           \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess) {                                                         \
+      (ctx)->err = std::string(#call) + ": " + cudaGetErrorString(e_);              \
+      return GF_ERR_CUDA;                                                            \
+    }                                                                                \
+  } while (0)
+
+static int fail(gf_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg; else g_create_error = msg;
+  return code;
+}
+
+static void* dalloc(gf_ctx* c, size_t bytes) {
+  void* p = nullptr;
+  if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+  cudaMemsetAsync(p, 0, bytes, c->stream);
+  c->allocs.push_back(p);
+  return p;
+}
+
+static bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+static size_t nspec(const gf_ctx* c) { return (size_t)c->g.nl * c->g.ny * c->g.ldk; }
+
+// upload a host double array of n values as the context's real type
+static int upload_real(gf_ctx* c, void* dst, const double* src, size_t n) {
+  if (c->prec == GF_F64) {
+    GF_CUDA(c, cudaMemcpyAsync(dst, src, n * 8, cudaMemcpyHostToDevice, c->stream));
+  } else {
+    std::vector<float> f(n);
+    for (size_t i = 0; i < n; ++i) f[i] = (float)src[i];
+    GF_CUDA(c, cudaMemcpyAsync(dst, f.data(), n * 4, cudaMemcpyHostToDevice, c->stream));
+    GF_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  return GF_OK;
+}
+// upload a host double table defined on [j][kr] (nkr x ny) into [j][ldk]
+static int upload_table(gf_ctx* c, void* dst, const std::vector<double>& v, int cplx) {
+  const Geom& g = c->g;
+  const int w = cplx ? 2 : 1;
+  std::vector<double> pad((size_t)g.ny * g.ldk * w, 0.0);
+  for (int j = 0; j < g.ny; ++j)
+    for (int k = 0; k < g.nkr * w; ++k) pad[(size_t)j * g.ldk * w + k] = v[((size_t)j * g.nkr) * w + k];
+  int r = upload_real(c, dst, pad.data(), pad.size());
+  if (r) return r;
+  GF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GF_OK;
+}
+
+static Bufs bufs(gf_ctx* c) { return Bufs{c->twid, c->W, c->P}; }
+static Geom full_geom(const gf_ctx* c) {
+  Geom g = c->g;
+  g.kcut = g.nkr; g.lA = 1; g.lB = 0; g.ldw = g.ldk;
+  return g;
+}
+
+#define DISPATCH(c, fn, ...) ((c)->prec == GF_F64 ? fn<double>(__VA_ARGS__) : fn<float>(__VA_ARGS__))
+
+// symmetric Jacobi eigen-decomposition (small n), A overwritten, Q columns = eigenvectors
+static void jacobi_eig(int n, std::vector<double>& A, std::vector<double>& Q, std::vector<double>& lam) {
+  Q.assign(n * n, 0.0);
+  for (int i = 0; i < n; ++i) Q[i * n + i] = 1.0;
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0;
+    for (int p = 0; p < n; ++p) for (int q = p + 1; q < n; ++q) off += A[p * n + q] * A[p * n + q];
+    if (off < 1e-30) break;
+    for (int p = 0; p < n; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        const double apq = A[p * n + q];
+        if (std::fabs(apq) < 1e-300) continue;
+        const double th = (A[q * n + q] - A[p * n + p]) / (2 * apq);
+        const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1));
+        const double cs = 1 / std::sqrt(t * t + 1), sn = t * cs;
+        for (int k = 0; k < n; ++k) {  // A = J^T A J
+          const double akp = A[k * n + p], akq = A[k * n + q];
+          A[k * n + p] = cs * akp - sn * akq;
+          A[k * n + q] = sn * akp + cs * akq;
+        }
+        for (int k = 0; k < n; ++k) {
+          const double apk = A[p * n + k], aqk = A[q * n + k];
+          A[p * n + k] = cs * apk - sn * aqk;
+          A[q * n + k] = sn * apk + cs * aqk;
+        }
+        for (int k = 0; k < n; ++k) {
+          const double qkp = Q[k * n + p], qkq = Q[k * n + q];
+          Q[k * n + p] = cs * qkp - sn * qkq;
+          Q[k * n + q] = sn * qkp + cs * qkq;
+        }
+      }
+  }
+  lam.resize(n);
+  for (int i = 0; i < n; ++i) lam[i] = A[i * n + i];
+}
+
+// second y-derivative of a periodic 1-D profile by an exact DFT (setup only)
+static std::vector<double> d2dy2(const std::vector<double>& u, double Ly) {
+  const int n = (int)u.size();
+  std::vector<std::complex<double>> uh(n);
+  for (int k = 0; k < n; ++k) {
+    std::complex<double> s = 0;
+    for (int j = 0; j < n; ++j) s += u[j] * std::polar(1.0, -2 * M_PI * (double)((long long)k * j % n) / n);
+    const double l = 2 * M_PI / Ly * (k < n / 2 ? k : k - n);
+    uh[k] = -l * l * s;
+  }
+  std::vector<double> r(n);
+  for (int j = 0; j < n; ++j) {
+    std::complex<double> s = 0;
+    for (int k = 0; k < n; ++k) s += uh[k] * std::polar(1.0, 2 * M_PI * (double)((long long)k * j % n) / n);
+    r[j] = s.real() / n;
+  }
+  return r;
+}
+
+static double powi_h(double x, int n) {
+  if (n == 0) return 1.0;
+  double r = 1.0, b = n > 0 ? x : 1.0 / x;
+  for (int e = n > 0 ? n : -n; e; e >>= 1) { if (e & 1) r *= b; b *= b; }
+  return r;
+}
+
+// forward transform of nl physical fields (device, context type) into out (internal layout)
+static int fwd_transform(gf_ctx* c, const void* phys_dev, void* out, int zero_mean) {
+  Geom g = full_geom(c);
+  GF_CUDA(c, DISPATCH(c, launch_row_r2c, g, bufs(c), g.nl, phys_dev, c->stream));
+  GF_CUDA(c, DISPATCH(c, launch_col_fwd, g, bufs(c), g.nl, out, zero_mean, c->stream));
+  return GF_OK;
+}
+// inverse transform of kind(src) for all layers into physical out[nl][ny][nx]
+static int inv_transform(gf_ctx* c, const void* src, int kind, int mask, void* out) {
+  Geom g = full_geom(c);
+  GF_CUDA(c, DISPATCH(c, launch_col_inv, g, c->m, src, kind, mask, bufs(c), c->stream));
+  GF_CUDA(c, DISPATCH(c, launch_row_c2r, g, bufs(c), g.nl, out, c->stream));
+  return GF_OK;
+}
+
+// ------------------------------------------------------------------------------- create
+extern "C" int gf_abi_version(void) { return GFCUDA_ABI_VERSION; }
+
+extern "C" const char* gf_last_error(const gf_ctx* c) { return c ? c->err.c_str() : g_create_error.c_str(); }
+
+static int build(gf_ctx* c, const gf_config* cfg) {
+  const gf_config& k = *cfg;
+  Geom& g = c->g;
+  g.nx = k.nx; g.ny = k.ny; g.nkr = k.nx / 2 + 1;
+  g.nl = (k.module == GF_MULTILAYERQG) ? k.nlayers : 1;
+  g.ldk = (g.nkr + 15) / 16 * 16;
+  // dealias ranges (FourierFlows TwoDGrid with aliased_fraction)
+  const double af = k.aliased_fraction;
+  if (af > 0) {
+    const double L = (1 - af) / 2, R = (1 + af) / 2;
+    const int iLx = (int)std::floor(L * k.nx) + 1;
+    const int iLy = (int)std::floor(L * k.ny) + 1, iRy = (int)std::ceil(R * k.ny);
+    g.kcut = std::min(iLx - 1, g.nkr);
+    g.lA = iLy - 1; g.lB = iRy - 1;
+  } else {
+    g.kcut = g.nkr; g.lA = 1; g.lB = 0;
+  }
+  g.ldw = (g.kcut + 15) / 16 * 16;
+  g.dkx = 2 * M_PI / k.Lx; g.dky = 2 * M_PI / k.Ly;
+  g.inv_nxny = 1.0 / ((double)k.nx * k.ny);
+  c->prec = k.precision;
+  c->rb = k.precision == GF_F64 ? 8 : 4;
+  c->cb = 2 * c->rb;
+  const int st = k.stepper;
+  c->filtered = (st == GF_FILTEREDFORWARDEULER || st == GF_FILTEREDRK4 || st == GF_FILTEREDETDRK4 || st == GF_FILTEREDAB3);
+  c->kind = (st <= 1) ? SK_FE : (st <= 3) ? SK_RK4 : (st <= 5) ? SK_ETDRK4 : SK_AB3;
+  c->nstages = (c->kind == SK_RK4 || c->kind == SK_ETDRK4) ? 4 : 1;
+
+  const size_t nsp = nspec(c), tsz = (size_t)g.ny * g.ldk;
+  const size_t cb = c->cb, rb = c->rb;
+  // ----- twiddles
+  {
+    std::vector<double> tw(2 * TWN);
+    for (int i = 0; i < TWN; ++i) {
+      tw[2 * i] = std::cos(2 * M_PI * i / TWN);
+      tw[2 * i + 1] = -std::sin(2 * M_PI * i / TWN);
+    }
+    if (!(c->twid = dalloc(c, 2 * TWN * rb))) return fail(c, GF_ERR_NOMEM, "twiddles");
+    if (int r = upload_real(c, c->twid, tw.data(), tw.size())) return r;
+  }
+  // ----- wavenumber tables on the host (double)
+  std::vector<double> K2((size_t)g.ny * g.nkr), krv(g.nkr), lv(g.ny);
+  for (int i = 0; i < g.nkr; ++i) krv[i] = g.dkx * i;
+  for (int j = 0; j < g.ny; ++j) lv[j] = g.dky * (j < g.ny / 2 ? j : j - g.ny);
+  for (int j = 0; j < g.ny; ++j)
+    for (int i = 0; i < g.nkr; ++i) K2[(size_t)j * g.nkr + i] = krv[i] * krv[i] + lv[j] * lv[j];
+
+  // ----- module parameters and the linear operator L (real or complex)
+  ModArgs& m = c->m;
+  std::memset(&m, 0, sizeof(m));
+  m.module = k.module;
+  m.hasB = 1;
+  m.nu = k.nu; m.nnu = k.nnu; m.mu_visc = k.mu; m.nmu = k.nmu;
+  std::vector<double> Lre((size_t)g.ny * g.nkr, 0.0), Lim;
+  auto K2pow = [&](size_t e, int n) { return powi_h(K2[e], n); };
+  const size_t nt = (size_t)g.ny * g.nkr;
+  if (k.module == GF_TWODNAVIERSTOKES) {
+    m.psi_kind = PSI_INVK2;
+    for (size_t e = 1; e < nt; ++e) Lre[e] = -k.nu * K2pow(e, k.nnu) - k.mu * K2pow(e, k.nmu);
+  } else if (k.module == GF_SURFACEQG) {
+    m.psi_kind = PSI_TABLE;
+    const double H = (k.H_sqg > 0) ? k.H_sqg : INFINITY;
+    std::vector<double> M(nt, 0.0);
+    for (size_t e = 1; e < nt; ++e) {
+      const double Kk = std::sqrt(K2[e]);
+      M[e] = (std::isinf(H) ? 1.0 : 1.0 / std::tanh(H * Kk)) / Kk;
+      Lre[e] = -k.nu * K2pow(e, k.nnu);
+    }
+    if (!(c->mult = dalloc(c, tsz * rb))) return fail(c, GF_ERR_NOMEM, "mult");
+    if (int r = upload_table(c, c->mult, M, 0)) return r;
+    m.mult = c->mult;
+  } else if (k.module == GF_SINGLELAYERQG) {
+    const bool barotropic = !(k.deformation_radius > 0) || std::isinf(k.deformation_radius);
+    m.psi_kind = barotropic ? PSI_INVK2 : PSI_HELMHOLTZ;
+    m.ell_inv2 = barotropic ? 0.0 : 1.0 / (k.deformation_radius * k.deformation_radius);
+    Lim.assign(nt, 0.0);
+    const bool Uconst = (k.U_y == nullptr);
+    for (size_t e = 1; e < nt; ++e) {
+      const int kr = e % g.nkr;
+      Lre[e] = -k.mu - k.nu * K2pow(e, k.nnu);
+      Lim[e] = barotropic ? k.beta * krv[kr] / K2[e] : k.beta * krv[kr] / (K2[e] + m.ell_inv2);
+      if (Uconst) Lim[e] -= k.U * krv[kr];
+    }
+    m.U0 = Uconst ? k.U : 0.0;
+  } else {  // MultiLayerQG
+    const int n = g.nl;
+    for (size_t e = 1; e < nt; ++e) Lre[e] = -k.nu * K2pow(e, k.nnu);
+    m.hasB = k.linear ? 0 : 1;
+    m.hasC = 1;
+    m.linear = k.linear;
+    m.drag = (k.mu != 0);
+    m.mu = k.mu;
+    c->f0 = k.f0;
+    c->Hl.assign(k.H, k.H + n);
+    c->Hsum = 0;
+    for (int j = 0; j < n; ++j) c->Hsum += k.H[j];
+    std::vector<double> Fp(n > 1 ? n - 1 : 0), Fm(n > 1 ? n - 1 : 0);
+    if (n == 1) {
+      m.psi_kind = PSI_INVK2;
+    } else {
+      m.psi_kind = PSI_EIGEN;
+      c->gprime.resize(n - 1);
+      for (int j = 0; j < n - 1; ++j) {
+        c->gprime[j] = k.b[j] - k.b[j + 1];
+        Fm[j] = k.f0 * k.f0 / (c->gprime[j] * k.H[j + 1]);
+        Fp[j] = k.f0 * k.f0 / (c->gprime[j] * k.H[j]);
+      }
+      std::vector<double> F(n * n, 0.0);
+      for (int j = 0; j < n - 1; ++j) { F[j * n + j + 1] = Fp[j]; F[(j + 1) * n + j] = Fm[j]; }
+      for (int j = 0; j < n; ++j) F[j * n + j] = -((j < n - 1 ? Fp[j] : 0) + (j > 0 ? Fm[j - 1] : 0));
+      // diag(sqrt H) F diag(1/sqrt H) is symmetric: F = D^-1 Q Lam Q^T D
+      std::vector<double> A(n * n), Q, lam;
+      for (int a = 0; a < n; ++a)
+        for (int b = 0; b < n; ++b) A[a * n + b] = std::sqrt(k.H[a]) * F[a * n + b] / std::sqrt(k.H[b]);
+      for (int a = 0; a < n; ++a)
+        for (int b = a + 1; b < n; ++b) { const double s = 0.5 * (A[a * n + b] + A[b * n + a]); A[a * n + b] = A[b * n + a] = s; }
+      jacobi_eig(n, A, Q, lam);
+      for (int a = 0; a < n; ++a) {
+        m.lam[a] = lam[a];
+        for (int b = 0; b < n; ++b) {
+          m.V[a * MAXL + b] = Q[a * n + b] / std::sqrt(k.H[a]);      // D^-1 Q
+          m.Vinv[a * MAXL + b] = Q[b * n + a] * std::sqrt(k.H[b]);   // Q^T D
+        }
+      }
+    }
+    // U(y) per layer, Qy1D = beta - Uyy - (F dU terms)
+    std::vector<double> U((size_t)n * g.ny, 0.0), Qy((size_t)n * g.ny, 0.0);
+    if (k.U_y) for (size_t i = 0; i < U.size(); ++i) U[i] = k.U_y[i];
+    for (int L = 0; L < n; ++L) {
+      std::vector<double> u(U.begin() + (size_t)L * g.ny, U.begin() + (size_t)(L + 1) * g.ny);
+      auto uyy = d2dy2(u, k.Ly);
+      for (int j = 0; j < g.ny; ++j) Qy[(size_t)L * g.ny + j] = k.beta - uyy[j];
+    }
+    if (n >= 2) {
+      for (int j = 0; j < g.ny; ++j) {
+        auto Uv = [&](int L) { return U[(size_t)L * g.ny + j]; };
+        Qy[j] -= Fp[0] * (Uv(1) - Uv(0));
+        for (int L = 1; L < n - 1; ++L) Qy[(size_t)L * g.ny + j] -= Fp[L] * (Uv(L + 1) - Uv(L)) + Fm[L - 1] * (Uv(L - 1) - Uv(L));
+        Qy[(size_t)(n - 1) * g.ny + j] -= Fm[n - 2] * (Uv(n - 2) - Uv(n - 1));
+      }
+    }
+    if (!(c->U1D = dalloc(c, U.size() * rb)) || !(c->Qy1D = dalloc(c, Qy.size() * rb))) return fail(c, GF_ERR_NOMEM, "U");
+    if (int r = upload_real(c, c->U1D, U.data(), U.size())) return r;
+    if (int r = upload_real(c, c->Qy1D, Qy.data(), Qy.size())) return r;
+    m.U1D = c->U1D; m.Qy1D = c->Qy1D;
+  }
+  c->hasL = 0;
+  for (size_t e = 0; e < nt; ++e) if (Lre[e] != 0 || (!Lim.empty() && Lim[e] != 0)) { c->hasL = 1; break; }
+  c->cplxL = !Lim.empty();
+
+  // ----- buffers
+  const size_t Wn = std::max((size_t)3 * g.nl * g.ny * g.ldw, nsp);
+  if (!(c->sol = dalloc(c, nsp * cb)) || !(c->W = dalloc(c, Wn * cb)) || !(c->P = dalloc(c, 3 * nsp * cb)) ||
+      !(c->D = dalloc(c, tsz * cb)) || !(c->tmp_spec = dalloc(c, nsp * cb)) || !(c->tmp_spec2 = dalloc(c, nsp * cb)) ||
+      !(c->phys = dalloc(c, (size_t)4 * g.nl * g.ny * g.nx * rb)))
+    return fail(c, GF_ERR_NOMEM, "state buffers");
+  m.D = c->D;
+  if (c->kind == SK_RK4) {
+    if (!(c->acc = dalloc(c, nsp * cb))) return fail(c, GF_ERR_NOMEM, "acc");
+    if (c->hasL && !(c->X = dalloc(c, nsp * cb))) return fail(c, GF_ERR_NOMEM, "X");
+  } else if (c->kind == SK_ETDRK4) {
+    if (!(c->acc = dalloc(c, nsp * cb)) || !(c->s1 = dalloc(c, nsp * cb)) || !(c->N1 = dalloc(c, nsp * cb)))
+      return fail(c, GF_ERR_NOMEM, "etdrk4 state");
+  } else if (c->kind == SK_AB3) {
+    for (int i = 0; i < 3; ++i) if (!(c->R3[i] = dalloc(c, nsp * cb))) return fail(c, GF_ERR_NOMEM, "ab3 state");
+  }
+  // ----- L, filter, ETDRK4 coefficients
+  const int w = c->cplxL ? 2 : 1;
+  if (c->hasL && c->kind != SK_ETDRK4) {
+    std::vector<double> Lt(nt * w);
+    for (size_t e = 0; e < nt; ++e) {
+      if (c->cplxL) { Lt[2 * e] = Lre[e]; Lt[2 * e + 1] = Lim[e]; } else Lt[e] = Lre[e];
+    }
+    if (!(c->Ltab = dalloc(c, tsz * w * rb))) return fail(c, GF_ERR_NOMEM, "L");
+    if (int r = upload_table(c, c->Ltab, Lt, c->cplxL)) return r;
+  }
+  if (c->filtered) {
+    const double order = k.filter_order > 0 ? k.filter_order : 4.0;
+    const double inner = k.filter_innerK > 0 ? k.filter_innerK : 0.65;
+    const double outer = k.filter_outerK > 0 ? k.filter_outerK : 1.0;
+    const double decay = 15 * std::log(10.0) / std::pow(outer - inner, order);
+    const double dx = k.Lx / k.nx, dy = k.Ly / k.ny;
+    std::vector<double> f(nt);
+    for (int j = 0; j < g.ny; ++j)
+      for (int i = 0; i < g.nkr; ++i) {
+        const double a = krv[i] * dx / M_PI, b = lv[j] * dy / M_PI;
+        const double Kf = std::sqrt(a * a + b * b);
+        f[(size_t)j * g.nkr + i] = Kf < inner ? 1.0 : std::exp(-decay * std::pow(Kf - inner, order));
+      }
+    if (!(c->filt = dalloc(c, tsz * rb))) return fail(c, GF_ERR_NOMEM, "filter");
+    if (int r = upload_table(c, c->filt, f, 0)) return r;
+  }
+  if (c->kind == SK_ETDRK4) {
+    for (int q = 0; q < 6; ++q) if (!(c->etd[q] = dalloc(c, tsz * w * rb))) return fail(c, GF_ERR_NOMEM, "etdrk4 coefficients");
+    double *dLr = nullptr, *dLi = nullptr;
+    GF_CUDA(c, cudaMalloc(&dLr, nt * 8));
+    if (c->cplxL) GF_CUDA(c, cudaMalloc(&dLi, nt * 8));
+    GF_CUDA(c, cudaMemcpyAsync(dLr, Lre.data(), nt * 8, cudaMemcpyHostToDevice, c->stream));
+    if (dLi) GF_CUDA(c, cudaMemcpyAsync(dLi, Lim.data(), nt * 8, cudaMemcpyHostToDevice, c->stream));
+    const int ncirc = k.etdrk4_ncirc > 0 ? k.etdrk4_ncirc : 32;
+    const double rcirc = k.etdrk4_rcirc > 0 ? k.etdrk4_rcirc : 1.0;
+    const int nb = (int)std::min<size_t>((nt + 255) / 256, 4096);
+    if (c->prec == GF_F64)
+      etd_coeffs_kernel<double><<<nb, 256, 0, c->stream>>>((int)nt, dLr, dLi, k.dt, ncirc, rcirc, c->cplxL,
+          (double*)c->etd[0], (double*)c->etd[1], (double*)c->etd[2], (double*)c->etd[3], (double*)c->etd[4],
+          (double*)c->etd[5], g.nkr, g.ldk);
+    else
+      etd_coeffs_kernel<float><<<nb, 256, 0, c->stream>>>((int)nt, dLr, dLi, k.dt, ncirc, rcirc, c->cplxL,
+          (float*)c->etd[0], (float*)c->etd[1], (float*)c->etd[2], (float*)c->etd[3], (float*)c->etd[4],
+          (float*)c->etd[5], g.nkr, g.ldk);
+    GF_CUDA(c, cudaGetLastError());
+    GF_CUDA(c, cudaStreamSynchronize(c->stream));
+    cudaFree(dLr);
+    if (dLi) cudaFree(dLi);
+  }
+  // ----- topography (eta) derived fields
+  if (k.eta && (k.module == GF_SINGLELAYERQG || k.module == GF_MULTILAYERQG)) {
+    const size_t np = (size_t)g.ny * g.nx;
+    void* eta_d = dalloc(c, np * rb);
+    if (!eta_d || !(c->etah = dalloc(c, nsp * cb))) return fail(c, GF_ERR_NOMEM, "eta");
+    if (int r = upload_real(c, eta_d, k.eta, np)) return r;
+    // etah = rfft(eta) (one layer)
+    Geom g1 = full_geom(c); g1.nl = 1;
+    GF_CUDA(c, DISPATCH(c, launch_row_r2c, g1, bufs(c), 1, eta_d, c->stream));
+    GF_CUDA(c, DISPATCH(c, launch_col_fwd, g1, bufs(c), 1, c->etah, 0, c->stream));
+    // Qx = irfft(i kr etah), Qy = irfft(i l etah) (src/singlelayerqg.jl:185-186,
+    // src/multilayerqg.jl:262-264), plus the large-scale topographic PV gradient
+    const bool needQ = (k.module == GF_MULTILAYERQG) || (k.U_y != nullptr);
+    if (needQ) {
+      if (!(c->Qx2D = dalloc(c, np * rb)) || !(c->Qy2D = dalloc(c, np * rb))) return fail(c, GF_ERR_NOMEM, "Q");
+      GF_CUDA(c, DISPATCH(c, launch_col_inv, g1, m, c->etah, (int)SF_DX, 0, bufs(c), c->stream));
+      GF_CUDA(c, DISPATCH(c, launch_row_c2r, g1, bufs(c), 1, c->Qx2D, c->stream));
+      GF_CUDA(c, DISPATCH(c, launch_col_inv, g1, m, c->etah, (int)SF_DY, 0, bufs(c), c->stream));
+      GF_CUDA(c, DISPATCH(c, launch_row_c2r, g1, bufs(c), 1, c->Qy2D, c->stream));
+      if (k.module == GF_MULTILAYERQG) {
+        const int nb = 256;
+        if (c->prec == GF_F64) {
+          add_scalar_kernel<double><<<nb, 256, 0, c->stream>>>((double*)c->Qx2D, np, k.topographic_pv_gradient[0]);
+          add_scalar_kernel<double><<<nb, 256, 0, c->stream>>>((double*)c->Qy2D, np, k.topographic_pv_gradient[1]);
+        } else {
+          add_scalar_kernel<float><<<nb, 256, 0, c->stream>>>((float*)c->Qx2D, np, k.topographic_pv_gradient[0]);
+          add_scalar_kernel<float><<<nb, 256, 0, c->stream>>>((float*)c->Qy2D, np, k.topographic_pv_gradient[1]);
+        }
+        GF_CUDA(c, cudaGetLastError());
+      }
+      m.Qx2D = c->Qx2D; m.Qy2D = c->Qy2D;
+    }
+    if (k.module == GF_SINGLELAYERQG) {
+      if (k.U_y == nullptr) m.eta = eta_d;  // q + eta in the products (constant-U path)
+      m.etah = c->etah;                     // -i kr U etah term and the enstrophy diagnostic
+    }
+    GF_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  if (k.module == GF_MULTILAYERQG && !k.eta &&
+      (k.topographic_pv_gradient[0] != 0 || k.topographic_pv_gradient[1] != 0)) {
+    const size_t np = (size_t)g.ny * g.nx;
+    std::vector<double> gx(np, k.topographic_pv_gradient[0]), gy(np, k.topographic_pv_gradient[1]);
+    if (!(c->Qx2D = dalloc(c, np * rb)) || !(c->Qy2D = dalloc(c, np * rb))) return fail(c, GF_ERR_NOMEM, "Q");
+    if (int r = upload_real(c, c->Qx2D, gx.data(), np)) return r;
+    if (int r = upload_real(c, c->Qy2D, gy.data(), np)) return r;
+    m.Qx2D = c->Qx2D; m.Qy2D = c->Qy2D;
+  }
+  if (k.module == GF_SINGLELAYERQG && k.U_y != nullptr) {
+    // U(y) path: u' = u + U, C = u' Qx + v Qy with Qy = d(eta)/dy - Uyy
+    std::vector<double> U(k.U_y, k.U_y + g.ny);
+    auto uyy = d2dy2(U, k.Ly);
+    std::vector<double> Qy(g.ny);
+    for (int j = 0; j < g.ny; ++j) Qy[j] = -uyy[j];
+    if (!(c->U1D = dalloc(c, g.ny * rb)) || !(c->Qy1D = dalloc(c, g.ny * rb))) return fail(c, GF_ERR_NOMEM, "U");
+    if (int r = upload_real(c, c->U1D, U.data(), g.ny)) return r;
+    if (int r = upload_real(c, c->Qy1D, Qy.data(), g.ny)) return r;
+    m.U1D = c->U1D; m.Qy1D = c->Qy1D; m.hasC = 1;
+  }
+  // ----- forcing buffers
+  if (k.forcing_kind != GF_FORCING_NONE) {
+    if (!(c->Fh = dalloc(c, nsp * cb))) return fail(c, GF_ERR_NOMEM, "forcing");
+    if (k.forcing_kind >= GF_FORCING_STOCHASTIC) {
+      if (!(c->fspec = dalloc(c, tsz * rb)) || !(c->prevsol = dalloc(c, nsp * cb)))
+        return fail(c, GF_ERR_NOMEM, "stochastic forcing");
+      c->Fstore = c->Fh;
+    }
+  }
+  c->diag_blocks = (int)std::min<size_t>((nt + DIAG_BLOCK - 1) / DIAG_BLOCK, 1024);
+  if (!(c->dpart = (double*)dalloc(c, (size_t)NDIAG * c->diag_blocks * 8)) || !(c->dout = (double*)dalloc(c, NDIAG * 8)))
+    return fail(c, GF_ERR_NOMEM, "diagnostics");
+  GF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GF_OK;
+}
+
+extern "C" int gf_create(const gf_config* cfg, void* stream, gf_ctx** out) {
+  if (!cfg || !out) return fail(nullptr, GF_ERR_ARG, "null argument");
+  *out = nullptr;
+  const gf_config& k = *cfg;
+  if (k.module < 0 || k.module > 3) return fail(nullptr, GF_ERR_ARG, "unknown module");
+  if (k.precision != GF_F32 && k.precision != GF_F64) return fail(nullptr, GF_ERR_ARG, "unknown precision");
+  if (k.stepper < 0 || k.stepper > 7) return fail(nullptr, GF_ERR_ARG, "unknown stepper");
+  if (k.nx <= 0 || k.ny <= 0 || !(k.Lx > 0) || !(k.Ly > 0) || !(k.dt > 0))
+    return fail(nullptr, GF_ERR_ARG, "nx, ny, Lx, Ly and dt must be positive");
+  if (!is_pow2(k.nx) || !is_pow2(k.ny) || k.nx < 32 || k.ny < 32 || k.nx > 2048 || k.ny > 2048)
+    return fail(nullptr, GF_ERR_UNSUPPORTED, "nx and ny must be powers of two in [32, 2048]");
+  if (!(k.aliased_fraction >= 0) || !(k.aliased_fraction < 1))
+    return fail(nullptr, GF_ERR_ARG, "`aliased_fraction` must be less than 1");
+  if (k.module == GF_MULTILAYERQG) {
+    if (k.nlayers < 1) return fail(nullptr, GF_ERR_ARG, "nlayers must be >= 1");
+    if (k.nlayers > MAXL) return fail(nullptr, GF_ERR_UNSUPPORTED, "at most 8 layers");
+    if (k.nlayers > 1 && (!k.H || !k.b)) return fail(nullptr, GF_ERR_ARG, "MultiLayerQG needs H and b");
+    if (k.nlayers > 1)
+      for (int j = 0; j + 1 < k.nlayers; ++j)
+        if (k.b[j] == k.b[j + 1]) return fail(nullptr, GF_ERR_ARG, "equal buoyancies give zero reduced gravity");
+  } else if (k.nlayers > 1) {
+    return fail(nullptr, GF_ERR_ARG, "nlayers > 1 is only valid for MultiLayerQG");
+  }
+  if (k.forcing_kind < 0 || k.forcing_kind > 4) return fail(nullptr, GF_ERR_ARG, "unknown forcing kind");
+  gf_ctx* c = new gf_ctx();
+  c->cfg = k;
+  c->stream = (cudaStream_t)stream;
+  const int r = build(c, cfg);
+  if (r != GF_OK) {
+    g_create_error = c->err.empty() ? g_create_error : c->err;
+    gf_destroy(c);
+    return r;
+  }
+  *out = c;
+  return GF_OK;
+}
+
+extern "C" int gf_destroy(gf_ctx* c) {
+  if (!c) return GF_OK;
+  if (c->stream) cudaStreamSynchronize(c->stream); else cudaDeviceSynchronize();
+  for (void* p : c->allocs) cudaFree(p);
+  for (auto e : c->ev_free) cudaEventDestroy(e);
+  for (auto& u : c->ev_used) { cudaEventDestroy(u.second.first); cudaEventDestroy(u.second.second); }
+  delete c;
+  return GF_OK;
+}
+
+extern "C" int gf_get_dims(const gf_ctx* c, int32_t* nkr, int32_t* ny, int32_t* nl, int32_t* rbytes) {
+  if (!c) return GF_ERR_ARG;
+  if (nkr) *nkr = c->g.nkr;
+  if (ny) *ny = c->g.ny;
+  if (nl) *nl = c->g.nl;
+  if (rbytes) *rbytes = (int32_t)c->rb;
+  return GF_OK;
+}
+
+// ------------------------------------------------------------------------------- state
+static int copy_spec_in(gf_ctx* c, void* dst, const void* src, int where) {
+  const Geom& g = c->g;
+  GF_CUDA(c, cudaMemcpy2DAsync(dst, g.ldk * c->cb, src, g.nkr * c->cb, g.nkr * c->cb, (size_t)g.ny * g.nl,
+                               where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream));
+  if (where == GF_HOST) GF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GF_OK;
+}
+static int copy_spec_out(gf_ctx* c, void* dst, const void* src, int where) {
+  const Geom& g = c->g;
+  GF_CUDA(c, cudaMemcpy2DAsync(dst, g.nkr * c->cb, src, g.ldk * c->cb, g.nkr * c->cb, (size_t)g.ny * g.nl,
+                               where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->stream));
+  if (where == GF_HOST) GF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GF_OK;
+}
+
+extern "C" int gf_set_state(gf_ctx* c, const void* sol, int where) {
+  if (!c || !sol) return GF_ERR_ARG;
+  c->W_valid = false;
+  return copy_spec_in(c, c->sol, sol, where);
+}
+extern "C" int gf_get_state(gf_ctx* c, void* sol, int where) {
+  if (!c || !sol) return GF_ERR_ARG;
+  return copy_spec_out(c, sol, c->sol, where);
+}
+extern "C" int gf_get_clock(const gf_ctx* c, double* t, int64_t* step) {
+  if (!c) return GF_ERR_ARG;
+  if (t) *t = c->t;
+  if (step) *step = c->step;
+  return GF_OK;
+}
+extern "C" int gf_set_clock(gf_ctx* c, double t, int64_t step) {
+  if (!c) return GF_ERR_ARG;
+  c->t = t; c->step = step;
+  return GF_OK;
+}
+extern "C" int gf_synchronize(gf_ctx* c) {
+  if (!c) return GF_ERR_ARG;
+  GF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GF_OK;
+}
+
+extern "C" int gf_updatevars(gf_ctx* c) {
+  if (!c) return GF_ERR_ARG;
+  const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->rb;
+  GF_CUDA(c, DISPATCH(c, launch_mask_inplace, c->g, c->sol, c->stream));
+  c->W_valid = false;
+  const int kinds[4] = {SF_X, SF_PSI, SF_U, SF_V};
+  for (int f = 0; f < 4; ++f)
+    if (int r = inv_transform(c, c->sol, kinds[f], 0, (char*)c->phys + f * pf)) return r;
+  return GF_OK;
+}
+
+extern "C" int gf_get_field(gf_ctx* c, int which, void* out, int where) {
+  if (!c || !out) return GF_ERR_ARG;
+  if (which < 0 || which > 3) return fail(c, GF_ERR_ARG, "unknown field");
+  const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->rb;
+  GF_CUDA(c, cudaMemcpyAsync(out, (char*)c->phys + which * pf, pf,
+                             where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->stream));
+  if (where == GF_HOST) GF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GF_OK;
+}
+
+extern "C" int gf_fwdtransform(gf_ctx* c, void* fieldh, const void* field, int where) {
+  if (!c || !fieldh || !field) return GF_ERR_ARG;
+  const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->rb;
+  void* ph = (char*)c->phys + 3 * pf;
+  GF_CUDA(c, cudaMemcpyAsync(ph, field, pf, where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream));
+  if (int r = fwd_transform(c, ph, c->tmp_spec, 0)) return r;
+  return copy_spec_out(c, fieldh, c->tmp_spec, where);
+}
+
+extern "C" int gf_invtransform(gf_ctx* c, void* field, const void* fieldh, int where) {
+  if (!c || !fieldh || !field) return GF_ERR_ARG;
+  const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->rb;
+  if (int r = copy_spec_in(c, c->tmp_spec, fieldh, where)) return r;
+  void* ph = (char*)c->phys + 3 * pf;
+  if (int r = inv_transform(c, c->tmp_spec, SF_RAW, 0, ph)) return r;
+  GF_CUDA(c, cudaMemcpyAsync(field, ph, pf, where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->stream));
+  if (where == GF_HOST) GF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GF_OK;
+}
+
+extern "C" int gf_set_physical(gf_ctx* c, int which, const void* field, int where) {
+  if (!c || !field) return GF_ERR_ARG;
+  const int mod = c->cfg.module;
+  if (which != GF_FIELD_Q && !(which == GF_FIELD_PSI && mod == GF_MULTILAYERQG))
+    return fail(c, GF_ERR_ARG, "set_physical supports q/zeta/b, and psi for MultiLayerQG");
+  const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->rb;
+  void* ph = (char*)c->phys + 3 * pf;
+  GF_CUDA(c, cudaMemcpyAsync(ph, field, pf, where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream));
+  if (which == GF_FIELD_PSI) {
+    // q = irfft(S rfft(psi)), then set_q!
+    if (int r = fwd_transform(c, ph, c->tmp_spec, 0)) return r;
+    GF_CUDA(c, DISPATCH(c, launch_spec_apply, c->g, c->m, c->tmp_spec, c->tmp_spec2, 0, c->stream));
+    if (int r = inv_transform(c, c->tmp_spec2, SF_RAW, 0, ph)) return r;
+  }
+  const int zero_mean = (mod != GF_SINGLELAYERQG);  // SingleLayerQG set_q! keeps the mean
+  if (int r = fwd_transform(c, ph, c->sol, zero_mean)) return r;
+  c->W_valid = false;
+  if (where == GF_HOST) GF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return gf_updatevars(c);
+}
+
+extern "C" int gf_set_forcing(gf_ctx* c, const void* data, int where) {
+  if (!c || !data) return GF_ERR_ARG;
+  const int fk = c->cfg.forcing_kind;
+  if (fk == GF_FORCING_NONE) return fail(c, GF_ERR_STATE, "problem was created without forcing");
+  if (fk == GF_FORCING_STATIC || fk == GF_FORCING_HARMONIC) return copy_spec_in(c, c->Fh, data, where);
+  // stochastic: spectrum (real, nkr x ny) -> sqrt(spectrum / dt), one table for all layers
+  const Geom& g = c->g;
+  const size_t nt = (size_t)g.ny * g.nkr;
+  std::vector<double> spec(nt);
+  if (where == GF_DEVICE) {
+    std::vector<char> tmp(nt * c->rb);
+    GF_CUDA(c, cudaMemcpy(tmp.data(), data, nt * c->rb, cudaMemcpyDeviceToHost));
+    for (size_t e = 0; e < nt; ++e) spec[e] = c->rb == 8 ? ((double*)tmp.data())[e] : ((float*)tmp.data())[e];
+  } else {
+    for (size_t e = 0; e < nt; ++e) spec[e] = c->rb == 8 ? ((const double*)data)[e] : ((const float*)data)[e];
+  }
+  for (size_t e = 0; e < nt; ++e) {
+    if (spec[e] < 0) return fail(c, GF_ERR_ARG, "forcing spectrum must be non-negative");
+    spec[e] = std::sqrt(spec[e] / c->cfg.dt);
+  }
+  return upload_table(c, c->fspec, spec, 0);
+}
+
+// ------------------------------------------------------------------------------- stepping
+static StepArgs stage_args(gf_ctx* c, int stage, double tstage) {
+  StepArgs s{};
+  s.kind = c->kind; s.stage = stage; s.filtered = c->filtered; s.hasL = c->hasL; s.cplxL = c->cplxL;
+  s.ab3_euler = c->step < 3;
+  s.do_fwd = 1; s.do_inv = 1;
+  s.dt = c->cfg.dt;
+  s.Ltab = c->Ltab; s.filt = c->filt;
+  s.e = c->etd[0]; s.e2 = c->etd[1]; s.zeta = c->etd[2]; s.alpha = c->etd[3]; s.beta = c->etd[4]; s.gamma = c->etd[5];
+  s.sol = c->sol; s.X = c->X; s.acc = c->acc; s.s1 = c->s1; s.N1 = c->N1;
+  if (c->kind == SK_AB3) { s.Rout = c->R3[c->ab3_out]; s.Rm1 = c->R3[c->ab3_m1]; s.Rm2 = c->R3[c->ab3_m2]; }
+  s.fkind = c->cfg.forcing_kind;
+  s.Fh = c->Fh;
+  s.fspec = c->fspec; s.Fstore = c->Fstore; s.prevsol = c->prevsol;
+  s.seed = c->cfg.seed; s.step = (uint64_t)c->step;
+  s.draw = (stage == 1);
+  if (s.fkind == FK_HARMONIC) s.fscale = std::cos(c->cfg.forcing_omega * tstage + c->cfg.forcing_phase);
+  else s.fscale = 1.0;
+  return s;
+}
+
+static cudaEvent_t take_event(gf_ctx* c) {
+  if (!c->ev_free.empty()) { cudaEvent_t e = c->ev_free.back(); c->ev_free.pop_back(); return e; }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// one row (products) and/or column (stage) launch, timed when profiling is on
+static int launch_stage(gf_ctx* c, const StepArgs& s, int with_row) {
+  for (int which = with_row ? 0 : 1; which < 2; ++which) {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (c->profiling) { e0 = take_event(c); e1 = take_event(c); GF_CUDA(c, cudaEventRecord(e0, c->stream)); }
+    if (which == 0) GF_CUDA(c, DISPATCH(c, launch_row, c->g, c->m, bufs(c), c->stream));
+    else GF_CUDA(c, DISPATCH(c, launch_col, c->g, c->m, s, bufs(c), c->stream));
+    c->launches++;
+    if (c->profiling) { GF_CUDA(c, cudaEventRecord(e1, c->stream)); c->ev_used.push_back({which, {e0, e1}}); }
+  }
+  return GF_OK;
+}
+
+extern "C" int gf_profile_enable(gf_ctx* c, int on) {
+  if (!c) return GF_ERR_ARG;
+  c->profiling = on != 0;
+  return GF_OK;
+}
+
+extern "C" int gf_profile_read(gf_ctx* c, double* ms, int64_t* n, int64_t* launches) {
+  if (!c) return GF_ERR_ARG;
+  GF_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (auto& u : c->ev_used) {
+    float t = 0;
+    GF_CUDA(c, cudaEventElapsedTime(&t, u.second.first, u.second.second));
+    c->prof_ms[u.first] += t;
+    c->prof_n[u.first] += 1;
+    c->ev_free.push_back(u.second.first);
+    c->ev_free.push_back(u.second.second);
+  }
+  c->ev_used.clear();
+  if (ms) { ms[0] = c->prof_ms[0]; ms[1] = c->prof_ms[1]; }
+  if (n) { n[0] = c->prof_n[0]; n[1] = c->prof_n[1]; }
+  if (launches) *launches = c->launches;
+  c->prof_ms[0] = c->prof_ms[1] = 0;
+  c->prof_n[0] = c->prof_n[1] = 0;
+  c->launches = 0;
+  return GF_OK;
+}
+
+static int ensure_W(gf_ctx* c) {
+  if (c->W_valid) return GF_OK;
+  StepArgs s = stage_args(c, 0, c->t);
+  s.do_fwd = 0; s.do_inv = 1;
+  if (int r = launch_stage(c, s, 0)) return r;
+  c->W_valid = true;
+  return GF_OK;
+}
+
+static int one_step(gf_ctx* c) {
+  if (int r = ensure_W(c)) return r;
+  const double dt = c->cfg.dt;
+  for (int stg = 1; stg <= c->nstages; ++stg) {
+    const double ts = c->t + (c->nstages == 4 ? (stg == 1 ? 0.0 : stg == 4 ? dt : 0.5 * dt) : 0.0);
+    StepArgs s = stage_args(c, stg, ts);
+    if (int r = launch_stage(c, s, 1)) return r;
+    if (s.fkind == FK_HARMONIC) c->last_fscale = s.fscale;
+    else if (s.fkind != FK_NONE) c->last_fscale = 1.0;
+  }
+  if (c->kind == SK_AB3) {  // RHS_{-2} <- RHS_{-1} <- RHS
+    const int o = c->ab3_out, m1 = c->ab3_m1, m2 = c->ab3_m2;
+    c->ab3_m1 = o; c->ab3_m2 = m1; c->ab3_out = m2;
+  }
+  c->t += dt;
+  c->step += 1;
+  return GF_OK;
+}
+
+extern "C" int gf_step(gf_ctx* c, int64_t nsteps) {
+  if (!c || nsteps < 0) return GF_ERR_ARG;
+  if (c->cfg.forcing_kind >= GF_FORCING_STOCHASTIC && !c->fspec) return fail(c, GF_ERR_STATE, "no forcing spectrum");
+  for (int64_t i = 0; i < nsteps; ++i)
+    if (int r = one_step(c)) return r;
+  return GF_OK;
+}
+
+extern "C" int gf_diagnostics(gf_ctx* c, const int32_t* which, int32_t nd, double* out);
+
+extern "C" int gf_step_diags(gf_ctx* c, int64_t nsteps, const int32_t* which, int32_t nd, double* out) {
+  if (!c || nsteps < 0 || (nd > 0 && (!which || !out))) return GF_ERR_ARG;
+  for (int64_t i = 0; i < nsteps; ++i) {
+    if (int r = one_step(c)) return r;
+    if (nd > 0)
+      if (int r = gf_diagnostics(c, which, nd, out + i * nd)) return r;
+  }
+  return GF_OK;
+}
+
+extern "C" int gf_calcN(gf_ctx* c, void* N, void* sol, double t, int where) {
+  if (!c || !N || !sol) return GF_ERR_ARG;
+  if (c->cfg.forcing_kind >= GF_FORCING_STOCHASTIC && !c->fspec) return fail(c, GF_ERR_STATE, "no forcing spectrum");
+  if (int r = copy_spec_in(c, c->tmp_spec, sol, where)) return r;
+  // first half of calcN! (dealias + inversion + inverse y-FFTs) on the caller's sol
+  StepArgs s = stage_args(c, 1, t);
+  s.sol = c->tmp_spec;
+  s.do_fwd = 0; s.do_inv = 1;
+  if (int r = launch_stage(c, s, 0)) return r;
+  // products, forward FFTs, N = -i kr A - i l B - C + extras + forcing, written to tmp_spec2
+  s = stage_args(c, 1, t);
+  s.kind = SK_NOUT; s.sol = c->tmp_spec; s.acc = c->tmp_spec2; s.do_fwd = 1; s.do_inv = 0;
+  s.draw = (t == c->t);  // stochastic forcing is redrawn only when t == clock.t
+  if (s.fkind >= FK_STOCH && !s.draw) s.Fh = c->Fstore;
+  if (int r = launch_stage(c, s, 1)) return r;
+  if (s.fkind == FK_HARMONIC) c->last_fscale = s.fscale;
+  else if (s.fkind != FK_NONE) c->last_fscale = 1.0;
+  // like the reference, calcN! leaves sol dealiased
+  GF_CUDA(c, DISPATCH(c, launch_mask_inplace, c->g, c->tmp_spec, c->stream));
+  c->W_valid = false;
+  if (int r = copy_spec_out(c, N, c->tmp_spec2, where)) return r;
+  return copy_spec_out(c, sol, c->tmp_spec, where);
+}
+
+// ------------------------------------------------------------------------------- diagnostics
+extern "C" int gf_diagnostics(gf_ctx* c, const int32_t* which, int32_t nd, double* out) {
+  if (!c || (nd > 0 && (!which || !out))) return GF_ERR_ARG;
+  const int mod = c->cfg.module;
+  const bool finite_ell = (mod == GF_SINGLELAYERQG) && c->m.psi_kind == PSI_HELMHOLTZ;
+  uint32_t mask = 0;
+  for (int i = 0; i < nd; ++i) {
+    const int d = which[i];
+    if (mod == GF_MULTILAYERQG) {
+      const int n = c->g.nl;
+      if (d >= 0 && d < n) mask |= 1u << d;
+      else if (d >= GF_D_MLQG_PE0 && d < GF_D_MLQG_PE0 + n - 1) mask |= 1u << (n + d - GF_D_MLQG_PE0);
+      else return fail(c, GF_ERR_ARG, "unknown MultiLayerQG diagnostic");
+      continue;
+    }
+    const int maxd = mod == GF_TWODNAVIERSTOKES ? 8 : mod == GF_SINGLELAYERQG ? 9 : 4;
+    if (d < 0 || d > maxd) return fail(c, GF_ERR_ARG, "unknown diagnostic");
+    if (mod == GF_SINGLELAYERQG && d == GF_D_SLQG_ENERGY) { mask |= 3u; continue; }
+    if (finite_ell && d >= 3) return fail(c, GF_ERR_NOT_IMPLEMENTED, "not implemented for finite deformation radius");
+    mask |= 1u << d;
+  }
+  const void* Fh = (c->cfg.forcing_kind != GF_FORCING_NONE) ? c->Fh : nullptr;
+  const void* prev = (c->cfg.forcing_kind >= GF_FORCING_STOCHASTIC) ? c->prevsol : nullptr;
+  GF_CUDA(c, DISPATCH(c, launch_diag, c->g, c->m, c->sol, prev, Fh, mask, c->dpart, c->diag_blocks, c->stream));
+  diag_finish<<<1, 256, 0, c->stream>>>(c->dpart, c->diag_blocks, mask, c->dout);
+  GF_CUDA(c, cudaGetLastError());
+  double h[NDIAG];
+  GF_CUDA(c, cudaMemcpyAsync(h, c->dout, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  GF_CUDA(c, cudaStreamSynchronize(c->stream));
+  const double nn = (double)c->g.nx * c->g.ny, norm = 1.0 / (nn * nn);
+  const double fs = (c->cfg.forcing_kind == GF_FORCING_HARMONIC || c->cfg.forcing_kind == GF_FORCING_STATIC) ? c->last_fscale : 1.0;
+  for (int i = 0; i < nd; ++i) {
+    const int d = which[i];
+    double v;
+    if (mod == GF_MULTILAYERQG) {
+      const int n = c->g.nl;
+      if (n == 1) v = h[0] * norm / 2;
+      else if (d < n) v = h[d] * norm * c->Hl[d] / (2 * c->Hsum);
+      else { const int j = d - GF_D_MLQG_PE0; v = h[n + j] * norm * c->f0 * c->f0 / (c->gprime[j] * 2 * c->Hsum); }
+    } else if (mod == GF_SINGLELAYERQG && d == GF_D_SLQG_ENERGY) {
+      v = (h[0] + h[1]) * norm;
+    } else {
+      v = h[d] * norm;
+      const bool work = (mod == GF_TWODNAVIERSTOKES && (d == 7 || d == 8)) || (mod == GF_SINGLELAYERQG && (d == 5 || d == 6)) ||
+                        (mod == GF_SURFACEQG && d == 4);
+      if (work) v *= fs;
+    }
+    out[i] = v;
+  }
+  return GF_OK;
+}

@@ -1,0 +1,6 @@
+// Row-pass kernel instantiations for double storage and arithmetic.
+#include "gf_inst.cuh"
+
+namespace gf {
+GF_INSTANTIATE_ROW(double)
+}  // namespace gf

@@ -1,0 +1,150 @@
+// Shared-memory Stockham FFT building blocks for the fused pseudospectral step.
+//
+// The FFT here replaces the FFTW/CUFFT plans that FourierFlows builds for every
+// TwoDGrid (`grid.rfftplan`, called through `mul!`/`ldiv!` at e.g.
+// src/twodnavierstokes.jl:258-270 and src/multilayerqg.jl:471,478).  A length-N complex
+// transform is executed by N/R threads as a sequence of radix-R Stockham passes
+// (Govindaraju et al., "High performance discrete Fourier transforms on graphics
+// processors", SC'08): every pass reads R elements strided by N/R, applies the twiddles
+// w^(r*(j mod Ns)), does an in-register R-point DFT and writes the results to their
+// expanded positions, so input and output are both in natural order.  The in-register
+// DFT is a fully unrolled radix-2 decimation-in-time network; its constant twiddles are
+// the 16th roots of unity, special-cased where they are 1, -i, or (1-i)/sqrt(2).
+//
+// Twiddles between passes come from one table of TWN = 4096 entries exp(-2 pi i k / TWN)
+// computed in double precision on the host, so every FFT length N <= TWN indexes it with
+// a stride of TWN / N.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gf {
+
+constexpr int TWN = 4096;  // twiddle table length (largest supported transform)
+
+template <class T> struct cplx;
+template <> struct __align__(8) cplx<float> { float x, y; };
+template <> struct __align__(16) cplx<double> { double x, y; };
+
+template <class T> __host__ __device__ __forceinline__ cplx<T> mk(T a, T b) { cplx<T> r; r.x = a; r.y = b; return r; }
+template <class T> __device__ __forceinline__ cplx<T> operator+(cplx<T> a, cplx<T> b) { return mk<T>(a.x + b.x, a.y + b.y); }
+template <class T> __device__ __forceinline__ cplx<T> operator-(cplx<T> a, cplx<T> b) { return mk<T>(a.x - b.x, a.y - b.y); }
+template <class T> __device__ __forceinline__ cplx<T> operator*(cplx<T> a, cplx<T> b) {
+  return mk<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <class T> __device__ __forceinline__ cplx<T> operator*(T s, cplx<T> a) { return mk<T>(s * a.x, s * a.y); }
+template <class T> __device__ __forceinline__ cplx<T> conj(cplx<T> a) { return mk<T>(a.x, -a.y); }
+template <class T> __device__ __forceinline__ cplx<T> mul_i(cplx<T> a) { return mk<T>(-a.y, a.x); }   //  i*a
+template <class T> __device__ __forceinline__ cplx<T> mul_mi(cplx<T> a) { return mk<T>(a.y, -a.x); }  // -i*a
+template <class T> __device__ __forceinline__ cplx<T> czero() { return mk<T>(T(0), T(0)); }
+
+// cos and sin of pi*m/8 for m = 1, 3 (exact decimal expansions of the algebraic numbers)
+constexpr double kC1 = 0.92387953251128675612818318939678828682241662586364;  // cos(pi/8)
+constexpr double kS1 = 0.38268343236508977172845998403039886676134456248563;  // sin(pi/8)
+constexpr double kH = 0.70710678118654752440084436210484903928483593768847;   // sqrt(1/2)
+
+// x * exp(DIR * 2 pi i * m / 16) with DIR = -1 (forward) or +1 (inverse), 0 <= m < 8
+template <int m, int DIR, class T>
+__device__ __forceinline__ cplx<T> rot16(cplx<T> a) {
+  if constexpr (m == 0) {
+    return a;
+  } else if constexpr (m == 4) {
+    return DIR < 0 ? mul_mi(a) : mul_i(a);
+  } else if constexpr (m == 2 || m == 6) {
+    const T h = T(kH);
+    // exp(-i pi/4) = h(1 - i); exp(-3 i pi/4) = h(-1 - i)
+    if constexpr (m == 2) {
+      return DIR < 0 ? mk<T>(h * (a.x + a.y), h * (a.y - a.x)) : mk<T>(h * (a.x - a.y), h * (a.y + a.x));
+    } else {
+      return DIR < 0 ? mk<T>(h * (a.y - a.x), -h * (a.x + a.y)) : mk<T>(-h * (a.x + a.y), h * (a.x - a.y));
+    }
+  } else {
+    // general angle theta = pi m / 8 with (c, s) = (cos theta, sin theta)
+    constexpr double c = (m == 1) ? kC1 : (m == 3) ? kS1 : (m == 5) ? -kS1 : -kC1;
+    constexpr double s = (m == 1 || m == 7) ? kS1 : kC1;
+    const T cc = T(c), ss = T(s);
+    if constexpr (DIR < 0) return mk<T>(a.x * cc + a.y * ss, a.y * cc - a.x * ss);
+    else return mk<T>(a.x * cc - a.y * ss, a.y * cc + a.x * ss);
+  }
+}
+
+// In-register R-point DFT (R = 1,2,4,8,16), natural order in and out.
+template <int R, int DIR, class T>
+__device__ __forceinline__ void dft(cplx<T>* v) {
+  if constexpr (R == 1) {
+    return;
+  } else if constexpr (R == 2) {
+    cplx<T> a = v[0], b = v[1];
+    v[0] = a + b;
+    v[1] = a - b;
+  } else {
+    constexpr int H = R / 2;
+    cplx<T> e[H], o[H];
+#pragma unroll
+    for (int i = 0; i < H; ++i) { e[i] = v[2 * i]; o[i] = v[2 * i + 1]; }
+    dft<H, DIR>(e);
+    dft<H, DIR>(o);
+    auto step = [&](auto kk) {
+      constexpr int k = decltype(kk)::value;
+      cplx<T> t = rot16<k * (16 / R), DIR>(o[k]);
+      v[k] = e[k] + t;
+      v[k + H] = e[k] - t;
+    };
+    // unrolled over k = 0..H-1 with k a compile-time constant
+    [&]<int... ks>(std::integer_sequence<int, ks...>) {
+      (step(std::integral_constant<int, ks>{}), ...);
+    }(std::make_integer_sequence<int, H>{});
+  }
+}
+
+template <int DIR, class T>
+__device__ __forceinline__ cplx<T> twiddle(const cplx<T>* __restrict__ tw, int idx) {
+  cplx<T> w = tw[idx];
+  return DIR < 0 ? w : conj(w);
+}
+
+// One radix pass of a length-N Stockham FFT on a column of shared memory whose
+// consecutive elements are S apart.  Threads t in [0, N/R) each do R/Rp butterflies of
+// radix Rp = min(R, N/Ns).  The caller must have synchronised before the first pass.
+template <class T, int N, int R, int DIR, int Ns>
+__device__ __forceinline__ void fft_passes(cplx<T>* buf, int S, int t, const cplx<T>* __restrict__ tw) {
+  if constexpr (Ns < N) {
+    constexpr int Rp = (N / Ns < R) ? (N / Ns) : R;
+    constexpr int NB = R / Rp;
+    constexpr int TPF = N / R;
+    constexpr int TWS = TWN / (Ns * Rp);
+    cplx<T> v[NB][Rp];
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const int j = t + b * TPF;
+#pragma unroll
+      for (int r = 0; r < Rp; ++r) v[b][r] = buf[(j + r * (N / Rp)) * S];
+      if constexpr (Ns > 1) {
+        const int k = j & (Ns - 1);
+#pragma unroll
+        for (int r = 1; r < Rp; ++r) v[b][r] = v[b][r] * twiddle<DIR>(tw, r * k * TWS);
+      }
+      dft<Rp, DIR>(v[b]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const int j = t + b * TPF;
+      const int idxD = (j / Ns) * Ns * Rp + (j & (Ns - 1));
+#pragma unroll
+      for (int r = 0; r < Rp; ++r) buf[(idxD + r * Ns) * S] = v[b][r];
+    }
+    __syncthreads();
+    fft_passes<T, N, R, DIR, Ns * Rp>(buf, S, t, tw);
+  }
+}
+
+// In-place length-N FFT (DIR = -1 forward, unnormalised; +1 inverse, unnormalised) of the
+// column buf[0], buf[S], ..., buf[(N-1) S] by threads t in [0, N/R).  All threads of the
+// block must call it (it synchronises the block); threads with t >= N/R must not exist.
+template <class T, int N, int R, int DIR>
+__device__ __forceinline__ void fft_smem(cplx<T>* buf, int S, int t, const cplx<T>* __restrict__ tw) {
+  fft_passes<T, N, R, DIR, 1>(buf, S, t, tw);
+}
+
+}  // namespace gf

@@ -1,0 +1,91 @@
+// Internal (non-ABI) declarations shared by the C-ABI layer and the kernel translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gf {
+
+template <class T> struct cplx;
+
+enum Module { MOD_TWODNS = 0, MOD_SLQG = 1, MOD_MLQG = 2, MOD_SQG = 3 };
+enum StepKind { SK_FE = 0, SK_RK4 = 1, SK_ETDRK4 = 2, SK_AB3 = 3, SK_NOUT = 4 /* write N to acc (calcN!) */ };
+enum PsiKind { PSI_INVK2 = 0, PSI_HELMHOLTZ = 1, PSI_TABLE = 2, PSI_EIGEN = 3 };
+enum ForceKind { FK_NONE = 0, FK_STATIC = 1, FK_HARMONIC = 2, FK_STOCH = 3, FK_STOCH_PHASE = 4 };
+constexpr int MAXL = 8;  // largest number of layers
+
+// Grid geometry in the internal layout: spectral arrays are [layer][j][kr] with row stride
+// ldk (>= nkr); the pruned inverse intermediates are [field][layer][j][kr < kcut] with row
+// stride ldw; physical arrays are [layer][j][i] with row stride nx.
+struct Geom {
+  int nx, ny, nkr, ldk, ldw, nl;
+  int kcut;    // kr indices >= kcut are aliased
+  int lA, lB;  // l indices in [lA, lB] are aliased (empty when lA > lB)
+  double dkx, dky, inv_nxny;
+};
+
+// How psi-hat follows from the layer PV/vorticity/buoyancy X, and what the physical-space
+// products are.  The inverse fields of every layer are (X, -i l psi, i kr psi) = (q, u, v).
+struct ModArgs {
+  int module, psi_kind;
+  double ell_inv2;       // 1/ell^2 for PSI_HELMHOLTZ
+  const void* mult;      // PSI_TABLE: real [j][kr] table, psi = -mult * X
+  // PSI_EIGEN: S_k^-1 = V diag(1/(lam - K^2)) Vinv (K = 0 -> 0)
+  double lam[MAXL], V[MAXL * MAXL], Vinv[MAXL * MAXL];
+  // physical-space products
+  int hasB, hasC, linear;
+  const void* eta;       // real [j][i] or null: q' = q + eta
+  const void* U1D;       // real [layer][j] or null: u' = u + U
+  const void* Qy1D;      // real [layer][j] or null
+  const void* Qx2D;      // real [j][i] or null (last layer)
+  const void* Qy2D;      // real [j][i] or null (last layer)
+  // spectral-side extras
+  const void* etah;      // complex [j][kr] or null: N -= i kr U0 etah
+  double U0;
+  int drag; double mu;   // N_last += mu K^2 psi_last (MultiLayerQG bottom drag)
+  // dissipation parameters used by the diagnostics (nu, nnu; mu_visc, nmu)
+  double nu, mu_visc; int nnu, nmu;
+  void* D;               // complex [j][kr] buffer carrying mu K^2 psi_last between kernels
+};
+
+struct StepArgs {
+  int kind, stage, filtered, hasL, cplxL, ab3_euler, do_fwd, do_inv;
+  double dt;
+  const void *Ltab, *filt, *e, *e2, *zeta, *alpha, *beta, *gamma;  // [j][kr]
+  void *sol, *X, *acc, *s1, *N1, *Rm1, *Rm2, *Rout;                // [layer][j][kr]
+  // forcing
+  int fkind, draw;
+  double fscale;
+  const void* Fh;      // static / harmonic F-hat, or the stored stochastic draw
+  const void* fspec;   // real [j][kr]: sqrt(spectrum / dt) (stochastic)
+  void* Fstore;        // stochastic draw written at the first stage
+  void* prevsol;       // sol at the first stage (stochastic budgets)
+  uint64_t seed, step;
+};
+
+struct Bufs {
+  const void* twid;  // TWN twiddles
+  void* W;           // [3][layer][j][ldw]
+  void* P;           // [3][layer][j][ldk]
+};
+
+// Generic transforms (updatevars!, set_*!, fwdtransform!/invtransform!).
+enum SpecField { SF_X = 0, SF_PSI = 1, SF_U = 2, SF_V = 3, SF_UY = 4, SF_RAW = 5, SF_DX = 6, SF_DY = 7 };
+
+template <class T> cudaError_t launch_row(const Geom&, const ModArgs&, const Bufs&, cudaStream_t);
+template <class T> cudaError_t launch_col(const Geom&, const ModArgs&, const StepArgs&, const Bufs&, cudaStream_t);
+template <class T> cudaError_t launch_col_inv(const Geom&, const ModArgs&, const void* src, int kind, int mask,
+                                              const Bufs&, cudaStream_t);
+template <class T> cudaError_t launch_row_c2r(const Geom&, const Bufs&, int nf, void* out, cudaStream_t);
+template <class T> cudaError_t launch_row_r2c(const Geom&, const Bufs&, int nf, const void* in, cudaStream_t);
+template <class T> cudaError_t launch_col_fwd(const Geom&, const Bufs&, int nf, void* out, int zero_mean,
+                                              cudaStream_t);
+template <class T> cudaError_t launch_diag(const Geom&, const ModArgs&, const void* sol, const void* prevsol,
+                                           const void* Fh, uint32_t mask, double* partial, int nblocks,
+                                           cudaStream_t);
+template <class T> cudaError_t launch_mask_inplace(const Geom&, void* sol, cudaStream_t);
+template <class T> cudaError_t launch_spec_apply(const Geom&, const ModArgs&, const void* in, void* out, int op,
+                                                 cudaStream_t);
+
+constexpr int DIAG_BLOCK = 256;
+constexpr int NDIAG = 24;  // number of reduction slots
+}  // namespace gf

@@ -1,0 +1,11 @@
+"""gfcuda: GB300 (sm_103a) pseudospectral time step of GeophysicalFlows.jl behind a C ABI.
+
+Host-side mirror of the reference's module API; every computation runs in libgfcuda.so.
+"""
+from . import _abi
+from ._abi import load, GFError, GFNotImplemented
+from .core import Diagnostic, Forcing, stepforward
+from . import TwoDNavierStokes, SingleLayerQG, MultiLayerQG, SurfaceQG
+
+__all__ = ["load", "GFError", "GFNotImplemented", "Diagnostic", "Forcing", "stepforward", "TwoDNavierStokes",
+           "SingleLayerQG", "MultiLayerQG", "SurfaceQG"]

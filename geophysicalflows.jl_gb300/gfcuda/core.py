@@ -1,0 +1,271 @@
+"""Host-side mirror of FourierFlows.Problem / stepforward! / Diagnostic over libgfcuda.
+
+The reference's user-facing objects (FourierFlows 0.10.5, re-exported at
+src/GeophysicalFlows.jl:15) are mirrored with the same names and meaning; the state lives
+on the GPU and crosses the boundary only when a field is read:
+
+    prob.sol          spectral state (numpy copy, shape (nlayers?, ny, nkr))
+    prob.clock        t, dt, step
+    prob.grid         TwoDGrid quantities (x, y, kr, l, Krsq, invKrsq, ...)
+    prob.vars         physical fields after updatevars!
+    stepforward(prob, nsteps) / stepforward(prob, diags, nsteps)
+
+NumPy arrays are C-ordered with shape (ny, nx) / (ny, nkr), the same memory order as the
+reference's column-major (nx, ny) / (nkr, ny) Julia arrays.
+"""
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _abi as A
+
+
+class Grid:
+    """Wavenumber and grid-point arrays of FourierFlows.TwoDGrid (x in [-Lx/2, Lx/2))."""
+
+    def __init__(self, nx, ny, Lx, Ly, aliased_fraction, T):
+        self.nx, self.ny, self.Lx, self.Ly = nx, ny, Lx, Ly
+        self.nkr, self.nl, self.nk = nx // 2 + 1, ny, nx
+        self.dx, self.dy = Lx / nx, Ly / ny
+        self.x = (-Lx / 2 + self.dx * np.arange(nx)).astype(T)
+        self.y = (-Ly / 2 + self.dy * np.arange(ny)).astype(T)
+        self.kr = (2 * np.pi / Lx) * np.arange(self.nkr)[None, :]
+        self.l = (2 * np.pi / Ly) * (np.fft.fftfreq(ny) * ny)[:, None]
+        self.Krsq = self.kr ** 2 + self.l ** 2
+        self.invKrsq = np.where(self.Krsq == 0, 0.0, 1.0 / np.where(self.Krsq == 0, 1.0, self.Krsq))
+        self.aliased_fraction = aliased_fraction
+        self.T = T
+
+    def gridpoints(self):
+        return np.meshgrid(self.x, self.y, indexing="xy")
+
+
+class Clock:
+    def __init__(self, prob, dt):
+        self._prob, self.dt = prob, dt
+
+    @property
+    def t(self):
+        t = C.c_double()
+        A.check(self._prob._lib, self._prob._ctx, self._prob._lib.gf_get_clock(self._prob._ctx, C.byref(t), None))
+        return t.value
+
+    @property
+    def step(self):
+        s = C.c_int64()
+        A.check(self._prob._lib, self._prob._ctx, self._prob._lib.gf_get_clock(self._prob._ctx, None, C.byref(s)))
+        return s.value
+
+
+class Forcing:
+    """Device-side forms of the reference's calcF! callbacks (see include/gfcuda.h)."""
+
+    def __init__(self, kind=None, Fh=None, spectrum=None, omega=0.0, phase=0.0, seed=0):
+        if kind not in A.FORCING:
+            raise ValueError(f"unknown forcing kind {kind}")
+        self.kind, self.Fh, self.spectrum, self.omega, self.phase, self.seed = kind, Fh, spectrum, omega, phase, seed
+
+    @property
+    def stochastic(self):
+        return self.kind in ("stochastic", "stochastic_phase")
+
+
+class Vars:
+    """Physical fields of prob.vars, filled by updatevars!."""
+
+    def __init__(self, names):
+        self._names = names
+        for n in names.values():
+            setattr(self, n, None)
+
+
+class Problem:
+    """FourierFlows.Problem backed by a libgfcuda context."""
+
+    module = None
+    field_names = {A.FIELD_Q: "q", A.FIELD_PSI: "psi", A.FIELD_U: "u", A.FIELD_V: "v"}
+
+    def __init__(self, cfg_kwargs, nx, ny, Lx, Ly, dt, stepper, T, aliased_fraction, forcing, nlayers=1,
+                 stream=None):
+        self._lib = A.load()
+        self._ctx = C.c_void_p()
+        if stepper not in A.STEPPERS:
+            raise ValueError(f"unknown stepper {stepper}")
+        T = np.dtype(T).type
+        if T not in (np.float32, np.float64):
+            raise ValueError("T must be Float32 or Float64")
+        self.T, self.CT = T, (np.complex64 if T == np.float32 else np.complex128)
+        self.nlayers = nlayers
+        self.grid = Grid(nx, ny, Lx, Ly, aliased_fraction, T)
+        self.forcing = forcing if forcing is not None else Forcing(None)
+        self.stepper = stepper
+        cfg = A.gf_config()
+        cfg.module = A.MODULES[self.module]
+        cfg.precision = A.F32 if T == np.float32 else A.F64
+        cfg.stepper = A.STEPPERS[stepper]
+        cfg.nx, cfg.ny, cfg.nlayers = nx, ny, nlayers
+        cfg.Lx, cfg.Ly, cfg.dt, cfg.aliased_fraction = Lx, Ly, dt, aliased_fraction
+        cfg.forcing_kind = A.FORCING[self.forcing.kind]
+        cfg.seed = int(self.forcing.seed)
+        cfg.forcing_omega, cfg.forcing_phase = self.forcing.omega, self.forcing.phase
+        self._keep = []  # arrays referenced by cfg during gf_create
+        for k, v in cfg_kwargs.items():
+            if isinstance(v, np.ndarray):
+                a = np.ascontiguousarray(v, dtype=np.float64)
+                self._keep.append(a)
+                setattr(cfg, k, a.ctypes.data_as(C.POINTER(C.c_double)))
+            elif k == "topographic_pv_gradient":
+                cfg.topographic_pv_gradient[0], cfg.topographic_pv_gradient[1] = float(v[0]), float(v[1])
+            else:
+                setattr(cfg, k, v)
+        A.check(self._lib, None, self._lib.gf_create(C.byref(cfg), stream, C.byref(self._ctx)))
+        self._keep = []
+        self.clock = Clock(self, dt)
+        self.vars = Vars(self.field_names)
+        if self.forcing.kind in ("static", "harmonic") and self.forcing.Fh is not None:
+            self.set_forcing(self.forcing.Fh)
+        elif self.forcing.stochastic and self.forcing.spectrum is not None:
+            self.set_forcing(self.forcing.spectrum)
+
+    # -- shapes
+    @property
+    def spec_shape(self):
+        g = self.grid
+        return (self.nlayers, g.ny, g.nkr) if self.module == "MultiLayerQG" else (g.ny, g.nkr)
+
+    @property
+    def phys_shape(self):
+        g = self.grid
+        return (self.nlayers, g.ny, g.nx) if self.module == "MultiLayerQG" else (g.ny, g.nx)
+
+    def _c(self, code):
+        A.check(self._lib, self._ctx, code)
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            self._lib.gf_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- state
+    @property
+    def sol(self):
+        out = np.empty(self.spec_shape, dtype=self.CT)
+        self._c(self._lib.gf_get_state(self._ctx, out.ctypes.data, A.HOST))
+        return out
+
+    @sol.setter
+    def sol(self, value):
+        a = np.ascontiguousarray(np.broadcast_to(value, self.spec_shape), dtype=self.CT)
+        self._c(self._lib.gf_set_state(self._ctx, a.ctypes.data, A.HOST))
+
+    def set_clock(self, t, step):
+        self._c(self._lib.gf_set_clock(self._ctx, float(t), int(step)))
+
+    def set_forcing(self, data):
+        if self.forcing.stochastic:
+            a = np.ascontiguousarray(data, dtype=self.T).reshape(self.grid.ny, self.grid.nkr)
+        else:
+            a = np.ascontiguousarray(np.broadcast_to(data, self.spec_shape), dtype=self.CT)
+        self._c(self._lib.gf_set_forcing(self._ctx, a.ctypes.data, A.HOST))
+
+    def _set_physical(self, which, field):
+        a = np.ascontiguousarray(np.asarray(field).reshape(self.phys_shape), dtype=self.T)
+        self._c(self._lib.gf_set_physical(self._ctx, which, a.ctypes.data, A.HOST))
+        self._pull_vars()
+
+    def updatevars(self):
+        self._c(self._lib.gf_updatevars(self._ctx))
+        self._pull_vars()
+
+    def _pull_vars(self):
+        for which, name in self.field_names.items():
+            out = np.empty(self.phys_shape, dtype=self.T)
+            self._c(self._lib.gf_get_field(self._ctx, which, out.ctypes.data, A.HOST))
+            setattr(self.vars, name, out)
+
+    def calcN(self, sol, t):
+        """calcN!(N, sol, t, ...): returns (N, dealiased sol)."""
+        s = np.ascontiguousarray(np.broadcast_to(sol, self.spec_shape), dtype=self.CT).copy()
+        N = np.empty(self.spec_shape, dtype=self.CT)
+        self._c(self._lib.gf_calcN(self._ctx, N.ctypes.data, s.ctypes.data, float(t), A.HOST))
+        return N, s
+
+    def fwdtransform(self, field):
+        a = np.ascontiguousarray(np.asarray(field).reshape(self.phys_shape), dtype=self.T)
+        out = np.empty(self.spec_shape, dtype=self.CT)
+        self._c(self._lib.gf_fwdtransform(self._ctx, out.ctypes.data, a.ctypes.data, A.HOST))
+        return out
+
+    def invtransform(self, fieldh):
+        a = np.ascontiguousarray(np.broadcast_to(fieldh, self.spec_shape), dtype=self.CT)
+        out = np.empty(self.phys_shape, dtype=self.T)
+        self._c(self._lib.gf_invtransform(self._ctx, out.ctypes.data, a.ctypes.data, A.HOST))
+        return out
+
+    def diagnostics(self, ids):
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        out = np.empty(len(ids), dtype=np.float64)
+        self._c(self._lib.gf_diagnostics(self._ctx, ids.ctypes.data_as(C.POINTER(C.c_int32)), len(ids),
+                                         out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
+    def synchronize(self):
+        self._c(self._lib.gf_synchronize(self._ctx))
+
+
+class Diagnostic:
+    """FourierFlows.Diagnostic: a time series recorded after every step (freq=1)."""
+
+    def __init__(self, calc, prob, nsteps=100):
+        self.calc, self.prob = calc, prob
+        self.data = [calc(prob)]
+        self.t = [prob.clock.t]
+        self.steps = [prob.clock.step]
+
+    @property
+    def i(self):
+        return len(self.data)
+
+    def __getitem__(self, k):
+        return np.asarray(self.data)[k]
+
+    def increment(self):
+        self.data.append(self.calc(self.prob))
+        self.t.append(self.prob.clock.t)
+        self.steps.append(self.prob.clock.step)
+
+
+def stepforward(prob, *args):
+    """stepforward!(prob[, nsteps]) or stepforward!(prob, diags, nsteps)."""
+    if len(args) == 0:
+        diags, n = None, 1
+    elif len(args) == 1:
+        diags, n = None, int(args[0])
+    else:
+        diags, n = args[0], int(args[1])
+    if not diags:
+        prob._c(prob._lib.gf_step(prob._ctx, n))
+        return
+    diags = diags if isinstance(diags, (list, tuple)) else [diags]
+    for _ in range(n):
+        prob._c(prob._lib.gf_step(prob._ctx, 1))
+        for d in diags:
+            d.increment()
+
+
+def dealias(prob):
+    """dealias!(prob.sol, prob.grid) on the device state (updatevars! does it too)."""
+    prob._c(prob._lib.gf_updatevars(prob._ctx))
+
+
+def _check_dev(dev):
+    """The reference takes dev = CPU() | GPU(); this library runs on the GPU only."""
+    if str(dev).upper().rstrip("()") != "GPU":
+        raise ValueError("libgfcuda runs on the GPU only: pass dev='GPU'")

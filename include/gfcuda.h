@@ -1,0 +1,200 @@
+/* libgfcuda -- C ABI of the GB300 (sm_103a) pseudospectral time step.
+ *
+ * Drop-in boundary for the hot path of GeophysicalFlows.jl v0.16.5 / FourierFlows.jl 0.10.5:
+ * Problem construction, stepforward!, calcN!, updatevars!, set_*! and the Parseval-sum
+ * diagnostics of TwoDNavierStokes, SingleLayerQG, MultiLayerQG and SurfaceQG.  Every call
+ * returns GF_OK (0) or a negative gf_status; gf_last_error() gives the message.
+ *
+ * Array conventions (identical to the reference's Julia arrays, column-major):
+ *   spectral  (nkr, ny[, nlayers]) complex, nkr = nx/2 + 1, element (ik, j, L) at
+ *             ik + nkr*(j + ny*L);   physical (nx, ny[, nlayers]) real, (i, j, L) at
+ *             i + nx*(j + ny*L).
+ *   Element type: float/complex-float for GF_F32 contexts, double/complex-double otherwise.
+ *   `where` = GF_HOST (pageable or pinned host memory) or GF_DEVICE (device pointer on the
+ *   context's GPU, e.g. from a CuArray).
+ * One context = one problem on one stream; a context is not thread-safe, separate
+ * contexts are independent.  nx and ny must be powers of two in [32, 2048].
+ */
+#ifndef GFCUDA_H
+#define GFCUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GFCUDA_ABI_VERSION 1
+
+typedef struct gf_ctx gf_ctx;
+
+typedef enum {
+  GF_OK = 0,
+  GF_ERR_ARG = -1,          /* invalid argument / configuration */
+  GF_ERR_UNSUPPORTED = -2,  /* valid for the reference but not supported here (e.g. nx not 2^k) */
+  GF_ERR_CUDA = -3,         /* CUDA runtime error */
+  GF_ERR_NOMEM = -4,        /* device allocation failed */
+  GF_ERR_STATE = -5,        /* call not valid in the current state */
+  GF_ERR_NOT_IMPLEMENTED = -6 /* the reference raises for this case (e.g. finite deformation radius budgets) */
+} gf_status;
+
+typedef enum { GF_TWODNAVIERSTOKES = 0, GF_SINGLELAYERQG = 1, GF_MULTILAYERQG = 2, GF_SURFACEQG = 3 } gf_module;
+
+/* GF_F64: IEEE double throughout.  GF_F32: float bulk (FFTs, products, stage combination);
+ * FP64 stays in the setup (ETDRK4 coefficients, inversion factorisation) and in the
+ * diagnostics reductions. */
+typedef enum { GF_F32 = 0, GF_F64 = 1 } gf_precision;
+
+/* FourierFlows timestepper names (test/runtests.jl:58) */
+typedef enum {
+  GF_FORWARDEULER = 0, GF_FILTEREDFORWARDEULER = 1, GF_RK4 = 2, GF_FILTEREDRK4 = 3,
+  GF_ETDRK4 = 4, GF_FILTEREDETDRK4 = 5, GF_AB3 = 6, GF_FILTEREDAB3 = 7
+} gf_stepper;
+
+/* Forcing kinds: the device-side forms of the reference's calcF! callbacks.
+ *   STATIC:     F-hat fixed (set with gf_set_forcing; e.g. test/test_twodnavierstokes.jl:237-241)
+ *   HARMONIC:   F-hat * cos(omega t + phase), evaluated at every stage time
+ *               (test/test_twodnavierstokes.jl:136-141)
+ *   STOCHASTIC: randn(complex) * sqrt(spectrum / dt), drawn once per step at the first stage
+ *               with Philox4x32-10 (examples/singlelayerqg_betaforced.jl:86-90); `stochastic=true`
+ *               semantics (prevsol kept, Stratonovich budgets)
+ *   STOCHASTIC_PHASE: exp(2 pi i u) * sqrt(spectrum / dt), [0,0] = 0 (test/test_twodnavierstokes.jl:41-46) */
+typedef enum {
+  GF_FORCING_NONE = 0, GF_FORCING_STATIC = 1, GF_FORCING_HARMONIC = 2,
+  GF_FORCING_STOCHASTIC = 3, GF_FORCING_STOCHASTIC_PHASE = 4
+} gf_forcing_kind;
+
+typedef enum { GF_HOST = 0, GF_DEVICE = 1 } gf_where;
+
+/* Problem configuration: the keyword arguments of the four modules' Problem() constructors
+ * (src/twodnavierstokes.jl:71-89, src/singlelayerqg.jl:91-112, src/multilayerqg.jl:87-114,
+ * src/surfaceqg.jl:76-90).  Zero-initialise, then set what the module needs. */
+typedef struct gf_config {
+  int32_t module, precision, stepper;
+  int32_t nx, ny, nlayers;          /* nlayers: MultiLayerQG only (1..8); others use 1 */
+  double Lx, Ly, dt, aliased_fraction;
+  /* (hyper)viscosity: TwoDNavierStokes nu, nnu, mu, nmu; SingleLayerQG nu, nnu, mu (drag);
+   * MultiLayerQG nu, nnu, mu (bottom drag); SurfaceQG nu, nnu */
+  double nu, mu;
+  int32_t nnu, nmu;
+  /* SingleLayerQG / MultiLayerQG */
+  double beta;
+  double deformation_radius;        /* SingleLayerQG; <= 0 or inf = barotropic */
+  double U;                         /* SingleLayerQG constant U (used when U_y is NULL) */
+  const double* U_y;                /* SingleLayerQG U(y) [ny] or NULL; MultiLayerQG U [nlayers*ny]
+                                       (layer-major, U_y[L*ny + j]) or NULL for zero */
+  const double* eta;                /* topographic PV (nx, ny) physical, or NULL for flat */
+  double f0;                        /* MultiLayerQG */
+  const double* H;                  /* MultiLayerQG rest layer depths [nlayers] */
+  const double* b;                  /* MultiLayerQG layer buoyancies [nlayers] */
+  double topographic_pv_gradient[2];/* MultiLayerQG */
+  int32_t linear;                   /* MultiLayerQG linear=true */
+  double H_sqg;                     /* SurfaceQG layer depth; <= 0 or inf = infinite depth */
+  /* forcing */
+  int32_t forcing_kind;
+  uint64_t seed;
+  double forcing_omega, forcing_phase;
+  /* spectral filter of the Filtered* steppers (FourierFlows makefilter); 0 = defaults
+   * order=4, innerK=0.65, outerK=1 */
+  double filter_order, filter_innerK, filter_outerK;
+  /* ETDRK4 contour (FourierFlows getetdcoeffs); 0 = defaults ncirc=32, rcirc=1 */
+  int32_t etdrk4_ncirc;
+  double etdrk4_rcirc;
+} gf_config;
+
+/* Field selectors for gf_get_field / gf_set_physical */
+typedef enum {
+  GF_FIELD_Q = 0,     /* TwoDNavierStokes zeta / SingleLayerQG, MultiLayerQG q / SurfaceQG b */
+  GF_FIELD_PSI = 1,
+  GF_FIELD_U = 2,
+  GF_FIELD_V = 3
+} gf_field;
+
+/* Diagnostic selectors (gf_diagnostics).  Values are the reference functions' values. */
+typedef enum {
+  /* TwoDNavierStokes (src/twodnavierstokes.jl:374-535) */
+  GF_D_2DNS_ENERGY = 0, GF_D_2DNS_ENSTROPHY = 1, GF_D_2DNS_PALINSTROPHY = 2,
+  GF_D_2DNS_ENERGY_DISSIPATION_HYPERVISCOSITY = 3, GF_D_2DNS_ENERGY_DISSIPATION_HYPOVISCOSITY = 4,
+  GF_D_2DNS_ENSTROPHY_DISSIPATION_HYPERVISCOSITY = 5, GF_D_2DNS_ENSTROPHY_DISSIPATION_HYPOVISCOSITY = 6,
+  GF_D_2DNS_ENERGY_WORK = 7, GF_D_2DNS_ENSTROPHY_WORK = 8,
+  /* SingleLayerQG (src/singlelayerqg.jl:546-715) */
+  GF_D_SLQG_KINETIC_ENERGY = 0, GF_D_SLQG_POTENTIAL_ENERGY = 1, GF_D_SLQG_ENSTROPHY = 2,
+  GF_D_SLQG_ENERGY_DISSIPATION = 3, GF_D_SLQG_ENSTROPHY_DISSIPATION = 4, GF_D_SLQG_ENERGY_WORK = 5,
+  GF_D_SLQG_ENSTROPHY_WORK = 6, GF_D_SLQG_ENERGY_DRAG = 7, GF_D_SLQG_ENSTROPHY_DRAG = 8,
+  GF_D_SLQG_ENERGY = 9,
+  /* SurfaceQG (src/surfaceqg.jl:390-483) */
+  GF_D_SQG_KINETIC_ENERGY = 0, GF_D_SQG_BUOYANCY_VARIANCE = 1, GF_D_SQG_TOTAL_3D_ENERGY = 2,
+  GF_D_SQG_BUOYANCY_DISSIPATION = 3, GF_D_SQG_BUOYANCY_WORK = 4,
+  /* MultiLayerQG energies (src/multilayerqg.jl:918-951): KE_j = j, PE_{j+1/2} = nlayers + j */
+  GF_D_MLQG_KE0 = 0, GF_D_MLQG_PE0 = 8
+} gf_diag;
+
+/* ---- lifetime ------------------------------------------------------------------------- */
+/* Replaces Problem(dev; kw...) (e.g. src/twodnavierstokes.jl:71-100,
+ * src/multilayerqg.jl:87-135): grid, params, vars, equation (L) and timestepper state
+ * (ETDRK4 coefficients, filter) are built on the GPU.  `stream` is a cudaStream_t or NULL. */
+int gf_create(const gf_config* cfg, void* stream, gf_ctx** out);
+int gf_destroy(gf_ctx* ctx);
+/* Message of the last failed call on ctx (or of the last failed gf_create when ctx is NULL). */
+const char* gf_last_error(const gf_ctx* ctx);
+int gf_abi_version(void);
+/* Sizes: nkr, nl(=ny), nlayers, element size in bytes of a real value */
+int gf_get_dims(const gf_ctx* ctx, int32_t* nkr, int32_t* ny, int32_t* nlayers, int32_t* real_bytes);
+
+/* ---- state (prob.sol, prob.clock) ----------------------------------------------------- */
+int gf_set_state(gf_ctx* ctx, const void* sol, int where);
+int gf_get_state(gf_ctx* ctx, void* sol, int where);
+int gf_get_clock(const gf_ctx* ctx, double* t, int64_t* step);
+int gf_set_clock(gf_ctx* ctx, double t, int64_t step);
+
+/* set_zeta!/set_q!/set_b! (src/twodnavierstokes.jl:352-360, src/singlelayerqg.jl:525-534,
+ * src/surfaceqg.jl:356-364, src/multilayerqg.jl:842-870) with which = GF_FIELD_Q, and
+ * MultiLayerQG set_psi! (src/multilayerqg.jl:872-894) with which = GF_FIELD_PSI: forward
+ * transform of a physical field into sol (domain mean zeroed where the reference does),
+ * then updatevars!. */
+int gf_set_physical(gf_ctx* ctx, int which, const void* field, int where);
+
+/* ---- the hot path ----------------------------------------------------------------------- */
+/* stepforward!(prob, nsteps) (FourierFlows; calls calcN! 4x per ETDRK4/RK4 step). */
+int gf_step(gf_ctx* ctx, int64_t nsteps);
+/* stepforward!(prob, diags, nsteps): also records the diagnostics `which[0..nd)` after
+ * every step into out[step*nd + d] (host memory, nsteps*nd doubles). */
+int gf_step_diags(gf_ctx* ctx, int64_t nsteps, const int32_t* which, int32_t nd, double* out);
+/* One calcN!(N, sol, t, ...) evaluation (e.g. src/twodnavierstokes.jl:286-294) on
+ * caller arrays; like the reference it dealiases `sol` in place. */
+int gf_calcN(gf_ctx* ctx, void* N, void* sol, double t, int where);
+
+/* updatevars!(prob) (src/twodnavierstokes.jl:331-345 and siblings): dealias sol in place and
+ * compute the physical fields; gf_get_field copies one of them out. */
+int gf_updatevars(gf_ctx* ctx);
+int gf_get_field(gf_ctx* ctx, int which, void* out, int where);
+
+/* MultiLayerQG fwdtransform!/invtransform! (src/multilayerqg.jl:483-493) and the plain
+ * rfft/irfft of FourierFlows' rfftplan, applied to nlayers fields at once. */
+int gf_fwdtransform(gf_ctx* ctx, void* fieldh, const void* field, int where);
+int gf_invtransform(gf_ctx* ctx, void* field, const void* fieldh, int where);
+
+/* Parseval-sum diagnostics (reductions in FP64 with compensated sums on the GPU). */
+int gf_diagnostics(gf_ctx* ctx, const int32_t* which, int32_t nd, double* out);
+
+/* F-hat for GF_FORCING_STATIC / HARMONIC (same layout as sol), or the forcing spectrum
+ * (real, (nkr, ny), the reference's `forcing_spectrum`) for the stochastic kinds.  This is
+ * also the per-step escape hatch for an arbitrary Julia calcF!: call it before each step. */
+int gf_set_forcing(gf_ctx* ctx, const void* data, int where);
+
+/* Block until the context's stream has finished. */
+int gf_synchronize(gf_ctx* ctx);
+
+/* Kernel timing for benchmarks: while enabled, CUDA events are recorded on the context's
+ * stream around every row-pass and column-pass kernel launch.  gf_profile_read waits for the
+ * stream, returns the summed milliseconds ms[0] (row pass) and ms[1] (column pass), the
+ * launch counts n[0], n[1], and the number of kernels libgfcuda launched since the last
+ * read, then resets the counters.  No counterpart in the reference (which has no timing). */
+int gf_profile_enable(gf_ctx* ctx, int on);
+int gf_profile_read(gf_ctx* ctx, double* ms, int64_t* n, int64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GFCUDA_H */
