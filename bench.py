@@ -1,0 +1,357 @@
+"""Benchmark of the pseudospectral time step on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Headline workload: TwoDNavierStokes 2048^2, FilteredRK4, nu = 0, peaked isotropic initial
+vorticity (k0 = 6, E = 0.5) -- the configuration the task's FP32-fused vs FP64-plain target is
+quoted on.  A "step" is one FilteredRK4 time step (4 calcN! stages).  `value` is FP32-fused
+grid-point*steps/s with the state resident in HBM; the FP64-plain arm, its roofline and the
+FP32-vs-FP64 error are reported beside it, and so is configs[1] (SingleLayerQG 512^2 ETDRK4
+with stochastic forcing, FP32 vs FP64).  L2 is flushed (256 MiB write) between timed steps.
+`--impl reference` times the FP64 CPU restatement of the reference (oracle/, scipy.fft on all
+host cores) on the same workload.  For N > 1 (torchrun) every rank runs an independent
+replica (the path does not shard) and rank 0 reports the aggregate.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "geophysicalflows.jl_gb300"), os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "grid-pt·steps/s FP32-fused vs FP64-plain (≤1e-5 rel L2); adjoint/forward step time"
+UNIT = "grid-pt*steps/s"
+HEADLINE = dict(module="TwoDNavierStokes", nx=2048, ny=2048, stepper="FilteredRK4", dt=5e-4)
+CONFIG1 = dict(module="SingleLayerQG", nx=512, ny=512, stepper="ETDRK4", dt=0.05, beta=10.0, mu=0.01)
+
+
+def algorithmic_words(module, stepper, nlayers=1, eta=False):
+    """Words per grid point per step of the two-sweep model: per calcN! stage read the stage
+    input (1), write k column-pass intermediates, read them in the row pass (k), write m
+    products, read them in the column pass (m), write N (1), read a physical parameter arrays;
+    plus C stage-combination sweeps per step (RK4 16, ETDRK4 23).  Returns (per step, row
+    kernel per launch, column kernel per launch)."""
+    k, m, a = 3, 2, 0
+    if module == "MultiLayerQG":
+        m = 3
+    if module == "SingleLayerQG" and eta:
+        a = 1
+    C = 23 if "ETDRK4" in stepper else 16
+    row = k + m + a
+    col = 2 + k + m + C / 4
+    return 4 * (row + col), row, col
+
+
+def is_rank0():
+    return int(os.environ.get("RANK", "0")) == 0
+
+
+def dist_setup(n):
+    if n <= 1 and int(os.environ.get("WORLD_SIZE", "1")) <= 1:
+        return None
+    import torch
+    import torch.distributed as dist
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return dist
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __enter__(self):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            self.p.wait()
+        self.f.flush()
+
+    def summary(self, dev=0):
+        rows = []
+        try:
+            for line in open(self.f.name):
+                parts = [s.strip() for s in line.split(",")]
+                if len(parts) >= 9 and parts[0] == str(dev):
+                    rows.append(parts)
+        finally:
+            os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": float(rows[0][2]) if rows[0][2].replace(".", "").isdigit() else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0}, "fallback"
+
+
+def ncu_traffic(kernel, workload):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary of `workload`
+    (profiles/<kernel>_<workload>.md, line 'traffic_bytes_per_launch: B'), else None."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def make_problem(w, T):
+    import gfcuda
+    if w["module"] == "TwoDNavierStokes":
+        return gfcuda.TwoDNavierStokes.Problem("GPU", nx=w["nx"], ny=w["ny"], dt=w["dt"], stepper=w["stepper"], T=T)
+    import gf_oracle as O
+    g = O.Grid(w["nx"])
+    spec = O.ring_forcing_spectrum(g, 14.0 * 2 * np.pi / g.Lx, 1.5 * 2 * np.pi / g.Lx, 1e-3)
+    f = gfcuda.Forcing("stochastic", spectrum=spec, seed=1234)
+    return gfcuda.SingleLayerQG.Problem("GPU", nx=w["nx"], beta=w["beta"], mu=w["mu"], dt=w["dt"],
+                                        stepper=w["stepper"], forcing=f, T=T)
+
+
+def initial_state(w):
+    import gf_oracle as O
+    if w["module"] == "TwoDNavierStokes":
+        g = O.Grid(w["nx"])
+        return O.peakedisotropicspectrum(g, 6, 0.5, mask=O.makefilter(g), seed=1234)
+    return np.zeros((w["ny"], w["nx"]))
+
+
+def time_arm(w, T, steps, warmup, flush, with_e2e):
+    """Run one precision arm: warm-up, K timed steps (CUDA events on the library's stream,
+    L2 flushed between steps), kernel timing, optional end-to-end timing."""
+    import torch
+    import gfcuda
+    prob = make_problem(w, T)
+    z0 = initial_state(w)
+    if w["module"] == "TwoDNavierStokes":
+        gfcuda.TwoDNavierStokes.set_zeta(prob, z0)
+    else:
+        gfcuda.SingleLayerQG.set_q(prob, z0)
+    gfcuda.stepforward(prob, warmup)
+    prob.synchronize()
+    lib, ctx = prob._lib, prob._ctx
+    import ctypes as C
+    ms2 = (C.c_double * 2)()
+    n2 = (C.c_int64 * 2)()
+    nl = C.c_int64()
+    lib.gf_profile_read(ctx, ms2, n2, C.byref(nl))  # reset counters
+    lib.gf_profile_enable(ctx, 1)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for i in range(steps):
+        flush.zero_()
+        ev[i][0].record()
+        prob._c(lib.gf_step(ctx, 1))
+        ev[i][1].record()
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    prob._c(lib.gf_profile_read(ctx, ms2, n2, C.byref(nl)))
+    lib.gf_profile_enable(ctx, 0)
+    res = {"ms_per_step": sum(ms) / steps, "ms_row": ms2[0] / max(n2[0], 1), "ms_col": ms2[1] / max(n2[1], 1),
+           "n_row": n2[0], "n_col": n2[1], "launches": nl.value}
+    if with_e2e:
+        shape = prob.spec_shape
+        hin = torch.empty(int(np.prod(shape)) * 2, dtype=torch.float32 if T == np.float32 else torch.float64,
+                          pin_memory=True)
+        hout = torch.empty_like(hin, pin_memory=True)
+        hin_np, hout_np = hin.numpy(), hout.numpy()
+        prob._c(lib.gf_get_state(ctx, hin_np.ctypes.data, 0))
+        tot = 0.0
+        for i in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            prob._c(lib.gf_set_state(ctx, hin_np.ctypes.data, 0))
+            prob._c(lib.gf_step(ctx, 1))
+            prob._c(lib.gf_get_state(ctx, hout_np.ctypes.data, 0))
+            tot += time.perf_counter() - t0
+            hin_np[:] = hout_np
+        res["e2e_s_per_step"] = tot / steps
+        res["state_bytes"] = hin.numel() * hin.element_size()
+    res["sol"] = prob.sol
+    prob.close()
+    return res
+
+
+def cpu_baseline(w, seconds=20.0, max_steps=5):
+    """The FP64 restatement (oracle) stepping the same workload on the host cores."""
+    import gf_oracle as O
+    cores = os.cpu_count() or 1
+    O.set_fft_workers(cores)
+    try:
+        if w["module"] == "TwoDNavierStokes":
+            r = O.TwoDNavierStokes(nx=w["nx"], dt=w["dt"], stepper=w["stepper"])
+            r.set_zeta(initial_state(w))
+        else:
+            g = O.Grid(w["nx"])
+            spec = O.ring_forcing_spectrum(g, 14.0, 1.5, 1e-3)
+            r = O.SingleLayerQG(nx=w["nx"], beta=w["beta"], mu=w["mu"], dt=w["dt"], stepper=w["stepper"],
+                                forcing=O.Forcing("stochastic", spectrum=spec, seed=1234))
+        r.stepforward(1)
+        n, t0 = 0, time.perf_counter()
+        while n < max_steps and time.perf_counter() - t0 < seconds:
+            r.stepforward(1)
+            n += 1
+        dt = time.perf_counter() - t0
+    finally:
+        O.set_fft_workers(None)
+    return {"value": w["nx"] * w["ny"] * n / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{n} {w['stepper']} steps of {w['module']} {w['nx']}x{w['ny']} FP64 (numpy/scipy.fft "
+                      f"restatement, {cores} FFT threads), {dt:.1f} s"}
+
+
+def run_reference(args):
+    if not is_rank0():
+        return 0
+    w = HEADLINE
+    import gf_oracle as O
+    cores = os.cpu_count() or 1
+    O.set_fft_workers(cores)
+    r = O.TwoDNavierStokes(nx=w["nx"], dt=w["dt"], stepper=w["stepper"])
+    r.set_zeta(initial_state(w))
+    r.stepforward(args.warmup)
+    t0 = time.perf_counter()
+    r.stepforward(args.steps)
+    dt = time.perf_counter() - t0
+    v = w["nx"] * w["ny"] * args.steps / dt
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "TwoDNavierStokes 2048^2 FilteredRK4 dt=5e-4 nu=0, peaked isotropic IC",
+                       "nx": w["nx"], "ny": w["ny"], "stepper": w["stepper"]},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{args.steps} steps after {args.warmup} warm-up, FP64 restatement of the "
+                                       f"reference (numpy/scipy.fft, {cores} threads)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    dist = dist_setup(args.gpus)
+    world = dist.get_world_size() if dist else 1
+    if not torch.cuda.is_available():
+        raise RuntimeError("bench.py needs a GPU")
+    import gfcuda
+    gfcuda.load()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
+    peaks, peak_src = measured_peaks()
+    w = HEADLINE
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with Clocks() as clk:
+        r32 = time_arm(w, np.float32, args.steps, args.warmup, flush, with_e2e=True)
+    r64 = time_arm(w, np.float64, args.steps, args.warmup, flush, with_e2e=True)
+    c32 = time_arm(CONFIG1, np.float32, args.steps, args.warmup, flush, with_e2e=False)
+    c64 = time_arm(CONFIG1, np.float64, args.steps, args.warmup, flush, with_e2e=False)
+    ms = r32["ms_per_step"]
+    if dist:
+        t = torch.tensor([ms, r64["ms_per_step"], r32["e2e_s_per_step"]], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms, ms64, e2e_s = t.tolist()
+    else:
+        ms64, e2e_s = r64["ms_per_step"], r32["e2e_s_per_step"]
+    if not is_rank0():
+        return 0
+    pts = w["nx"] * w["ny"]
+    value = world * pts / (ms * 1e-3)
+    v64 = world * pts / (ms64 * 1e-3)
+
+    def roofline(res, wbytes):
+        words, row_w, col_w = algorithmic_words(w["module"], w["stepper"])
+        dom = "col_stage" if res["ms_col"] >= res["ms_row"] else "row_nl"
+        per_launch = (col_w if dom == "col_stage" else row_w) * wbytes * pts
+        t = res["ms_col"] if dom == "col_stage" else res["ms_row"]
+        ach = per_launch / (t * 1e-3) / 1e9
+        tag = "fp32" if wbytes == 4 else "fp64"
+        return {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": ach / peaks["hbm_gbs"], "peak_source": peak_src,
+                "traffic": ncu_traffic(dom, f"twodns2048_{tag}"), "algorithmic_bytes_per_launch": per_launch,
+                "launch_ms": t, "row_ms": res["ms_row"], "col_ms": res["ms_col"],
+                "step_words_per_pt": words}
+
+    err = float(np.linalg.norm(r32["sol"] - r64["sol"]) / np.linalg.norm(r64["sol"]))
+    cerr = float(np.linalg.norm(c32["sol"] - c64["sol"]) / np.linalg.norm(c64["sol"]))
+    cpu = cpu_baseline(w)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "TwoDNavierStokes 2048^2 FilteredRK4 dt=5e-4 nu=0, peaked isotropic IC (k0=6, E=0.5)",
+                   "nx": w["nx"], "ny": w["ny"], "stepper": w["stepper"], "precision": "FP32 bulk",
+                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}"},
+        "roofline": roofline(r32, 4),
+        "cpu_baseline": cpu,
+        "e2e": {"value": world * pts / e2e_s, "unit": UNIT, "h2d_bytes_per_step": r32["state_bytes"],
+                "d2h_bytes_per_step": r32["state_bytes"]},
+        "gpu_launches": r32["launches"],
+        "clocks": clk.summary(int(os.environ.get("LOCAL_RANK", "0"))),
+        "fp64_plain": {"value": v64, "ms_per_step": ms64, "roofline": roofline(r64, 8),
+                       "e2e": {"value": world * pts / r64["e2e_s_per_step"], "unit": UNIT}},
+        "fp32_over_fp64": value / v64,
+        "fp32_vs_fp64_rel_l2": err,
+        "fp32_vs_fp64_steps": args.warmup + args.steps,
+        "configs1": {"workload": "SingleLayerQG 512^2 beta=10 mu=0.01 ETDRK4 dt=0.05, stochastic ring forcing "
+                                 "kf=14 eps=1e-3, q0=0 (L2-resident: latency, no HBM fraction)",
+                     "fp32": CONFIG1["nx"] * CONFIG1["ny"] / (c32["ms_per_step"] * 1e-3),
+                     "fp64": CONFIG1["nx"] * CONFIG1["ny"] / (c64["ms_per_step"] * 1e-3),
+                     "ms_per_step_fp32": c32["ms_per_step"], "ms_per_step_fp64": c64["ms_per_step"],
+                     "fp32_vs_fp64_rel_l2": cerr},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -148,13 +148,29 @@ class Grid:
         return m
 
 
+_FFT_WORKERS = None  # None: numpy.fft (single thread); n: scipy.fft with n worker threads
+
+
+def set_fft_workers(n):
+    """Use scipy.fft with n threads (the CPU-baseline timing uses all host cores, like the
+    reference's FFTW.set_num_threads, README.md:79-86); None restores numpy.fft."""
+    global _FFT_WORKERS
+    _FFT_WORKERS = n
+
+
 def rfft2(f):
     """Unnormalised r2c along x then c2c along y (FFTW `mul!(fh, rfftplan, f)`)."""
+    if _FFT_WORKERS:
+        import scipy.fft as sf
+        return sf.rfft2(f, axes=(-2, -1), workers=_FFT_WORKERS)
     return np.fft.rfft2(f, axes=(-2, -1))
 
 
 def irfft2(fh, grid):
     """Normalised c2r (FFTW `ldiv!(f, rfftplan, fh)`), y-pass first, then x c2r."""
+    if _FFT_WORKERS:
+        import scipy.fft as sf
+        return sf.irfft2(fh, s=(grid.ny, grid.nx), axes=(-2, -1), workers=_FFT_WORKERS)
     return np.fft.irfft2(fh, s=(grid.ny, grid.nx), axes=(-2, -1))
 
 
