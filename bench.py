@@ -339,13 +339,35 @@ def run_ours(args):
     return 0
 
 
+SINGLE = {"twodns2048_fp32": (HEADLINE, np.float32), "twodns2048_fp64": (HEADLINE, np.float64),
+          "slqg512_fp32": (CONFIG1, np.float32), "slqg512_fp64": (CONFIG1, np.float64)}
+
+
+def run_single(args):
+    """One arm only (for profiler captures and quick checks); not the benchmark line."""
+    import torch
+    import gfcuda
+    gfcuda.load()
+    w, T = SINGLE[args.single]
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    r = time_arm(w, T, args.steps, args.warmup, flush, with_e2e=False)
+    r.pop("sol")
+    r["workload"] = args.single
+    r["pt_steps_per_s"] = w["nx"] * w["ny"] / (r["ms_per_step"] * 1e-3)
+    print(json.dumps(r), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--single", choices=sorted(SINGLE), help="time one arm only (profiling mode)")
     args = ap.parse_args()
+    if args.single:
+        return run_single(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
