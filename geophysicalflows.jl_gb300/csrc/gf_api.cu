@@ -16,6 +16,8 @@ using namespace gf;
 
 static std::string g_create_error;
 
+void gf::set_global_error(const std::string& msg) { g_create_error = msg; }
+
 struct gf_ctx {
   gf_config cfg;
   int prec = GF_F32;

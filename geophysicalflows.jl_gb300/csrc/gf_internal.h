@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 namespace gf {
 
 template <class T> struct cplx;
@@ -85,6 +87,9 @@ template <class T> cudaError_t launch_diag(const Geom&, const ModArgs&, const vo
 template <class T> cudaError_t launch_mask_inplace(const Geom&, void* sol, cudaStream_t);
 template <class T> cudaError_t launch_spec_apply(const Geom&, const ModArgs&, const void* in, void* out, int op,
                                                  cudaStream_t);
+
+// message returned by gf_last_error(NULL)
+void set_global_error(const std::string& msg);
 
 constexpr int DIAG_BLOCK = 256;
 constexpr int NDIAG = 24;  // number of reduction slots

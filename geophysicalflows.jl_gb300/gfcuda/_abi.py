@@ -18,7 +18,8 @@ FIELD_Q, FIELD_PSI, FIELD_U, FIELD_V = 0, 1, 2, 3
 EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_abi_version", "gf_get_dims", "gf_set_state",
            "gf_get_state", "gf_get_clock", "gf_set_clock", "gf_set_physical", "gf_step", "gf_step_diags",
            "gf_calcN", "gf_updatevars", "gf_get_field", "gf_fwdtransform", "gf_invtransform",
-           "gf_diagnostics", "gf_set_forcing", "gf_synchronize", "gf_profile_enable", "gf_profile_read"]
+           "gf_diagnostics", "gf_set_forcing", "gf_synchronize", "gf_profile_enable", "gf_profile_read",
+           "gf_rfft2_noalloc"]
 
 
 class gf_config(C.Structure):
@@ -73,6 +74,7 @@ def load(path=LIBPATH):
         "gf_synchronize": ([vp], C.c_int),
         "gf_profile_enable": ([vp, C.c_int], C.c_int),
         "gf_profile_read": ([vp, C.POINTER(dbl), C.POINTER(i64), C.POINTER(i64)], C.c_int),
+        "gf_rfft2_noalloc": ([vp, vp, i32, i32, i32, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

@@ -14,7 +14,7 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(HERE, "libgfcuda.so")
-UNITS = ["gf_f64_col.cu", "gf_f32_col.cu", "gf_f64_row.cu", "gf_f32_row.cu", "gf_api.cu"]
+UNITS = ["gf_f64_col.cu", "gf_f32_col.cu", "gf_f64_row.cu", "gf_f32_row.cu", "gf_api.cu", "gf_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++20", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", f"-I{INCLUDE}", f"-I{CSRC}"]
 

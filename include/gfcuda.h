@@ -194,6 +194,23 @@ int gf_synchronize(gf_ctx* ctx);
 int gf_profile_enable(gf_ctx* ctx, int on);
 int gf_profile_read(gf_ctx* ctx, double* ms, int64_t* n, int64_t* launches);
 
+/* ---- allocation-free forward transform ------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device memory (code
+ * running inside another runtime that owns the GPU's memory, such as a Julia session whose
+ * CUDA.jl pool holds the device and enforces a memory limit, or a latency-critical loop
+ * where cudaMalloc/cudaFree and their device synchronisation are not acceptable).
+ * Computes the unnormalised 2-D r2c transform of the device field (nx, ny) into the device
+ * spectrum (nx/2+1, ny) (the same result as gf_fwdtransform) without allocating: its
+ * intermediate rows and twiddle tables live in fixed __device__ arrays that every GPU
+ * loading the library keeps until exit (about 2.2 MB of scratch plus 96 KB of tables).
+ * nx, ny: powers of two in [32, GF_NOALLOC_MAX_N]; larger sizes return GF_ERR_UNSUPPORTED.
+ * precision: GF_F32 (float in, complex-float out) or GF_F64.  stream: cudaStream_t or NULL.
+ * The first call on a device sets that device up (it must be current); make it before any
+ * stream capture.  All calls share the scratch: calls that overlap on the GPU race.
+ * Errors: gf_last_error(NULL). */
+#define GF_NOALLOC_MAX_N 512
+int gf_rfft2_noalloc(const void* field, void* fieldh, int32_t nx, int32_t ny, int32_t precision, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
