@@ -311,6 +311,7 @@ static int build(gf_ctx* c, const gf_config* cfg) {
   g.ldw = (g.kcut + 15) / 16 * 16;
   g.dkx = 2 * M_PI / k.Lx; g.dky = 2 * M_PI / k.Ly;
   g.inv_nxny = 1.0 / ((double)k.nx * k.ny);
+  g.dkx_f = (float)g.dkx; g.dky_f = (float)g.dky; g.inv_nxny_f = (float)g.inv_nxny;
   c->prec = k.precision;
   c->rb = k.precision == GF_F64 ? 8 : 4;
   c->cb = 2 * c->rb;
@@ -564,6 +565,11 @@ static int build(gf_ctx* c, const gf_config* cfg) {
     if (int r = upload_real(c, c->Qy1D, Qy.data(), g.ny)) return r;
     m.U1D = c->U1D; m.Qy1D = c->Qy1D; m.hasC = 1;
   }
+  // float mirrors of the per-element scalars
+  m.Ueta = (m.etah != nullptr && m.U0 != 0.0);
+  m.ell_inv2_f = (float)m.ell_inv2; m.U0_f = (float)m.U0; m.mu_f = (float)m.mu;
+  for (int a = 0; a < MAXL; ++a) m.lam_f[a] = (float)m.lam[a];
+  for (int a = 0; a < MAXL * MAXL; ++a) { m.V_f[a] = (float)m.V[a]; m.Vinv_f[a] = (float)m.Vinv[a]; }
   // ----- forcing buffers
   if (k.forcing_kind != GF_FORCING_NONE) {
     if (!(c->Fh = dalloc(c, nsp * cb))) return fail(c, GF_ERR_NOMEM, "forcing");
@@ -781,6 +787,7 @@ static StepArgs stage_args(gf_ctx* c, int stage, double tstage) {
   s.draw = (stage == 1);
   if (s.fkind == FK_HARMONIC) s.fscale = std::cos(c->cfg.forcing_omega * tstage + c->cfg.forcing_phase);
   else s.fscale = 1.0;
+  s.dt_f = (float)s.dt; s.fscale_f = (float)s.fscale;
   return s;
 }
 
@@ -891,6 +898,7 @@ extern "C" int gf_calcN(gf_ctx* c, void* N, void* sol, double t, int where) {
   // products, forward FFTs, N = -i kr A - i l B - C + extras + forcing, written to tmp_spec2
   s = stage_args(c, 1, t);
   s.kind = SK_NOUT; s.sol = c->tmp_spec; s.acc = c->tmp_spec2; s.do_fwd = 1; s.do_inv = 0;
+  s.dt_f = (float)s.dt; s.fscale_f = (float)s.fscale;
   s.draw = (t == c->t);  // stochastic forcing is redrawn only when t == clock.t
   if (s.fkind >= FK_STOCH && !s.draw) s.Fh = c->Fstore;
   if (int r = launch_stage(c, s, 1)) return r;

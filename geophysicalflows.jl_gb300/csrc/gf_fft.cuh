@@ -18,6 +18,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <utility>
+
 namespace gf {
 
 constexpr int TWN = 4096;  // twiddle table length (largest supported transform)
@@ -97,17 +99,41 @@ __device__ __forceinline__ void dft(cplx<T>* v) {
   }
 }
 
+// Asynchronous global -> shared copies (cp.async, sm_80+): 8- or 16-byte elements.
+template <class T>
+__device__ __forceinline__ void cp_async_elem(cplx<T>* smem, const cplx<T>* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  if constexpr (sizeof(cplx<T>) == 16) asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+  else asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
 template <int DIR, class T>
 __device__ __forceinline__ cplx<T> twiddle(const cplx<T>* __restrict__ tw, int idx) {
   cplx<T> w = tw[idx];
   return DIR < 0 ? w : conj(w);
 }
 
-// One radix pass of a length-N Stockham FFT on a column of shared memory whose
-// consecutive elements are S apart.  Threads t in [0, N/R) each do R/Rp butterflies of
-// radix Rp = min(R, N/Ns).  The caller must have synchronised before the first pass.
+// Shared-memory slot of logical element a of an FFT buffer: an XOR swizzle inside each
+// aligned block of 16 (8-byte elements) or 8 (16-byte elements) slots.  With it, every
+// access pattern of the radix-8 Stockham passes -- consecutive reads, the stride-8 writes
+// of the first pass, the (j/8)*64 + j%8 writes of the second -- hits distinct banks
+// within a 128-byte shared-memory wavefront, without padding.
+template <class T>
+__device__ __forceinline__ int swz(int a) {
+  if constexpr (sizeof(cplx<T>) == 8) return a ^ (((a >> 4) & 7) | ((a >> 3) & 8));
+  else return a ^ ((a >> 3) & 7);
+}
+// Threads per 128-byte shared-memory wavefront for T's complex element.
+template <class T> constexpr int wave_threads() { return 128 / (int)sizeof(cplx<T>); }
+
+// One radix pass of a length-N Stockham FFT on a swizzled shared-memory buffer.  Threads t in
+// [0, N/R) each do R/Rp butterflies of radix Rp = min(R, N/Ns).  The caller must have
+// synchronised before the first pass.
 template <class T, int N, int R, int DIR, int Ns>
-__device__ __forceinline__ void fft_passes(cplx<T>* buf, int S, int t, const cplx<T>* __restrict__ tw) {
+__device__ __forceinline__ void fft_passes(cplx<T>* buf, int t, const cplx<T>* __restrict__ tw) {
   if constexpr (Ns < N) {
     constexpr int Rp = (N / Ns < R) ? (N / Ns) : R;
     constexpr int NB = R / Rp;
@@ -118,11 +144,23 @@ __device__ __forceinline__ void fft_passes(cplx<T>* buf, int S, int t, const cpl
     for (int b = 0; b < NB; ++b) {
       const int j = t + b * TPF;
 #pragma unroll
-      for (int r = 0; r < Rp; ++r) v[b][r] = buf[(j + r * (N / Rp)) * S];
+      for (int r = 0; r < Rp; ++r) v[b][r] = buf[swz<T>(j + r * (N / Rp))];
       if constexpr (Ns > 1) {
         const int k = j & (Ns - 1);
+        if constexpr (sizeof(T) == 4) {
+          // FP32: one table load, the other powers by complex multiplication
+          // (w^r error ~ r ulp, far below the FP32 path's tolerance); fewer L1 requests
+          const cplx<T> w1 = twiddle<DIR>(tw, k * TWS);
+          cplx<T> wr = w1;
 #pragma unroll
-        for (int r = 1; r < Rp; ++r) v[b][r] = v[b][r] * twiddle<DIR>(tw, r * k * TWS);
+          for (int r = 1; r < Rp; ++r) {
+            v[b][r] = v[b][r] * wr;
+            if (r + 1 < Rp) wr = wr * w1;
+          }
+        } else {
+#pragma unroll
+          for (int r = 1; r < Rp; ++r) v[b][r] = v[b][r] * twiddle<DIR>(tw, r * k * TWS);
+        }
       }
       dft<Rp, DIR>(v[b]);
     }
@@ -132,19 +170,19 @@ __device__ __forceinline__ void fft_passes(cplx<T>* buf, int S, int t, const cpl
       const int j = t + b * TPF;
       const int idxD = (j / Ns) * Ns * Rp + (j & (Ns - 1));
 #pragma unroll
-      for (int r = 0; r < Rp; ++r) buf[(idxD + r * Ns) * S] = v[b][r];
+      for (int r = 0; r < Rp; ++r) buf[swz<T>(idxD + r * Ns)] = v[b][r];
     }
     __syncthreads();
-    fft_passes<T, N, R, DIR, Ns * Rp>(buf, S, t, tw);
+    fft_passes<T, N, R, DIR, Ns * Rp>(buf, t, tw);
   }
 }
 
-// In-place length-N FFT (DIR = -1 forward, unnormalised; +1 inverse, unnormalised) of the
-// column buf[0], buf[S], ..., buf[(N-1) S] by threads t in [0, N/R).  All threads of the
-// block must call it (it synchronises the block); threads with t >= N/R must not exist.
+// In-place length-N FFT (DIR = -1 forward, +1 inverse; both unnormalised) of the swizzled
+// buffer buf (logical element a at buf[swz<T>(a)]) by threads t in [0, N/R).  Every thread
+// of the block must call it (it synchronises the block).
 template <class T, int N, int R, int DIR>
-__device__ __forceinline__ void fft_smem(cplx<T>* buf, int S, int t, const cplx<T>* __restrict__ tw) {
-  fft_passes<T, N, R, DIR, 1>(buf, S, t, tw);
+__device__ __forceinline__ void fft_smem(cplx<T>* buf, int t, const cplx<T>* __restrict__ tw) {
+  fft_passes<T, N, R, DIR, 1>(buf, t, tw);
 }
 
 }  // namespace gf

@@ -23,6 +23,8 @@ struct Geom {
   int kcut;    // kr indices >= kcut are aliased
   int lA, lB;  // l indices in [lA, lB] are aliased (empty when lA > lB)
   double dkx, dky, inv_nxny;
+  float dkx_f, dky_f, inv_nxny_f;  // float copies (the FP32 kernels never touch FP64)
+  int cs;                          // column stride (elements) of the column kernels' buffers
 };
 
 // How psi-hat follows from the layer PV/vorticity/buoyancy X, and what the physical-space
@@ -47,6 +49,9 @@ struct ModArgs {
   // dissipation parameters used by the diagnostics (nu, nnu; mu_visc, nmu)
   double nu, mu_visc; int nnu, nmu;
   void* D;               // complex [j][kr] buffer carrying mu K^2 psi_last between kernels
+  int Ueta;              // U0 != 0 and etah present
+  float ell_inv2_f, U0_f, mu_f;
+  float lam_f[MAXL], V_f[MAXL * MAXL], Vinv_f[MAXL * MAXL];
 };
 
 struct StepArgs {
@@ -62,7 +67,13 @@ struct StepArgs {
   void* Fstore;        // stochastic draw written at the first stage
   void* prevsol;       // sol at the first stage (stochastic budgets)
   uint64_t seed, step;
+  float dt_f, fscale_f;
 };
+
+// value of a host-prepared scalar in the arithmetic type T
+template <class T> __host__ __device__ __forceinline__ T sel(double d, float f);
+template <> __host__ __device__ __forceinline__ double sel<double>(double d, float) { return d; }
+template <> __host__ __device__ __forceinline__ float sel<float>(double, float f) { return f; }
 
 struct Bufs {
   const void* twid;  // TWN twiddles

@@ -13,17 +13,24 @@
 //
 // So every stage costs one HBM sweep of the products and one of the pruned inverse fields,
 // instead of the reference's 5-7 FFT library calls plus ~8 broadcast sweeps per calcN!.
+// Per-element wavenumber arithmetic runs in the storage type T (FP64 only in the FP64 path).
 #pragma once
 #include <utility>
 
 #include "gf_fft.cuh"
 #include "gf_internal.h"
 
+// Minimum resident blocks per SM requested for the FP32 step kernels (register budget).
+#ifndef GF_MINBLOCKS_F32
+#define GF_MINBLOCKS_F32 2
+#endif
+
 namespace gf {
 
 // ------------------------------------------------------------------------------ helpers
 __device__ __forceinline__ bool kept(const Geom& g, int kr, int j) { return kr < g.kcut && (j < g.lA || j > g.lB); }
-__device__ __forceinline__ double lval(const Geom& g, int j) { return (j < g.ny / 2 ? j : j - g.ny) * g.dky; }
+// signed wavenumber index of row j (fftfreq order)
+__device__ __forceinline__ int lidx(const Geom& g, int j) { return j < g.ny / 2 ? j : j - g.ny; }
 
 template <class T>
 __device__ __forceinline__ cplx<T> ldc(const void* p, size_t i, int is_cplx) {
@@ -71,92 +78,144 @@ __device__ __forceinline__ cplx<T> draw(uint64_t e, uint64_t step, uint64_t seed
   return mk<T>(r * co, r * s);
 }
 
-// psi-hat of one layer from the layer values X[0..nl) at one wavenumber (K2 = |k|^2).
+// The per-layer psi factor f of single-layer modules (psi = f X) at |k|^2 = K2.
 template <class T>
-__device__ __forceinline__ void psi_all(const ModArgs& m, int nl, double K2, const cplx<T>* X, cplx<T>* psi,
-                                        size_t tidx) {
-  if (m.psi_kind == PSI_EIGEN) {
-    if (K2 == 0.0) {
-      for (int a = 0; a < nl; ++a) psi[a] = czero<T>();
-      return;
-    }
-    cplx<T> y[MAXL];
-    for (int a = 0; a < nl; ++a) {
-      cplx<T> s = czero<T>();
-      for (int b = 0; b < nl; ++b) s = s + T(m.Vinv[a * MAXL + b]) * X[b];
-      y[a] = T(1.0 / (m.lam[a] - K2)) * s;
-    }
-    for (int a = 0; a < nl; ++a) {
-      cplx<T> s = czero<T>();
-      for (int b = 0; b < nl; ++b) s = s + T(m.V[a * MAXL + b]) * y[b];
-      psi[a] = s;
-    }
+__device__ __forceinline__ T psi_factor(int kind, T K2, T ell2, const void* mult, size_t ti) {
+  if (kind == PSI_INVK2) return K2 == T(0) ? T(0) : T(-1) / K2;
+  if (kind == PSI_HELMHOLTZ) return T(-1) / (K2 + ell2);
+  return -static_cast<const T*>(mult)[ti];
+}
+
+// MultiLayerQG: psi = V diag(1/(lam - K^2)) Vinv X (zero at K = 0); e = [lam | V | Vinv].
+template <class T>
+__device__ __forceinline__ void psi_eigen(int nl, const T* e, T K2, const cplx<T>* X, cplx<T>* psi) {
+  if (K2 == T(0)) {
+    for (int a = 0; a < nl; ++a) psi[a] = czero<T>();
     return;
   }
-  T f;
-  if (m.psi_kind == PSI_INVK2) f = K2 == 0.0 ? T(0) : T(-1.0 / K2);
-  else if (m.psi_kind == PSI_HELMHOLTZ) f = T(-1.0 / (K2 + m.ell_inv2));
-  else f = -static_cast<const T*>(m.mult)[tidx];
+  const T* V = e + MAXL;
+  const T* Vi = e + MAXL + MAXL * MAXL;
+  cplx<T> y[MAXL];
+  for (int a = 0; a < nl; ++a) {
+    cplx<T> s = czero<T>();
+    for (int q = 0; q < nl; ++q) s = s + Vi[a * MAXL + q] * X[q];
+    y[a] = (T(1) / (e[a] - K2)) * s;
+  }
+  for (int a = 0; a < nl; ++a) {
+    cplx<T> s = czero<T>();
+    for (int q = 0; q < nl; ++q) s = s + V[a * MAXL + q] * y[q];
+    psi[a] = s;
+  }
+}
+
+// psi for all layers (any module) -- used outside the hot kernels, constants read from m
+template <class T>
+__device__ __forceinline__ void psi_all(const ModArgs& m, int nl, T K2, const cplx<T>* X, cplx<T>* psi, size_t ti) {
+  if (m.psi_kind == PSI_EIGEN) {
+    T e[MAXL + 2 * MAXL * MAXL];
+    for (int a = 0; a < MAXL; ++a) e[a] = T(m.lam[a]);
+    for (int a = 0; a < MAXL * MAXL; ++a) { e[MAXL + a] = T(m.V[a]); e[MAXL + MAXL * MAXL + a] = T(m.Vinv[a]); }
+    psi_eigen<T>(nl, e, K2, X, psi);
+    return;
+  }
+  const T f = psi_factor<T>(m.psi_kind, K2, T(m.ell_inv2), m.mult, ti);
   for (int a = 0; a < nl; ++a) psi[a] = f * X[a];
 }
 
 // ------------------------------------------------------------------------ column kernel
-// Block: C adjacent kr columns x (NY/R) threads per column; thread (c, t) = (tid % C, tid / C)
-// owns rows j = t + i (NY/R), i < R.  Shared memory: F (C x NY work column, interleaved
-// [j][c]) and, for more than one layer, Xs and Ps (nl x C x NY each).
+// Block: C adjacent kr columns x (NY/R) threads per column.  Two thread mappings:
+//   element mapping (global loads/stores, epilogue): c = tid % C, t = tid / C, so a warp's
+//     global accesses are C-wide contiguous; thread (c, t) owns rows j = t + i (NY/R);
+//   FFT mapping: column cf = tid / TPF, butterfly index tf = tid % TPF, so a warp works on
+//     one column and the swizzled Stockham accesses are conflict-free.
+// Shared memory: two work buffers F0/F1 (C columns of g.cs slots each; the product fields
+// are prefetched with cp.async into one while the other is transformed), Xs (N, then the
+// next stage X; nl x NY x C interleaved, thread-owned) and, for more than one layer, Ps.
 template <class T, int NY, int R>
-__global__ void __launch_bounds__(512) col_stage_kernel(Geom g, ModArgs m, StepArgs s, Bufs b, int C) {
+__global__ void __launch_bounds__(512, sizeof(T) == 4 ? GF_MINBLOCKS_F32 : 1)
+    col_stage_kernel(Geom g, ModArgs m, StepArgs s, Bufs b, int C) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ T eig[MAXL + 2 * MAXL * MAXL];
   constexpr int TPF = NY / R;
-  cplx<T>* F = reinterpret_cast<cplx<T>*>(smem_raw);
+  const int cs = g.cs;
   const int nl = g.nl;
-  cplx<T>* Xs = F + C * NY;
-  cplx<T>* Ps = Xs + nl * C * NY;
+  cplx<T>* F0 = reinterpret_cast<cplx<T>*>(smem_raw);
+  cplx<T>* F1 = F0 + C * cs;
+  cplx<T>* Xs = F1 + C * cs;
+  cplx<T>* Ps = Xs + nl * NY * C;
   const int tid = threadIdx.x, c = tid % C, t = tid / C;
+  const int cf = tid / TPF, tf = tid % TPF;
   const int kr = blockIdx.x * C + c;
   const bool kin = kr < g.nkr;
-  const double krv = kr * g.dkx;
   const cplx<T>* tw = static_cast<const cplx<T>*>(b.twid);
   const size_t lstride = (size_t)g.ny * g.ldk;
+  const T dky = sel<T>(g.dky, g.dky_f), krT = T(kr) * sel<T>(g.dkx, g.dkx_f);
+  const T dt = sel<T>(s.dt, s.dt_f), ell2 = sel<T>(m.ell_inv2, m.ell_inv2_f), muT = sel<T>(m.mu, m.mu_f);
+  if (m.psi_kind == PSI_EIGEN) {
+    for (int a = tid; a < MAXL + 2 * MAXL * MAXL; a += blockDim.x)
+      eig[a] = a < MAXL ? sel<T>(m.lam[a], m.lam_f[a])
+             : a < MAXL + MAXL * MAXL ? sel<T>(m.V[a - MAXL], m.V_f[a - MAXL])
+                                      : sel<T>(m.Vinv[a - MAXL - MAXL * MAXL], m.Vinv_f[a - MAXL - MAXL * MAXL]);
+  }
 
   if (s.do_fwd) {
-    cplx<T>* P = static_cast<cplx<T>*>(b.P);
+    const cplx<T>* P = static_cast<const cplx<T>*>(b.P);
     const int nslot = 1 + m.hasB + m.hasC;
-    for (int L = 0; L < nl; ++L) {
-      cplx<T> nacc[R];
+    const int nseq = nl * nslot;
+    const T fscale = sel<T>(s.fscale, s.fscale_f), U0 = sel<T>(m.U0, m.U0_f);
+    // asynchronous copy of product field q = L * nslot + f into work buffer Fb
+    auto issue = [&](int q, cplx<T>* Fb) {
+      const int L = q / nslot, f = q - L * nslot;
+      const cplx<T>* Pf = P + ((size_t)f * nl + L) * lstride + kr;
+      cplx<T>* Fc = Fb + c * cs;
 #pragma unroll
-      for (int i = 0; i < R; ++i) nacc[i] = czero<T>();
-      for (int f = 0; f < nslot; ++f) {
-        const cplx<T>* Pf = P + ((size_t)f * nl + L) * lstride;
-#pragma unroll
-        for (int i = 0; i < R; ++i) {
-          const int j = t + i * TPF;
-          F[j * C + c] = kin ? Pf[(size_t)j * g.ldk + kr] : czero<T>();
-        }
-        __syncthreads();
-        fft_smem<T, NY, R, -1>(F + c, C, t, tw);
-        const int slot = (f == 0) ? 0 : (f == 1 && m.hasB) ? 1 : 2;
-#pragma unroll
-        for (int i = 0; i < R; ++i) {
-          const int j = t + i * TPF;
-          const cplx<T> v = F[j * C + c];
-          if (slot == 0) nacc[i] = nacc[i] + T(krv) * mul_mi(v);               // -i kr A
-          else if (slot == 1) nacc[i] = nacc[i] + T(lval(g, j)) * mul_mi(v);   // -i l B
-          else nacc[i] = nacc[i] - v;                                         // -C
-        }
-        __syncthreads();
+      for (int i = 0; i < R; ++i) {
+        const int j = t + i * TPF;
+        if (kin) cp_async_elem<T>(Fc + swz<T>(j), Pf + (size_t)j * g.ldk);
+        else Fc[swz<T>(j)] = czero<T>();
       }
-      // epilogue: forcing, drag, stage combination
+      cp_async_commit();
+    };
+    issue(0, F0);
+    for (int q = 0; q < nseq; ++q) {
+      cplx<T>* Fb = (q & 1) ? F1 : F0;
+      if (q + 1 < nseq) {
+        issue(q + 1, (q & 1) ? F0 : F1);
+        cp_async_wait<1>();
+      } else {
+        cp_async_wait<0>();
+      }
+      __syncthreads();
+      fft_smem<T, NY, R, -1>(Fb + cf * cs, tf, tw);
+      const int L = q / nslot, f = q - L * nslot;
+      const int slot = (f == 0) ? 0 : (f == 1 && m.hasB) ? 1 : 2;
+      cplx<T>* XL = Xs + L * NY * C + c;  // this thread's N / next-X slots: XL[j * C]
+      const cplx<T>* Fc = Fb + c * cs;
 #pragma unroll
+      for (int i = 0; i < R; ++i) {
+        const int j = t + i * TPF;
+        const cplx<T> v = Fc[swz<T>(j)];
+        cplx<T> d;
+        if (slot == 0) d = krT * mul_mi(v);                          // -i kr A
+        else if (slot == 1) d = (T(lidx(g, j)) * dky) * mul_mi(v);   // -i l B
+        else d = czero<T>() - v;                                     // -C
+        XL[j * C] = (f == 0) ? d : XL[j * C] + d;
+      }
+      __syncthreads();  // Fb is the target of the prefetch issued in the next iteration
+      if (f != nslot - 1) continue;
+      // epilogue for layer L: forcing, drag, stage combination (rolled, two elements per
+      // iteration; each thread reads back only the Xs slots it wrote)
+#pragma unroll 2
       for (int i = 0; i < R; ++i) {
         const int j = t + i * TPF;
         cplx<T> xn = czero<T>();
         if (kin) {
           const size_t ti = (size_t)j * g.ldk + kr;       // table index
           const size_t si = (size_t)L * lstride + ti;     // state index
-          const T mk_ = kept(g, kr, j) ? T(1) : T(0);
-          cplx<T> N = nacc[i];
-          if (m.etah && m.U0 != 0.0) N = N - T(m.U0 * krv) * mul_i(static_cast<const cplx<T>*>(m.etah)[ti]);
+          const bool keep = kept(g, kr, j);
+          const T mk_ = keep ? T(1) : T(0);
+          cplx<T> N = XL[j * C];
+          if (m.Ueta) N = N - (U0 * krT) * mul_i(static_cast<const cplx<T>*>(m.etah)[ti]);
           if (m.drag && L == nl - 1) N = N + static_cast<const cplx<T>*>(m.D)[ti];
           cplx<T>* sol = static_cast<cplx<T>*>(s.sol);
           const cplx<T> solm = mk_ * sol[si];
@@ -164,7 +223,7 @@ __global__ void __launch_bounds__(512) col_stage_kernel(Geom g, ModArgs m, StepA
           if (s.fkind == FK_STATIC) {
             N = N + static_cast<const cplx<T>*>(s.Fh)[si];
           } else if (s.fkind == FK_HARMONIC) {
-            N = N + T(s.fscale) * static_cast<const cplx<T>*>(s.Fh)[si];
+            N = N + fscale * static_cast<const cplx<T>*>(s.Fh)[si];
           } else if (s.fkind == FK_STOCH || s.fkind == FK_STOCH_PHASE) {
             cplx<T> Fv;
             if (s.draw) {
@@ -180,7 +239,6 @@ __global__ void __launch_bounds__(512) col_stage_kernel(Geom g, ModArgs m, StepA
             }
             N = N + Fv;
           }
-          const T dt = T(s.dt);
           auto Lmul = [&](cplx<T> x) { return mulc(ldc<T>(s.Ltab, ti, s.cplxL), x, s.cplxL); };
           auto finish = [&](cplx<T> v) {
             if (s.filtered) v = static_cast<const T*>(s.filt)[ti] * v;
@@ -241,9 +299,9 @@ __global__ void __launch_bounds__(512) col_stage_kernel(Geom g, ModArgs m, StepA
             static_cast<cplx<T>*>(s.Rout)[si] = Rv;
             xn = finish(solm + dt * upd);
           }
-          xn = (kept(g, kr, j) ? T(1) : T(0)) * xn;
+          if (!keep) xn = czero<T>();
         }
-        Xs[(L * NY + j) * C + c] = xn;
+        XL[j * C] = xn;
       }
     }
   } else {
@@ -260,59 +318,91 @@ __global__ void __launch_bounds__(512) col_stage_kernel(Geom g, ModArgs m, StepA
   }
   if (!s.do_inv) return;
   if ((int)blockIdx.x * C >= g.kcut) return;  // whole block aliased: W is never read there
+  __syncthreads();  // eig[] filled; F0 free
 
-  // PV inversion for every owned element (each thread reads back only what it wrote)
+  // PV inversion for more than one layer (each thread reads back only what it wrote)
+  if (nl > 1) {
 #pragma unroll
-  for (int i = 0; i < R; ++i) {
-    const int j = t + i * TPF;
-    const double lv = lval(g, j);
-    const double K2 = krv * krv + lv * lv;
-    const size_t ti = (size_t)j * g.ldk + (kin ? kr : 0);
-    if (nl == 1) {
-      cplx<T> x = Xs[j * C + c], p;
-      psi_all<T>(m, 1, K2, &x, &p, ti);
-      Ps[j * C + c] = p;
-      if (m.drag && kin) static_cast<cplx<T>*>(m.D)[ti] = T(m.mu * K2) * p;
-    } else {
+    for (int i = 0; i < R; ++i) {
+      const int j = t + i * TPF;
+      const T lv = T(lidx(g, j)) * dky;
+      const T K2 = krT * krT + lv * lv;
       cplx<T> X[MAXL], ps[MAXL];
       for (int L = 0; L < nl; ++L) X[L] = Xs[(L * NY + j) * C + c];
-      psi_all<T>(m, nl, K2, X, ps, ti);
+      if (m.psi_kind == PSI_EIGEN) {
+        psi_eigen<T>(nl, eig, K2, X, ps);
+      } else {
+        const T f = psi_factor<T>(m.psi_kind, K2, ell2, m.mult, (size_t)j * g.ldk + (kin ? kr : 0));
+        for (int L = 0; L < nl; ++L) ps[L] = f * X[L];
+      }
       for (int L = 0; L < nl; ++L) Ps[(L * NY + j) * C + c] = ps[L];
-      if (m.drag && kin) static_cast<cplx<T>*>(m.D)[ti] = T(m.mu * K2) * ps[nl - 1];
+      if (m.drag && kin) static_cast<cplx<T>*>(m.D)[(size_t)j * g.ldk + kr] = (muT * K2) * ps[nl - 1];
+    }
+  } else if (m.drag && kin) {
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int j = t + i * TPF;
+      const T lv = T(lidx(g, j)) * dky;
+      const T K2 = krT * krT + lv * lv;
+      const size_t ti = (size_t)j * g.ldk + kr;
+      const T f = psi_factor<T>(m.psi_kind, K2, ell2, m.mult, ti);
+      static_cast<cplx<T>*>(m.D)[ti] = (muT * K2 * f) * Xs[j * C + c];
     }
   }
   // y-direction inverse FFT of (q, u, v) for every layer
   cplx<T>* W = static_cast<cplx<T>*>(b.W);
-  const T sc = T(g.inv_nxny);
+  const T sc = sel<T>(g.inv_nxny, g.inv_nxny_f);
   for (int L = 0; L < nl; ++L) {
     for (int f = 0; f < 3; ++f) {
-      __syncthreads();
+      cplx<T>* Fb = ((L * 3 + f) & 1) ? F1 : F0;  // alternate so stores of one field overlap the next
+      cplx<T>* Fe = Fb + c * cs;
 #pragma unroll
       for (int i = 0; i < R; ++i) {
         const int j = t + i * TPF;
         const cplx<T> x = Xs[(L * NY + j) * C + c];
-        const cplx<T> p = Ps[(L * NY + j) * C + c];
+        const T lv = T(lidx(g, j)) * dky;
         cplx<T> v;
-        if (f == 0) v = x;
-        else if (f == 1) v = T(lval(g, j)) * mul_mi(p);  // u = -i l psi
-        else v = T(krv) * mul_i(p);                        // v =  i kr psi
-        F[j * C + c] = sc * v;
+        if (f == 0) {
+          v = x;
+        } else {
+          cplx<T> p;
+          if (nl > 1) {
+            p = Ps[(L * NY + j) * C + c];
+          } else {
+            const T K2 = krT * krT + lv * lv;
+            p = psi_factor<T>(m.psi_kind, K2, ell2, m.mult, (size_t)j * g.ldk + (kin ? kr : 0)) * x;
+          }
+          v = (f == 1) ? lv * mul_mi(p)     // u = -i l psi
+                       : krT * mul_i(p);    // v =  i kr psi
+        }
+        Fe[swz<T>(j)] = sc * v;
       }
       __syncthreads();
-      fft_smem<T, NY, R, +1>(F + c, C, t, tw);
+      fft_smem<T, NY, R, +1>(Fb + cf * cs, tf, tw);
       if (kr < g.kcut) {
-        cplx<T>* Wf = W + ((size_t)f * nl + L) * g.ny * g.ldw;
+        cplx<T>* Wf = W + ((size_t)f * nl + L) * g.ny * g.ldw + kr;
 #pragma unroll
         for (int i = 0; i < R; ++i) {
           const int j = t + i * TPF;
-          Wf[(size_t)j * g.ldw + kr] = F[j * C + c];
+          Wf[(size_t)j * g.ldw] = Fe[swz<T>(j)];
         }
       }
     }
   }
 }
 
+// shared-memory bytes of col_stage_kernel for C columns with column stride cs
+__host__ __forceinline__ size_t col_stage_smem(int NY, int C, int cs, int nl, size_t elem) {
+  return ((size_t)2 * C * cs + (size_t)nl * NY * C * (nl > 1 ? 2 : 1)) * elem;
+}
+
 // --------------------------------------------------------------------------- row kernel
+// Slots per row-pair buffer: NX, staggered by TPF when several pairs share a wavefront.
+template <class T>
+__host__ __device__ constexpr int row_stride(int NX, int TPF) {
+  return NX + (TPF < wave_threads<T>() ? TPF : 0);
+}
+
 // Block: B row pairs x (NX/R) threads; the pair (j0, j0+1) is packed as one complex
 // length-NX FFT (row j0 in the real part, j0+1 in the imaginary part).
 template <class T>
@@ -330,21 +420,23 @@ __device__ __forceinline__ cplx<T> packed_spec(const cplx<T>* Wa, const cplx<T>*
   return mk<T>(A.x + B.y, B.x - A.y);                    // conj(A) + i conj(B)
 }
 
+// unpack the spectra of the two packed rows from the swizzled buf at kr index k
 template <class T>
 __device__ __forceinline__ void unpack_store(const cplx<T>* buf, int k, int NX, cplx<T>* Pa, cplx<T>* Pb) {
-  const cplx<T> z = buf[k], w = buf[(NX - k) & (NX - 1)];
+  const cplx<T> z = buf[swz<T>(k)], w = buf[swz<T>((NX - k) & (NX - 1))];
   Pa[k] = mk<T>(T(0.5) * (z.x + w.x), T(0.5) * (z.y - w.y));
   Pb[k] = mk<T>(T(0.5) * (z.y + w.y), T(0.5) * (w.x - z.x));
 }
 
 template <class T, int NX, int R>
-__global__ void __launch_bounds__(512) row_nl_kernel(Geom g, ModArgs m, Bufs b, int B) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) row_nl_kernel(Geom g, ModArgs m, Bufs b, int B) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int TPF = NX / R;
   constexpr int M = NX / 2;
+  constexpr int PS = row_stride<T>(NX, NX / R);
   const int tid = threadIdx.x, bp = tid / TPF, t = tid % TPF;
   const int j0 = 2 * (blockIdx.x * B + bp);
-  cplx<T>* buf = reinterpret_cast<cplx<T>*>(smem_raw) + (size_t)bp * 3 * NX;
+  cplx<T>* buf = reinterpret_cast<cplx<T>*>(smem_raw) + (size_t)bp * 3 * PS;
   const cplx<T>* tw = static_cast<const cplx<T>*>(b.twid);
   const cplx<T>* W = static_cast<const cplx<T>*>(b.W);
   cplx<T>* P = static_cast<cplx<T>*>(b.P);
@@ -363,11 +455,11 @@ __global__ void __launch_bounds__(512) row_nl_kernel(Geom g, ModArgs m, Bufs b, 
 #pragma unroll
       for (int i = 0; i < R; ++i) {
         const int k = t + i * TPF;
-        buf[f * NX + k] = packed_spec<T>(Wa, Wb, k, NX, g.kcut);
+        buf[f * PS + swz<T>(k)] = packed_spec<T>(Wa, Wb, k, NX, g.kcut);
       }
     }
     __syncthreads();
-    for (int f = 0; f < 3; ++f) fft_smem<T, NX, R, +1>(buf + f * NX, 1, t, tw);
+    for (int f = 0; f < 3; ++f) fft_smem<T, NX, R, +1>(buf + f * PS, t, tw);
     // physical-space products on the packed pairs
     const T Ua = U1D ? U1D[L * g.ny + j0] : T(0), Ub = U1D ? U1D[L * g.ny + j0 + 1] : T(0);
     const T Qa = Qy1D ? Qy1D[L * g.ny + j0] : T(0), Qb = Qy1D ? Qy1D[L * g.ny + j0 + 1] : T(0);
@@ -375,7 +467,8 @@ __global__ void __launch_bounds__(512) row_nl_kernel(Geom g, ModArgs m, Bufs b, 
 #pragma unroll
     for (int i = 0; i < R; ++i) {
       const int x = t + i * TPF;
-      cplx<T> q = buf[x], u = buf[NX + x], v = buf[2 * NX + x];
+      const int px = swz<T>(x);
+      cplx<T> q = buf[px], u = buf[PS + px], v = buf[2 * PS + px];
       const cplx<T> Up = mk<T>(Ua, Ub);
       u = u + Up;
       if (eta) q = q + mk<T>(eta[(size_t)j0 * NX + x], eta[(size_t)(j0 + 1) * NX + x]);
@@ -389,18 +482,18 @@ __global__ void __launch_bounds__(512) row_nl_kernel(Geom g, ModArgs m, Bufs b, 
         if (last && Qx2D) Qx = mk<T>(Qx2D[(size_t)j0 * NX + x], Qx2D[(size_t)(j0 + 1) * NX + x]);
         Cv = mk<T>(u.x * Qx.x + v.x * Qy.x, u.y * Qx.y + v.y * Qy.y);
       }
-      buf[x] = A;
-      if (m.hasB) { buf[NX + x] = Bv; if (m.hasC) buf[2 * NX + x] = Cv; }
-      else buf[NX + x] = Cv;
+      buf[px] = A;
+      if (m.hasB) { buf[PS + px] = Bv; if (m.hasC) buf[2 * PS + px] = Cv; }
+      else buf[PS + px] = Cv;
     }
     __syncthreads();
-    for (int f = 0; f < nslot; ++f) fft_smem<T, NX, R, -1>(buf + f * NX, 1, t, tw);
+    for (int f = 0; f < nslot; ++f) fft_smem<T, NX, R, -1>(buf + f * PS, t, tw);
     for (int f = 0; f < nslot; ++f) {
       cplx<T>* Pa = P + ((size_t)f * nl + L) * g.ny * g.ldk + (size_t)j0 * g.ldk;
 #pragma unroll
       for (int i = 0; i < R; ++i) {
         const int k = t + i * TPF;
-        if (k <= M) unpack_store<T>(buf + f * NX, k, NX, Pa, Pa + g.ldk);
+        if (k <= M) unpack_store<T>(buf + f * PS, k, NX, Pa, Pa + g.ldk);
       }
     }
     __syncthreads();
@@ -409,22 +502,26 @@ __global__ void __launch_bounds__(512) row_nl_kernel(Geom g, ModArgs m, Bufs b, 
 
 // ------------------------------------------------------------------ generic transforms
 // y-direction inverse FFT of a derived spectral field of every layer into W (full kr
-// range, row stride ldk): kind selects X, psi, u, v, du/dy or the raw array.
+// range, row stride ldk): kind selects X, psi, u, v, du/dy, d/dx, d/dy or the raw array.
 template <class T, int NY, int R>
 __global__ void __launch_bounds__(512) col_inv_generic(Geom g, ModArgs m, const void* src, int kind, int mask,
                                                         Bufs b, int C) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int TPF = NY / R;
-  cplx<T>* F = reinterpret_cast<cplx<T>*>(smem_raw);
+  const int cs = g.cs;
   const int tid = threadIdx.x, c = tid % C, t = tid / C;
+  const int cf = tid / TPF, tf = tid % TPF;
   const int kr = blockIdx.x * C + c;
   const bool kin = kr < g.nkr;
-  const double krv = kr * g.dkx;
+  cplx<T>* F = reinterpret_cast<cplx<T>*>(smem_raw);
+  cplx<T>* Fc = F + c * cs;
+  const T krT = T(kr) * T(g.dkx), dky = T(g.dky);
   const cplx<T>* S = static_cast<const cplx<T>*>(src);
   const cplx<T>* tw = static_cast<const cplx<T>*>(b.twid);
   cplx<T>* W = static_cast<cplx<T>*>(b.W);
   const size_t lstride = (size_t)g.ny * g.ldk;
   const int nl = g.nl;
+  const T sc = T(g.inv_nxny);
   for (int L = 0; L < nl; ++L) {
 #pragma unroll
     for (int i = 0; i < R; ++i) {
@@ -435,31 +532,31 @@ __global__ void __launch_bounds__(512) col_inv_generic(Geom g, ModArgs m, const 
         cplx<T> X[MAXL], ps[MAXL];
         for (int a = 0; a < nl; ++a) X[a] = S[a * lstride + ti];
         if (mask && !kept(g, kr, j)) for (int a = 0; a < nl; ++a) X[a] = czero<T>();
-        const double lv = lval(g, j);
+        const T lv = T(lidx(g, j)) * dky;
         if (kind == SF_X || kind == SF_RAW) {
           v = X[L];
         } else if (kind == SF_DX) {
-          v = T(krv) * mul_i(X[L]);
+          v = krT * mul_i(X[L]);
         } else if (kind == SF_DY) {
-          v = T(lv) * mul_i(X[L]);
+          v = lv * mul_i(X[L]);
         } else {
-          psi_all<T>(m, nl, krv * krv + lv * lv, X, ps, ti);
+          psi_all<T>(m, nl, krT * krT + lv * lv, X, ps, ti);
           const cplx<T> p = ps[L];
           if (kind == SF_PSI) v = p;
-          else if (kind == SF_U) v = T(lv) * mul_mi(p);   // u = -i l psi
-          else if (kind == SF_V) v = T(krv) * mul_i(p);   // v =  i kr psi
-          else v = T(lv * lv) * p;                        // du/dy = i l u = l^2 psi
+          else if (kind == SF_U) v = lv * mul_mi(p);   // u = -i l psi
+          else if (kind == SF_V) v = krT * mul_i(p);   // v =  i kr psi
+          else v = (lv * lv) * p;                     // du/dy = i l u = l^2 psi
         }
       }
-      F[j * C + c] = T(g.inv_nxny) * v;
+      Fc[swz<T>(j)] = sc * v;
     }
     __syncthreads();
-    fft_smem<T, NY, R, +1>(F + c, C, t, tw);
+    fft_smem<T, NY, R, +1>(F + cf * cs, tf, tw);
     if (kin) {
 #pragma unroll
       for (int i = 0; i < R; ++i) {
         const int j = t + i * TPF;
-        W[(size_t)L * lstride + (size_t)j * g.ldk + kr] = F[j * C + c];
+        W[(size_t)L * lstride + (size_t)j * g.ldk + kr] = Fc[swz<T>(j)];
       }
     }
     __syncthreads();
@@ -473,7 +570,7 @@ __global__ void __launch_bounds__(512) row_c2r_generic(Geom g, Bufs b, int nf, T
   constexpr int TPF = NX / R;
   const int tid = threadIdx.x, bp = tid / TPF, t = tid % TPF;
   const int j0 = 2 * (blockIdx.x * B + bp);
-  cplx<T>* buf = reinterpret_cast<cplx<T>*>(smem_raw) + (size_t)bp * NX;
+  cplx<T>* buf = reinterpret_cast<cplx<T>*>(smem_raw) + (size_t)bp * row_stride<T>(NX, TPF);
   const cplx<T>* tw = static_cast<const cplx<T>*>(b.twid);
   const cplx<T>* W = static_cast<const cplx<T>*>(b.W);
   for (int f = 0; f < nf; ++f) {
@@ -481,15 +578,15 @@ __global__ void __launch_bounds__(512) row_c2r_generic(Geom g, Bufs b, int nf, T
 #pragma unroll
     for (int i = 0; i < R; ++i) {
       const int k = t + i * TPF;
-      buf[k] = packed_spec<T>(Wa, Wa + g.ldk, k, NX, g.nkr);
+      buf[swz<T>(k)] = packed_spec<T>(Wa, Wa + g.ldk, k, NX, g.nkr);
     }
     __syncthreads();
-    fft_smem<T, NX, R, +1>(buf, 1, t, tw);
+    fft_smem<T, NX, R, +1>(buf, t, tw);
     T* o = out + (size_t)f * g.ny * NX + (size_t)j0 * NX;
 #pragma unroll
     for (int i = 0; i < R; ++i) {
       const int x = t + i * TPF;
-      const cplx<T> z = buf[x];
+      const cplx<T> z = buf[swz<T>(x)];
       o[x] = z.x;
       o[NX + x] = z.y;
     }
@@ -505,7 +602,7 @@ __global__ void __launch_bounds__(512) row_r2c_generic(Geom g, Bufs b, int nf, c
   constexpr int M = NX / 2;
   const int tid = threadIdx.x, bp = tid / TPF, t = tid % TPF;
   const int j0 = 2 * (blockIdx.x * B + bp);
-  cplx<T>* buf = reinterpret_cast<cplx<T>*>(smem_raw) + (size_t)bp * NX;
+  cplx<T>* buf = reinterpret_cast<cplx<T>*>(smem_raw) + (size_t)bp * row_stride<T>(NX, TPF);
   const cplx<T>* tw = static_cast<const cplx<T>*>(b.twid);
   cplx<T>* P = static_cast<cplx<T>*>(b.P);
   for (int f = 0; f < nf; ++f) {
@@ -513,10 +610,10 @@ __global__ void __launch_bounds__(512) row_r2c_generic(Geom g, Bufs b, int nf, c
 #pragma unroll
     for (int i = 0; i < R; ++i) {
       const int x = t + i * TPF;
-      buf[x] = mk<T>(src[x], src[NX + x]);
+      buf[swz<T>(x)] = mk<T>(src[x], src[NX + x]);
     }
     __syncthreads();
-    fft_smem<T, NX, R, -1>(buf, 1, t, tw);
+    fft_smem<T, NX, R, -1>(buf, t, tw);
     cplx<T>* Pa = P + (size_t)f * g.ny * g.ldk + (size_t)j0 * g.ldk;
 #pragma unroll
     for (int i = 0; i < R; ++i) {
@@ -532,10 +629,13 @@ template <class T, int NY, int R>
 __global__ void __launch_bounds__(512) col_fwd_generic(Geom g, Bufs b, int nf, cplx<T>* out, int zero_mean, int C) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int TPF = NY / R;
-  cplx<T>* F = reinterpret_cast<cplx<T>*>(smem_raw);
+  const int cs = g.cs;
   const int tid = threadIdx.x, c = tid % C, t = tid / C;
+  const int cf = tid / TPF, tf = tid % TPF;
   const int kr = blockIdx.x * C + c;
   const bool kin = kr < g.nkr;
+  cplx<T>* F = reinterpret_cast<cplx<T>*>(smem_raw);
+  cplx<T>* Fc = F + c * cs;
   const cplx<T>* tw = static_cast<const cplx<T>*>(b.twid);
   const cplx<T>* P = static_cast<const cplx<T>*>(b.P);
   const size_t lstride = (size_t)g.ny * g.ldk;
@@ -543,15 +643,15 @@ __global__ void __launch_bounds__(512) col_fwd_generic(Geom g, Bufs b, int nf, c
 #pragma unroll
     for (int i = 0; i < R; ++i) {
       const int j = t + i * TPF;
-      F[j * C + c] = kin ? P[(size_t)f * lstride + (size_t)j * g.ldk + kr] : czero<T>();
+      Fc[swz<T>(j)] = kin ? P[(size_t)f * lstride + (size_t)j * g.ldk + kr] : czero<T>();
     }
     __syncthreads();
-    fft_smem<T, NY, R, -1>(F + c, C, t, tw);
+    fft_smem<T, NY, R, -1>(F + cf * cs, tf, tw);
     if (kin) {
 #pragma unroll
       for (int i = 0; i < R; ++i) {
         const int j = t + i * TPF;
-        cplx<T> v = F[j * C + c];
+        cplx<T> v = Fc[swz<T>(j)];
         if (zero_mean && kr == 0 && j == 0) v = czero<T>();
         out[(size_t)f * lstride + (size_t)j * g.ldk + kr] = v;
       }
@@ -582,11 +682,11 @@ __global__ void spec_apply_kernel(Geom g, ModArgs m, const cplx<T>* in, cplx<T>*
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
     const int kr = e % g.nkr, j = e / g.nkr;
     const size_t ti = (size_t)j * g.ldk + kr;
-    const double krv = kr * g.dkx, lv = lval(g, j), K2 = krv * krv + lv * lv;
+    const double krv = kr * g.dkx, lv = lidx(g, j) * g.dky, K2 = krv * krv + lv * lv;
     cplx<T> X[MAXL], Y[MAXL];
     for (int a = 0; a < nl; ++a) X[a] = in[a * lstride + ti];
     if (op == 1) {
-      psi_all<T>(m, nl, K2, X, Y, ti);
+      psi_all<T>(m, nl, T(K2), X, Y, ti);
     } else if (m.psi_kind == PSI_EIGEN) {
       // S = -K^2 I + F with F = V diag(lam) Vinv
       for (int a = 0; a < nl; ++a) {
@@ -637,24 +737,26 @@ __global__ void __launch_bounds__(DIAG_BLOCK) diag_kernel(Geom g, ModArgs m, con
     const int kr = e % g.nkr, j = e / g.nkr;
     const size_t ti = (size_t)j * g.ldk + kr;
     const double w = (kr == 0 || (g.nx % 2 == 0 && kr == g.nkr - 1)) ? 1.0 : 2.0;
-    const double krv = kr * g.dkx, lv = lval(g, j), K2 = krv * krv + lv * lv;
+    const double krv = kr * g.dkx, lv = lidx(g, j) * g.dky, K2 = krv * krv + lv * lv;
     const double iK2 = K2 == 0.0 ? 0.0 : 1.0 / K2;
     const bool k0 = (kr == 0 && j == 0);
-    cplx<T> Xt[MAXL], Pt[MAXL];
-    for (int a = 0; a < nl; ++a) Xt[a] = sol[a * lstride + ti];
     if (m.module == MOD_MLQG) {
-      psi_all<T>(m, nl, K2, Xt, Pt, ti);
+      // psi in double from the stored layer values
+      cplx<double> Xd[MAXL], Pd[MAXL];
+      for (int a = 0; a < nl; ++a) { const cplx<T> x = sol[a * lstride + ti]; Xd[a] = mk<double>(x.x, x.y); }
+      psi_all<double>(m, nl, K2, Xd, Pd, ti);
       for (int a = 0; a < nl; ++a) {
-        const double pr = Pt[a].x, pi = Pt[a].y;
+        const double pr = Pd[a].x, pi = Pd[a].y;
         if (mask & (1u << a)) acc[a].add(w * K2 * (pr * pr + pi * pi));
         if (a + 1 < nl && (mask & (1u << (nl + a)))) {
-          const double dr = pr - (double)Pt[a + 1].x, di = pi - (double)Pt[a + 1].y;
+          const double dr = pr - Pd[a + 1].x, di = pi - Pd[a + 1].y;
           acc[nl + a].add(w * (dr * dr + di * di));
         }
       }
       continue;
     }
-    const double sr = Xt[0].x, si = Xt[0].y, s2 = sr * sr + si * si;
+    const cplx<T> x0 = sol[ti];
+    const double sr = x0.x, si = x0.y, s2 = sr * sr + si * si;
     // forcing work term Re(S conj(F)), S = sol or (prevsol + sol)/2
     double wr = 0;
     if (Fh) {
@@ -678,8 +780,8 @@ __global__ void __launch_bounds__(DIAG_BLOCK) diag_kernel(Geom g, ModArgs m, con
       v[7] = iK2 * wr;
       v[8] = wr;
     } else if (m.module == MOD_SLQG) {
-      psi_all<T>(m, 1, K2, Xt, Pt, ti);
-      const double p2 = (double)Pt[0].x * Pt[0].x + (double)Pt[0].y * Pt[0].y;
+      const double f = m.psi_kind == PSI_INVK2 ? -iK2 : -1.0 / (K2 + m.ell_inv2);
+      const double p2 = f * f * s2;
       v[0] = 0.5 * K2 * p2;
       v[1] = 0.5 * m.ell_inv2 * p2;
       double er = sr, ei = si;
@@ -717,8 +819,5 @@ __global__ void __launch_bounds__(DIAG_BLOCK) diag_kernel(Geom g, ModArgs m, con
     __syncthreads();
   }
 }
-
-// final reduction of the block partials (one block, compensated)
-__global__ void diag_finish_kernel(const double* partial, int nblocks, uint32_t mask, double* out);
 
 }  // namespace gf

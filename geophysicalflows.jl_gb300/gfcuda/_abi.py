@@ -42,9 +42,12 @@ class gf_config(C.Structure):
 _lib = None
 
 
-def load(path=LIBPATH):
-    """Load libgfcuda.so (built in-tree).  Raises if it is missing: there is no fallback."""
+def load(path=None):
+    """Load libgfcuda.so (built in-tree; GFCUDA_LIB may name another build of it, e.g. a
+    variant compiled with different tuning macros).  Raises if it is missing: there is no
+    fallback."""
     global _lib
+    path = path or os.environ.get("GFCUDA_LIB") or LIBPATH
     if _lib is not None:
         return _lib
     if not os.path.exists(path):

@@ -37,15 +37,16 @@ def up_to_date():
     return all(os.path.getmtime(s) <= t for s in _sources())
 
 
-def build(force=False, verbose=True):
-    if not force and up_to_date():
+def build(force=False, verbose=True, defines=(), lib=None):
+    lib = lib or LIB
+    if not force and lib == LIB and up_to_date():
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     nvcc = _nvcc()
 
     def compile_unit(u):
         obj = os.path.join(BUILD, u.replace(".cu", ".o"))
-        cmd = [nvcc, *ARCH, *FLAGS, "-c", os.path.join(CSRC, u), "-o", obj]
+        cmd = [nvcc, *ARCH, *FLAGS, *[f"-D{d}" for d in defines], "-c", os.path.join(CSRC, u), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {u}:\n{r.stderr}")
@@ -53,16 +54,19 @@ def build(force=False, verbose=True):
 
     with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         objs = list(ex.map(compile_unit, UNITS))
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib)
     if verbose:
-        print(f"built {LIB}")
-    return LIB
+        print(f"built {lib}")
+    return lib
 
 
 if __name__ == "__main__":
-    build(force="--force" in sys.argv)
+    # python build.py [--force] [-DNAME=VALUE ...] [--out PATH]
+    defs = [a[2:] for a in sys.argv[1:] if a.startswith("-D")]
+    out = sys.argv[sys.argv.index("--out") + 1] if "--out" in sys.argv else None
+    build(force="--force" in sys.argv or bool(defs) or out is not None, defines=defs, lib=out)
