@@ -132,16 +132,17 @@ def ncu_traffic(kernel, workload):
     return None
 
 
-def make_problem(w, T):
+def make_problem(w, T, precision=None):
     import gfcuda
     if w["module"] == "TwoDNavierStokes":
-        return gfcuda.TwoDNavierStokes.Problem("GPU", nx=w["nx"], ny=w["ny"], dt=w["dt"], stepper=w["stepper"], T=T)
+        return gfcuda.TwoDNavierStokes.Problem("GPU", nx=w["nx"], ny=w["ny"], dt=w["dt"], stepper=w["stepper"], T=T,
+                                               precision=precision)
     import gf_oracle as O
     g = O.Grid(w["nx"])
     spec = O.ring_forcing_spectrum(g, 14.0 * 2 * np.pi / g.Lx, 1.5 * 2 * np.pi / g.Lx, 1e-3)
     f = gfcuda.Forcing("stochastic", spectrum=spec, seed=1234)
     return gfcuda.SingleLayerQG.Problem("GPU", nx=w["nx"], beta=w["beta"], mu=w["mu"], dt=w["dt"],
-                                        stepper=w["stepper"], forcing=f, T=T)
+                                        stepper=w["stepper"], forcing=f, T=T, precision=precision)
 
 
 def initial_state(w):
@@ -152,12 +153,12 @@ def initial_state(w):
     return np.zeros((w["ny"], w["nx"]))
 
 
-def time_arm(w, T, steps, warmup, flush, with_e2e):
+def time_arm(w, T, steps, warmup, flush, with_e2e, precision=None):
     """Run one precision arm: warm-up, K timed steps (CUDA events on the library's stream,
     L2 flushed between steps), kernel timing, optional end-to-end timing."""
     import torch
     import gfcuda
-    prob = make_problem(w, T)
+    prob = make_problem(w, T, precision)
     z0 = initial_state(w)
     if w["module"] == "TwoDNavierStokes":
         gfcuda.TwoDNavierStokes.set_zeta(prob, z0)
@@ -278,20 +279,24 @@ def run_ours(args):
     torch.cuda.synchronize()
     with Clocks() as clk:
         r32 = time_arm(w, np.float32, args.steps, args.warmup, flush, with_e2e=True)
-    r64 = time_arm(w, np.float64, args.steps, args.warmup, flush, with_e2e=True)
+    rdf = time_arm(w, np.float64, args.steps, args.warmup, flush, with_e2e=True, precision="DF64")
+    r64 = time_arm(w, np.float64, args.steps, args.warmup, flush, with_e2e=False)
     c32 = time_arm(CONFIG1, np.float32, args.steps, args.warmup, flush, with_e2e=False)
+    cdf = time_arm(CONFIG1, np.float64, args.steps, args.warmup, flush, with_e2e=False, precision="DF64")
     c64 = time_arm(CONFIG1, np.float64, args.steps, args.warmup, flush, with_e2e=False)
     ms = r32["ms_per_step"]
     if dist:
-        t = torch.tensor([ms, r64["ms_per_step"], r32["e2e_s_per_step"]], device="cuda")
+        t = torch.tensor([ms, rdf["ms_per_step"], r64["ms_per_step"], r32["e2e_s_per_step"], rdf["e2e_s_per_step"]],
+                         device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms, ms64, e2e_s = t.tolist()
+        ms, msdf, ms64, e2e_s, e2e_df = t.tolist()
     else:
-        ms64, e2e_s = r64["ms_per_step"], r32["e2e_s_per_step"]
+        msdf, ms64, e2e_s, e2e_df = rdf["ms_per_step"], r64["ms_per_step"], r32["e2e_s_per_step"], rdf["e2e_s_per_step"]
     if not is_rank0():
         return 0
     pts = w["nx"] * w["ny"]
     value = world * pts / (ms * 1e-3)
+    vdf = world * pts / (msdf * 1e-3)
     v64 = world * pts / (ms64 * 1e-3)
 
     def roofline(res, wbytes):
@@ -300,15 +305,20 @@ def run_ours(args):
         per_launch = (col_w if dom == "col_stage" else row_w) * wbytes * pts
         t = res["ms_col"] if dom == "col_stage" else res["ms_row"]
         ach = per_launch / (t * 1e-3) / 1e9
-        tag = "fp32" if wbytes == 4 else "fp64"
+        tag = "fp32" if res is r32 else "df64" if res is rdf else "fp64"
         return {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": ach / peaks["hbm_gbs"], "peak_source": peak_src,
                 "traffic": ncu_traffic(dom, f"twodns2048_{tag}"), "algorithmic_bytes_per_launch": per_launch,
                 "launch_ms": t, "row_ms": res["ms_row"], "col_ms": res["ms_col"],
                 "step_words_per_pt": words}
 
-    err = float(np.linalg.norm(r32["sol"] - r64["sol"]) / np.linalg.norm(r64["sol"]))
-    cerr = float(np.linalg.norm(c32["sol"] - c64["sol"]) / np.linalg.norm(c64["sol"]))
+    def relerr(a, b):
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+    err = relerr(r32["sol"], r64["sol"])
+    dferr = relerr(rdf["sol"], r64["sol"])
+    cerr = relerr(c32["sol"], c64["sol"])
+    cdferr = relerr(cdf["sol"], c64["sol"])
     cpu = cpu_baseline(w)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -323,24 +333,31 @@ def run_ours(args):
                 "d2h_bytes_per_step": r32["state_bytes"]},
         "gpu_launches": r32["launches"],
         "clocks": clk.summary(int(os.environ.get("LOCAL_RANK", "0"))),
-        "fp64_plain": {"value": v64, "ms_per_step": ms64, "roofline": roofline(r64, 8),
-                       "e2e": {"value": world * pts / r64["e2e_s_per_step"], "unit": UNIT}},
-        "fp32_over_fp64": value / v64,
+        "fp64_plain": {"arithmetic": "df64 (double-float pairs, 48-bit significand, FP32 pipes)", "value": vdf,
+                       "ms_per_step": msdf, "roofline": roofline(rdf, 8),
+                       "e2e": {"value": world * pts / e2e_df, "unit": UNIT},
+                       "rel_l2_vs_ieee_fp64": dferr},
+        "fp64_ieee": {"value": v64, "ms_per_step": ms64, "roofline": roofline(r64, 8)},
+        "fp32_over_fp64": value / vdf,
+        "fp32_over_ieee_fp64": value / v64,
         "fp32_vs_fp64_rel_l2": err,
         "fp32_vs_fp64_steps": args.warmup + args.steps,
         "configs1": {"workload": "SingleLayerQG 512^2 beta=10 mu=0.01 ETDRK4 dt=0.05, stochastic ring forcing "
                                  "kf=14 eps=1e-3, q0=0 (L2-resident: latency, no HBM fraction)",
                      "fp32": CONFIG1["nx"] * CONFIG1["ny"] / (c32["ms_per_step"] * 1e-3),
-                     "fp64": CONFIG1["nx"] * CONFIG1["ny"] / (c64["ms_per_step"] * 1e-3),
-                     "ms_per_step_fp32": c32["ms_per_step"], "ms_per_step_fp64": c64["ms_per_step"],
-                     "fp32_vs_fp64_rel_l2": cerr},
+                     "fp64_plain_df64": CONFIG1["nx"] * CONFIG1["ny"] / (cdf["ms_per_step"] * 1e-3),
+                     "fp64_ieee": CONFIG1["nx"] * CONFIG1["ny"] / (c64["ms_per_step"] * 1e-3),
+                     "ms_per_step_fp32": c32["ms_per_step"], "ms_per_step_df64": cdf["ms_per_step"],
+                     "ms_per_step_fp64": c64["ms_per_step"],
+                     "fp32_vs_fp64_rel_l2": cerr, "df64_vs_fp64_rel_l2": cdferr},
     }
     print(json.dumps(line), flush=True)
     return 0
 
 
-SINGLE = {"twodns2048_fp32": (HEADLINE, np.float32), "twodns2048_fp64": (HEADLINE, np.float64),
-          "slqg512_fp32": (CONFIG1, np.float32), "slqg512_fp64": (CONFIG1, np.float64)}
+SINGLE = {"twodns2048_fp32": (HEADLINE, np.float32, None), "twodns2048_fp64": (HEADLINE, np.float64, None),
+          "twodns2048_df64": (HEADLINE, np.float64, "DF64"), "slqg512_fp32": (CONFIG1, np.float32, None),
+          "slqg512_fp64": (CONFIG1, np.float64, None), "slqg512_df64": (CONFIG1, np.float64, "DF64")}
 
 
 def run_single(args):
@@ -348,9 +365,9 @@ def run_single(args):
     import torch
     import gfcuda
     gfcuda.load()
-    w, T = SINGLE[args.single]
+    w, T, prec = SINGLE[args.single]
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
-    r = time_arm(w, T, args.steps, args.warmup, flush, with_e2e=False)
+    r = time_arm(w, T, args.steps, args.warmup, flush, with_e2e=False, precision=prec)
     r.pop("sol")
     r["workload"] = args.single
     r["pt_steps_per_s"] = w["nx"] * w["ny"] / (r["ms_per_step"] * 1e-3)

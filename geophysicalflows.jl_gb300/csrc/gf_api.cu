@@ -43,6 +43,7 @@ struct gf_ctx {
   void *phys = nullptr;     // [4][nl][ny][nx] physical fields from updatevars!
   void *tmp_spec = nullptr; // [nl][ny][ldk] scratch spectral array
   void *tmp_spec2 = nullptr;
+  void *stage = nullptr;    // df64 contexts: double staging for spectral/physical transfers
   double *dpart = nullptr, *dout = nullptr;
   int diag_blocks = 0;
   int ab3_out = 0, ab3_m1 = 1, ab3_m2 = 2;
@@ -145,7 +146,29 @@ __global__ void diag_finish(const double* __restrict__ partial, int nblocks, uin
 
 template <class T>
 __global__ void add_scalar_kernel(T* a, size_t n, double v) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) a[i] += (T)v;
+  const T tv = T(v);
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    a[i] = a[i] + tv;
+}
+
+// double <-> df64 copies of `rows` rows of `w` reals with their own row strides (in reals)
+__global__ void to_df64_kernel(const double* __restrict__ src, size_t ss, df64* __restrict__ dst, size_t ds,
+                               size_t rows, size_t w) {
+  const size_t n = rows * w;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = e / w, k = e - r * w;
+    const double d = src[r * ss + k];
+    const float h = (float)d;
+    dst[r * ds + k] = df64(h, (float)(d - (double)h));
+  }
+}
+__global__ void from_df64_kernel(const df64* __restrict__ src, size_t ss, double* __restrict__ dst, size_t ds,
+                                 size_t rows, size_t w) {
+  const size_t n = rows * w;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = e / w, k = e - r * w;
+    dst[r * ds + k] = to_double(src[r * ss + k]);
+  }
 }
 
 // ------------------------------------------------------------------------------- helpers
@@ -179,6 +202,11 @@ static size_t nspec(const gf_ctx* c) { return (size_t)c->g.nl * c->g.ny * c->g.l
 static int upload_real(gf_ctx* c, void* dst, const double* src, size_t n) {
   if (c->prec == GF_F64) {
     GF_CUDA(c, cudaMemcpyAsync(dst, src, n * 8, cudaMemcpyHostToDevice, c->stream));
+  } else if (c->prec == GF_DF64) {
+    std::vector<float> f(2 * n);
+    for (size_t i = 0; i < n; ++i) split_hl(src[i], &f[2 * i], &f[2 * i + 1]);
+    GF_CUDA(c, cudaMemcpyAsync(dst, f.data(), n * 8, cudaMemcpyHostToDevice, c->stream));
+    GF_CUDA(c, cudaStreamSynchronize(c->stream));
   } else {
     std::vector<float> f(n);
     for (size_t i = 0; i < n; ++i) f[i] = (float)src[i];
@@ -207,7 +235,9 @@ static Geom full_geom(const gf_ctx* c) {
   return g;
 }
 
-#define DISPATCH(c, fn, ...) ((c)->prec == GF_F64 ? fn<double>(__VA_ARGS__) : fn<float>(__VA_ARGS__))
+#define DISPATCH(c, fn, ...)                                      \
+  ((c)->prec == GF_F64 ? fn<double>(__VA_ARGS__)                  \
+                       : (c)->prec == GF_DF64 ? fn<df64>(__VA_ARGS__) : fn<float>(__VA_ARGS__))
 
 // symmetric Jacobi eigen-decomposition (small n), A overwritten, Q columns = eigenvectors
 static void jacobi_eig(int n, std::vector<double>& A, std::vector<double>& Q, std::vector<double>& lam) {
@@ -311,9 +341,11 @@ static int build(gf_ctx* c, const gf_config* cfg) {
   g.ldw = (g.kcut + 15) / 16 * 16;
   g.dkx = 2 * M_PI / k.Lx; g.dky = 2 * M_PI / k.Ly;
   g.inv_nxny = 1.0 / ((double)k.nx * k.ny);
-  g.dkx_f = (float)g.dkx; g.dky_f = (float)g.dky; g.inv_nxny_f = (float)g.inv_nxny;
+  split_hl(g.dkx, &g.dkx_f, &g.dkx_l);
+  split_hl(g.dky, &g.dky_f, &g.dky_l);
+  split_hl(g.inv_nxny, &g.inv_nxny_f, &g.inv_nxny_l);
   c->prec = k.precision;
-  c->rb = k.precision == GF_F64 ? 8 : 4;
+  c->rb = k.precision == GF_F32 ? 4 : 8;
   c->cb = 2 * c->rb;
   const int st = k.stepper;
   c->filtered = (st == GF_FILTEREDFORWARDEULER || st == GF_FILTEREDRK4 || st == GF_FILTEREDETDRK4 || st == GF_FILTEREDAB3);
@@ -449,6 +481,9 @@ static int build(gf_ctx* c, const gf_config* cfg) {
       !(c->phys = dalloc(c, (size_t)4 * g.nl * g.ny * g.nx * rb)))
     return fail(c, GF_ERR_NOMEM, "state buffers");
   m.D = c->D;
+  if (c->prec == GF_DF64 &&
+      !(c->stage = dalloc(c, std::max(nsp * cb, (size_t)g.nl * g.ny * g.nx * rb))))
+    return fail(c, GF_ERR_NOMEM, "df64 staging");
   if (c->kind == SK_RK4) {
     if (!(c->acc = dalloc(c, nsp * cb))) return fail(c, GF_ERR_NOMEM, "acc");
     if (c->hasL && !(c->X = dalloc(c, nsp * cb))) return fail(c, GF_ERR_NOMEM, "X");
@@ -498,6 +533,10 @@ static int build(gf_ctx* c, const gf_config* cfg) {
       etd_coeffs_kernel<double><<<nb, 256, 0, c->stream>>>((int)nt, dLr, dLi, k.dt, ncirc, rcirc, c->cplxL,
           (double*)c->etd[0], (double*)c->etd[1], (double*)c->etd[2], (double*)c->etd[3], (double*)c->etd[4],
           (double*)c->etd[5], g.nkr, g.ldk);
+    else if (c->prec == GF_DF64)
+      etd_coeffs_kernel<df64><<<nb, 256, 0, c->stream>>>((int)nt, dLr, dLi, k.dt, ncirc, rcirc, c->cplxL,
+          (df64*)c->etd[0], (df64*)c->etd[1], (df64*)c->etd[2], (df64*)c->etd[3], (df64*)c->etd[4],
+          (df64*)c->etd[5], g.nkr, g.ldk);
     else
       etd_coeffs_kernel<float><<<nb, 256, 0, c->stream>>>((int)nt, dLr, dLi, k.dt, ncirc, rcirc, c->cplxL,
           (float*)c->etd[0], (float*)c->etd[1], (float*)c->etd[2], (float*)c->etd[3], (float*)c->etd[4],
@@ -531,6 +570,9 @@ static int build(gf_ctx* c, const gf_config* cfg) {
         if (c->prec == GF_F64) {
           add_scalar_kernel<double><<<nb, 256, 0, c->stream>>>((double*)c->Qx2D, np, k.topographic_pv_gradient[0]);
           add_scalar_kernel<double><<<nb, 256, 0, c->stream>>>((double*)c->Qy2D, np, k.topographic_pv_gradient[1]);
+        } else if (c->prec == GF_DF64) {
+          add_scalar_kernel<df64><<<nb, 256, 0, c->stream>>>((df64*)c->Qx2D, np, k.topographic_pv_gradient[0]);
+          add_scalar_kernel<df64><<<nb, 256, 0, c->stream>>>((df64*)c->Qy2D, np, k.topographic_pv_gradient[1]);
         } else {
           add_scalar_kernel<float><<<nb, 256, 0, c->stream>>>((float*)c->Qx2D, np, k.topographic_pv_gradient[0]);
           add_scalar_kernel<float><<<nb, 256, 0, c->stream>>>((float*)c->Qy2D, np, k.topographic_pv_gradient[1]);
@@ -567,9 +609,14 @@ static int build(gf_ctx* c, const gf_config* cfg) {
   }
   // float mirrors of the per-element scalars
   m.Ueta = (m.etah != nullptr && m.U0 != 0.0);
-  m.ell_inv2_f = (float)m.ell_inv2; m.U0_f = (float)m.U0; m.mu_f = (float)m.mu;
-  for (int a = 0; a < MAXL; ++a) m.lam_f[a] = (float)m.lam[a];
-  for (int a = 0; a < MAXL * MAXL; ++a) { m.V_f[a] = (float)m.V[a]; m.Vinv_f[a] = (float)m.Vinv[a]; }
+  split_hl(m.ell_inv2, &m.ell_inv2_f, &m.ell_inv2_l);
+  split_hl(m.U0, &m.U0_f, &m.U0_l);
+  split_hl(m.mu, &m.mu_f, &m.mu_l);
+  for (int a = 0; a < MAXL; ++a) split_hl(m.lam[a], &m.lam_f[a], &m.lam_l[a]);
+  for (int a = 0; a < MAXL * MAXL; ++a) {
+    split_hl(m.V[a], &m.V_f[a], &m.V_l[a]);
+    split_hl(m.Vinv[a], &m.Vinv_f[a], &m.Vinv_l[a]);
+  }
   // ----- forcing buffers
   if (k.forcing_kind != GF_FORCING_NONE) {
     if (!(c->Fh = dalloc(c, nsp * cb))) return fail(c, GF_ERR_NOMEM, "forcing");
@@ -591,7 +638,8 @@ extern "C" int gf_create(const gf_config* cfg, void* stream, gf_ctx** out) {
   *out = nullptr;
   const gf_config& k = *cfg;
   if (k.module < 0 || k.module > 3) return fail(nullptr, GF_ERR_ARG, "unknown module");
-  if (k.precision != GF_F32 && k.precision != GF_F64) return fail(nullptr, GF_ERR_ARG, "unknown precision");
+  if (k.precision != GF_F32 && k.precision != GF_F64 && k.precision != GF_DF64)
+    return fail(nullptr, GF_ERR_ARG, "unknown precision");
   if (k.stepper < 0 || k.stepper > 7) return fail(nullptr, GF_ERR_ARG, "unknown stepper");
   if (k.nx <= 0 || k.ny <= 0 || !(k.Lx > 0) || !(k.Ly > 0) || !(k.dt > 0))
     return fail(nullptr, GF_ERR_ARG, "nx, ny, Lx, Ly and dt must be positive");
@@ -643,17 +691,64 @@ extern "C" int gf_get_dims(const gf_ctx* c, int32_t* nkr, int32_t* ny, int32_t* 
 }
 
 // ------------------------------------------------------------------------------- state
+static int convert_launch(gf_ctx* c, bool to_df, const void* src, size_t ss, void* dst, size_t ds, size_t rows,
+                          size_t w) {
+  const int nb = (int)std::min<size_t>((rows * w + 255) / 256, 4096);
+  if (to_df) to_df64_kernel<<<nb, 256, 0, c->stream>>>((const double*)src, ss, (df64*)dst, ds, rows, w);
+  else from_df64_kernel<<<nb, 256, 0, c->stream>>>((const df64*)src, ss, (double*)dst, ds, rows, w);
+  GF_CUDA(c, cudaGetLastError());
+  return GF_OK;
+}
+
+// caller spectral array (Julia layout, row stride nkr) -> internal array (row stride ldk)
 static int copy_spec_in(gf_ctx* c, void* dst, const void* src, int where) {
   const Geom& g = c->g;
-  GF_CUDA(c, cudaMemcpy2DAsync(dst, g.ldk * c->cb, src, g.nkr * c->cb, g.nkr * c->cb, (size_t)g.ny * g.nl,
-                               where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream));
+  const cudaMemcpyKind kind = where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  if (c->prec == GF_DF64) {
+    GF_CUDA(c, cudaMemcpyAsync(c->stage, src, (size_t)g.nkr * g.ny * g.nl * 16, kind, c->stream));
+    if (int r = convert_launch(c, true, c->stage, 2 * (size_t)g.nkr, dst, 2 * (size_t)g.ldk, (size_t)g.ny * g.nl,
+                               2 * (size_t)g.nkr)) return r;
+  } else {
+    GF_CUDA(c, cudaMemcpy2DAsync(dst, g.ldk * c->cb, src, g.nkr * c->cb, g.nkr * c->cb, (size_t)g.ny * g.nl, kind,
+                                 c->stream));
+  }
   if (where == GF_HOST) GF_CUDA(c, cudaStreamSynchronize(c->stream));
   return GF_OK;
 }
 static int copy_spec_out(gf_ctx* c, void* dst, const void* src, int where) {
   const Geom& g = c->g;
-  GF_CUDA(c, cudaMemcpy2DAsync(dst, g.nkr * c->cb, src, g.ldk * c->cb, g.nkr * c->cb, (size_t)g.ny * g.nl,
-                               where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->stream));
+  const cudaMemcpyKind kind = where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  if (c->prec == GF_DF64) {
+    if (int r = convert_launch(c, false, src, 2 * (size_t)g.ldk, c->stage, 2 * (size_t)g.nkr, (size_t)g.ny * g.nl,
+                               2 * (size_t)g.nkr)) return r;
+    GF_CUDA(c, cudaMemcpyAsync(dst, c->stage, (size_t)g.nkr * g.ny * g.nl * 16, kind, c->stream));
+  } else {
+    GF_CUDA(c, cudaMemcpy2DAsync(dst, g.nkr * c->cb, src, g.ldk * c->cb, g.nkr * c->cb, (size_t)g.ny * g.nl, kind,
+                                 c->stream));
+  }
+  if (where == GF_HOST) GF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GF_OK;
+}
+// caller physical array (nl x ny x nx reals) <-> internal physical array
+static int copy_phys_in(gf_ctx* c, void* dst, const void* src, int where) {
+  const size_t n = (size_t)c->g.nl * c->g.ny * c->g.nx;
+  const cudaMemcpyKind kind = where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  if (c->prec == GF_DF64) {
+    GF_CUDA(c, cudaMemcpyAsync(c->stage, src, n * 8, kind, c->stream));
+    return convert_launch(c, true, c->stage, n, dst, n, 1, n);
+  }
+  GF_CUDA(c, cudaMemcpyAsync(dst, src, n * c->rb, kind, c->stream));
+  return GF_OK;
+}
+static int copy_phys_out(gf_ctx* c, void* dst, const void* src, int where) {
+  const size_t n = (size_t)c->g.nl * c->g.ny * c->g.nx;
+  const cudaMemcpyKind kind = where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  if (c->prec == GF_DF64) {
+    if (int r = convert_launch(c, false, src, n, c->stage, n, 1, n)) return r;
+    GF_CUDA(c, cudaMemcpyAsync(dst, c->stage, n * 8, kind, c->stream));
+  } else {
+    GF_CUDA(c, cudaMemcpyAsync(dst, src, n * c->rb, kind, c->stream));
+  }
   if (where == GF_HOST) GF_CUDA(c, cudaStreamSynchronize(c->stream));
   return GF_OK;
 }
@@ -699,17 +794,14 @@ extern "C" int gf_get_field(gf_ctx* c, int which, void* out, int where) {
   if (!c || !out) return GF_ERR_ARG;
   if (which < 0 || which > 3) return fail(c, GF_ERR_ARG, "unknown field");
   const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->rb;
-  GF_CUDA(c, cudaMemcpyAsync(out, (char*)c->phys + which * pf, pf,
-                             where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->stream));
-  if (where == GF_HOST) GF_CUDA(c, cudaStreamSynchronize(c->stream));
-  return GF_OK;
+  return copy_phys_out(c, out, (char*)c->phys + which * pf, where);
 }
 
 extern "C" int gf_fwdtransform(gf_ctx* c, void* fieldh, const void* field, int where) {
   if (!c || !fieldh || !field) return GF_ERR_ARG;
   const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->rb;
   void* ph = (char*)c->phys + 3 * pf;
-  GF_CUDA(c, cudaMemcpyAsync(ph, field, pf, where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream));
+  if (int r = copy_phys_in(c, ph, field, where)) return r;
   if (int r = fwd_transform(c, ph, c->tmp_spec, 0)) return r;
   return copy_spec_out(c, fieldh, c->tmp_spec, where);
 }
@@ -720,9 +812,7 @@ extern "C" int gf_invtransform(gf_ctx* c, void* field, const void* fieldh, int w
   if (int r = copy_spec_in(c, c->tmp_spec, fieldh, where)) return r;
   void* ph = (char*)c->phys + 3 * pf;
   if (int r = inv_transform(c, c->tmp_spec, SF_RAW, 0, ph)) return r;
-  GF_CUDA(c, cudaMemcpyAsync(field, ph, pf, where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->stream));
-  if (where == GF_HOST) GF_CUDA(c, cudaStreamSynchronize(c->stream));
-  return GF_OK;
+  return copy_phys_out(c, field, ph, where);
 }
 
 extern "C" int gf_set_physical(gf_ctx* c, int which, const void* field, int where) {
@@ -732,7 +822,7 @@ extern "C" int gf_set_physical(gf_ctx* c, int which, const void* field, int wher
     return fail(c, GF_ERR_ARG, "set_physical supports q/zeta/b, and psi for MultiLayerQG");
   const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->rb;
   void* ph = (char*)c->phys + 3 * pf;
-  GF_CUDA(c, cudaMemcpyAsync(ph, field, pf, where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream));
+  if (int r = copy_phys_in(c, ph, field, where)) return r;
   if (which == GF_FIELD_PSI) {
     // q = irfft(S rfft(psi)), then set_q!
     if (int r = fwd_transform(c, ph, c->tmp_spec, 0)) return r;
@@ -787,7 +877,8 @@ static StepArgs stage_args(gf_ctx* c, int stage, double tstage) {
   s.draw = (stage == 1);
   if (s.fkind == FK_HARMONIC) s.fscale = std::cos(c->cfg.forcing_omega * tstage + c->cfg.forcing_phase);
   else s.fscale = 1.0;
-  s.dt_f = (float)s.dt; s.fscale_f = (float)s.fscale;
+  split_hl(s.dt, &s.dt_f, &s.dt_l);
+  split_hl(s.fscale, &s.fscale_f, &s.fscale_l);
   return s;
 }
 
@@ -898,7 +989,6 @@ extern "C" int gf_calcN(gf_ctx* c, void* N, void* sol, double t, int where) {
   // products, forward FFTs, N = -i kr A - i l B - C + extras + forcing, written to tmp_spec2
   s = stage_args(c, 1, t);
   s.kind = SK_NOUT; s.sol = c->tmp_spec; s.acc = c->tmp_spec2; s.do_fwd = 1; s.do_inv = 0;
-  s.dt_f = (float)s.dt; s.fscale_f = (float)s.fscale;
   s.draw = (t == c->t);  // stochastic forcing is redrawn only when t == clock.t
   if (s.fkind >= FK_STOCH && !s.draw) s.Fh = c->Fstore;
   if (int r = launch_stage(c, s, 1)) return r;

@@ -1,0 +1,132 @@
+// Dispatch from runtime sizes to the per-size launchers, and the element-wise / reduction
+// launchers (the FFT kernels themselves are instantiated in the gf_k_<type>_<n>.cu units).
+#include "gf_kernels.cuh"
+#include "gf_launch.cuh"
+
+namespace gf {
+
+template <class T>
+cudaError_t launch_row(const Geom& g, const ModArgs& m, const Bufs& b, cudaStream_t st) {
+  switch (g.nx) {
+    case 32: return launch_row_n<T, 32>(g, m, b, st);
+    case 64: return launch_row_n<T, 64>(g, m, b, st);
+    case 128: return launch_row_n<T, 128>(g, m, b, st);
+    case 256: return launch_row_n<T, 256>(g, m, b, st);
+    case 512: return launch_row_n<T, 512>(g, m, b, st);
+    case 1024: return launch_row_n<T, 1024>(g, m, b, st);
+    case 2048: return launch_row_n<T, 2048>(g, m, b, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <class T>
+cudaError_t launch_col(const Geom& g, const ModArgs& m, const StepArgs& s, const Bufs& b, cudaStream_t st) {
+  switch (g.ny) {
+    case 32: return launch_col_n<T, 32>(g, m, s, b, st);
+    case 64: return launch_col_n<T, 64>(g, m, s, b, st);
+    case 128: return launch_col_n<T, 128>(g, m, s, b, st);
+    case 256: return launch_col_n<T, 256>(g, m, s, b, st);
+    case 512: return launch_col_n<T, 512>(g, m, s, b, st);
+    case 1024: return launch_col_n<T, 1024>(g, m, s, b, st);
+    case 2048: return launch_col_n<T, 2048>(g, m, s, b, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <class T>
+cudaError_t launch_col_inv(const Geom& g, const ModArgs& m, const void* src, int kind, int mask, const Bufs& b,
+                           cudaStream_t st) {
+  switch (g.ny) {
+    case 32: return launch_col_inv_n<T, 32>(g, m, src, kind, mask, b, st);
+    case 64: return launch_col_inv_n<T, 64>(g, m, src, kind, mask, b, st);
+    case 128: return launch_col_inv_n<T, 128>(g, m, src, kind, mask, b, st);
+    case 256: return launch_col_inv_n<T, 256>(g, m, src, kind, mask, b, st);
+    case 512: return launch_col_inv_n<T, 512>(g, m, src, kind, mask, b, st);
+    case 1024: return launch_col_inv_n<T, 1024>(g, m, src, kind, mask, b, st);
+    case 2048: return launch_col_inv_n<T, 2048>(g, m, src, kind, mask, b, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <class T>
+cudaError_t launch_row_c2r(const Geom& g, const Bufs& b, int nf, void* out, cudaStream_t st) {
+  switch (g.nx) {
+    case 32: return launch_row_c2r_n<T, 32>(g, b, nf, out, st);
+    case 64: return launch_row_c2r_n<T, 64>(g, b, nf, out, st);
+    case 128: return launch_row_c2r_n<T, 128>(g, b, nf, out, st);
+    case 256: return launch_row_c2r_n<T, 256>(g, b, nf, out, st);
+    case 512: return launch_row_c2r_n<T, 512>(g, b, nf, out, st);
+    case 1024: return launch_row_c2r_n<T, 1024>(g, b, nf, out, st);
+    case 2048: return launch_row_c2r_n<T, 2048>(g, b, nf, out, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <class T>
+cudaError_t launch_row_r2c(const Geom& g, const Bufs& b, int nf, const void* in, cudaStream_t st) {
+  switch (g.nx) {
+    case 32: return launch_row_r2c_n<T, 32>(g, b, nf, in, st);
+    case 64: return launch_row_r2c_n<T, 64>(g, b, nf, in, st);
+    case 128: return launch_row_r2c_n<T, 128>(g, b, nf, in, st);
+    case 256: return launch_row_r2c_n<T, 256>(g, b, nf, in, st);
+    case 512: return launch_row_r2c_n<T, 512>(g, b, nf, in, st);
+    case 1024: return launch_row_r2c_n<T, 1024>(g, b, nf, in, st);
+    case 2048: return launch_row_r2c_n<T, 2048>(g, b, nf, in, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <class T>
+cudaError_t launch_col_fwd(const Geom& g, const Bufs& b, int nf, void* out, int zero_mean, cudaStream_t st) {
+  switch (g.ny) {
+    case 32: return launch_col_fwd_n<T, 32>(g, b, nf, out, zero_mean, st);
+    case 64: return launch_col_fwd_n<T, 64>(g, b, nf, out, zero_mean, st);
+    case 128: return launch_col_fwd_n<T, 128>(g, b, nf, out, zero_mean, st);
+    case 256: return launch_col_fwd_n<T, 256>(g, b, nf, out, zero_mean, st);
+    case 512: return launch_col_fwd_n<T, 512>(g, b, nf, out, zero_mean, st);
+    case 1024: return launch_col_fwd_n<T, 1024>(g, b, nf, out, zero_mean, st);
+    case 2048: return launch_col_fwd_n<T, 2048>(g, b, nf, out, zero_mean, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <class T>
+cudaError_t launch_diag(const Geom& g, const ModArgs& m, const void* sol, const void* prevsol, const void* Fh,
+                        uint32_t mask, double* partial, int nblocks, cudaStream_t st) {
+  diag_kernel<T><<<nblocks, DIAG_BLOCK, 0, st>>>(g, m, static_cast<const cplx<T>*>(sol),
+                                                 static_cast<const cplx<T>*>(prevsol),
+                                                 static_cast<const cplx<T>*>(Fh), mask, partial);
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_mask_inplace(const Geom& g, void* sol, cudaStream_t st) {
+  mask_inplace_kernel<T><<<256, 256, 0, st>>>(g, static_cast<cplx<T>*>(sol));
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_spec_apply(const Geom& g, const ModArgs& m, const void* in, void* out, int op, cudaStream_t st) {
+  spec_apply_kernel<T><<<256, 256, 0, st>>>(g, m, static_cast<const cplx<T>*>(in), static_cast<cplx<T>*>(out), op);
+  return cudaGetLastError();
+}
+
+
+#define GF_INST_DISPATCH(T)                                                                                    \
+  template cudaError_t launch_row<T>(const Geom&, const ModArgs&, const Bufs&, cudaStream_t);                   \
+  template cudaError_t launch_col<T>(const Geom&, const ModArgs&, const StepArgs&, const Bufs&, cudaStream_t);  \
+  template cudaError_t launch_col_inv<T>(const Geom&, const ModArgs&, const void*, int, int, const Bufs&,       \
+                                         cudaStream_t);                                                        \
+  template cudaError_t launch_row_c2r<T>(const Geom&, const Bufs&, int, void*, cudaStream_t);                   \
+  template cudaError_t launch_row_r2c<T>(const Geom&, const Bufs&, int, const void*, cudaStream_t);             \
+  template cudaError_t launch_col_fwd<T>(const Geom&, const Bufs&, int, void*, int, cudaStream_t);              \
+  template cudaError_t launch_diag<T>(const Geom&, const ModArgs&, const void*, const void*, const void*,       \
+                                      uint32_t, double*, int, cudaStream_t);                                   \
+  template cudaError_t launch_mask_inplace<T>(const Geom&, void*, cudaStream_t);                                \
+  template cudaError_t launch_spec_apply<T>(const Geom&, const ModArgs&, const void*, void*, int, cudaStream_t);
+
+GF_INST_DISPATCH(float)
+GF_INST_DISPATCH(double)
+GF_INST_DISPATCH(df64)
+
+}  // namespace gf

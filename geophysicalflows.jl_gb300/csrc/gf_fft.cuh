@@ -24,9 +24,59 @@ namespace gf {
 
 constexpr int TWN = 4096;  // twiddle table length (largest supported transform)
 
+// ---------------------------------------------------------------------------------------
+// df64: a double-word ("double-float") number hi + lo with |lo| <= ulp(hi)/2, giving a
+// 48-bit significand with FP32 arithmetic.  GB300 runs FP64 at a small fraction of its FP32
+// rate; the FP64-plain mode of this library computes in df64 instead.  Algorithms: Knuth's
+// TwoSum and Dekker's FastTwoSum, FMA-based TwoProd, and the double-word sum (TwoSum of the
+// high parts plus the low parts, renormalised -- its error is bounded relative to
+// |a| + |b|, which is what a normwise FFT error bound needs) and product (TwoProd plus the
+// cross terms) analysed by Joldes, Muller & Popescu, "Tight and rigorous error bounds for
+// basic building blocks of double-word arithmetic" (ACM TOMS 2017).
+// ---------------------------------------------------------------------------------------
+struct __align__(8) df64 {
+  float hi, lo;
+  df64() = default;
+  __host__ __device__ constexpr df64(float h, float l) : hi(h), lo(l) {}
+  __host__ __device__ constexpr df64(int i) : hi((float)i), lo(0.0f) {}  // exact for |i| < 2^24
+  // from a double: constant-folded for compile-time constants; FP64 work otherwise
+  __host__ __device__ constexpr df64(double d) : hi((float)d), lo((float)(d - (double)(float)d)) {}
+};
+__host__ __device__ __forceinline__ double to_double(df64 a) { return (double)a.hi + (double)a.lo; }
+__host__ __device__ __forceinline__ double to_double(double a) { return a; }
+__host__ __device__ __forceinline__ double to_double(float a) { return (double)a; }
+
+__device__ __forceinline__ df64 fast_two_sum(float a, float b) {  // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return df64(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ df64 operator+(df64 a, df64 b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bb = __fsub_rn(s, a.hi);
+  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));  // TwoSum error
+  return fast_two_sum(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ df64 operator-(df64 a) { return df64(-a.hi, -a.lo); }
+__device__ __forceinline__ df64 operator-(df64 a, df64 b) { return a + (-b); }
+__device__ __forceinline__ df64 operator*(df64 a, df64 b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);  // TwoProd error
+  e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e));
+  return fast_two_sum(p, e);
+}
+__device__ __forceinline__ df64 operator/(df64 a, df64 b) {
+  const float q1 = __fdiv_rn(a.hi, b.hi);
+  const df64 r = a - b * df64(q1, 0.0f);
+  const float q2 = __fdiv_rn(r.hi, b.hi);
+  return fast_two_sum(q1, q2);
+}
+__device__ __forceinline__ bool operator==(df64 a, df64 b) { return a.hi == b.hi && a.lo == b.lo; }
+__device__ __forceinline__ bool operator!=(df64 a, df64 b) { return !(a == b); }
+
 template <class T> struct cplx;
 template <> struct __align__(8) cplx<float> { float x, y; };
 template <> struct __align__(16) cplx<double> { double x, y; };
+template <> struct __align__(16) cplx<df64> { df64 x, y; };
 
 template <class T> __host__ __device__ __forceinline__ cplx<T> mk(T a, T b) { cplx<T> r; r.x = a; r.y = b; return r; }
 template <class T> __device__ __forceinline__ cplx<T> operator+(cplx<T> a, cplx<T> b) { return mk<T>(a.x + b.x, a.y + b.y); }

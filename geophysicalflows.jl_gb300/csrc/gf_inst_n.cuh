@@ -1,0 +1,103 @@
+// Per-size launchers: block shapes for one FFT length NN and precision T, and the launch.
+#pragma once
+#include "gf_kernels.cuh"
+#include "gf_launch.cuh"
+
+namespace gf {
+
+template <class T, int NN>
+cudaError_t launch_row_n(const Geom& g, const ModArgs& m, const Bufs& b, cudaStream_t st) {
+
+  cudaError_t err = cudaSuccess;
+  const size_t e = sizeof(cplx<T>);
+  const int B = pick_B(NN, RADIX<T>, e, 3, g.ny / 2);
+  const size_t sm = (size_t)B * 3 * row_stride<T>(NN, NN / RADIX<T>) * e;
+  auto k = row_nl_kernel<T, NN, RADIX<T>>;
+  if ((err = set_smem(k, sm)) != cudaSuccess) return err;
+  k<<<g.ny / 2 / B, B * (NN / RADIX<T>), sm, st>>>(g, m, b, B);
+  return cudaGetLastError();
+}
+
+template <class T, int NN>
+cudaError_t launch_col_n(const Geom& g, const ModArgs& m, const StepArgs& s, const Bufs& b, cudaStream_t st) {
+
+  cudaError_t err = cudaSuccess;
+  const size_t e = sizeof(cplx<T>);
+  const int C = pick_C(NN, RADIX<T>, g.nkr, [&](int c) { return col_stage_smem(NN, c, col_stride<T>(NN, c), g.nl, e); });
+  Geom g2 = g;
+  g2.cs = col_stride<T>(NN, C);
+  const size_t sm = col_stage_smem(NN, C, g2.cs, g.nl, e);
+  auto k = col_stage_kernel<T, NN, RADIX<T>>;
+  if ((err = set_smem(k, sm)) != cudaSuccess) return err;
+  k<<<(g.nkr + C - 1) / C, C * (NN / RADIX<T>), sm, st>>>(g2, m, s, b, C);
+  return cudaGetLastError();
+}
+
+template <class T, int NN>
+cudaError_t launch_col_inv_n(const Geom& g, const ModArgs& m, const void* src, int kind, int mask, const Bufs& b,
+                           cudaStream_t st) {
+
+  cudaError_t err;
+  const size_t e = sizeof(cplx<T>);
+  const int C = pick_C(NN, RADIX<T>, g.nkr, [&](int c) { return (size_t)c * col_stride<T>(NN, c) * e; });
+  Geom g2 = g;
+  g2.cs = col_stride<T>(NN, C);
+  const size_t sm = (size_t)C * g2.cs * e;
+  auto k = col_inv_generic<T, NN, RADIX<T>>;
+  if ((err = set_smem(k, sm)) != cudaSuccess) return err;
+  k<<<(g.nkr + C - 1) / C, C * (NN / RADIX<T>), sm, st>>>(g2, m, src, kind, mask, b, C);
+  return cudaGetLastError();
+}
+
+template <class T, int NN>
+cudaError_t launch_row_c2r_n(const Geom& g, const Bufs& b, int nf, void* out, cudaStream_t st) {
+
+  cudaError_t err;
+  const size_t e = sizeof(cplx<T>);
+  const int B = pick_B(NN, RADIX<T>, e, 1, g.ny / 2);
+  const size_t sm = (size_t)B * row_stride<T>(NN, NN / RADIX<T>) * e;
+  auto k = row_c2r_generic<T, NN, RADIX<T>>;
+  if ((err = set_smem(k, sm)) != cudaSuccess) return err;
+  k<<<g.ny / 2 / B, B * (NN / RADIX<T>), sm, st>>>(g, b, nf, static_cast<T*>(out), B);
+  return cudaGetLastError();
+}
+
+template <class T, int NN>
+cudaError_t launch_row_r2c_n(const Geom& g, const Bufs& b, int nf, const void* in, cudaStream_t st) {
+
+  cudaError_t err;
+  const size_t e = sizeof(cplx<T>);
+  const int B = pick_B(NN, RADIX<T>, e, 1, g.ny / 2);
+  const size_t sm = (size_t)B * row_stride<T>(NN, NN / RADIX<T>) * e;
+  auto k = row_r2c_generic<T, NN, RADIX<T>>;
+  if ((err = set_smem(k, sm)) != cudaSuccess) return err;
+  k<<<g.ny / 2 / B, B * (NN / RADIX<T>), sm, st>>>(g, b, nf, static_cast<const T*>(in), B);
+  return cudaGetLastError();
+}
+
+template <class T, int NN>
+cudaError_t launch_col_fwd_n(const Geom& g, const Bufs& b, int nf, void* out, int zero_mean, cudaStream_t st) {
+
+  cudaError_t err;
+  const size_t e = sizeof(cplx<T>);
+  const int C = pick_C(NN, RADIX<T>, g.nkr, [&](int c) { return (size_t)c * col_stride<T>(NN, c) * e; });
+  Geom g2 = g;
+  g2.cs = col_stride<T>(NN, C);
+  const size_t sm = (size_t)C * g2.cs * e;
+  auto k = col_fwd_generic<T, NN, RADIX<T>>;
+  if ((err = set_smem(k, sm)) != cudaSuccess) return err;
+  k<<<(g.nkr + C - 1) / C, C * (NN / RADIX<T>), sm, st>>>(g2, b, nf, static_cast<cplx<T>*>(out), zero_mean, C);
+  return cudaGetLastError();
+}
+
+#define GF_INST_N(T, NN)                                                                                       \
+  template cudaError_t launch_row_n<T, NN>(const Geom&, const ModArgs&, const Bufs&, cudaStream_t);             \
+  template cudaError_t launch_col_n<T, NN>(const Geom&, const ModArgs&, const StepArgs&, const Bufs&,           \
+                                           cudaStream_t);                                                      \
+  template cudaError_t launch_col_inv_n<T, NN>(const Geom&, const ModArgs&, const void*, int, int, const Bufs&, \
+                                               cudaStream_t);                                                  \
+  template cudaError_t launch_row_c2r_n<T, NN>(const Geom&, const Bufs&, int, void*, cudaStream_t);             \
+  template cudaError_t launch_row_r2c_n<T, NN>(const Geom&, const Bufs&, int, const void*, cudaStream_t);       \
+  template cudaError_t launch_col_fwd_n<T, NN>(const Geom&, const Bufs&, int, void*, int, cudaStream_t);
+
+}  // namespace gf

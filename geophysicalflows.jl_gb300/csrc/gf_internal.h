@@ -7,6 +7,7 @@
 
 namespace gf {
 
+struct df64;
 template <class T> struct cplx;
 
 enum Module { MOD_TWODNS = 0, MOD_SLQG = 1, MOD_MLQG = 2, MOD_SQG = 3 };
@@ -24,6 +25,7 @@ struct Geom {
   int lA, lB;  // l indices in [lA, lB] are aliased (empty when lA > lB)
   double dkx, dky, inv_nxny;
   float dkx_f, dky_f, inv_nxny_f;  // float copies (the FP32 kernels never touch FP64)
+  float dkx_l, dky_l, inv_nxny_l;  // low words: (x_f, x_l) is the df64 value
   int cs;                          // column stride (elements) of the column kernels' buffers
 };
 
@@ -52,6 +54,8 @@ struct ModArgs {
   int Ueta;              // U0 != 0 and etah present
   float ell_inv2_f, U0_f, mu_f;
   float lam_f[MAXL], V_f[MAXL * MAXL], Vinv_f[MAXL * MAXL];
+  float ell_inv2_l, U0_l, mu_l;
+  float lam_l[MAXL], V_l[MAXL * MAXL], Vinv_l[MAXL * MAXL];
 };
 
 struct StepArgs {
@@ -67,13 +71,20 @@ struct StepArgs {
   void* Fstore;        // stochastic draw written at the first stage
   void* prevsol;       // sol at the first stage (stochastic budgets)
   uint64_t seed, step;
-  float dt_f, fscale_f;
+  float dt_f, fscale_f, dt_l, fscale_l;
 };
 
-// value of a host-prepared scalar in the arithmetic type T
-template <class T> __host__ __device__ __forceinline__ T sel(double d, float f);
-template <> __host__ __device__ __forceinline__ double sel<double>(double d, float) { return d; }
-template <> __host__ __device__ __forceinline__ float sel<float>(double, float f) { return f; }
+// value of a host-prepared scalar (double d, its float rounding h and the remainder l) in
+// the arithmetic type T; the kernels never convert doubles at run time
+template <class T> __host__ __device__ __forceinline__ T sel(double d, float h, float l);
+template <> __host__ __device__ __forceinline__ double sel<double>(double d, float, float) { return d; }
+template <> __host__ __device__ __forceinline__ float sel<float>(double, float h, float) { return h; }
+template <> __host__ __device__ __forceinline__ df64 sel<df64>(double, float h, float l) { return df64(h, l); }
+// split a double into the (h, l) pair used by sel
+inline void split_hl(double d, float* h, float* l) {
+  *h = (float)d;
+  *l = (float)(d - (double)*h);
+}
 
 struct Bufs {
   const void* twid;  // TWN twiddles

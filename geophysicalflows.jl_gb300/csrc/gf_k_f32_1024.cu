@@ -1,0 +1,6 @@
+// FFT-length-1024 kernels for float (one translation unit per precision and length).
+#include "gf_inst_n.cuh"
+
+namespace gf {
+GF_INST_N(float, 1024)
+}  // namespace gf

@@ -1,0 +1,6 @@
+// FFT-length-64 kernels for double (one translation unit per precision and length).
+#include "gf_inst_n.cuh"
+
+namespace gf {
+GF_INST_N(double, 64)
+}  // namespace gf

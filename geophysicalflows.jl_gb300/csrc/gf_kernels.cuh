@@ -78,6 +78,13 @@ __device__ __forceinline__ cplx<T> draw(uint64_t e, uint64_t step, uint64_t seed
   return mk<T>(r * co, r * s);
 }
 
+// df64: the draw is made in FP64 (forcing elements, first stage only) and split
+template <>
+__device__ __forceinline__ cplx<df64> draw<df64>(uint64_t e, uint64_t step, uint64_t seed, int phase) {
+  const cplx<double> z = draw<double>(e, step, seed, phase);
+  return mk<df64>(df64(z.x), df64(z.y));
+}
+
 // The per-layer psi factor f of single-layer modules (psi = f X) at |k|^2 = K2.
 template <class T>
 __device__ __forceinline__ T psi_factor(int kind, T K2, T ell2, const void* mult, size_t ti) {
@@ -149,20 +156,21 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? GF_MINBLOCKS_F32 : 1)
   const bool kin = kr < g.nkr;
   const cplx<T>* tw = static_cast<const cplx<T>*>(b.twid);
   const size_t lstride = (size_t)g.ny * g.ldk;
-  const T dky = sel<T>(g.dky, g.dky_f), krT = T(kr) * sel<T>(g.dkx, g.dkx_f);
-  const T dt = sel<T>(s.dt, s.dt_f), ell2 = sel<T>(m.ell_inv2, m.ell_inv2_f), muT = sel<T>(m.mu, m.mu_f);
+  const T dky = sel<T>(g.dky, g.dky_f, g.dky_l), krT = T(kr) * sel<T>(g.dkx, g.dkx_f, g.dkx_l);
+  const T dt = sel<T>(s.dt, s.dt_f, s.dt_l), ell2 = sel<T>(m.ell_inv2, m.ell_inv2_f, m.ell_inv2_l), muT = sel<T>(m.mu, m.mu_f, m.mu_l);
   if (m.psi_kind == PSI_EIGEN) {
     for (int a = tid; a < MAXL + 2 * MAXL * MAXL; a += blockDim.x)
-      eig[a] = a < MAXL ? sel<T>(m.lam[a], m.lam_f[a])
-             : a < MAXL + MAXL * MAXL ? sel<T>(m.V[a - MAXL], m.V_f[a - MAXL])
-                                      : sel<T>(m.Vinv[a - MAXL - MAXL * MAXL], m.Vinv_f[a - MAXL - MAXL * MAXL]);
+      eig[a] = a < MAXL ? sel<T>(m.lam[a], m.lam_f[a], m.lam_l[a])
+             : a < MAXL + MAXL * MAXL ? sel<T>(m.V[a - MAXL], m.V_f[a - MAXL], m.V_l[a - MAXL])
+                                      : sel<T>(m.Vinv[a - MAXL - MAXL * MAXL], m.Vinv_f[a - MAXL - MAXL * MAXL],
+                                               m.Vinv_l[a - MAXL - MAXL * MAXL]);
   }
 
   if (s.do_fwd) {
     const cplx<T>* P = static_cast<const cplx<T>*>(b.P);
     const int nslot = 1 + m.hasB + m.hasC;
     const int nseq = nl * nslot;
-    const T fscale = sel<T>(s.fscale, s.fscale_f), U0 = sel<T>(m.U0, m.U0_f);
+    const T fscale = sel<T>(s.fscale, s.fscale_f, s.fscale_l), U0 = sel<T>(m.U0, m.U0_f, m.U0_l);
     // asynchronous copy of product field q = L * nslot + f into work buffer Fb
     auto issue = [&](int q, cplx<T>* Fb) {
       const int L = q / nslot, f = q - L * nslot;
@@ -213,12 +221,11 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? GF_MINBLOCKS_F32 : 1)
           const size_t ti = (size_t)j * g.ldk + kr;       // table index
           const size_t si = (size_t)L * lstride + ti;     // state index
           const bool keep = kept(g, kr, j);
-          const T mk_ = keep ? T(1) : T(0);
           cplx<T> N = XL[j * C];
           if (m.Ueta) N = N - (U0 * krT) * mul_i(static_cast<const cplx<T>*>(m.etah)[ti]);
           if (m.drag && L == nl - 1) N = N + static_cast<const cplx<T>*>(m.D)[ti];
           cplx<T>* sol = static_cast<cplx<T>*>(s.sol);
-          const cplx<T> solm = mk_ * sol[si];
+          const cplx<T> solm = keep ? sol[si] : czero<T>();
           // forcing
           if (s.fkind == FK_STATIC) {
             N = N + static_cast<const cplx<T>*>(s.Fh)[si];
@@ -255,7 +262,7 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? GF_MINBLOCKS_F32 : 1)
             cplx<T>* X = static_cast<cplx<T>*>(s.X);
             cplx<T>* acc = static_cast<cplx<T>*>(s.acc);
             cplx<T> Rv = N;
-            if (s.hasL) Rv = Rv + Lmul(s.stage == 1 ? solm : mk_ * X[si]);
+            if (s.hasL) Rv = Rv + Lmul(s.stage == 1 ? solm : (keep ? X[si] : czero<T>()));
             if (s.stage == 1) {
               acc[si] = T(1.0 / 6.0) * Rv;
               xn = solm + T(0.5) * dt * Rv;
@@ -265,13 +272,13 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? GF_MINBLOCKS_F32 : 1)
             } else {
               xn = finish(solm + dt * (acc[si] + T(1.0 / 6.0) * Rv));
             }
-            if (s.hasL && s.stage < 4) X[si] = mk_ * xn;
+            if (s.hasL && s.stage < 4) X[si] = keep ? xn : czero<T>();
           } else if (s.kind == SK_ETDRK4) {
             const int cx = s.cplxL;
             cplx<T>* acc = static_cast<cplx<T>*>(s.acc);
             if (s.stage == 1) {
               xn = mulc(ldc<T>(s.e2, ti, cx), solm, cx) + mulc(ldc<T>(s.zeta, ti, cx), N, cx);
-              static_cast<cplx<T>*>(s.s1)[si] = mk_ * xn;
+              static_cast<cplx<T>*>(s.s1)[si] = keep ? xn : czero<T>();
               static_cast<cplx<T>*>(s.N1)[si] = N;
               acc[si] = mulc(ldc<T>(s.alpha, ti, cx), N, cx);
             } else if (s.stage == 2) {
@@ -351,7 +358,7 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? GF_MINBLOCKS_F32 : 1)
   }
   // y-direction inverse FFT of (q, u, v) for every layer
   cplx<T>* W = static_cast<cplx<T>*>(b.W);
-  const T sc = sel<T>(g.inv_nxny, g.inv_nxny_f);
+  const T sc = sel<T>(g.inv_nxny, g.inv_nxny_f, g.inv_nxny_l);
   for (int L = 0; L < nl; ++L) {
     for (int f = 0; f < 3; ++f) {
       cplx<T>* Fb = ((L * 3 + f) & 1) ? F1 : F0;  // alternate so stores of one field overlap the next
@@ -515,13 +522,13 @@ __global__ void __launch_bounds__(512) col_inv_generic(Geom g, ModArgs m, const 
   const bool kin = kr < g.nkr;
   cplx<T>* F = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* Fc = F + c * cs;
-  const T krT = T(kr) * T(g.dkx), dky = T(g.dky);
+  const T krT = T(kr) * sel<T>(g.dkx, g.dkx_f, g.dkx_l), dky = sel<T>(g.dky, g.dky_f, g.dky_l);
   const cplx<T>* S = static_cast<const cplx<T>*>(src);
   const cplx<T>* tw = static_cast<const cplx<T>*>(b.twid);
   cplx<T>* W = static_cast<cplx<T>*>(b.W);
   const size_t lstride = (size_t)g.ny * g.ldk;
   const int nl = g.nl;
-  const T sc = T(g.inv_nxny);
+  const T sc = sel<T>(g.inv_nxny, g.inv_nxny_f, g.inv_nxny_l);
   for (int L = 0; L < nl; ++L) {
 #pragma unroll
     for (int i = 0; i < R; ++i) {
@@ -743,7 +750,7 @@ __global__ void __launch_bounds__(DIAG_BLOCK) diag_kernel(Geom g, ModArgs m, con
     if (m.module == MOD_MLQG) {
       // psi in double from the stored layer values
       cplx<double> Xd[MAXL], Pd[MAXL];
-      for (int a = 0; a < nl; ++a) { const cplx<T> x = sol[a * lstride + ti]; Xd[a] = mk<double>(x.x, x.y); }
+      for (int a = 0; a < nl; ++a) { const cplx<T> x = sol[a * lstride + ti]; Xd[a] = mk<double>(to_double(x.x), to_double(x.y)); }
       psi_all<double>(m, nl, K2, Xd, Pd, ti);
       for (int a = 0; a < nl; ++a) {
         const double pr = Pd[a].x, pi = Pd[a].y;
@@ -756,13 +763,13 @@ __global__ void __launch_bounds__(DIAG_BLOCK) diag_kernel(Geom g, ModArgs m, con
       continue;
     }
     const cplx<T> x0 = sol[ti];
-    const double sr = x0.x, si = x0.y, s2 = sr * sr + si * si;
+    const double sr = to_double(x0.x), si = to_double(x0.y), s2 = sr * sr + si * si;
     // forcing work term Re(S conj(F)), S = sol or (prevsol + sol)/2
     double wr = 0;
     if (Fh) {
       double ar = sr, ai = si;
-      if (prevsol) { ar = 0.5 * (sr + (double)prevsol[ti].x); ai = 0.5 * (si + (double)prevsol[ti].y); }
-      const double fr = Fh[ti].x, fi = Fh[ti].y;
+      if (prevsol) { ar = 0.5 * (sr + to_double(prevsol[ti].x)); ai = 0.5 * (si + to_double(prevsol[ti].y)); }
+      const double fr = to_double(Fh[ti].x), fi = to_double(Fh[ti].y);
       wr = ar * fr + ai * fi;
     }
     const double nu = m.nu, mu = m.mu_visc;
@@ -785,7 +792,7 @@ __global__ void __launch_bounds__(DIAG_BLOCK) diag_kernel(Geom g, ModArgs m, con
       v[0] = 0.5 * K2 * p2;
       v[1] = 0.5 * m.ell_inv2 * p2;
       double er = sr, ei = si;
-      if (m.etah) { er += (double)static_cast<const cplx<T>*>(m.etah)[ti].x; ei += (double)static_cast<const cplx<T>*>(m.etah)[ti].y; }
+      if (m.etah) { er += to_double(static_cast<const cplx<T>*>(m.etah)[ti].x); ei += to_double(static_cast<const cplx<T>*>(m.etah)[ti].y); }
       v[2] = 0.5 * (er * er + ei * ei);
       v[3] = k0 ? 0.0 : nu * powi(K2, nnu - 1) * s2;
       v[4] = k0 ? 0.0 : nu * powi(K2, nnu) * s2;
@@ -794,7 +801,7 @@ __global__ void __launch_bounds__(DIAG_BLOCK) diag_kernel(Geom g, ModArgs m, con
       v[7] = k0 ? 0.0 : mu * iK2 * s2;
       v[8] = k0 ? 0.0 : mu * s2;
     } else {  // SQG
-      const double M = static_cast<const T*>(m.mult)[ti];
+      const double M = to_double(static_cast<const T*>(m.mult)[ti]);
       v[0] = 0.5 * K2 * M * M * s2;
       v[1] = s2;
       v[2] = 0.5 * M * s2;

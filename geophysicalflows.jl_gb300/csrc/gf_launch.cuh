@@ -1,0 +1,80 @@
+// Launch layer shared by the dispatch unit and the per-size kernel units: block-shape rules
+// and the declarations of the per-size launchers (defined in gf_inst_n.cuh, instantiated one
+// FFT length and precision per translation unit so that the build parallelises).
+#pragma once
+#include "gf_fft.cuh"
+#include "gf_internal.h"
+
+namespace gf {
+
+constexpr int SMEM_CAP = 200 * 1024;
+
+inline int num_sms() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
+  }
+  return n;
+}
+
+// Columns per column-kernel block: aim at ~512 threads, but shrink until the grid has at
+// least two blocks per SM; keep shared memory under SMEM_CAP.  smem(C) gives the block's
+// dynamic shared-memory bytes for C columns.
+template <class F>
+inline int pick_C(int NY, int R, int nkr, F smem) {
+  const int TPF = NY / R;
+  int C = 512 / TPF;
+  if (C < 1) C = 1;
+  if (C > 16) C = 16;
+  while (C > 1 && (C * TPF > 512 || smem(C) > (size_t)SMEM_CAP)) C /= 2;
+  while (C > 1 && (nkr + C - 1) / C < 2 * num_sms()) C /= 2;
+  return C;
+}
+// Row pairs per row-kernel block (same rule: >= 2 blocks per SM when possible).
+inline int pick_B(int NX, int R, size_t elem, int nbufs, int npairs) {
+  const int TPF = NX / R;
+  int B = 256 / TPF;
+  if (B < 1) B = 1;
+  while (B > 1 && ((size_t)B * (NX + NX / R) * elem * nbufs > SMEM_CAP || B * TPF > 256 || npairs % B != 0)) B /= 2;
+  while (B > 1 && npairs / B < 2 * num_sms()) B /= 2;
+  return B;
+}
+
+// Column stride of the column kernels' work buffers: NY slots, staggered so that the C
+// columns a wavefront touches in the element mapping fall into disjoint banks.
+template <class T>
+inline int col_stride(int NY, int C) {
+  const int unit = wave_threads<T>();
+  return C > 1 ? NY + (unit / C > 1 ? unit / C : 1) : NY;
+}
+
+// Opt in to large dynamic shared memory and ask for the maximum shared-memory carveout
+// (the FFT kernels are shared-memory bound; L1 is not used for reuse here).
+template <class K>
+inline cudaError_t set_smem(K kernel, size_t bytes) {
+  static_assert(sizeof(K) > 0, "");
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  if (e != cudaSuccess) return e;
+  if (bytes > 48 * 1024) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  return cudaSuccess;
+}
+
+// Radix of the Stockham passes (FP32 tunable at build time; FP64 uses 8).
+#ifndef GF_RADIX_F32
+#define GF_RADIX_F32 8
+#endif
+template <class T>
+constexpr int RADIX = sizeof(T) == 4 ? GF_RADIX_F32 : 8;
+
+// per-size launchers (NN = FFT length along the transformed direction)
+template <class T, int NN> cudaError_t launch_row_n(const Geom&, const ModArgs&, const Bufs&, cudaStream_t);
+template <class T, int NN> cudaError_t launch_col_n(const Geom&, const ModArgs&, const StepArgs&, const Bufs&, cudaStream_t);
+template <class T, int NN> cudaError_t launch_col_inv_n(const Geom&, const ModArgs&, const void*, int, int, const Bufs&,
+                                                        cudaStream_t);
+template <class T, int NN> cudaError_t launch_row_c2r_n(const Geom&, const Bufs&, int, void*, cudaStream_t);
+template <class T, int NN> cudaError_t launch_row_r2c_n(const Geom&, const Bufs&, int, const void*, cudaStream_t);
+template <class T, int NN> cudaError_t launch_col_fwd_n(const Geom&, const Bufs&, int, void*, int, cudaStream_t);
+
+}  // namespace gf

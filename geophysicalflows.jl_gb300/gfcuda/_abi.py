@@ -10,7 +10,7 @@ GF_OK, GF_ERR_ARG, GF_ERR_UNSUPPORTED, GF_ERR_CUDA, GF_ERR_NOMEM, GF_ERR_STATE, 
 MODULES = {"TwoDNavierStokes": 0, "SingleLayerQG": 1, "MultiLayerQG": 2, "SurfaceQG": 3}
 STEPPERS = {"ForwardEuler": 0, "FilteredForwardEuler": 1, "RK4": 2, "FilteredRK4": 3,
             "ETDRK4": 4, "FilteredETDRK4": 5, "AB3": 6, "FilteredAB3": 7}
-F32, F64 = 0, 1
+F32, F64, DF64 = 0, 1, 2
 FORCING = {None: 0, "static": 1, "harmonic": 2, "stochastic": 3, "stochastic_phase": 4}
 HOST, DEVICE = 0, 1
 FIELD_Q, FIELD_PSI, FIELD_U, FIELD_V = 0, 1, 2, 3

@@ -14,9 +14,13 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(HERE, "libgfcuda.so")
-UNITS = ["gf_f64_col.cu", "gf_f32_col.cu", "gf_f64_row.cu", "gf_f32_row.cu", "gf_api.cu", "gf_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++20", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", f"-I{INCLUDE}", f"-I{CSRC}"]
+
+
+def units():
+    """Translation units: the ABI, the dispatch layer and one unit per (precision, FFT length)."""
+    return sorted(f for f in os.listdir(CSRC) if f.endswith(".cu"))
 
 
 def _nvcc():
@@ -52,8 +56,11 @@ def build(force=False, verbose=True, defines=(), lib=None):
             raise RuntimeError(f"nvcc failed for {u}:\n{r.stderr}")
         return obj
 
-    with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
-        objs = list(ex.map(compile_unit, UNITS))
+    us = units()
+    # largest kernels first so the slowest units start early
+    us.sort(key=lambda u: (("df64" not in u) + ("f64" not in u), -int(u.rsplit("_", 1)[-1][:-3]) if u.startswith("gf_k_") else 0))
+    with cf.ThreadPoolExecutor(max_workers=max(1, os.cpu_count() or 1)) as ex:
+        objs = list(ex.map(compile_unit, us))
     tmp = lib + ".tmp"
     cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)

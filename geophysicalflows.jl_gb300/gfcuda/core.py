@@ -87,7 +87,7 @@ class Problem:
     field_names = {A.FIELD_Q: "q", A.FIELD_PSI: "psi", A.FIELD_U: "u", A.FIELD_V: "v"}
 
     def __init__(self, cfg_kwargs, nx, ny, Lx, Ly, dt, stepper, T, aliased_fraction, forcing, nlayers=1,
-                 stream=None):
+                 stream=None, precision=None):
         self._lib = A.load()
         self._ctx = C.c_void_p()
         if stepper not in A.STEPPERS:
@@ -102,7 +102,11 @@ class Problem:
         self.stepper = stepper
         cfg = A.gf_config()
         cfg.module = A.MODULES[self.module]
-        cfg.precision = A.F32 if T == np.float32 else A.F64
+        precision = (precision or ("F32" if T == np.float32 else "F64")).upper()
+        if precision not in ("F32", "F64", "DF64") or (precision == "F32") != (T == np.float32):
+            raise ValueError("precision must be F32 (T=Float32), F64 or DF64 (T=Float64)")
+        self.precision = precision
+        cfg.precision = {"F32": A.F32, "F64": A.F64, "DF64": A.DF64}[precision]
         cfg.stepper = A.STEPPERS[stepper]
         cfg.nx, cfg.ny, cfg.nlayers = nx, ny, nlayers
         cfg.Lx, cfg.Ly, cfg.dt, cfg.aliased_fraction = Lx, Ly, dt, aliased_fraction

@@ -9,7 +9,8 @@
  *   spectral  (nkr, ny[, nlayers]) complex, nkr = nx/2 + 1, element (ik, j, L) at
  *             ik + nkr*(j + ny*L);   physical (nx, ny[, nlayers]) real, (i, j, L) at
  *             i + nx*(j + ny*L).
- *   Element type: float/complex-float for GF_F32 contexts, double/complex-double otherwise.
+ *   Element type: float/complex-float for GF_F32 contexts, double/complex-double otherwise
+ *   (GF_F64 and GF_DF64).
  *   `where` = GF_HOST (pageable or pinned host memory) or GF_DEVICE (device pointer on the
  *   context's GPU, e.g. from a CuArray).
  * One context = one problem on one stream; a context is not thread-safe, separate
@@ -43,8 +44,11 @@ typedef enum { GF_TWODNAVIERSTOKES = 0, GF_SINGLELAYERQG = 1, GF_MULTILAYERQG = 
 
 /* GF_F64: IEEE double throughout.  GF_F32: float bulk (FFTs, products, stage combination);
  * FP64 stays in the setup (ETDRK4 coefficients, inversion factorisation) and in the
- * diagnostics reductions. */
-typedef enum { GF_F32 = 0, GF_F64 = 1 } gf_precision;
+ * diagnostics reductions.  GF_DF64: the FP64-plain mode computed in double-float
+ * arithmetic (48-bit significand from pairs of floats; GB300's FP64 units are a small
+ * fraction of its FP32 throughput); arrays at the ABI are double/complex-double as for
+ * GF_F64, and setup and diagnostics are FP64. */
+typedef enum { GF_F32 = 0, GF_F64 = 1, GF_DF64 = 2 } gf_precision;
 
 /* FourierFlows timestepper names (test/runtests.jl:58) */
 typedef enum {
