@@ -54,6 +54,11 @@ struct gf_ctx {
   double prof_ms[2] = {0, 0};
   int64_t prof_n[2] = {0, 0};
   int64_t launches = 0;
+  // device clock and graph replay of multi-step sequences
+  DevClock* dclk = nullptr;
+  int graph_steps = 4;
+  cudaGraphExec_t gexec[3] = {nullptr, nullptr, nullptr};
+  bool own_stream = false;
   std::string err;
 };
 
@@ -124,11 +129,12 @@ __global__ void etd_coeffs_kernel(int n, const double* __restrict__ Lre, const d
 
 __global__ void diag_finish(const double* __restrict__ partial, int nblocks, uint32_t mask, double* out) {
   __shared__ double red[256];
+  const int nb = gridDim.x, ib = blockIdx.x;  // one block per ensemble instance
   for (int q = 0; q < NDIAG; ++q) {
-    if (!(mask & (1u << q))) { if (threadIdx.x == 0) out[q] = 0; continue; }
+    if (!(mask & (1u << q))) { if (threadIdx.x == 0) out[(size_t)q * nb + ib] = 0; continue; }
     double s = 0, c = 0;
     for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
-      const double x = partial[(size_t)q * nblocks + b];
+      const double x = partial[((size_t)q * nb + ib) * nblocks + b];
       const double t = s + x;
       c += (fabs(s) >= fabs(x)) ? (s - t) + x : (x - t) + s;
       s = t;
@@ -139,8 +145,24 @@ __global__ void diag_finish(const double* __restrict__ partial, int nblocks, uin
       if ((int)threadIdx.x < st) red[threadIdx.x] += red[threadIdx.x + st];
       __syncthreads();
     }
-    if (threadIdx.x == 0) out[q] = red[0];
+    if (threadIdx.x == 0) out[(size_t)q * nb + ib] = red[0];
     __syncthreads();
+  }
+}
+
+// clock advance after a step, and the harmonic forcing scales of the next step's stages
+__global__ void advance_clock_kernel(DevClock* clk, double dt, double omega, double phase, int harmonic, int nst) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  clk->t += dt;
+  clk->step += 1;
+  if (harmonic) {
+    for (int k = 0; k < 4; ++k) {
+      const double off = (nst == 4) ? (k == 0 ? 0.0 : k == 3 ? 1.0 : 0.5) : 0.0;
+      const double v = cos(omega * (clk->t + off * dt) + phase);
+      clk->fs[k] = v;
+      clk->fs_f[k] = (float)v;
+      clk->fs_l[k] = (float)(v - (double)clk->fs_f[k]);
+    }
   }
 }
 
@@ -233,6 +255,23 @@ static Geom full_geom(const gf_ctx* c) {
   Geom g = c->g;
   g.kcut = g.nkr; g.lA = 1; g.lB = 0; g.ldw = g.ldk;
   return g;
+}
+
+// host copy of the device clock for the step starting at c->t (stage forcing scales)
+static int upload_clock(gf_ctx* c) {
+  DevClock h{};
+  h.t = c->t;
+  h.step = c->step;
+  for (int k = 0; k < 4; ++k) {
+    const double off = (c->nstages == 4) ? (k == 0 ? 0.0 : k == 3 ? 1.0 : 0.5) : 0.0;
+    h.fs[k] = c->cfg.forcing_kind == GF_FORCING_HARMONIC
+                  ? std::cos(c->cfg.forcing_omega * (c->t + off * c->cfg.dt) + c->cfg.forcing_phase)
+                  : 1.0;
+    split_hl(h.fs[k], &h.fs_f[k], &h.fs_l[k]);
+  }
+  GF_CUDA(c, cudaMemcpyAsync(c->dclk, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
+  GF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GF_OK;
 }
 
 #define DISPATCH(c, fn, ...)                                      \
@@ -354,6 +393,8 @@ static int build(gf_ctx* c, const gf_config* cfg) {
 
   const size_t nsp = nspec(c), tsz = (size_t)g.ny * g.ldk;
   const size_t cb = c->cb, rb = c->rb;
+  g.nb = k.batch > 1 ? k.batch : 1;
+  const size_t NB = g.nb;
   // ----- twiddles
   {
     std::vector<double> tw(2 * TWN);
@@ -476,22 +517,25 @@ static int build(gf_ctx* c, const gf_config* cfg) {
 
   // ----- buffers
   const size_t Wn = std::max((size_t)3 * g.nl * g.ny * g.ldw, nsp);
-  if (!(c->sol = dalloc(c, nsp * cb)) || !(c->W = dalloc(c, Wn * cb)) || !(c->P = dalloc(c, 3 * nsp * cb)) ||
-      !(c->D = dalloc(c, tsz * cb)) || !(c->tmp_spec = dalloc(c, nsp * cb)) || !(c->tmp_spec2 = dalloc(c, nsp * cb)) ||
-      !(c->phys = dalloc(c, (size_t)4 * g.nl * g.ny * g.nx * rb)))
+  g.bs_spec = nsp; g.bs_w = Wn; g.bs_p = 3 * nsp; g.bs_d = tsz; g.bs_phys = (size_t)g.nl * g.ny * g.nx;
+  if (!(c->sol = dalloc(c, NB * nsp * cb)) || !(c->W = dalloc(c, NB * Wn * cb)) ||
+      !(c->P = dalloc(c, NB * 3 * nsp * cb)) || !(c->D = dalloc(c, NB * tsz * cb)) ||
+      !(c->tmp_spec = dalloc(c, NB * nsp * cb)) || !(c->tmp_spec2 = dalloc(c, NB * nsp * cb)) ||
+      !(c->phys = dalloc(c, NB * 4 * g.bs_phys * rb)) || !(c->dclk = (DevClock*)dalloc(c, sizeof(DevClock))))
     return fail(c, GF_ERR_NOMEM, "state buffers");
   m.D = c->D;
   if (c->prec == GF_DF64 &&
-      !(c->stage = dalloc(c, std::max(nsp * cb, (size_t)g.nl * g.ny * g.nx * rb))))
+      !(c->stage = dalloc(c, NB * std::max(nsp * cb, g.bs_phys * rb))))
     return fail(c, GF_ERR_NOMEM, "df64 staging");
   if (c->kind == SK_RK4) {
-    if (!(c->acc = dalloc(c, nsp * cb))) return fail(c, GF_ERR_NOMEM, "acc");
-    if (c->hasL && !(c->X = dalloc(c, nsp * cb))) return fail(c, GF_ERR_NOMEM, "X");
+    if (!(c->acc = dalloc(c, NB * nsp * cb))) return fail(c, GF_ERR_NOMEM, "acc");
+    if (c->hasL && !(c->X = dalloc(c, NB * nsp * cb))) return fail(c, GF_ERR_NOMEM, "X");
   } else if (c->kind == SK_ETDRK4) {
-    if (!(c->acc = dalloc(c, nsp * cb)) || !(c->s1 = dalloc(c, nsp * cb)) || !(c->N1 = dalloc(c, nsp * cb)))
+    if (!(c->acc = dalloc(c, NB * nsp * cb)) || !(c->s1 = dalloc(c, NB * nsp * cb)) ||
+        !(c->N1 = dalloc(c, NB * nsp * cb)))
       return fail(c, GF_ERR_NOMEM, "etdrk4 state");
   } else if (c->kind == SK_AB3) {
-    for (int i = 0; i < 3; ++i) if (!(c->R3[i] = dalloc(c, nsp * cb))) return fail(c, GF_ERR_NOMEM, "ab3 state");
+    for (int i = 0; i < 3; ++i) if (!(c->R3[i] = dalloc(c, NB * nsp * cb))) return fail(c, GF_ERR_NOMEM, "ab3 state");
   }
   // ----- L, filter, ETDRK4 coefficients
   const int w = c->cplxL ? 2 : 1;
@@ -553,7 +597,7 @@ static int build(gf_ctx* c, const gf_config* cfg) {
     if (!eta_d || !(c->etah = dalloc(c, nsp * cb))) return fail(c, GF_ERR_NOMEM, "eta");
     if (int r = upload_real(c, eta_d, k.eta, np)) return r;
     // etah = rfft(eta) (one layer)
-    Geom g1 = full_geom(c); g1.nl = 1;
+    Geom g1 = full_geom(c); g1.nl = 1; g1.nb = 1;
     GF_CUDA(c, DISPATCH(c, launch_row_r2c, g1, bufs(c), 1, eta_d, c->stream));
     GF_CUDA(c, DISPATCH(c, launch_col_fwd, g1, bufs(c), 1, c->etah, 0, c->stream));
     // Qx = irfft(i kr etah), Qy = irfft(i l etah) (src/singlelayerqg.jl:185-186,
@@ -619,16 +663,18 @@ static int build(gf_ctx* c, const gf_config* cfg) {
   }
   // ----- forcing buffers
   if (k.forcing_kind != GF_FORCING_NONE) {
-    if (!(c->Fh = dalloc(c, nsp * cb))) return fail(c, GF_ERR_NOMEM, "forcing");
+    if (!(c->Fh = dalloc(c, NB * nsp * cb))) return fail(c, GF_ERR_NOMEM, "forcing");
     if (k.forcing_kind >= GF_FORCING_STOCHASTIC) {
-      if (!(c->fspec = dalloc(c, tsz * rb)) || !(c->prevsol = dalloc(c, nsp * cb)))
+      if (!(c->fspec = dalloc(c, tsz * rb)) || !(c->prevsol = dalloc(c, NB * nsp * cb)))
         return fail(c, GF_ERR_NOMEM, "stochastic forcing");
       c->Fstore = c->Fh;
     }
   }
   c->diag_blocks = (int)std::min<size_t>((nt + DIAG_BLOCK - 1) / DIAG_BLOCK, 1024);
-  if (!(c->dpart = (double*)dalloc(c, (size_t)NDIAG * c->diag_blocks * 8)) || !(c->dout = (double*)dalloc(c, NDIAG * 8)))
+  if (!(c->dpart = (double*)dalloc(c, (size_t)NDIAG * NB * c->diag_blocks * 8)) ||
+      !(c->dout = (double*)dalloc(c, (size_t)NDIAG * NB * 8)))
     return fail(c, GF_ERR_NOMEM, "diagnostics");
+  if (int r = upload_clock(c)) return r;
   GF_CUDA(c, cudaStreamSynchronize(c->stream));
   return GF_OK;
 }
@@ -658,9 +704,19 @@ extern "C" int gf_create(const gf_config* cfg, void* stream, gf_ctx** out) {
     return fail(nullptr, GF_ERR_ARG, "nlayers > 1 is only valid for MultiLayerQG");
   }
   if (k.forcing_kind < 0 || k.forcing_kind > 4) return fail(nullptr, GF_ERR_ARG, "unknown forcing kind");
+  if (k.batch < 0 || k.batch > 65535) return fail(nullptr, GF_ERR_ARG, "batch must be in [0, 65535]");
   gf_ctx* c = new gf_ctx();
   c->cfg = k;
   c->stream = (cudaStream_t)stream;
+  if (!c->stream) {
+    // a stream of our own (graph capture needs one); blocking, so it orders with the legacy
+    // default stream like the caller's other work
+    if (cudaStreamCreate(&c->stream) != cudaSuccess) {
+      delete c;
+      return fail(nullptr, GF_ERR_CUDA, "cudaStreamCreate failed");
+    }
+    c->own_stream = true;
+  }
   const int r = build(c, cfg);
   if (r != GF_OK) {
     g_create_error = c->err.empty() ? g_create_error : c->err;
@@ -677,6 +733,8 @@ extern "C" int gf_destroy(gf_ctx* c) {
   for (void* p : c->allocs) cudaFree(p);
   for (auto e : c->ev_free) cudaEventDestroy(e);
   for (auto& u : c->ev_used) { cudaEventDestroy(u.second.first); cudaEventDestroy(u.second.second); }
+  for (auto& gx : c->gexec) if (gx) cudaGraphExecDestroy(gx);
+  if (c->own_stream) cudaStreamDestroy(c->stream);
   delete c;
   return GF_OK;
 }
@@ -705,12 +763,12 @@ static int copy_spec_in(gf_ctx* c, void* dst, const void* src, int where) {
   const Geom& g = c->g;
   const cudaMemcpyKind kind = where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   if (c->prec == GF_DF64) {
-    GF_CUDA(c, cudaMemcpyAsync(c->stage, src, (size_t)g.nkr * g.ny * g.nl * 16, kind, c->stream));
-    if (int r = convert_launch(c, true, c->stage, 2 * (size_t)g.nkr, dst, 2 * (size_t)g.ldk, (size_t)g.ny * g.nl,
-                               2 * (size_t)g.nkr)) return r;
+    GF_CUDA(c, cudaMemcpyAsync(c->stage, src, (size_t)g.nkr * g.ny * g.nl * g.nb * 16, kind, c->stream));
+    if (int r = convert_launch(c, true, c->stage, 2 * (size_t)g.nkr, dst, 2 * (size_t)g.ldk,
+                               (size_t)g.ny * g.nl * g.nb, 2 * (size_t)g.nkr)) return r;
   } else {
-    GF_CUDA(c, cudaMemcpy2DAsync(dst, g.ldk * c->cb, src, g.nkr * c->cb, g.nkr * c->cb, (size_t)g.ny * g.nl, kind,
-                                 c->stream));
+    GF_CUDA(c, cudaMemcpy2DAsync(dst, g.ldk * c->cb, src, g.nkr * c->cb, g.nkr * c->cb, (size_t)g.ny * g.nl * g.nb,
+                                 kind, c->stream));
   }
   if (where == GF_HOST) GF_CUDA(c, cudaStreamSynchronize(c->stream));
   return GF_OK;
@@ -719,19 +777,19 @@ static int copy_spec_out(gf_ctx* c, void* dst, const void* src, int where) {
   const Geom& g = c->g;
   const cudaMemcpyKind kind = where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
   if (c->prec == GF_DF64) {
-    if (int r = convert_launch(c, false, src, 2 * (size_t)g.ldk, c->stage, 2 * (size_t)g.nkr, (size_t)g.ny * g.nl,
-                               2 * (size_t)g.nkr)) return r;
-    GF_CUDA(c, cudaMemcpyAsync(dst, c->stage, (size_t)g.nkr * g.ny * g.nl * 16, kind, c->stream));
+    if (int r = convert_launch(c, false, src, 2 * (size_t)g.ldk, c->stage, 2 * (size_t)g.nkr,
+                               (size_t)g.ny * g.nl * g.nb, 2 * (size_t)g.nkr)) return r;
+    GF_CUDA(c, cudaMemcpyAsync(dst, c->stage, (size_t)g.nkr * g.ny * g.nl * g.nb * 16, kind, c->stream));
   } else {
-    GF_CUDA(c, cudaMemcpy2DAsync(dst, g.nkr * c->cb, src, g.ldk * c->cb, g.nkr * c->cb, (size_t)g.ny * g.nl, kind,
-                                 c->stream));
+    GF_CUDA(c, cudaMemcpy2DAsync(dst, g.nkr * c->cb, src, g.ldk * c->cb, g.nkr * c->cb, (size_t)g.ny * g.nl * g.nb,
+                                 kind, c->stream));
   }
   if (where == GF_HOST) GF_CUDA(c, cudaStreamSynchronize(c->stream));
   return GF_OK;
 }
 // caller physical array (nl x ny x nx reals) <-> internal physical array
 static int copy_phys_in(gf_ctx* c, void* dst, const void* src, int where) {
-  const size_t n = (size_t)c->g.nl * c->g.ny * c->g.nx;
+  const size_t n = (size_t)c->g.nl * c->g.ny * c->g.nx * c->g.nb;
   const cudaMemcpyKind kind = where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   if (c->prec == GF_DF64) {
     GF_CUDA(c, cudaMemcpyAsync(c->stage, src, n * 8, kind, c->stream));
@@ -741,7 +799,7 @@ static int copy_phys_in(gf_ctx* c, void* dst, const void* src, int where) {
   return GF_OK;
 }
 static int copy_phys_out(gf_ctx* c, void* dst, const void* src, int where) {
-  const size_t n = (size_t)c->g.nl * c->g.ny * c->g.nx;
+  const size_t n = (size_t)c->g.nl * c->g.ny * c->g.nx * c->g.nb;
   const cudaMemcpyKind kind = where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
   if (c->prec == GF_DF64) {
     if (int r = convert_launch(c, false, src, n, c->stage, n, 1, n)) return r;
@@ -771,7 +829,7 @@ extern "C" int gf_get_clock(const gf_ctx* c, double* t, int64_t* step) {
 extern "C" int gf_set_clock(gf_ctx* c, double t, int64_t step) {
   if (!c) return GF_ERR_ARG;
   c->t = t; c->step = step;
-  return GF_OK;
+  return upload_clock(c);
 }
 extern "C" int gf_synchronize(gf_ctx* c) {
   if (!c) return GF_ERR_ARG;
@@ -781,7 +839,7 @@ extern "C" int gf_synchronize(gf_ctx* c) {
 
 extern "C" int gf_updatevars(gf_ctx* c) {
   if (!c) return GF_ERR_ARG;
-  const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->rb;
+  const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->g.nb * c->rb;
   GF_CUDA(c, DISPATCH(c, launch_mask_inplace, c->g, c->sol, c->stream));
   c->W_valid = false;
   const int kinds[4] = {SF_X, SF_PSI, SF_U, SF_V};
@@ -793,13 +851,13 @@ extern "C" int gf_updatevars(gf_ctx* c) {
 extern "C" int gf_get_field(gf_ctx* c, int which, void* out, int where) {
   if (!c || !out) return GF_ERR_ARG;
   if (which < 0 || which > 3) return fail(c, GF_ERR_ARG, "unknown field");
-  const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->rb;
+  const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->g.nb * c->rb;
   return copy_phys_out(c, out, (char*)c->phys + which * pf, where);
 }
 
 extern "C" int gf_fwdtransform(gf_ctx* c, void* fieldh, const void* field, int where) {
   if (!c || !fieldh || !field) return GF_ERR_ARG;
-  const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->rb;
+  const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->g.nb * c->rb;
   void* ph = (char*)c->phys + 3 * pf;
   if (int r = copy_phys_in(c, ph, field, where)) return r;
   if (int r = fwd_transform(c, ph, c->tmp_spec, 0)) return r;
@@ -808,7 +866,7 @@ extern "C" int gf_fwdtransform(gf_ctx* c, void* fieldh, const void* field, int w
 
 extern "C" int gf_invtransform(gf_ctx* c, void* field, const void* fieldh, int where) {
   if (!c || !fieldh || !field) return GF_ERR_ARG;
-  const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->rb;
+  const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->g.nb * c->rb;
   if (int r = copy_spec_in(c, c->tmp_spec, fieldh, where)) return r;
   void* ph = (char*)c->phys + 3 * pf;
   if (int r = inv_transform(c, c->tmp_spec, SF_RAW, 0, ph)) return r;
@@ -820,7 +878,7 @@ extern "C" int gf_set_physical(gf_ctx* c, int which, const void* field, int wher
   const int mod = c->cfg.module;
   if (which != GF_FIELD_Q && !(which == GF_FIELD_PSI && mod == GF_MULTILAYERQG))
     return fail(c, GF_ERR_ARG, "set_physical supports q/zeta/b, and psi for MultiLayerQG");
-  const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->rb;
+  const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->g.nb * c->rb;
   void* ph = (char*)c->phys + 3 * pf;
   if (int r = copy_phys_in(c, ph, field, where)) return r;
   if (which == GF_FIELD_PSI) {
@@ -938,15 +996,14 @@ static int ensure_W(gf_ctx* c) {
   return GF_OK;
 }
 
-static int one_step(gf_ctx* c) {
-  if (int r = ensure_W(c)) return r;
+// Host bookkeeping of one step (clock, AB3 ring, forcing scale of the last calcN!).
+static void host_advance(gf_ctx* c) {
   const double dt = c->cfg.dt;
-  for (int stg = 1; stg <= c->nstages; ++stg) {
-    const double ts = c->t + (c->nstages == 4 ? (stg == 1 ? 0.0 : stg == 4 ? dt : 0.5 * dt) : 0.0);
-    StepArgs s = stage_args(c, stg, ts);
-    if (int r = launch_stage(c, s, 1)) return r;
-    if (s.fkind == FK_HARMONIC) c->last_fscale = s.fscale;
-    else if (s.fkind != FK_NONE) c->last_fscale = 1.0;
+  if (c->cfg.forcing_kind == GF_FORCING_HARMONIC) {
+    const double tl = c->t + (c->nstages == 4 ? dt : 0.0);  // time of the step's last calcN!
+    c->last_fscale = std::cos(c->cfg.forcing_omega * tl + c->cfg.forcing_phase);
+  } else if (c->cfg.forcing_kind != GF_FORCING_NONE) {
+    c->last_fscale = 1.0;
   }
   if (c->kind == SK_AB3) {  // RHS_{-2} <- RHS_{-1} <- RHS
     const int o = c->ab3_out, m1 = c->ab3_m1, m2 = c->ab3_m2;
@@ -954,14 +1011,109 @@ static int one_step(gf_ctx* c) {
   }
   c->t += dt;
   c->step += 1;
+}
+
+// Launches of one step: the stages (row + column kernels each) and the device-clock advance.
+// W must be valid (the first half of the step's first calcN! done).
+static int enqueue_step(gf_ctx* c) {
+  const double dt = c->cfg.dt;
+  for (int stg = 1; stg <= c->nstages; ++stg) {
+    const double ts = c->t + (c->nstages == 4 ? (stg == 1 ? 0.0 : stg == 4 ? dt : 0.5 * dt) : 0.0);
+    StepArgs s = stage_args(c, stg, ts);
+    s.clk = c->dclk;
+    if (int r = launch_stage(c, s, 1)) return r;
+  }
+  advance_clock_kernel<<<1, 32, 0, c->stream>>>(c->dclk, dt, c->cfg.forcing_omega, c->cfg.forcing_phase,
+                                                c->cfg.forcing_kind == GF_FORCING_HARMONIC, c->nstages);
+  GF_CUDA(c, cudaGetLastError());
+  c->launches++;
+  return GF_OK;
+}
+
+static int one_step(gf_ctx* c) {
+  if (int r = ensure_W(c)) return r;
+  if (int r = enqueue_step(c)) return r;
+  host_advance(c);
+  return GF_OK;
+}
+
+static void drop_graphs(gf_ctx* c) {
+  for (auto& gx : c->gexec)
+    if (gx) { cudaGraphExecDestroy(gx); gx = nullptr; }
+}
+
+// Capture G steps (starting from the current AB3 ring phase) into an executable graph.
+static int capture_steps(gf_ctx* c, int G, cudaGraphExec_t* out) {
+  const double t0 = c->t;
+  const int64_t s0 = c->step, l0 = c->launches;
+  const int r0 = c->ab3_out, r1 = c->ab3_m1, r2 = c->ab3_m2;
+  const double f0 = c->last_fscale;
+  GF_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = GF_OK;
+  for (int i = 0; i < G && rc == GF_OK; ++i) {
+    rc = enqueue_step(c);
+    host_advance(c);
+  }
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+  c->t = t0; c->step = s0; c->launches = l0;
+  c->ab3_out = r0; c->ab3_m1 = r1; c->ab3_m2 = r2;
+  c->last_fscale = f0;
+  if (rc != GF_OK) { if (graph) cudaGraphDestroy(graph); return rc; }
+  if (e != cudaSuccess) return fail(c, GF_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  const cudaError_t e2 = cudaGraphInstantiate(out, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e2 != cudaSuccess) return fail(c, GF_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e2));
+  return GF_OK;
+}
+
+extern "C" int gf_set_graph_steps(gf_ctx* c, int32_t steps) {
+  if (!c || steps < 0) return GF_ERR_ARG;
+  drop_graphs(c);
+  c->graph_steps = steps;
   return GF_OK;
 }
 
 extern "C" int gf_step(gf_ctx* c, int64_t nsteps) {
   if (!c || nsteps < 0) return GF_ERR_ARG;
   if (c->cfg.forcing_kind >= GF_FORCING_STOCHASTIC && !c->fspec) return fail(c, GF_ERR_STATE, "no forcing spectrum");
-  for (int64_t i = 0; i < nsteps; ++i)
-    if (int r = one_step(c)) return r;
+  // AB3 rotates three RHS buffers: a graph covers three steps so that it can be replayed
+  const int G = c->graph_steps <= 0 ? 0 : (c->kind == SK_AB3 ? 3 : c->graph_steps);
+  while (nsteps > 0) {
+    if (G > 0 && nsteps >= G && !c->profiling) {
+      if (int r = ensure_W(c)) return r;
+      const int phase = (c->kind == SK_AB3) ? c->ab3_out : 0;
+      if (!c->gexec[phase])
+        if (int r = capture_steps(c, G, &c->gexec[phase])) return r;
+      GF_CUDA(c, cudaGraphLaunch(c->gexec[phase], c->stream));
+      for (int i = 0; i < G; ++i) host_advance(c);
+      c->launches += (int64_t)G * (2 * c->nstages + 1);
+      nsteps -= G;
+    } else {
+      if (int r = one_step(c)) return r;
+      nsteps -= 1;
+    }
+  }
+  return GF_OK;
+}
+
+// Several independent problems (e.g. the size classes of an ensemble) stepped together: each
+// context's launches go to its own stream, so the GPU runs them concurrently.
+extern "C" int gf_ensemble_step(gf_ctx* const* ctxs, int32_t n, int64_t nsteps) {
+  if (!ctxs || n <= 0 || nsteps < 0) return fail(nullptr, GF_ERR_ARG, "gf_ensemble_step: bad arguments");
+  for (int32_t i = 0; i < n; ++i)
+    if (!ctxs[i]) return fail(nullptr, GF_ERR_ARG, "gf_ensemble_step: null context");
+  for (int32_t i = 0; i < n; ++i)
+    if (int r = gf_step(ctxs[i], nsteps)) {
+      g_create_error = ctxs[i]->err;
+      return r;
+    }
+  return GF_OK;
+}
+
+extern "C" int gf_get_batch(const gf_ctx* c, int32_t* nb) {
+  if (!c || !nb) return GF_ERR_ARG;
+  *nb = c->g.nb;
   return GF_OK;
 }
 
@@ -972,7 +1124,7 @@ extern "C" int gf_step_diags(gf_ctx* c, int64_t nsteps, const int32_t* which, in
   for (int64_t i = 0; i < nsteps; ++i) {
     if (int r = one_step(c)) return r;
     if (nd > 0)
-      if (int r = gf_diagnostics(c, which, nd, out + i * nd)) return r;
+      if (int r = gf_diagnostics(c, which, nd, out + i * nd * c->g.nb)) return r;
   }
   return GF_OK;
 }
@@ -1024,31 +1176,35 @@ extern "C" int gf_diagnostics(gf_ctx* c, const int32_t* which, int32_t nd, doubl
   }
   const void* Fh = (c->cfg.forcing_kind != GF_FORCING_NONE) ? c->Fh : nullptr;
   const void* prev = (c->cfg.forcing_kind >= GF_FORCING_STOCHASTIC) ? c->prevsol : nullptr;
+  const int NB = c->g.nb;
   GF_CUDA(c, DISPATCH(c, launch_diag, c->g, c->m, c->sol, prev, Fh, mask, c->dpart, c->diag_blocks, c->stream));
-  diag_finish<<<1, 256, 0, c->stream>>>(c->dpart, c->diag_blocks, mask, c->dout);
+  diag_finish<<<NB, 256, 0, c->stream>>>(c->dpart, c->diag_blocks, mask, c->dout);
   GF_CUDA(c, cudaGetLastError());
-  double h[NDIAG];
-  GF_CUDA(c, cudaMemcpyAsync(h, c->dout, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  std::vector<double> hv((size_t)NDIAG * NB);
+  GF_CUDA(c, cudaMemcpyAsync(hv.data(), c->dout, hv.size() * 8, cudaMemcpyDeviceToHost, c->stream));
   GF_CUDA(c, cudaStreamSynchronize(c->stream));
   const double nn = (double)c->g.nx * c->g.ny, norm = 1.0 / (nn * nn);
   const double fs = (c->cfg.forcing_kind == GF_FORCING_HARMONIC || c->cfg.forcing_kind == GF_FORCING_STATIC) ? c->last_fscale : 1.0;
-  for (int i = 0; i < nd; ++i) {
-    const int d = which[i];
-    double v;
-    if (mod == GF_MULTILAYERQG) {
-      const int n = c->g.nl;
-      if (n == 1) v = h[0] * norm / 2;
-      else if (d < n) v = h[d] * norm * c->Hl[d] / (2 * c->Hsum);
-      else { const int j = d - GF_D_MLQG_PE0; v = h[n + j] * norm * c->f0 * c->f0 / (c->gprime[j] * 2 * c->Hsum); }
-    } else if (mod == GF_SINGLELAYERQG && d == GF_D_SLQG_ENERGY) {
-      v = (h[0] + h[1]) * norm;
-    } else {
-      v = h[d] * norm;
-      const bool work = (mod == GF_TWODNAVIERSTOKES && (d == 7 || d == 8)) || (mod == GF_SINGLELAYERQG && (d == 5 || d == 6)) ||
-                        (mod == GF_SURFACEQG && d == 4);
-      if (work) v *= fs;
+  for (int ib = 0; ib < NB; ++ib) {
+    auto h = [&](int q) { return hv[(size_t)q * NB + ib]; };
+    for (int i = 0; i < nd; ++i) {
+      const int d = which[i];
+      double v;
+      if (mod == GF_MULTILAYERQG) {
+        const int n = c->g.nl;
+        if (n == 1) v = h(0) * norm / 2;
+        else if (d < n) v = h(d) * norm * c->Hl[d] / (2 * c->Hsum);
+        else { const int j = d - GF_D_MLQG_PE0; v = h(n + j) * norm * c->f0 * c->f0 / (c->gprime[j] * 2 * c->Hsum); }
+      } else if (mod == GF_SINGLELAYERQG && d == GF_D_SLQG_ENERGY) {
+        v = (h(0) + h(1)) * norm;
+      } else {
+        v = h(d) * norm;
+        const bool work = (mod == GF_TWODNAVIERSTOKES && (d == 7 || d == 8)) || (mod == GF_SINGLELAYERQG && (d == 5 || d == 6)) ||
+                          (mod == GF_SURFACEQG && d == 4);
+        if (work) v *= fs;
+      }
+      out[(size_t)ib * nd + i] = v;
     }
-    out[i] = v;
   }
   return GF_OK;
 }

@@ -93,7 +93,7 @@ cudaError_t launch_col_fwd(const Geom& g, const Bufs& b, int nf, void* out, int 
 template <class T>
 cudaError_t launch_diag(const Geom& g, const ModArgs& m, const void* sol, const void* prevsol, const void* Fh,
                         uint32_t mask, double* partial, int nblocks, cudaStream_t st) {
-  diag_kernel<T><<<nblocks, DIAG_BLOCK, 0, st>>>(g, m, static_cast<const cplx<T>*>(sol),
+  diag_kernel<T><<<dim3(nblocks, g.nb), DIAG_BLOCK, 0, st>>>(g, m, static_cast<const cplx<T>*>(sol),
                                                  static_cast<const cplx<T>*>(prevsol),
                                                  static_cast<const cplx<T>*>(Fh), mask, partial);
   return cudaGetLastError();
@@ -107,7 +107,7 @@ cudaError_t launch_mask_inplace(const Geom& g, void* sol, cudaStream_t st) {
 
 template <class T>
 cudaError_t launch_spec_apply(const Geom& g, const ModArgs& m, const void* in, void* out, int op, cudaStream_t st) {
-  spec_apply_kernel<T><<<256, 256, 0, st>>>(g, m, static_cast<const cplx<T>*>(in), static_cast<cplx<T>*>(out), op);
+  spec_apply_kernel<T><<<dim3(256, g.nb), 256, 0, st>>>(g, m, static_cast<const cplx<T>*>(in), static_cast<cplx<T>*>(out), op);
   return cudaGetLastError();
 }
 

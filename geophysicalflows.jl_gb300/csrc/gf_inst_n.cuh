@@ -10,11 +10,11 @@ cudaError_t launch_row_n(const Geom& g, const ModArgs& m, const Bufs& b, cudaStr
 
   cudaError_t err = cudaSuccess;
   const size_t e = sizeof(cplx<T>);
-  const int B = pick_B(NN, RADIX<T>, e, 3, g.ny / 2);
+  const int B = pick_B(NN, RADIX<T>, e, 3, g.ny / 2, g.nb);
   const size_t sm = (size_t)B * 3 * row_stride<T>(NN, NN / RADIX<T>) * e;
   auto k = row_nl_kernel<T, NN, RADIX<T>>;
   if ((err = set_smem(k, sm)) != cudaSuccess) return err;
-  k<<<g.ny / 2 / B, B * (NN / RADIX<T>), sm, st>>>(g, m, b, B);
+  k<<<dim3(g.ny / 2 / B, g.nb), B * (NN / RADIX<T>), sm, st>>>(g, m, b, B);
   return cudaGetLastError();
 }
 
@@ -23,13 +23,13 @@ cudaError_t launch_col_n(const Geom& g, const ModArgs& m, const StepArgs& s, con
 
   cudaError_t err = cudaSuccess;
   const size_t e = sizeof(cplx<T>);
-  const int C = pick_C(NN, RADIX<T>, g.nkr, [&](int c) { return col_stage_smem(NN, c, col_stride<T>(NN, c), g.nl, e); });
+  const int C = pick_C(NN, RADIX<T>, g.nkr, [&](int c) { return col_stage_smem(NN, c, col_stride<T>(NN, c), g.nl, e); }, g.nb);
   Geom g2 = g;
   g2.cs = col_stride<T>(NN, C);
   const size_t sm = col_stage_smem(NN, C, g2.cs, g.nl, e);
   auto k = col_stage_kernel<T, NN, RADIX<T>>;
   if ((err = set_smem(k, sm)) != cudaSuccess) return err;
-  k<<<(g.nkr + C - 1) / C, C * (NN / RADIX<T>), sm, st>>>(g2, m, s, b, C);
+  k<<<dim3((g.nkr + C - 1) / C, g.nb), C * (NN / RADIX<T>), sm, st>>>(g2, m, s, b, C);
   return cudaGetLastError();
 }
 
@@ -39,13 +39,13 @@ cudaError_t launch_col_inv_n(const Geom& g, const ModArgs& m, const void* src, i
 
   cudaError_t err;
   const size_t e = sizeof(cplx<T>);
-  const int C = pick_C(NN, RADIX<T>, g.nkr, [&](int c) { return (size_t)c * col_stride<T>(NN, c) * e; });
+  const int C = pick_C(NN, RADIX<T>, g.nkr, [&](int c) { return (size_t)c * col_stride<T>(NN, c) * e; }, g.nb);
   Geom g2 = g;
   g2.cs = col_stride<T>(NN, C);
   const size_t sm = (size_t)C * g2.cs * e;
   auto k = col_inv_generic<T, NN, RADIX<T>>;
   if ((err = set_smem(k, sm)) != cudaSuccess) return err;
-  k<<<(g.nkr + C - 1) / C, C * (NN / RADIX<T>), sm, st>>>(g2, m, src, kind, mask, b, C);
+  k<<<dim3((g.nkr + C - 1) / C, g.nb), C * (NN / RADIX<T>), sm, st>>>(g2, m, src, kind, mask, b, C);
   return cudaGetLastError();
 }
 
@@ -54,11 +54,11 @@ cudaError_t launch_row_c2r_n(const Geom& g, const Bufs& b, int nf, void* out, cu
 
   cudaError_t err;
   const size_t e = sizeof(cplx<T>);
-  const int B = pick_B(NN, RADIX<T>, e, 1, g.ny / 2);
+  const int B = pick_B(NN, RADIX<T>, e, 1, g.ny / 2, g.nb);
   const size_t sm = (size_t)B * row_stride<T>(NN, NN / RADIX<T>) * e;
   auto k = row_c2r_generic<T, NN, RADIX<T>>;
   if ((err = set_smem(k, sm)) != cudaSuccess) return err;
-  k<<<g.ny / 2 / B, B * (NN / RADIX<T>), sm, st>>>(g, b, nf, static_cast<T*>(out), B);
+  k<<<dim3(g.ny / 2 / B, g.nb), B * (NN / RADIX<T>), sm, st>>>(g, b, nf, static_cast<T*>(out), B);
   return cudaGetLastError();
 }
 
@@ -67,11 +67,11 @@ cudaError_t launch_row_r2c_n(const Geom& g, const Bufs& b, int nf, const void* i
 
   cudaError_t err;
   const size_t e = sizeof(cplx<T>);
-  const int B = pick_B(NN, RADIX<T>, e, 1, g.ny / 2);
+  const int B = pick_B(NN, RADIX<T>, e, 1, g.ny / 2, g.nb);
   const size_t sm = (size_t)B * row_stride<T>(NN, NN / RADIX<T>) * e;
   auto k = row_r2c_generic<T, NN, RADIX<T>>;
   if ((err = set_smem(k, sm)) != cudaSuccess) return err;
-  k<<<g.ny / 2 / B, B * (NN / RADIX<T>), sm, st>>>(g, b, nf, static_cast<const T*>(in), B);
+  k<<<dim3(g.ny / 2 / B, g.nb), B * (NN / RADIX<T>), sm, st>>>(g, b, nf, static_cast<const T*>(in), B);
   return cudaGetLastError();
 }
 
@@ -80,13 +80,13 @@ cudaError_t launch_col_fwd_n(const Geom& g, const Bufs& b, int nf, void* out, in
 
   cudaError_t err;
   const size_t e = sizeof(cplx<T>);
-  const int C = pick_C(NN, RADIX<T>, g.nkr, [&](int c) { return (size_t)c * col_stride<T>(NN, c) * e; });
+  const int C = pick_C(NN, RADIX<T>, g.nkr, [&](int c) { return (size_t)c * col_stride<T>(NN, c) * e; }, g.nb);
   Geom g2 = g;
   g2.cs = col_stride<T>(NN, C);
   const size_t sm = (size_t)C * g2.cs * e;
   auto k = col_fwd_generic<T, NN, RADIX<T>>;
   if ((err = set_smem(k, sm)) != cudaSuccess) return err;
-  k<<<(g.nkr + C - 1) / C, C * (NN / RADIX<T>), sm, st>>>(g2, b, nf, static_cast<cplx<T>*>(out), zero_mean, C);
+  k<<<dim3((g.nkr + C - 1) / C, g.nb), C * (NN / RADIX<T>), sm, st>>>(g2, b, nf, static_cast<cplx<T>*>(out), zero_mean, C);
   return cudaGetLastError();
 }
 

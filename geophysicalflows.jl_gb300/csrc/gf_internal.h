@@ -27,6 +27,20 @@ struct Geom {
   float dkx_f, dky_f, inv_nxny_f;  // float copies (the FP32 kernels never touch FP64)
   float dkx_l, dky_l, inv_nxny_l;  // low words: (x_f, x_l) is the df64 value
   int cs;                          // column stride (elements) of the column kernels' buffers
+  // batch of independent instances (an ensemble): instance blockIdx.y of every kernel works
+  // on its own slice; strides (elements) of the per-instance arrays
+  int nb;
+  size_t bs_spec, bs_w, bs_p, bs_d, bs_phys;
+};
+
+// Device-resident clock, advanced on the GPU after every step so that a captured graph of
+// several steps can be replayed: stage forcing scales for the harmonic forcing of the step
+// about to run, and the step number used by the stochastic draws and AB3's start-up.
+struct DevClock {
+  double t;
+  long long step;
+  double fs[4];
+  float fs_f[4], fs_l[4];
 };
 
 // How psi-hat follows from the layer PV/vorticity/buoyancy X, and what the physical-space
@@ -72,6 +86,7 @@ struct StepArgs {
   void* prevsol;       // sol at the first stage (stochastic budgets)
   uint64_t seed, step;
   float dt_f, fscale_f, dt_l, fscale_l;
+  const DevClock* clk;  // if set, step / fscale / AB3 start-up come from the device clock
 };
 
 // value of a host-prepared scalar (double d, its float rounding h and the remainder l) in

@@ -156,8 +156,21 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? GF_MINBLOCKS_F32 : 1)
   const bool kin = kr < g.nkr;
   const cplx<T>* tw = static_cast<const cplx<T>*>(b.twid);
   const size_t lstride = (size_t)g.ny * g.ldk;
+  const size_t ib = blockIdx.y;                          // ensemble instance
+  const size_t ioff = ib * g.bs_spec;                    // its state arrays
+  cplx<T>* Dp = m.D ? static_cast<cplx<T>*>(m.D) + ib * g.bs_d : nullptr;
   const T dky = sel<T>(g.dky, g.dky_f, g.dky_l), krT = T(kr) * sel<T>(g.dkx, g.dkx_f, g.dkx_l);
   const T dt = sel<T>(s.dt, s.dt_f, s.dt_l), ell2 = sel<T>(m.ell_inv2, m.ell_inv2_f, m.ell_inv2_l), muT = sel<T>(m.mu, m.mu_f, m.mu_l);
+  // clock-dependent values: from the device clock when the launch is part of a graph
+  uint64_t step = s.step;
+  T fscale = sel<T>(s.fscale, s.fscale_f, s.fscale_l);
+  int ab3_euler = s.ab3_euler;
+  if (s.clk) {
+    step = (uint64_t)s.clk->step;
+    const int k = s.stage >= 1 ? s.stage - 1 : 0;
+    fscale = sel<T>(s.clk->fs[k], s.clk->fs_f[k], s.clk->fs_l[k]);
+    ab3_euler = s.clk->step < 3;
+  }
   if (m.psi_kind == PSI_EIGEN) {
     for (int a = tid; a < MAXL + 2 * MAXL * MAXL; a += blockDim.x)
       eig[a] = a < MAXL ? sel<T>(m.lam[a], m.lam_f[a], m.lam_l[a])
@@ -167,10 +180,10 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? GF_MINBLOCKS_F32 : 1)
   }
 
   if (s.do_fwd) {
-    const cplx<T>* P = static_cast<const cplx<T>*>(b.P);
+    const cplx<T>* P = static_cast<const cplx<T>*>(b.P) + ib * g.bs_p;
     const int nslot = 1 + m.hasB + m.hasC;
     const int nseq = nl * nslot;
-    const T fscale = sel<T>(s.fscale, s.fscale_f, s.fscale_l), U0 = sel<T>(m.U0, m.U0_f, m.U0_l);
+    const T U0 = sel<T>(m.U0, m.U0_f, m.U0_l);
     // asynchronous copy of product field q = L * nslot + f into work buffer Fb
     auto issue = [&](int q, cplx<T>* Fb) {
       const int L = q / nslot, f = q - L * nslot;
@@ -219,11 +232,11 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? GF_MINBLOCKS_F32 : 1)
         cplx<T> xn = czero<T>();
         if (kin) {
           const size_t ti = (size_t)j * g.ldk + kr;       // table index
-          const size_t si = (size_t)L * lstride + ti;     // state index
+          const size_t si = ioff + (size_t)L * lstride + ti;  // state index
           const bool keep = kept(g, kr, j);
           cplx<T> N = XL[j * C];
           if (m.Ueta) N = N - (U0 * krT) * mul_i(static_cast<const cplx<T>*>(m.etah)[ti]);
-          if (m.drag && L == nl - 1) N = N + static_cast<const cplx<T>*>(m.D)[ti];
+          if (m.drag && L == nl - 1) N = N + Dp[ti];
           cplx<T>* sol = static_cast<cplx<T>*>(s.sol);
           const cplx<T> solm = keep ? sol[si] : czero<T>();
           // forcing
@@ -238,7 +251,7 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? GF_MINBLOCKS_F32 : 1)
               const uint64_t e = (uint64_t)kr + (uint64_t)g.nkr * ((uint64_t)j + (uint64_t)g.ny * L);
               Fv = czero<T>();
               const bool zero_mean = (s.fkind == FK_STOCH_PHASE) && kr == 0 && j == 0;
-              if (sp != T(0) && !zero_mean) Fv = sp * draw<T>(e, s.step, s.seed, s.fkind == FK_STOCH_PHASE);
+              if (sp != T(0) && !zero_mean) Fv = sp * draw<T>(e, step, s.seed + ib, s.fkind == FK_STOCH_PHASE);
               static_cast<cplx<T>*>(s.Fstore)[si] = Fv;
               static_cast<cplx<T>*>(s.prevsol)[si] = solm;
             } else {
@@ -296,7 +309,7 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? GF_MINBLOCKS_F32 : 1)
             cplx<T> Rv = N;
             if (s.hasL) Rv = Rv + Lmul(solm);
             cplx<T> upd;
-            if (s.ab3_euler) {
+            if (ab3_euler) {
               upd = Rv;
             } else {
               const cplx<T> r1 = static_cast<const cplx<T>*>(s.Rm1)[si];
@@ -318,7 +331,7 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? GF_MINBLOCKS_F32 : 1)
       for (int i = 0; i < R; ++i) {
         const int j = t + i * TPF;
         cplx<T> xn = czero<T>();
-        if (kin && kept(g, kr, j)) xn = sol[(size_t)L * lstride + (size_t)j * g.ldk + kr];
+        if (kin && kept(g, kr, j)) xn = sol[ioff + (size_t)L * lstride + (size_t)j * g.ldk + kr];
         Xs[(L * NY + j) * C + c] = xn;
       }
     }
@@ -343,7 +356,7 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? GF_MINBLOCKS_F32 : 1)
         for (int L = 0; L < nl; ++L) ps[L] = f * X[L];
       }
       for (int L = 0; L < nl; ++L) Ps[(L * NY + j) * C + c] = ps[L];
-      if (m.drag && kin) static_cast<cplx<T>*>(m.D)[(size_t)j * g.ldk + kr] = (muT * K2) * ps[nl - 1];
+      if (m.drag && kin) Dp[(size_t)j * g.ldk + kr] = (muT * K2) * ps[nl - 1];
     }
   } else if (m.drag && kin) {
 #pragma unroll
@@ -353,11 +366,11 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? GF_MINBLOCKS_F32 : 1)
       const T K2 = krT * krT + lv * lv;
       const size_t ti = (size_t)j * g.ldk + kr;
       const T f = psi_factor<T>(m.psi_kind, K2, ell2, m.mult, ti);
-      static_cast<cplx<T>*>(m.D)[ti] = (muT * K2 * f) * Xs[j * C + c];
+      Dp[ti] = (muT * K2 * f) * Xs[j * C + c];
     }
   }
   // y-direction inverse FFT of (q, u, v) for every layer
-  cplx<T>* W = static_cast<cplx<T>*>(b.W);
+  cplx<T>* W = static_cast<cplx<T>*>(b.W) + ib * g.bs_w;
   const T sc = sel<T>(g.inv_nxny, g.inv_nxny_f, g.inv_nxny_l);
   for (int L = 0; L < nl; ++L) {
     for (int f = 0; f < 3; ++f) {
@@ -445,8 +458,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) row_nl_kernel(Geo
   const int j0 = 2 * (blockIdx.x * B + bp);
   cplx<T>* buf = reinterpret_cast<cplx<T>*>(smem_raw) + (size_t)bp * 3 * PS;
   const cplx<T>* tw = static_cast<const cplx<T>*>(b.twid);
-  const cplx<T>* W = static_cast<const cplx<T>*>(b.W);
-  cplx<T>* P = static_cast<cplx<T>*>(b.P);
+  const cplx<T>* W = static_cast<const cplx<T>*>(b.W) + blockIdx.y * g.bs_w;
+  cplx<T>* P = static_cast<cplx<T>*>(b.P) + blockIdx.y * g.bs_p;
   const int nl = g.nl;
   const T* eta = static_cast<const T*>(m.eta);
   const T* U1D = static_cast<const T*>(m.U1D);
@@ -523,9 +536,9 @@ __global__ void __launch_bounds__(512) col_inv_generic(Geom g, ModArgs m, const 
   cplx<T>* F = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* Fc = F + c * cs;
   const T krT = T(kr) * sel<T>(g.dkx, g.dkx_f, g.dkx_l), dky = sel<T>(g.dky, g.dky_f, g.dky_l);
-  const cplx<T>* S = static_cast<const cplx<T>*>(src);
+  const cplx<T>* S = static_cast<const cplx<T>*>(src) + blockIdx.y * g.bs_spec;
   const cplx<T>* tw = static_cast<const cplx<T>*>(b.twid);
-  cplx<T>* W = static_cast<cplx<T>*>(b.W);
+  cplx<T>* W = static_cast<cplx<T>*>(b.W) + blockIdx.y * g.bs_w;
   const size_t lstride = (size_t)g.ny * g.ldk;
   const int nl = g.nl;
   const T sc = sel<T>(g.inv_nxny, g.inv_nxny_f, g.inv_nxny_l);
@@ -579,7 +592,8 @@ __global__ void __launch_bounds__(512) row_c2r_generic(Geom g, Bufs b, int nf, T
   const int j0 = 2 * (blockIdx.x * B + bp);
   cplx<T>* buf = reinterpret_cast<cplx<T>*>(smem_raw) + (size_t)bp * row_stride<T>(NX, TPF);
   const cplx<T>* tw = static_cast<const cplx<T>*>(b.twid);
-  const cplx<T>* W = static_cast<const cplx<T>*>(b.W);
+  const cplx<T>* W = static_cast<const cplx<T>*>(b.W) + blockIdx.y * g.bs_w;
+  out += blockIdx.y * g.bs_phys;
   for (int f = 0; f < nf; ++f) {
     const cplx<T>* Wa = W + (size_t)f * g.ny * g.ldk + (size_t)j0 * g.ldk;
 #pragma unroll
@@ -611,7 +625,8 @@ __global__ void __launch_bounds__(512) row_r2c_generic(Geom g, Bufs b, int nf, c
   const int j0 = 2 * (blockIdx.x * B + bp);
   cplx<T>* buf = reinterpret_cast<cplx<T>*>(smem_raw) + (size_t)bp * row_stride<T>(NX, TPF);
   const cplx<T>* tw = static_cast<const cplx<T>*>(b.twid);
-  cplx<T>* P = static_cast<cplx<T>*>(b.P);
+  cplx<T>* P = static_cast<cplx<T>*>(b.P) + blockIdx.y * g.bs_p;
+  in += blockIdx.y * g.bs_phys;
   for (int f = 0; f < nf; ++f) {
     const T* src = in + (size_t)f * g.ny * NX + (size_t)j0 * NX;
 #pragma unroll
@@ -644,7 +659,8 @@ __global__ void __launch_bounds__(512) col_fwd_generic(Geom g, Bufs b, int nf, c
   cplx<T>* F = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* Fc = F + c * cs;
   const cplx<T>* tw = static_cast<const cplx<T>*>(b.twid);
-  const cplx<T>* P = static_cast<const cplx<T>*>(b.P);
+  const cplx<T>* P = static_cast<const cplx<T>*>(b.P) + blockIdx.y * g.bs_p;
+  out += blockIdx.y * g.bs_spec;
   const size_t lstride = (size_t)g.ny * g.ldk;
   for (int f = 0; f < nf; ++f) {
 #pragma unroll
@@ -670,7 +686,7 @@ __global__ void __launch_bounds__(512) col_fwd_generic(Geom g, Bufs b, int nf, c
 // ----------------------------------------------------------------- elementwise helpers
 template <class T>
 __global__ void mask_inplace_kernel(Geom g, cplx<T>* sol) {
-  const size_t n = (size_t)g.nl * g.ny * g.nkr;
+  const size_t n = (size_t)g.nl * g.nb * g.ny * g.nkr;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
     const int kr = e % g.nkr;
     const size_t r = e / g.nkr;
@@ -683,6 +699,8 @@ __global__ void mask_inplace_kernel(Geom g, cplx<T>* sol) {
 // op 0: out = S psi (MultiLayerQG pvfromstreamfunction!); op 1: out = psi(in)
 template <class T>
 __global__ void spec_apply_kernel(Geom g, ModArgs m, const cplx<T>* in, cplx<T>* out, int op) {
+  in += blockIdx.y * g.bs_spec;
+  out += blockIdx.y * g.bs_spec;
   const size_t n = (size_t)g.ny * g.nkr;
   const int nl = g.nl;
   const size_t lstride = (size_t)g.ny * g.ldk;
@@ -740,6 +758,9 @@ __global__ void __launch_bounds__(DIAG_BLOCK) diag_kernel(Geom g, ModArgs m, con
   const size_t n = (size_t)g.ny * g.nkr;
   const int nl = g.nl;
   const size_t lstride = (size_t)g.ny * g.ldk;
+  sol += blockIdx.y * g.bs_spec;
+  if (prevsol) prevsol += blockIdx.y * g.bs_spec;
+  if (Fh) Fh += blockIdx.y * g.bs_spec;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
     const int kr = e % g.nkr, j = e / g.nkr;
     const size_t ti = (size_t)j * g.ldk + kr;
@@ -822,7 +843,7 @@ __global__ void __launch_bounds__(DIAG_BLOCK) diag_kernel(Geom g, ModArgs m, con
       if ((int)threadIdx.x < st) red[threadIdx.x] += red[threadIdx.x + st];
       __syncthreads();
     }
-    if (threadIdx.x == 0) partial[(size_t)q * gridDim.x + blockIdx.x] = red[0];
+    if (threadIdx.x == 0) partial[((size_t)q * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = red[0];
     __syncthreads();
   }
 }

@@ -23,22 +23,22 @@ inline int num_sms() {
 // least two blocks per SM; keep shared memory under SMEM_CAP.  smem(C) gives the block's
 // dynamic shared-memory bytes for C columns.
 template <class F>
-inline int pick_C(int NY, int R, int nkr, F smem) {
+inline int pick_C(int NY, int R, int nkr, F smem, int nb = 1) {
   const int TPF = NY / R;
   int C = 512 / TPF;
   if (C < 1) C = 1;
   if (C > 16) C = 16;
   while (C > 1 && (C * TPF > 512 || smem(C) > (size_t)SMEM_CAP)) C /= 2;
-  while (C > 1 && (nkr + C - 1) / C < 2 * num_sms()) C /= 2;
+  while (C > 1 && (size_t)nb * ((nkr + C - 1) / C) < (size_t)2 * num_sms()) C /= 2;
   return C;
 }
 // Row pairs per row-kernel block (same rule: >= 2 blocks per SM when possible).
-inline int pick_B(int NX, int R, size_t elem, int nbufs, int npairs) {
+inline int pick_B(int NX, int R, size_t elem, int nbufs, int npairs, int nb = 1) {
   const int TPF = NX / R;
   int B = 256 / TPF;
   if (B < 1) B = 1;
   while (B > 1 && ((size_t)B * (NX + NX / R) * elem * nbufs > SMEM_CAP || B * TPF > 256 || npairs % B != 0)) B /= 2;
-  while (B > 1 && npairs / B < 2 * num_sms()) B /= 2;
+  while (B > 1 && (size_t)nb * (npairs / B) < (size_t)2 * num_sms()) B /= 2;
   return B;
 }
 

@@ -96,6 +96,7 @@ extern "C" int gf_rfft2_noalloc(const void* field, void* fieldh, int32_t nx, int
   gf::Geom g{};
   g.nx = nx; g.ny = ny; g.nkr = nx / 2 + 1; g.ldk = g.nkr; g.ldw = g.nkr; g.nl = 1;
   g.kcut = g.nkr; g.lA = 1; g.lB = 0;
+  g.nb = 1;  // one field: a single instance (the per-instance strides are never used)
   g.dkx = 1; g.dky = 1; g.inv_nxny = 1.0 / ((double)nx * ny);
   g.dkx_f = 1.0f; g.dky_f = 1.0f; g.inv_nxny_f = (float)g.inv_nxny;
   cudaStream_t st = (cudaStream_t)stream;

@@ -16,7 +16,7 @@ class Problem(_Problem):
 
     def __init__(self, nlayers, dev="GPU", nx=128, ny=None, Lx=2 * np.pi, Ly=None, f0=1.0, beta=0.0, U=None,
                  H=None, b=None, eta=None, topographic_pv_gradient=(0.0, 0.0), mu=0.0, nu=0.0, nnu=1, dt=0.01,
-                 stepper="RK4", forcing=None, linear=False, aliased_fraction=1 / 3, T=np.float64, stream=None, precision=None):
+                 stepper="RK4", forcing=None, linear=False, aliased_fraction=1 / 3, T=np.float64, stream=None, precision=None, batch=1):
         _check_dev(dev)
         ny = nx if ny is None else ny
         Ly = Lx if Ly is None else Ly
@@ -40,7 +40,7 @@ class Problem(_Problem):
                   topographic_pv_gradient=tuple(float(v) for v in topographic_pv_gradient))
         if eta is not None:
             kw["eta"] = np.asarray(eta, dtype=np.float64).reshape(ny, nx)
-        super().__init__(kw, nx, ny, Lx, Ly, dt, stepper, T, aliased_fraction, forcing, nlayers=n, stream=stream, precision=precision)
+        super().__init__(kw, nx, ny, Lx, Ly, dt, stepper, T, aliased_fraction, forcing, nlayers=n, stream=stream, precision=precision, batch=batch)
         self.H, self.b, self.f0, self.Uy = H, b, f0, Uy
 
 

@@ -15,7 +15,7 @@ class Problem(_Problem):
 
     def __init__(self, dev="GPU", nx=256, ny=None, Lx=2 * np.pi, Ly=None, beta=0.0, deformation_radius=np.inf,
                  U=0.0, eta=None, nu=0.0, nnu=1, mu=0.0, dt=0.01, stepper="RK4", forcing=None,
-                 aliased_fraction=1 / 3, T=np.float64, stream=None, precision=None):
+                 aliased_fraction=1 / 3, T=np.float64, stream=None, precision=None, batch=1):
         _check_dev(dev)
         ny = nx if ny is None else ny
         Ly = Lx if Ly is None else Ly
@@ -34,7 +34,7 @@ class Problem(_Problem):
                 X, Y = np.meshgrid(x, y, indexing="xy")
                 eta = np.asarray(eta(X, Y), dtype=np.float64) * np.ones((ny, nx))
             kw["eta"] = np.asarray(eta, dtype=np.float64).reshape(ny, nx)
-        super().__init__(kw, nx, ny, Lx, Ly, dt, stepper, T, aliased_fraction, forcing, stream=stream, precision=precision)
+        super().__init__(kw, nx, ny, Lx, Ly, dt, stepper, T, aliased_fraction, forcing, stream=stream, precision=precision, batch=batch)
         self.beta, self.U, self.mu, self.nu, self.nnu = beta, U, mu, nu, nnu
 
 

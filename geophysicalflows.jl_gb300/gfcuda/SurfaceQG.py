@@ -13,12 +13,12 @@ class Problem(_Problem):
     field_names = {A.FIELD_Q: "b", A.FIELD_PSI: "psi", A.FIELD_U: "u", A.FIELD_V: "v"}
 
     def __init__(self, dev="GPU", nx=256, ny=None, Lx=2 * np.pi, Ly=None, H=np.inf, nu=0.0, nnu=1, dt=0.01,
-                 stepper="RK4", forcing=None, aliased_fraction=1 / 3, T=np.float64, stream=None, precision=None):
+                 stepper="RK4", forcing=None, aliased_fraction=1 / 3, T=np.float64, stream=None, precision=None, batch=1):
         _check_dev(dev)
         ny = nx if ny is None else ny
         Ly = Lx if Ly is None else Ly
         super().__init__(dict(nu=float(nu), nnu=int(nnu), H_sqg=(0.0 if np.isinf(H) else float(H))), nx, ny, Lx,
-                         Ly, dt, stepper, T, aliased_fraction, forcing, stream=stream, precision=precision)
+                         Ly, dt, stepper, T, aliased_fraction, forcing, stream=stream, precision=precision, batch=batch)
         self.H = H
 
 

@@ -23,12 +23,12 @@ class Problem(_Problem):
     field_names = {A.FIELD_Q: "zeta", A.FIELD_PSI: "psi", A.FIELD_U: "u", A.FIELD_V: "v"}
 
     def __init__(self, dev="GPU", nx=256, ny=None, Lx=2 * np.pi, Ly=None, nu=0.0, nnu=1, mu=0.0, nmu=0,
-                 dt=0.01, stepper="RK4", forcing=None, aliased_fraction=1 / 3, T=np.float64, stream=None, precision=None):
+                 dt=0.01, stepper="RK4", forcing=None, aliased_fraction=1 / 3, T=np.float64, stream=None, precision=None, batch=1):
         _check_dev(dev)
         ny = nx if ny is None else ny
         Ly = Lx if Ly is None else Ly
         super().__init__(dict(nu=float(nu), nnu=int(nnu), mu=float(mu), nmu=int(nmu)), nx, ny, Lx, Ly, dt,
-                         stepper, T, aliased_fraction, forcing, stream=stream, precision=precision)
+                         stepper, T, aliased_fraction, forcing, stream=stream, precision=precision, batch=batch)
         self.params = Params(nu, nnu, mu, nmu)
 
 

@@ -4,8 +4,8 @@ Host-side mirror of the reference's module API; every computation runs in libgfc
 """
 from . import _abi
 from ._abi import load, GFError, GFNotImplemented
-from .core import Diagnostic, Forcing, stepforward
+from .core import Diagnostic, Forcing, ensemble_step, stepforward
 from . import TwoDNavierStokes, SingleLayerQG, MultiLayerQG, SurfaceQG
 
-__all__ = ["load", "GFError", "GFNotImplemented", "Diagnostic", "Forcing", "stepforward", "TwoDNavierStokes",
+__all__ = ["load", "GFError", "GFNotImplemented", "Diagnostic", "Forcing", "ensemble_step", "stepforward", "TwoDNavierStokes",
            "SingleLayerQG", "MultiLayerQG", "SurfaceQG"]

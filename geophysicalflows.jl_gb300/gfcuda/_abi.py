@@ -19,7 +19,7 @@ EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_abi_version", "gf_get
            "gf_get_state", "gf_get_clock", "gf_set_clock", "gf_set_physical", "gf_step", "gf_step_diags",
            "gf_calcN", "gf_updatevars", "gf_get_field", "gf_fwdtransform", "gf_invtransform",
            "gf_diagnostics", "gf_set_forcing", "gf_synchronize", "gf_profile_enable", "gf_profile_read",
-           "gf_rfft2_noalloc"]
+           "gf_rfft2_noalloc", "gf_get_batch", "gf_set_graph_steps", "gf_ensemble_step"]
 
 
 class gf_config(C.Structure):
@@ -36,6 +36,7 @@ class gf_config(C.Structure):
         ("forcing_kind", C.c_int32), ("seed", C.c_uint64), ("forcing_omega", C.c_double), ("forcing_phase", C.c_double),
         ("filter_order", C.c_double), ("filter_innerK", C.c_double), ("filter_outerK", C.c_double),
         ("etdrk4_ncirc", C.c_int32), ("etdrk4_rcirc", C.c_double),
+        ("batch", C.c_int32),
     ]
 
 
@@ -78,6 +79,9 @@ def load(path=None):
         "gf_profile_enable": ([vp, C.c_int], C.c_int),
         "gf_profile_read": ([vp, C.POINTER(dbl), C.POINTER(i64), C.POINTER(i64)], C.c_int),
         "gf_rfft2_noalloc": ([vp, vp, i32, i32, i32, vp], C.c_int),
+        "gf_get_batch": ([vp, C.POINTER(i32)], C.c_int),
+        "gf_set_graph_steps": ([vp, i32], C.c_int),
+        "gf_ensemble_step": ([C.POINTER(vp), i32, i64], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

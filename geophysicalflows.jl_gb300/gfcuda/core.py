@@ -87,7 +87,7 @@ class Problem:
     field_names = {A.FIELD_Q: "q", A.FIELD_PSI: "psi", A.FIELD_U: "u", A.FIELD_V: "v"}
 
     def __init__(self, cfg_kwargs, nx, ny, Lx, Ly, dt, stepper, T, aliased_fraction, forcing, nlayers=1,
-                 stream=None, precision=None):
+                 stream=None, precision=None, batch=1):
         self._lib = A.load()
         self._ctx = C.c_void_p()
         if stepper not in A.STEPPERS:
@@ -112,6 +112,8 @@ class Problem:
         cfg.Lx, cfg.Ly, cfg.dt, cfg.aliased_fraction = Lx, Ly, dt, aliased_fraction
         cfg.forcing_kind = A.FORCING[self.forcing.kind]
         cfg.seed = int(self.forcing.seed)
+        self.batch = int(batch)
+        cfg.batch = self.batch
         cfg.forcing_omega, cfg.forcing_phase = self.forcing.omega, self.forcing.phase
         self._keep = []  # arrays referenced by cfg during gf_create
         for k, v in cfg_kwargs.items():
@@ -136,12 +138,14 @@ class Problem:
     @property
     def spec_shape(self):
         g = self.grid
-        return (self.nlayers, g.ny, g.nkr) if self.module == "MultiLayerQG" else (g.ny, g.nkr)
+        shp = (self.nlayers, g.ny, g.nkr) if self.module == "MultiLayerQG" else (g.ny, g.nkr)
+        return ((self.batch,) + shp) if self.batch > 1 else shp
 
     @property
     def phys_shape(self):
         g = self.grid
-        return (self.nlayers, g.ny, g.nx) if self.module == "MultiLayerQG" else (g.ny, g.nx)
+        shp = (self.nlayers, g.ny, g.nx) if self.module == "MultiLayerQG" else (g.ny, g.nx)
+        return ((self.batch,) + shp) if self.batch > 1 else shp
 
     def _c(self, code):
         A.check(self._lib, self._ctx, code)
@@ -171,6 +175,10 @@ class Problem:
 
     def set_clock(self, t, step):
         self._c(self._lib.gf_set_clock(self._ctx, float(t), int(step)))
+
+    def set_graph_steps(self, n):
+        """Steps per captured CUDA graph (0: launch kernel by kernel)."""
+        self._c(self._lib.gf_set_graph_steps(self._ctx, int(n)))
 
     def set_forcing(self, data):
         if self.forcing.stochastic:
@@ -214,11 +222,12 @@ class Problem:
         return out
 
     def diagnostics(self, ids):
+        """Values of the diagnostics `ids`; shape (len(ids),) or (batch, len(ids))."""
         ids = np.ascontiguousarray(ids, dtype=np.int32)
-        out = np.empty(len(ids), dtype=np.float64)
+        out = np.empty(len(ids) * self.batch, dtype=np.float64)
         self._c(self._lib.gf_diagnostics(self._ctx, ids.ctypes.data_as(C.POINTER(C.c_int32)), len(ids),
                                          out.ctypes.data_as(C.POINTER(C.c_double))))
-        return out
+        return out.reshape(self.batch, len(ids)) if self.batch > 1 else out
 
     def synchronize(self):
         self._c(self._lib.gf_synchronize(self._ctx))
@@ -262,6 +271,16 @@ def stepforward(prob, *args):
         prob._c(prob._lib.gf_step(prob._ctx, 1))
         for d in diags:
             d.increment()
+
+
+def ensemble_step(probs, nsteps):
+    """Step several problems (e.g. batched problems of different grid sizes) together; each
+    runs on its own stream, so they execute concurrently on the GPU."""
+    lib = probs[0]._lib
+    arr = (C.c_void_p * len(probs))(*[p._ctx.value for p in probs])
+    code = lib.gf_ensemble_step(arr, len(probs), int(nsteps))
+    if code != A.GF_OK:
+        raise A.GFError(code, lib.gf_last_error(None).decode(errors="replace"))
 
 
 def dealias(prob):

@@ -105,6 +105,11 @@ typedef struct gf_config {
   /* ETDRK4 contour (FourierFlows getetdcoeffs); 0 = defaults ncirc=32, rcirc=1 */
   int32_t etdrk4_ncirc;
   double etdrk4_rcirc;
+  /* ensemble: number of independent instances of this problem in the context (0 or 1 =
+   * one).  Instances share grid, parameters and stepper; each has its own state, forcing
+   * draws (Philox key seed + instance) and diagnostics.  Arrays at the ABI gain a leading
+   * (slowest) instance dimension. */
+  int32_t batch;
 } gf_config;
 
 /* Field selectors for gf_get_field / gf_set_physical */
@@ -179,8 +184,22 @@ int gf_get_field(gf_ctx* ctx, int which, void* out, int where);
 int gf_fwdtransform(gf_ctx* ctx, void* fieldh, const void* field, int where);
 int gf_invtransform(gf_ctx* ctx, void* field, const void* fieldh, int where);
 
-/* Parseval-sum diagnostics (reductions in FP64 with compensated sums on the GPU). */
+/* Parseval-sum diagnostics (reductions in FP64 with compensated sums on the GPU);
+ * out[instance * nd + i] for a batched context. */
 int gf_diagnostics(gf_ctx* ctx, const int32_t* which, int32_t nd, double* out);
+int gf_get_batch(const gf_ctx* ctx, int32_t* batch);
+
+/* ---- graphs and ensembles -------------------------------------------------------------
+ * gf_step replays a CUDA graph of `steps` captured time steps (the step counter, time and
+ * harmonic-forcing phases live on the GPU, so one graph serves every later step); AB3
+ * problems always use graphs of 3 steps (their right-hand-side ring has period 3).
+ * steps = 0 launches kernel by kernel.  Default 4.  No counterpart in the reference
+ * (its steps are launched broadcast by broadcast). */
+int gf_set_graph_steps(gf_ctx* ctx, int32_t steps);
+/* Steps n contexts (e.g. one batched context per grid size of an ensemble) by nsteps each;
+ * every context runs on its own stream, so the size classes execute concurrently.
+ * Errors: gf_last_error(NULL). */
+int gf_ensemble_step(gf_ctx* const* ctxs, int32_t n, int64_t nsteps);
 
 /* F-hat for GF_FORCING_STATIC / HARMONIC (same layout as sol), or the forcing spectrum
  * (real, (nkr, ny), the reference's `forcing_spectrum`) for the stochastic kinds.  This is
