@@ -3,14 +3,16 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 Headline workload: TwoDNavierStokes 2048^2, FilteredRK4, nu = 0, peaked isotropic initial
-vorticity (k0 = 6, E = 0.5) -- the configuration the task's FP32-fused vs FP64-plain target is
+vorticity (k0 = 6, E = 0.5) -- the configuration the FP32-fused vs FP64-plain target is
 quoted on.  A "step" is one FilteredRK4 time step (4 calcN! stages).  `value` is FP32-fused
 grid-point*steps/s with the state resident in HBM; the FP64-plain arm, its roofline and the
-FP32-vs-FP64 error are reported beside it, and so is configs[1] (SingleLayerQG 512^2 ETDRK4
-with stochastic forcing, FP32 vs FP64).  L2 is flushed (256 MiB write) between timed steps.
+FP32-vs-FP64 error are reported beside it, and so are the other GPU workloads: SingleLayerQG
+512^2 ETDRK4 with stochastic forcing, MultiLayerQG 3 x 1024^2 ETDRK4, and the 1536-run
+TwoDNavierStokes ensemble (1024 x 64^2 + 384 x 128^2 + 128 x 256^2).  L2 is flushed (256 MiB
+write) between timed steps; graph-replayed multi-step timings are reported beside them.
 `--impl reference` times the FP64 CPU restatement of the reference (oracle/, scipy.fft on all
 host cores) on the same workload.  For N > 1 (torchrun) every rank runs an independent
-replica (the path does not shard) and rank 0 reports the aggregate.
+replica (the path does not shard) and rank 0 reports the aggregate over the slowest rank.
 """
 import argparse
 import json
@@ -33,6 +35,15 @@ METRIC = "grid-pt·steps/s FP32-fused vs FP64-plain (≤1e-5 rel L2); adjoint/fo
 UNIT = "grid-pt*steps/s"
 HEADLINE = dict(module="TwoDNavierStokes", nx=2048, ny=2048, stepper="FilteredRK4", dt=5e-4)
 CONFIG1 = dict(module="SingleLayerQG", nx=512, ny=512, stepper="ETDRK4", dt=0.05, beta=10.0, mu=0.01)
+# 3 layers, H = [.2,.3,.5], rho = [4, 5, 5.5] -> b with g' = g (rho_{j+1} - rho_j) / rho_{j+1}, g = 1
+CONFIG2 = dict(module="MultiLayerQG", nx=1024, ny=1024, nlayers=3, stepper="ETDRK4", dt=2.5e-3, f0=1.0, beta=5.0,
+               H=[0.2, 0.3, 0.5], b=[-1.0, -1.2, -1.2 - 0.5 / 5.5], U=[1.0, 0.5, 0.0], mu=0.05)
+# gradient of the final kinetic energy: SingleLayerQG 256^2, deformation radius 0.35,
+# topography |k| <= 8 amplitude 0.1, ETDRK4 dt = 0.01, 500 steps, checkpoint every 25
+CONFIG3 = dict(module="SingleLayerQG", nx=256, ny=256, stepper="ETDRK4", dt=0.01, ell=0.35, nsteps=500, every=25)
+# 1536 independent TwoDNavierStokes runs in three batched size classes (size, instances)
+ENSEMBLE = dict(classes=((64, 1024), (128, 384), (256, 128)), stepper="FilteredRK4", dt=0.01, nu=1e-4, nnu=1,
+                kf=8.0, dkf=1.5, eps=1e-3)
 
 
 def algorithmic_words(module, stepper, nlayers=1, eta=False):
@@ -137,43 +148,70 @@ def make_problem(w, T, precision=None):
     if w["module"] == "TwoDNavierStokes":
         return gfcuda.TwoDNavierStokes.Problem("GPU", nx=w["nx"], ny=w["ny"], dt=w["dt"], stepper=w["stepper"], T=T,
                                                precision=precision)
-    import gf_oracle as O
-    g = O.Grid(w["nx"])
-    spec = O.ring_forcing_spectrum(g, 14.0 * 2 * np.pi / g.Lx, 1.5 * 2 * np.pi / g.Lx, 1e-3)
+    if w["module"] == "MultiLayerQG":
+        return gfcuda.MultiLayerQG.Problem(w["nlayers"], "GPU", nx=w["nx"], ny=w["ny"], f0=w["f0"], beta=w["beta"],
+                                           H=w["H"], b=w["b"], U=w["U"], mu=w["mu"], dt=w["dt"],
+                                           stepper=w["stepper"], T=T, precision=precision)
+    from gfcuda.core import Grid
+    g = Grid(w["nx"], w["ny"], 2 * np.pi, 2 * np.pi, 1 / 3, np.float64)
+    spec = gfcuda.utils.ring_forcing_spectrum(g, 14.0, 1.5, 1e-3)
     f = gfcuda.Forcing("stochastic", spectrum=spec, seed=1234)
     return gfcuda.SingleLayerQG.Problem("GPU", nx=w["nx"], beta=w["beta"], mu=w["mu"], dt=w["dt"],
                                         stepper=w["stepper"], forcing=f, T=T, precision=precision)
 
 
-def initial_state(w):
+def set_initial_state(prob, w):
+    """The workload's initial condition, made by the library (peaked isotropic vorticity on the
+    device) or from a seeded generator (MultiLayerQG white noise); SingleLayerQG starts at rest."""
+    import gfcuda
+    if w["module"] == "TwoDNavierStokes":
+        z0 = gfcuda.peakedisotropicspectrum(prob.grid, 6, 0.5, mask=prob.timestepper.filter, seed=1234)
+        gfcuda.TwoDNavierStokes.set_zeta(prob, z0)
+    elif w["module"] == "MultiLayerQG":
+        q0 = 1e-2 * np.random.default_rng(1234).standard_normal((w["nlayers"], w["ny"], w["nx"]))
+        gfcuda.MultiLayerQG.set_q(prob, q0)
+
+
+def initial_state_oracle(w):
+    """The same initial condition from the oracle, for the CPU legs."""
     import gf_oracle as O
     if w["module"] == "TwoDNavierStokes":
         g = O.Grid(w["nx"])
         return O.peakedisotropicspectrum(g, 6, 0.5, mask=O.makefilter(g), seed=1234)
+    if w["module"] == "MultiLayerQG":
+        return 1e-2 * np.random.default_rng(1234).standard_normal((w["nlayers"], w["ny"], w["nx"]))
     return np.zeros((w["ny"], w["nx"]))
 
 
-def time_arm(w, T, steps, warmup, flush, with_e2e, precision=None):
-    """Run one precision arm: warm-up, K timed steps (CUDA events on the library's stream,
-    L2 flushed between steps), kernel timing, optional end-to-end timing."""
+def points(w):
+    return w["nx"] * w["ny"] * w.get("nlayers", 1)
+
+
+def _events(n):
+    import torch
+    return [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+
+
+def time_arm(w, T, steps, warmup, flush, with_e2e, precision=None, graph=True):
+    """Run one precision arm: warm-up, K timed steps launched one gf_step at a time (CUDA
+    events on the legacy default stream, which orders with the library's blocking stream;
+    L2 flushed between steps) with the library's per-kernel event timing on, then K steps
+    replayed from captured multi-step CUDA graphs (one event pair), then optionally the
+    end-to-end timing through the host-buffer API."""
+    import ctypes as C
     import torch
     import gfcuda
     prob = make_problem(w, T, precision)
-    z0 = initial_state(w)
-    if w["module"] == "TwoDNavierStokes":
-        gfcuda.TwoDNavierStokes.set_zeta(prob, z0)
-    else:
-        gfcuda.SingleLayerQG.set_q(prob, z0)
+    set_initial_state(prob, w)
     gfcuda.stepforward(prob, warmup)
     prob.synchronize()
     lib, ctx = prob._lib, prob._ctx
-    import ctypes as C
     ms2 = (C.c_double * 2)()
     n2 = (C.c_int64 * 2)()
     nl = C.c_int64()
     lib.gf_profile_read(ctx, ms2, n2, C.byref(nl))  # reset counters
     lib.gf_profile_enable(ctx, 1)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    ev = _events(steps)
     for i in range(steps):
         flush.zero_()
         ev[i][0].record()
@@ -185,6 +223,16 @@ def time_arm(w, T, steps, warmup, flush, with_e2e, precision=None):
     lib.gf_profile_enable(ctx, 0)
     res = {"ms_per_step": sum(ms) / steps, "ms_row": ms2[0] / max(n2[0], 1), "ms_col": ms2[1] / max(n2[1], 1),
            "n_row": n2[0], "n_col": n2[1], "launches": nl.value}
+    if graph:
+        gfcuda.stepforward(prob, 4)  # captures the graph outside the timed region
+        (e0, e1), = _events(1)
+        flush.zero_()
+        e0.record()
+        prob._c(lib.gf_step(ctx, steps))
+        e1.record()
+        torch.cuda.synchronize()
+        res["ms_per_step_graph"] = e0.elapsed_time(e1) / steps
+    res["sol"] = prob.sol   # the state after the same number of steps in every arm
     if with_e2e:
         shape = prob.spec_shape
         hin = torch.empty(int(np.prod(shape)) * 2, dtype=torch.float32 if T == np.float32 else torch.float64,
@@ -204,9 +252,64 @@ def time_arm(w, T, steps, warmup, flush, with_e2e, precision=None):
             hin_np[:] = hout_np
         res["e2e_s_per_step"] = tot / steps
         res["state_bytes"] = hin.numel() * hin.element_size()
-    res["sol"] = prob.sol
     prob.close()
     return res
+
+
+def accuracy_100_steps(w, nsteps=100):
+    """FP32 and FP64 (IEEE and df64) runs of the same workload from the same initial state:
+    relative L2 difference of the FP32 and df64 states from the IEEE FP64 state after
+    nsteps steps (the FP64 path itself matches the FP64 oracle to 1e-12 per step)."""
+    import gfcuda
+    sols = {}
+    for key, T, prec in (("f32", np.float32, None), ("df64", np.float64, "DF64"), ("f64", np.float64, None)):
+        p = make_problem(w, T, prec)
+        set_initial_state(p, w)
+        gfcuda.stepforward(p, nsteps)
+        sols[key] = p.sol
+        p.close()
+    return {"steps": nsteps, "fp32_vs_fp64": relerr(sols["f32"], sols["f64"]),
+            "df64_vs_fp64": relerr(sols["df64"], sols["f64"])}
+
+
+def time_ensemble(steps, warmup, flush):
+    """The 1536-run ensemble: one batched Problem per size class (instance i of a class
+    draws its forcing with seed + i), all stepped by gf_ensemble_step; each class runs on its
+    own stream, concurrently.  Per-step timing with L2 flushes, then graph replay."""
+    import torch
+    import gfcuda
+    from gfcuda.core import Grid
+    e = ENSEMBLE
+    probs = []
+    for n, B in e["classes"]:
+        g = Grid(n, n, 2 * np.pi, 2 * np.pi, 1 / 3, np.float64)
+        spec = gfcuda.utils.ring_forcing_spectrum(g, e["kf"], e["dkf"], e["eps"])
+        probs.append(gfcuda.TwoDNavierStokes.Problem(
+            "GPU", nx=n, dt=e["dt"], nu=e["nu"], nnu=e["nnu"], stepper=e["stepper"], T=np.float32, batch=B,
+            forcing=gfcuda.Forcing("stochastic", spectrum=spec, seed=1000 * n)))
+    gfcuda.ensemble_step(probs, warmup)
+    torch.cuda.synchronize()
+    ev = _events(steps)
+    for i in range(steps):
+        flush.zero_()
+        ev[i][0].record()
+        gfcuda.ensemble_step(probs, 1)
+        ev[i][1].record()
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+    gfcuda.ensemble_step(probs, 4)
+    (e0, e1), = _events(1)
+    flush.zero_()
+    e0.record()
+    gfcuda.ensemble_step(probs, steps)
+    e1.record()
+    torch.cuda.synchronize()
+    ms_graph = e0.elapsed_time(e1) / steps
+    E = [float(np.mean(p.diagnostics([0])[:, 0])) for p in probs]
+    for p in probs:
+        p.close()
+    pts = sum(n * n * B for n, B in e["classes"])
+    return {"ms_per_step": ms, "ms_per_step_graph": ms_graph, "points": pts, "mean_energy": E}
 
 
 def cpu_baseline(w, seconds=20.0, max_steps=5):
@@ -217,7 +320,7 @@ def cpu_baseline(w, seconds=20.0, max_steps=5):
     try:
         if w["module"] == "TwoDNavierStokes":
             r = O.TwoDNavierStokes(nx=w["nx"], dt=w["dt"], stepper=w["stepper"])
-            r.set_zeta(initial_state(w))
+            r.set_zeta(initial_state_oracle(w))
         else:
             g = O.Grid(w["nx"])
             spec = O.ring_forcing_spectrum(g, 14.0, 1.5, 1e-3)
@@ -244,7 +347,7 @@ def run_reference(args):
     cores = os.cpu_count() or 1
     O.set_fft_workers(cores)
     r = O.TwoDNavierStokes(nx=w["nx"], dt=w["dt"], stepper=w["stepper"])
-    r.set_zeta(initial_state(w))
+    r.set_zeta(initial_state_oracle(w))
     r.stepforward(args.warmup)
     t0 = time.perf_counter()
     r.stepforward(args.steps)
@@ -263,6 +366,91 @@ def run_reference(args):
     return 0
 
 
+def time_adjoint(flush, T=np.float32, precision=None, reps=2):
+    """Forward stepforward!(prob, 500) against gf_grad over the same 500 steps (forward
+    with checkpoints + loss + reverse sweep) with device-resident gradients, CUDA events on
+    the legacy default stream; best of `reps` after one untimed run of each."""
+    import torch
+    import gfcuda
+    from gfcuda.core import Grid
+    w = CONFIG3
+    g = Grid(w["nx"], w["ny"], 2 * np.pi, 2 * np.pi, 1 / 3, np.float64)
+    eta = gfcuda.utils.random_topography(g, 8, 0.1, seed=3)
+    p = gfcuda.SingleLayerQG.Problem("GPU", nx=w["nx"], deformation_radius=w["ell"], eta=eta, dt=w["dt"],
+                                     stepper=w["stepper"], T=T, precision=precision)
+    q0 = gfcuda.peakedisotropicspectrum(p.grid, 6, 0.5, seed=1234)
+    gfcuda.adjoint.setup(p, w["nsteps"], w["every"])
+    tdt = torch.float32 if T == np.float32 else torch.float64
+    dq0 = torch.empty((w["ny"], w["nx"]), dtype=tdt, device="cuda")
+    deta = torch.empty_like(dq0)
+    import ctypes as C
+    loss = C.c_double()
+    lib, ctx = p._lib, p._ctx
+
+    def fwd():
+        gfcuda.SingleLayerQG.set_q(p, q0)
+        flush.zero_()
+        (e0, e1), = _events(1)
+        e0.record()
+        p._c(lib.gf_step(ctx, w["nsteps"]))
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    def grad():
+        gfcuda.SingleLayerQG.set_q(p, q0)
+        flush.zero_()
+        (e0, e1), = _events(1)
+        e0.record()
+        p._c(lib.gf_grad(ctx, 0, C.c_void_p(dq0.data_ptr()), C.c_void_p(deta.data_ptr()), None, 1))
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    fwd(), grad()
+    tf = min(fwd() for _ in range(reps))
+    tg = min(grad() for _ in range(reps))
+    p.close()
+    n = w["nsteps"]
+    return {"forward_ms_per_step": tf / n, "grad_ms_per_step": tg / n,
+            "adjoint_over_forward": (tg - tf) / tf, "grad_over_forward": tg / tf}
+
+
+def reduce_max(dist, vals):
+    """Element-wise maximum of `vals` over ranks (the slowest replica sets each time)."""
+    if not dist:
+        return [float(v) for v in vals]
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(v) for v in vals], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def whole_job(points_per_rank, world, ms_max):
+    """Grid-point*steps/s of all replicas: every rank advanced points_per_rank points per
+    step, and the job took the slowest rank's time."""
+    return world * points_per_rank / (ms_max * 1e-3)
+
+
+def roofline(w, res, wbytes, tag, peaks, peak_src):
+    """HBM roofline of the dominant kernel of an arm: algorithmic bytes per launch of the
+    two-sweep model over the launch duration timed with CUDA events on the library stream."""
+    words, row_w, col_w = algorithmic_words(w["module"], w["stepper"], w.get("nlayers", 1))
+    dom = "col_stage" if res["ms_col"] >= res["ms_row"] else "row_nl"
+    per_launch = (col_w if dom == "col_stage" else row_w) * wbytes * points(w)
+    t = res["ms_col"] if dom == "col_stage" else res["ms_row"]
+    ach = per_launch / (t * 1e-3) / 1e9
+    return {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": ach / peaks["hbm_gbs"], "peak_source": peak_src, "traffic": ncu_traffic(dom, tag),
+            "algorithmic_bytes_per_launch": per_launch, "launch_ms": t, "row_ms": res["ms_row"],
+            "col_ms": res["ms_col"], "step_words_per_pt": words}
+
+
+def relerr(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
 def run_ours(args):
     import torch
     dist = dist_setup(args.gpus)
@@ -279,77 +467,92 @@ def run_ours(args):
     torch.cuda.synchronize()
     with Clocks() as clk:
         r32 = time_arm(w, np.float32, args.steps, args.warmup, flush, with_e2e=True)
-    rdf = time_arm(w, np.float64, args.steps, args.warmup, flush, with_e2e=True, precision="DF64")
-    r64 = time_arm(w, np.float64, args.steps, args.warmup, flush, with_e2e=False)
-    c32 = time_arm(CONFIG1, np.float32, args.steps, args.warmup, flush, with_e2e=False)
-    cdf = time_arm(CONFIG1, np.float64, args.steps, args.warmup, flush, with_e2e=False, precision="DF64")
-    c64 = time_arm(CONFIG1, np.float64, args.steps, args.warmup, flush, with_e2e=False)
-    ms = r32["ms_per_step"]
+        rdf = time_arm(w, np.float64, args.steps, args.warmup, flush, with_e2e=True, precision="DF64")
+        r64 = time_arm(w, np.float64, args.steps, args.warmup, flush, with_e2e=False)
+        c32 = time_arm(CONFIG1, np.float32, args.steps, args.warmup, flush, with_e2e=False)
+        cdf = time_arm(CONFIG1, np.float64, args.steps, args.warmup, flush, with_e2e=False, precision="DF64")
+        c64 = time_arm(CONFIG1, np.float64, args.steps, args.warmup, flush, with_e2e=False)
+        m32 = time_arm(CONFIG2, np.float32, args.steps, args.warmup, flush, with_e2e=False)
+        mdf = time_arm(CONFIG2, np.float64, args.steps, args.warmup, flush, with_e2e=False, precision="DF64")
+        ens = time_ensemble(args.steps, args.warmup, flush)
+        adj32 = time_adjoint(flush)
+        adj64 = time_adjoint(flush, np.float64)
+    acc = accuracy_100_steps(w)
+    ms, msg, msdf, ms64, e2e_s, e2e_df = reduce_max(dist, [
+        r32["ms_per_step"], r32["ms_per_step_graph"], rdf["ms_per_step"], r64["ms_per_step"],
+        1e3 * r32["e2e_s_per_step"], 1e3 * rdf["e2e_s_per_step"]])
     if dist:
-        t = torch.tensor([ms, rdf["ms_per_step"], r64["ms_per_step"], r32["e2e_s_per_step"], rdf["e2e_s_per_step"]],
-                         device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms, msdf, ms64, e2e_s, e2e_df = t.tolist()
-    else:
-        msdf, ms64, e2e_s, e2e_df = rdf["ms_per_step"], r64["ms_per_step"], r32["e2e_s_per_step"], rdf["e2e_s_per_step"]
+        dist.barrier()
     if not is_rank0():
         return 0
-    pts = w["nx"] * w["ny"]
-    value = world * pts / (ms * 1e-3)
-    vdf = world * pts / (msdf * 1e-3)
-    v64 = world * pts / (ms64 * 1e-3)
-
-    def roofline(res, wbytes):
-        words, row_w, col_w = algorithmic_words(w["module"], w["stepper"])
-        dom = "col_stage" if res["ms_col"] >= res["ms_row"] else "row_nl"
-        per_launch = (col_w if dom == "col_stage" else row_w) * wbytes * pts
-        t = res["ms_col"] if dom == "col_stage" else res["ms_row"]
-        ach = per_launch / (t * 1e-3) / 1e9
-        tag = "fp32" if res is r32 else "df64" if res is rdf else "fp64"
-        return {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": ach / peaks["hbm_gbs"], "peak_source": peak_src,
-                "traffic": ncu_traffic(dom, f"twodns2048_{tag}"), "algorithmic_bytes_per_launch": per_launch,
-                "launch_ms": t, "row_ms": res["ms_row"], "col_ms": res["ms_col"],
-                "step_words_per_pt": words}
-
-    def relerr(a, b):
-        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
-
+    pts = points(w)
+    value = whole_job(pts, world, ms)
+    vdf = whole_job(pts, world, msdf)
+    v64 = whole_job(pts, world, ms64)
     err = relerr(r32["sol"], r64["sol"])
     dferr = relerr(rdf["sol"], r64["sol"])
     cerr = relerr(c32["sol"], c64["sol"])
     cdferr = relerr(cdf["sol"], c64["sol"])
+    merr = relerr(m32["sol"], mdf["sol"])
     cpu = cpu_baseline(w)
+    c1p, c2p = points(CONFIG1), points(CONFIG2)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
         "config": {"workload": "TwoDNavierStokes 2048^2 FilteredRK4 dt=5e-4 nu=0, peaked isotropic IC (k0=6, E=0.5)",
                    "nx": w["nx"], "ny": w["ny"], "stepper": w["stepper"], "precision": "FP32 bulk",
-                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}"},
-        "roofline": roofline(r32, 4),
+                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}",
+                   "ms_per_step_graph": msg},
+        "roofline": roofline(w, r32, 4, "twodns2048_fp32", peaks, peak_src),
         "cpu_baseline": cpu,
-        "e2e": {"value": world * pts / e2e_s, "unit": UNIT, "h2d_bytes_per_step": r32["state_bytes"],
+        "e2e": {"value": whole_job(pts, world, e2e_s), "unit": UNIT, "h2d_bytes_per_step": r32["state_bytes"],
                 "d2h_bytes_per_step": r32["state_bytes"]},
         "gpu_launches": r32["launches"],
         "clocks": clk.summary(int(os.environ.get("LOCAL_RANK", "0"))),
         "fp64_plain": {"arithmetic": "df64 (double-float pairs, 48-bit significand, FP32 pipes)", "value": vdf,
-                       "ms_per_step": msdf, "roofline": roofline(rdf, 8),
-                       "e2e": {"value": world * pts / e2e_df, "unit": UNIT},
+                       "ms_per_step": msdf, "ms_per_step_graph": rdf["ms_per_step_graph"],
+                       "roofline": roofline(w, rdf, 8, "twodns2048_df64", peaks, peak_src),
+                       "e2e": {"value": whole_job(pts, world, e2e_df), "unit": UNIT},
                        "rel_l2_vs_ieee_fp64": dferr},
-        "fp64_ieee": {"value": v64, "ms_per_step": ms64, "roofline": roofline(r64, 8)},
+        "fp64_ieee": {"value": v64, "ms_per_step": ms64,
+                      "roofline": roofline(w, r64, 8, "twodns2048_fp64", peaks, peak_src)},
         "fp32_over_fp64": value / vdf,
         "fp32_over_ieee_fp64": value / v64,
-        "fp32_vs_fp64_rel_l2": err,
-        "fp32_vs_fp64_steps": args.warmup + args.steps,
-        "configs1": {"workload": "SingleLayerQG 512^2 beta=10 mu=0.01 ETDRK4 dt=0.05, stochastic ring forcing "
-                                 "kf=14 eps=1e-3, q0=0 (L2-resident: latency, no HBM fraction)",
-                     "fp32": CONFIG1["nx"] * CONFIG1["ny"] / (c32["ms_per_step"] * 1e-3),
-                     "fp64_plain_df64": CONFIG1["nx"] * CONFIG1["ny"] / (cdf["ms_per_step"] * 1e-3),
-                     "fp64_ieee": CONFIG1["nx"] * CONFIG1["ny"] / (c64["ms_per_step"] * 1e-3),
-                     "ms_per_step_fp32": c32["ms_per_step"], "ms_per_step_df64": cdf["ms_per_step"],
-                     "ms_per_step_fp64": c64["ms_per_step"],
-                     "fp32_vs_fp64_rel_l2": cerr, "df64_vs_fp64_rel_l2": cdferr},
+        "fp32_vs_fp64_rel_l2": acc["fp32_vs_fp64"],
+        "fp32_vs_fp64_steps": acc["steps"],
+        "df64_vs_fp64_rel_l2_100_steps": acc["df64_vs_fp64"],
+        "fp32_vs_fp64_rel_l2_after_timed_steps": err,
+        "timed_steps_per_arm": args.warmup + 2 * args.steps + 4,
+        "slqg512": {"workload": "SingleLayerQG 512^2 beta=10 mu=0.01 ETDRK4 dt=0.05, stochastic ring forcing "
+                                "kf=14 eps=1e-3, q0=0 (L2-resident: latency, no HBM fraction)",
+                    "fp32": c1p / (c32["ms_per_step"] * 1e-3),
+                    "fp64_plain_df64": c1p / (cdf["ms_per_step"] * 1e-3),
+                    "fp64_ieee": c1p / (c64["ms_per_step"] * 1e-3),
+                    "ms_per_step_fp32": c32["ms_per_step"], "ms_per_step_graph_fp32": c32["ms_per_step_graph"],
+                    "ms_per_step_df64": cdf["ms_per_step"], "ms_per_step_fp64": c64["ms_per_step"],
+                    "fp32_vs_fp64_rel_l2": cerr, "df64_vs_fp64_rel_l2": cdferr},
+        "mlqg1024x3": {"workload": "MultiLayerQG 3 layers 1024^2 ETDRK4 dt=2.5e-3, H=[.2,.3,.5], "
+                                   "b from rho=[4,5,5.5] (g=1), f0=1, beta=5, U=[1,.5,0], mu=0.05, q0 white noise 1e-2",
+                       "points": c2p, "fp32": c2p / (m32["ms_per_step"] * 1e-3),
+                       "fp64_plain_df64": c2p / (mdf["ms_per_step"] * 1e-3),
+                       "ms_per_step_fp32": m32["ms_per_step"], "ms_per_step_graph_fp32": m32["ms_per_step_graph"],
+                       "ms_per_step_df64": mdf["ms_per_step"],
+                       "fp32_vs_df64_rel_l2": merr, "steps_compared": args.warmup + 2 * args.steps + 4,
+                       "roofline_fp32": roofline(CONFIG2, m32, 4, "mlqg1024x3_fp32", peaks, peak_src)},
+        "ensemble1536": {"workload": "1536 TwoDNavierStokes runs: 1024 x 64^2 + 384 x 128^2 + 128 x 256^2, "
+                                     "FilteredRK4 dt=0.01 nu=1e-4 (nnu=1), per-instance stochastic ring forcing "
+                                     "kf=8 eps=1e-3, zeta0=0, FP32, three batched contexts on concurrent streams",
+                         "points": ens["points"], "value": ens["points"] / (ens["ms_per_step"] * 1e-3),
+                         "value_graph": ens["points"] / (ens["ms_per_step_graph"] * 1e-3),
+                         "ms_per_step": ens["ms_per_step"], "ms_per_step_graph": ens["ms_per_step_graph"],
+                         "mean_energy_per_class": ens["mean_energy"]},
+        "adjoint_slqg256": {"workload": "gradient of the final kinetic energy w.r.t. q0 and topography: "
+                                        "SingleLayerQG 256^2, deformation radius 0.35, topography |k|<=8 amp 0.1, "
+                                        "ETDRK4 dt=0.01, 500 steps, checkpoint every 25",
+                            "fp32": adj32, "fp64": adj64,
+                            "adjoint_over_forward_definition": "(gf_grad time - forward time) / forward time: the "
+                            "reverse sweep (segment recomputation + transposed stages) per forward step"},
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -357,7 +560,9 @@ def run_ours(args):
 
 SINGLE = {"twodns2048_fp32": (HEADLINE, np.float32, None), "twodns2048_fp64": (HEADLINE, np.float64, None),
           "twodns2048_df64": (HEADLINE, np.float64, "DF64"), "slqg512_fp32": (CONFIG1, np.float32, None),
-          "slqg512_fp64": (CONFIG1, np.float64, None), "slqg512_df64": (CONFIG1, np.float64, "DF64")}
+          "slqg512_fp64": (CONFIG1, np.float64, None), "slqg512_df64": (CONFIG1, np.float64, "DF64"),
+          "mlqg1024x3_fp32": (CONFIG2, np.float32, None), "mlqg1024x3_df64": (CONFIG2, np.float64, "DF64"),
+          "ensemble1536_fp32": (ENSEMBLE, np.float32, None)}
 
 
 def run_single(args):
@@ -367,10 +572,14 @@ def run_single(args):
     gfcuda.load()
     w, T, prec = SINGLE[args.single]
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
-    r = time_arm(w, T, args.steps, args.warmup, flush, with_e2e=False, precision=prec)
-    r.pop("sol")
+    if w is ENSEMBLE:
+        r = time_ensemble(args.steps, args.warmup, flush)
+        r["pt_steps_per_s"] = r["points"] / (r["ms_per_step"] * 1e-3)
+    else:
+        r = time_arm(w, T, args.steps, args.warmup, flush, with_e2e=False, precision=prec)
+        r.pop("sol")
+        r["pt_steps_per_s"] = points(w) / (r["ms_per_step"] * 1e-3)
     r["workload"] = args.single
-    r["pt_steps_per_s"] = w["nx"] * w["ny"] / (r["ms_per_step"] * 1e-3)
     print(json.dumps(r), flush=True)
     return 0
 

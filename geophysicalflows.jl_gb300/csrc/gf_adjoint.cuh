@@ -1,0 +1,221 @@
+// Adjoint (reverse mode) of the fused ETDRK4 / FilteredETDRK4 step of SingleLayerQG and
+// TwoDNavierStokes (one layer, constant U): the transpose of the discrete step that
+// gf_kernels.cuh computes, stage by stage in reverse, with the same two-kernel structure.
+//
+// Forward calcN! at a dealiased stage input X (src/singlelayerqg.jl:356-382, 443-451):
+//   psi = f X, u = irfft(-i l psi), v = irfft(i kr psi), q = irfft(X), qe = q + eta,
+//   N = -i kr rfft(u qe) - i l rfft(v qe) - i kr U eta_hat.
+// Its transpose for a cotangent Nbar (spectral arrays as real (Re, Im) vectors over the
+// stored half spectrum, physical arrays plain):
+//   abar = rfft^T(i kr Nbar), bbar = rfft^T(i l Nbar)                        [adj row kernel]
+//   ubar = abar qe, vbar = bbar qe, qbar = abar u + bbar v, etabar += qbar + U abar
+//   Xbar = irfft^T(qbar) + f (i l irfft^T(ubar) - i kr irfft^T(vbar))          [adj col kernel]
+// with rfft^T(Y) = sum over the half spectrum of Re(Y e^{i k x}) (the c2r path applied to
+// Y / w) and irfft^T(x) = w rfft(x) / (nx ny), w = 2 on interior kr columns, 1 on kr = 0 and
+// the Nyquist column.  The column kernel also runs the transposed stage combination:
+//   stage 4: Cbar = Xbar;  N3bar = 2 conj(b) ub + 2 conj(z) Cbar;  n1acc = conj(a) ub - conj(z) Cbar;
+//            xaacc = conj(e2) Cbar
+//   stage 3: Bbar = Xbar;  x1acc = conj(e) ub + conj(e2) Bbar;  N2bar = 2 conj(b) ub + conj(z) Bbar
+//   stage 2: Abar = M (xaacc + Xbar);  x1acc += conj(e2) Abar;  N1bar = n1acc + conj(z) Abar
+//   stage 1: ubar_n = M (x1acc + Xbar)
+// where ub = filter * (cotangent of the step's result) and M the dealias mask, and writes the
+// y-inverse transforms of (i kr Nbar / w, i l Nbar / w) of the next (earlier) stage.
+#pragma once
+#include "gf_kernels.cuh"
+
+namespace gf {
+
+// conj(c) x for a real (is_cplx = 0) or complex coefficient table
+template <class T>
+__device__ __forceinline__ cplx<T> mulcj(const void* p, size_t i, cplx<T> x, int is_cplx) {
+  if (!is_cplx) return static_cast<const T*>(p)[i] * x;
+  const cplx<T> c = static_cast<const cplx<T>*>(p)[i];
+  return mk<T>(c.x * x.x + c.y * x.y, c.x * x.y - c.y * x.x);
+}
+
+// Column kernel: y-direction FFT of the three adjoint products of stage a.stage (kr < kcut),
+// the transposed stage combination, and the y-direction inverse FFT of the next cotangent's
+// (i kr Nbar / w, i l Nbar / w) into Wb (all kr).  a.stage = 5: head only (start of a step
+// from a.ubar_in).  Block: C adjacent kr columns x NY / R threads per column.
+template <class T, int NY, int R>
+__global__ void __launch_bounds__(512, 1) adj_col_kernel(Geom g, ModArgs m, AdjArgs a, Bufs b, int C) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int TPF = NY / R;
+  const int cs = g.cs;
+  cplx<T>* F0 = reinterpret_cast<cplx<T>*>(smem_raw);
+  cplx<T>* F1 = F0 + C * cs;
+  cplx<T>* F2 = F1 + C * cs;
+  const int tid = threadIdx.x, c = tid % C, t = tid / C;
+  const int cf = tid / TPF, tf = tid % TPF;
+  const int kr = blockIdx.x * C + c;
+  const bool kin = kr < g.nkr;
+  const cplx<T>* tw = static_cast<const cplx<T>*>(b.twid);
+  const T dky = sel<T>(g.dky, g.dky_f, g.dky_l), krT = T(kr) * sel<T>(g.dkx, g.dkx_f, g.dkx_l);
+  const T ell2 = sel<T>(m.ell_inv2, m.ell_inv2_f, m.ell_inv2_l);
+  const T inv_n = sel<T>(g.inv_nxny, g.inv_nxny_f, g.inv_nxny_l);
+  const bool edge = (kr == 0) || (2 * kr == g.nx);
+  const T scale_in = edge ? inv_n : T(2) * inv_n;  // irfft^T: w / (nx ny)
+  const T scale_out = edge ? T(1) : T(0.5);       // rfft^T via the c2r path: 1 / w
+  const int cx = a.cplx;
+
+  // 1) Xbar of this stage: y-FFT of (qbar, ubar, vbar), combined and masked
+  cplx<T> xj[R];
+#pragma unroll
+  for (int i = 0; i < R; ++i) xj[i] = czero<T>();
+  if (a.stage <= 4 && (int)blockIdx.x * C < g.kcut) {
+    const cplx<T>* P = static_cast<const cplx<T>*>(a.Pb);
+    const size_t fs = (size_t)g.ny * g.ldk;
+    cplx<T>* Fs[3] = {F0, F1, F2};
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+      cplx<T>* Fc = Fs[f] + c * cs;
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        const int j = t + i * TPF;
+        Fc[swz<T>(j)] = (kr < g.kcut) ? P[f * fs + (size_t)j * g.ldk + kr] : czero<T>();
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int f = 0; f < 3; ++f) fft_smem<T, NY, R, -1>(Fs[f] + cf * cs, tf, tw);
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int j = t + i * TPF;
+      if (kin && kept(g, kr, j)) {
+        const T lv = T(lidx(g, j)) * dky;
+        const T K2 = krT * krT + lv * lv;
+        const T f = psi_factor<T>(m.psi_kind, K2, ell2, m.mult, (size_t)j * g.ldk + kr);
+        const cplx<T> Q = F0[c * cs + swz<T>(j)], Ub = F1[c * cs + swz<T>(j)], Vb = F2[c * cs + swz<T>(j)];
+        xj[i] = scale_in * (Q + f * (lv * mul_i(Ub) - krT * mul_i(Vb)));
+      }
+    }
+    __syncthreads();  // F0..F2 are reused below
+  }
+
+  // 2) transposed stage combination -> the next cotangent Nbar
+  cplx<T> nb[R];
+  bool out_w = true;
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int j = t + i * TPF;
+    nb[i] = czero<T>();
+    if (!kin) continue;
+    const size_t ti = (size_t)j * g.ldk + kr;
+    const bool keep = kept(g, kr, j);
+    cplx<T>* ub = static_cast<cplx<T>*>(a.ub);
+    auto start = [&](cplx<T> u) {  // cotangent of a step's result -> stage-4 Nbar
+      const cplx<T> v = a.filtered ? static_cast<const T*>(a.filt)[ti] * u : u;
+      ub[ti] = v;
+      return mulcj<T>(a.gamma, ti, v, cx);
+    };
+    if (a.stage == 5) {
+      nb[i] = start(static_cast<const cplx<T>*>(a.ubar_in)[ti]);
+    } else if (a.stage == 4) {
+      const cplx<T> u = ub[ti], Cb = xj[i];
+      nb[i] = T(2) * mulcj<T>(a.beta, ti, u, cx) + T(2) * mulcj<T>(a.zeta, ti, Cb, cx);
+      static_cast<cplx<T>*>(a.n1acc)[ti] = mulcj<T>(a.alpha, ti, u, cx) - mulcj<T>(a.zeta, ti, Cb, cx);
+      static_cast<cplx<T>*>(a.xaacc)[ti] = mulcj<T>(a.e2, ti, Cb, cx);
+    } else if (a.stage == 3) {
+      const cplx<T> u = ub[ti], Bb = xj[i];
+      static_cast<cplx<T>*>(a.x1acc)[ti] = mulcj<T>(a.e, ti, u, cx) + mulcj<T>(a.e2, ti, Bb, cx);
+      nb[i] = T(2) * mulcj<T>(a.beta, ti, u, cx) + mulcj<T>(a.zeta, ti, Bb, cx);
+    } else if (a.stage == 2) {
+      const cplx<T> Ab = keep ? static_cast<const cplx<T>*>(a.xaacc)[ti] + xj[i] : czero<T>();
+      cplx<T>* x1 = static_cast<cplx<T>*>(a.x1acc);
+      x1[ti] = x1[ti] + mulcj<T>(a.e2, ti, Ab, cx);
+      nb[i] = static_cast<const cplx<T>*>(a.n1acc)[ti] + mulcj<T>(a.zeta, ti, Ab, cx);
+    } else {  // stage 1
+      const cplx<T> un = keep ? static_cast<const cplx<T>*>(a.x1acc)[ti] + xj[i] : czero<T>();
+      static_cast<cplx<T>*>(a.ubar_out)[ti] = un;
+      if (a.head) nb[i] = start(un);
+    }
+  }
+  if (a.stage == 1 && !a.head) out_w = false;
+  if (!out_w) return;
+
+  // 3) y-inverse FFT of (i kr Nbar / w, i l Nbar / w) into Wb (every kr column)
+  cplx<T>* Wb = static_cast<cplx<T>*>(a.Wb);
+  for (int f = 0; f < 2; ++f) {
+    cplx<T>* Fb = f ? F1 : F0;
+    cplx<T>* Fe = Fb + c * cs;
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int j = t + i * TPF;
+      const T mlt = f ? T(lidx(g, j)) * dky : krT;
+      Fe[swz<T>(j)] = (scale_out * mlt) * mul_i(nb[i]);
+    }
+    __syncthreads();
+    fft_smem<T, NY, R, +1>(Fb + cf * cs, tf, tw);
+    if (kin) {
+      cplx<T>* Wf = Wb + (size_t)f * g.ny * g.ldk + kr;
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        const int j = t + i * TPF;
+        Wf[(size_t)j * g.ldk] = Fe[swz<T>(j)];
+      }
+    }
+  }
+}
+
+// shared-memory bytes of adj_col_kernel for C columns with column stride cs
+__host__ __forceinline__ size_t adj_col_smem(int C, int cs, size_t elem) { return (size_t)3 * C * cs * elem; }
+
+// Row kernel: for the row pair (j0, j0+1) packed as one complex FFT, the x-direction c2r of
+// (abar, bbar) from Wb, the transposed products against the stored forward fields
+// (qe, u, v) of the stage, the etabar accumulation, and the x-direction r2c of
+// (qbar, ubar, vbar) into Pb (kr < kcut).
+template <class T, int NX, int R>
+__global__ void __launch_bounds__(256, 1) adj_row_kernel(Geom g, AdjArgs a, Bufs b, int B) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int TPF = NX / R;
+  constexpr int PS = row_stride<T>(NX, NX / R);
+  const int tid = threadIdx.x, bp = tid / TPF, t = tid % TPF;
+  const int j0 = 2 * (blockIdx.x * B + bp);
+  cplx<T>* buf = reinterpret_cast<cplx<T>*>(smem_raw) + (size_t)bp * 3 * PS;
+  const cplx<T>* tw = static_cast<const cplx<T>*>(b.twid);
+  const cplx<T>* Wb = static_cast<const cplx<T>*>(a.Wb);
+  cplx<T>* Pb = static_cast<cplx<T>*>(a.Pb);
+  const T* ph = static_cast<const T*>(a.phys);
+  T* etab = static_cast<T*>(a.etab);
+  const size_t np = (size_t)g.ny * NX;
+  const T U = sel<T>(a.U, a.U_f, a.U_l);
+  for (int f = 0; f < 2; ++f) {
+    const cplx<T>* Wa = Wb + (size_t)f * g.ny * g.ldk + (size_t)j0 * g.ldk;
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int k = t + i * TPF;
+      buf[f * PS + swz<T>(k)] = packed_spec<T>(Wa, Wa + g.ldk, k, NX, g.nkr);
+    }
+  }
+  __syncthreads();
+  for (int f = 0; f < 2; ++f) fft_smem<T, NX, R, +1>(buf + f * PS, t, tw);
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int x = t + i * TPF;
+    const int px = swz<T>(x);
+    const size_t ia = (size_t)j0 * NX + x, ibb = ia + NX;
+    const cplx<T> ab = buf[px], bb = buf[PS + px];
+    const cplx<T> qe = mk<T>(ph[ia], ph[ibb]);
+    const cplx<T> u = mk<T>(ph[np + ia], ph[np + ibb]);
+    const cplx<T> v = mk<T>(ph[2 * np + ia], ph[2 * np + ibb]);
+    const cplx<T> qb = mk<T>(ab.x * u.x + bb.x * v.x, ab.y * u.y + bb.y * v.y);
+    etab[ia] = etab[ia] + (qb.x + U * ab.x);
+    etab[ibb] = etab[ibb] + (qb.y + U * ab.y);
+    buf[px] = qb;
+    buf[PS + px] = mk<T>(ab.x * qe.x, ab.y * qe.y);
+    buf[2 * PS + px] = mk<T>(bb.x * qe.x, bb.y * qe.y);
+  }
+  __syncthreads();
+  for (int f = 0; f < 3; ++f) fft_smem<T, NX, R, -1>(buf + f * PS, t, tw);
+  for (int f = 0; f < 3; ++f) {
+    cplx<T>* Pa = Pb + (size_t)f * g.ny * g.ldk + (size_t)j0 * g.ldk;
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int k = t + i * TPF;
+      if (k < g.kcut) unpack_store<T>(buf + f * PS, k, NX, Pa, Pa + g.ldk);
+    }
+  }
+}
+
+}  // namespace gf

@@ -10,6 +10,7 @@
 
 #include "gf_fft.cuh"
 #include "gf_internal.h"
+#include "gf_philox.cuh"
 #include "gfcuda.h"
 
 using namespace gf;
@@ -32,6 +33,7 @@ struct gf_ctx {
   double last_fscale = 0;  // forcing scale of the last calcN! (deterministic forcing)
   double Hsum = 1, f0 = 1;
   std::vector<double> gprime, Hl;
+  std::vector<double> filt_host;  // the Filtered steppers' filter, [ny][nx/2+1]
   // device buffers
   std::vector<void*> allocs;
   void *sol = nullptr, *X = nullptr, *acc = nullptr, *s1 = nullptr, *N1 = nullptr, *R3[3] = {nullptr, nullptr, nullptr};
@@ -59,6 +61,22 @@ struct gf_ctx {
   int graph_steps = 4;
   cudaGraphExec_t gexec[3] = {nullptr, nullptr, nullptr};
   bool own_stream = false;
+  // adjoint (gf_adjoint_setup): checkpoints, the recomputed forward fields of one segment,
+  // and the cotangent arrays; freed by gf_destroy or a new set-up
+  struct Adjoint {
+    bool ready = false, forward_done = false;
+    int64_t nsteps = 0;
+    int every = 1, nseg = 0;
+    std::vector<void*> mem;
+    void *ckpt = nullptr, *phys = nullptr, *ub = nullptr, *n1acc = nullptr, *xaacc = nullptr, *x1acc = nullptr;
+    void *ubar_in = nullptr, *ubar_out = nullptr, *Wb = nullptr, *Pb = nullptr, *etab = nullptr;
+    void *final_state = nullptr, *tmp = nullptr;
+    std::vector<double> ck_t;
+    std::vector<int64_t> ck_step;
+    double t_end = 0;
+    int64_t step_end = 0;
+  } adj;
+  void* row_phys = nullptr;  // forward row kernels also store (q + eta, u, v) here when set
   std::string err;
 };
 
@@ -250,7 +268,7 @@ static int upload_table(gf_ctx* c, void* dst, const std::vector<double>& v, int 
   return GF_OK;
 }
 
-static Bufs bufs(gf_ctx* c) { return Bufs{c->twid, c->W, c->P}; }
+static Bufs bufs(gf_ctx* c) { return Bufs{c->twid, c->W, c->P, c->row_phys}; }
 static Geom full_geom(const gf_ctx* c) {
   Geom g = c->g;
   g.kcut = g.nkr; g.lA = 1; g.lB = 0; g.ldw = g.ldk;
@@ -562,6 +580,7 @@ static int build(gf_ctx* c, const gf_config* cfg) {
       }
     if (!(c->filt = dalloc(c, tsz * rb))) return fail(c, GF_ERR_NOMEM, "filter");
     if (int r = upload_table(c, c->filt, f, 0)) return r;
+    c->filt_host = f;
   }
   if (c->kind == SK_ETDRK4) {
     for (int q = 0; q < 6; ++q) if (!(c->etd[q] = dalloc(c, tsz * w * rb))) return fail(c, GF_ERR_NOMEM, "etdrk4 coefficients");
@@ -734,6 +753,7 @@ extern "C" int gf_destroy(gf_ctx* c) {
   for (auto e : c->ev_free) cudaEventDestroy(e);
   for (auto& u : c->ev_used) { cudaEventDestroy(u.second.first); cudaEventDestroy(u.second.second); }
   for (auto& gx : c->gexec) if (gx) cudaGraphExecDestroy(gx);
+  for (void* p : c->adj.mem) cudaFree(p);
   if (c->own_stream) cudaStreamDestroy(c->stream);
   delete c;
   return GF_OK;
@@ -871,6 +891,116 @@ extern "C" int gf_invtransform(gf_ctx* c, void* field, const void* fieldh, int w
   void* ph = (char*)c->phys + 3 * pf;
   if (int r = inv_transform(c, c->tmp_spec, SF_RAW, 0, ph)) return r;
   return copy_phys_out(c, field, ph, where);
+}
+
+// ------------------------------------------------------------ peakedisotropicspectrum
+// src/utils.jl:29-54: psi_hat = mask * z * (K^2 (1 + (K/k0)^4))^(-1/2) with z complex normal
+// (allones: z = 1), energy e0 = sum over the HALF spectrum of K^2 |psi_hat|^2 / (nx ny)^2
+// (the reference's :50), zeta_hat = -K^2 psi_hat sqrt(E0 / e0), zeta = irfft(zeta_hat).
+// Draws: element e = j (nx/2+1) + ik, counter (e, 0, 0, TAG_INITIAL), key seed + instance.
+__device__ __forceinline__ double peaked_amp(const Geom& g, int ik, int j, double k0, double* K2out) {
+  const double kr = g.dkx * ik, l = g.dky * (j < g.ny / 2 ? j : j - g.ny);
+  const double K2 = kr * kr + l * l;
+  *K2out = K2;
+  if (K2 == 0.0) return 0.0;
+  const double r = sqrt(K2) / k0;
+  return 1.0 / sqrt(K2 * (1.0 + r * r * r * r));
+}
+
+__device__ __forceinline__ cplx<double> peaked_psih(const Geom& g, int ik, int j, double k0, int allones,
+                                                    const double* mask, uint64_t seed, double* K2) {
+  double a = peaked_amp(g, ik, j, k0, K2);
+  const size_t e = (size_t)j * g.nkr + ik;
+  if (mask) a *= mask[e];
+  if (allones) return mk<double>(a, 0.0);
+  const cplx<double> z = draw<double>(e, 0, seed, 0, TAG_INITIAL);
+  return mk<double>(a * z.x, a * z.y);
+}
+
+// per-block compensated partial sums of K^2 |psi_hat|^2, instance blockIdx.y
+__global__ void peaked_energy_kernel(Geom g, double k0, int allones, const double* mask, uint64_t seed,
+                                     double* partial) {
+  __shared__ double red[256];
+  const int ib = blockIdx.y;
+  const size_t n = (size_t)g.nkr * g.ny;
+  double s = 0, c = 0;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    double K2;
+    const cplx<double> p = peaked_psih(g, (int)(e % g.nkr), (int)(e / g.nkr), k0, allones, mask, seed + ib, &K2);
+    const double x = K2 * (p.x * p.x + p.y * p.y), t = s + x;
+    c += (fabs(s) >= fabs(x)) ? (s - t) + x : (x - t) + s;
+    s = t;
+  }
+  red[threadIdx.x] = s + c;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if ((int)threadIdx.x < st) red[threadIdx.x] += red[threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[(size_t)ib * gridDim.x + blockIdx.x] = red[0];
+}
+
+template <class T> __device__ __forceinline__ T from_d(double x) { return T(x); }
+template <> __device__ __forceinline__ df64 from_d<df64>(double x) { return df64(x); }
+
+template <class T>
+__global__ void peaked_zetah_kernel(Geom g, double k0, double E0, int allones, const double* mask, uint64_t seed,
+                                    const double* esum, cplx<T>* out) {
+  const int ib = blockIdx.y;
+  const size_t n = (size_t)g.nkr * g.ny;
+  const double e0 = esum[ib] / ((double)g.nx * g.ny * (double)g.nx * g.ny);
+  const double sc = e0 > 0 ? sqrt(E0 / e0) : 0.0;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const int ik = (int)(e % g.nkr), j = (int)(e / g.nkr);
+    double K2;
+    const cplx<double> p = peaked_psih(g, ik, j, k0, allones, mask, seed + ib, &K2);
+    out[(size_t)ib * g.bs_spec + (size_t)j * g.ldk + ik] = mk<T>(from_d<T>(-K2 * sc * p.x), from_d<T>(-K2 * sc * p.y));
+  }
+}
+
+extern "C" int gf_peakedisotropicspectrum(gf_ctx* c, double kpeak, double E0, const double* mask, int32_t allones,
+                                          uint64_t seed, void* zeta, int where) {
+  if (!c || !zeta) return GF_ERR_ARG;
+  if (c->g.nl != 1) return fail(c, GF_ERR_UNSUPPORTED, "peakedisotropicspectrum makes one 2-D field (nlayers = 1)");
+  if (c->cfg.Lx != c->cfg.Ly) return fail(c, GF_ERR_ARG, "the domain is not square");  // src/utils.jl:30
+  if (!(kpeak > 0) || !(E0 >= 0)) return fail(c, GF_ERR_ARG, "peakedisotropicspectrum: kpeak > 0 and E0 >= 0");
+  const Geom& g = c->g;
+  const size_t n = (size_t)g.nkr * g.ny;
+  double* dmask = nullptr;
+  if (mask) {
+    if (where == GF_DEVICE) {
+      dmask = const_cast<double*>(mask);
+    } else {
+      GF_CUDA(c, cudaMallocAsync((void**)&dmask, n * 8, c->stream));
+      GF_CUDA(c, cudaMemcpyAsync(dmask, mask, n * 8, cudaMemcpyHostToDevice, c->stream));
+    }
+  }
+  const double k0 = kpeak * 2 * M_PI / c->cfg.Lx;
+  const int nbk = c->diag_blocks;
+  dim3 grid(nbk, g.nb);
+  peaked_energy_kernel<<<grid, 256, 0, c->stream>>>(g, k0, allones, dmask, seed, c->dpart);
+  diag_finish<<<g.nb, 256, 0, c->stream>>>(c->dpart, nbk, 1u, c->dout);
+  if (c->prec == GF_F64)
+    peaked_zetah_kernel<double><<<grid, 256, 0, c->stream>>>(g, k0, E0, allones, dmask, seed, c->dout,
+                                                            (cplx<double>*)c->tmp_spec);
+  else if (c->prec == GF_DF64)
+    peaked_zetah_kernel<df64><<<grid, 256, 0, c->stream>>>(g, k0, E0, allones, dmask, seed, c->dout,
+                                                          (cplx<df64>*)c->tmp_spec);
+  else
+    peaked_zetah_kernel<float><<<grid, 256, 0, c->stream>>>(g, k0, E0, allones, dmask, seed, c->dout,
+                                                           (cplx<float>*)c->tmp_spec);
+  GF_CUDA(c, cudaGetLastError());
+  if (mask && where != GF_DEVICE) GF_CUDA(c, cudaFreeAsync(dmask, c->stream));
+  void* ph = (char*)c->phys + 3 * (size_t)g.bs_phys * g.nb * c->rb;
+  if (int r = inv_transform(c, c->tmp_spec, SF_RAW, 0, ph)) return r;
+  return copy_phys_out(c, zeta, ph, where);
+}
+
+extern "C" int gf_get_filter(const gf_ctx* c, double* out) {
+  if (!c || !out) return GF_ERR_ARG;
+  if (c->filt_host.empty()) return GF_ERR_STATE;
+  std::memcpy(out, c->filt_host.data(), c->filt_host.size() * sizeof(double));
+  return GF_OK;
 }
 
 extern "C" int gf_set_physical(gf_ctx* c, int which, const void* field, int where) {
@@ -1117,17 +1247,6 @@ extern "C" int gf_get_batch(const gf_ctx* c, int32_t* nb) {
   return GF_OK;
 }
 
-extern "C" int gf_diagnostics(gf_ctx* c, const int32_t* which, int32_t nd, double* out);
-
-extern "C" int gf_step_diags(gf_ctx* c, int64_t nsteps, const int32_t* which, int32_t nd, double* out) {
-  if (!c || nsteps < 0 || (nd > 0 && (!which || !out))) return GF_ERR_ARG;
-  for (int64_t i = 0; i < nsteps; ++i) {
-    if (int r = one_step(c)) return r;
-    if (nd > 0)
-      if (int r = gf_diagnostics(c, which, nd, out + i * nd * c->g.nb)) return r;
-  }
-  return GF_OK;
-}
 
 extern "C" int gf_calcN(gf_ctx* c, void* N, void* sol, double t, int where) {
   if (!c || !N || !sol) return GF_ERR_ARG;
@@ -1154,8 +1273,8 @@ extern "C" int gf_calcN(gf_ctx* c, void* N, void* sol, double t, int where) {
 }
 
 // ------------------------------------------------------------------------------- diagnostics
-extern "C" int gf_diagnostics(gf_ctx* c, const int32_t* which, int32_t nd, double* out) {
-  if (!c || (nd > 0 && (!which || !out))) return GF_ERR_ARG;
+// Which reduction slots the diagnostics `which` need (validation of the ids).
+static int diag_mask(gf_ctx* c, const int32_t* which, int32_t nd, uint32_t* maskp) {
   const int mod = c->cfg.module;
   const bool finite_ell = (mod == GF_SINGLELAYERQG) && c->m.psi_kind == PSI_HELMHOLTZ;
   uint32_t mask = 0;
@@ -1174,17 +1293,26 @@ extern "C" int gf_diagnostics(gf_ctx* c, const int32_t* which, int32_t nd, doubl
     if (finite_ell && d >= 3) return fail(c, GF_ERR_NOT_IMPLEMENTED, "not implemented for finite deformation radius");
     mask |= 1u << d;
   }
+  *maskp = mask;
+  return GF_OK;
+}
+
+// The reductions of the current state into dst[NDIAG][batch] (device), no host wait.
+static int diag_launch(gf_ctx* c, uint32_t mask, double* dst) {
   const void* Fh = (c->cfg.forcing_kind != GF_FORCING_NONE) ? c->Fh : nullptr;
   const void* prev = (c->cfg.forcing_kind >= GF_FORCING_STOCHASTIC) ? c->prevsol : nullptr;
-  const int NB = c->g.nb;
   GF_CUDA(c, DISPATCH(c, launch_diag, c->g, c->m, c->sol, prev, Fh, mask, c->dpart, c->diag_blocks, c->stream));
-  diag_finish<<<NB, 256, 0, c->stream>>>(c->dpart, c->diag_blocks, mask, c->dout);
+  diag_finish<<<c->g.nb, 256, 0, c->stream>>>(c->dpart, c->diag_blocks, mask, dst);
   GF_CUDA(c, cudaGetLastError());
-  std::vector<double> hv((size_t)NDIAG * NB);
-  GF_CUDA(c, cudaMemcpyAsync(hv.data(), c->dout, hv.size() * 8, cudaMemcpyDeviceToHost, c->stream));
-  GF_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->launches += 2;
+  return GF_OK;
+}
+
+// Host normalisation of the raw sums hv[NDIAG][batch] into out[batch][nd]; fs is the
+// forcing scale of the last calcN! (harmonic / static forcing work terms).
+static void diag_post(const gf_ctx* c, const int32_t* which, int32_t nd, const double* hv, double fs, double* out) {
+  const int mod = c->cfg.module, NB = c->g.nb;
   const double nn = (double)c->g.nx * c->g.ny, norm = 1.0 / (nn * nn);
-  const double fs = (c->cfg.forcing_kind == GF_FORCING_HARMONIC || c->cfg.forcing_kind == GF_FORCING_STATIC) ? c->last_fscale : 1.0;
   for (int ib = 0; ib < NB; ++ib) {
     auto h = [&](int q) { return hv[(size_t)q * NB + ib]; };
     for (int i = 0; i < nd; ++i) {
@@ -1206,5 +1334,245 @@ extern "C" int gf_diagnostics(gf_ctx* c, const int32_t* which, int32_t nd, doubl
       out[(size_t)ib * nd + i] = v;
     }
   }
+}
+
+static double diag_fscale(const gf_ctx* c) {
+  return (c->cfg.forcing_kind == GF_FORCING_HARMONIC || c->cfg.forcing_kind == GF_FORCING_STATIC) ? c->last_fscale : 1.0;
+}
+
+extern "C" int gf_diagnostics(gf_ctx* c, const int32_t* which, int32_t nd, double* out) {
+  if (!c || (nd > 0 && (!which || !out))) return GF_ERR_ARG;
+  uint32_t mask = 0;
+  if (int r = diag_mask(c, which, nd, &mask)) return r;
+  if (int r = diag_launch(c, mask, c->dout)) return r;
+  std::vector<double> hv((size_t)NDIAG * c->g.nb);
+  GF_CUDA(c, cudaMemcpyAsync(hv.data(), c->dout, hv.size() * 8, cudaMemcpyDeviceToHost, c->stream));
+  GF_CUDA(c, cudaStreamSynchronize(c->stream));
+  diag_post(c, which, nd, hv.data(), diag_fscale(c), out);
+  return GF_OK;
+}
+
+// stepforward!(prob, diags, nsteps) with the diagnostics of every step reduced into a
+// device ring buffer: the host waits once per ring fill (up to 64 MB of raw sums), not once
+// per step; out[step][instance][nd].
+extern "C" int gf_step_diags(gf_ctx* c, int64_t nsteps, const int32_t* which, int32_t nd, double* out) {
+  if (!c || nsteps < 0 || (nd > 0 && (!which || !out))) return GF_ERR_ARG;
+  if (nd == 0) return gf_step(c, nsteps);
+  uint32_t mask = 0;
+  if (int r = diag_mask(c, which, nd, &mask)) return r;
+  const size_t slot = (size_t)NDIAG * c->g.nb;
+  const int64_t cap = std::max<int64_t>(1, std::min<int64_t>(nsteps, (int64_t)((64u << 20) / (slot * 8))));
+  double* ring = nullptr;
+  GF_CUDA(c, cudaMallocAsync((void**)&ring, (size_t)cap * slot * 8, c->stream));
+  std::vector<double> hv((size_t)cap * slot), fs((size_t)cap);
+  int rc = GF_OK;
+  for (int64_t i0 = 0; i0 < nsteps && rc == GF_OK; i0 += cap) {
+    const int64_t n = std::min<int64_t>(cap, nsteps - i0);
+    for (int64_t k = 0; k < n && rc == GF_OK; ++k) {
+      rc = one_step(c);
+      if (rc == GF_OK) rc = diag_launch(c, mask, ring + k * slot);
+      fs[k] = diag_fscale(c);
+    }
+    if (rc != GF_OK) break;
+    if (cudaMemcpyAsync(hv.data(), ring, (size_t)n * slot * 8, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess) {
+      rc = fail(c, GF_ERR_CUDA, "diagnostics ring copy");
+      break;
+    }
+    for (int64_t k = 0; k < n; ++k)
+      diag_post(c, which, nd, hv.data() + k * slot, fs[k], out + (i0 + k) * nd * c->g.nb);
+  }
+  cudaFreeAsync(ring, c->stream);
+  return rc;
+}
+
+// ------------------------------------------------------------------------------- adjoint
+// Reverse-mode derivative of stepforward!(prob, nsteps) for TwoDNavierStokes and
+// SingleLayerQG (constant U) with ETDRK4 / FilteredETDRK4 (the kernels are in gf_adjoint.cuh).
+// Checkpointing: the forward pass stores the state every `every` steps; the reverse pass
+// recomputes one segment at a time from its checkpoint with the fused forward kernels,
+// keeping the physical fields (q + eta, u, v) of all its stages, then runs the transposed
+// stages of the segment's steps in reverse.  Work: one forward pass + one recomputation +
+// the transposed stages; memory: nsteps / every states + every x 4 x 3 physical fields.
+static int adj_check(gf_ctx* c) {
+  const int mod = c->cfg.module;
+  if (mod != GF_TWODNAVIERSTOKES && mod != GF_SINGLELAYERQG)
+    return fail(c, GF_ERR_UNSUPPORTED, "the adjoint covers TwoDNavierStokes and SingleLayerQG");
+  if (c->kind != SK_ETDRK4) return fail(c, GF_ERR_UNSUPPORTED, "the adjoint follows the ETDRK4 / FilteredETDRK4 stages");
+  if (c->g.nb != 1) return fail(c, GF_ERR_UNSUPPORTED, "the adjoint runs one instance (batch = 1)");
+  if (c->m.U1D || c->m.hasC || c->m.linear) return fail(c, GF_ERR_UNSUPPORTED, "the adjoint supports a constant U");
+  return GF_OK;
+}
+
+static void* adj_alloc(gf_ctx* c, size_t bytes) {
+  void* p = nullptr;
+  if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+  c->adj.mem.push_back(p);
+  return p;
+}
+
+extern "C" int gf_adjoint_setup(gf_ctx* c, int64_t nsteps, int32_t checkpoint_every) {
+  if (!c || nsteps < 1 || checkpoint_every < 1) return GF_ERR_ARG;
+  if (int r = adj_check(c)) return r;
+  GF_CUDA(c, cudaStreamSynchronize(c->stream));
+  auto& a = c->adj;
+  for (void* p : a.mem) cudaFree(p);
+  a = gf_ctx::Adjoint{};
+  const Geom& g = c->g;
+  a.nsteps = nsteps;
+  a.every = (int)std::min<int64_t>(checkpoint_every, nsteps);
+  a.nseg = (int)((nsteps + a.every - 1) / a.every);
+  const size_t spec = g.bs_spec * c->cb, plane = (size_t)g.ny * g.nx * c->rb;
+  const size_t wide = (size_t)g.ny * g.ldk * c->cb;
+  if (!(a.ckpt = adj_alloc(c, a.nseg * spec)) || !(a.phys = adj_alloc(c, (size_t)a.every * 4 * 3 * plane)) ||
+      !(a.ub = adj_alloc(c, spec)) || !(a.n1acc = adj_alloc(c, spec)) || !(a.xaacc = adj_alloc(c, spec)) ||
+      !(a.x1acc = adj_alloc(c, spec)) || !(a.ubar_in = adj_alloc(c, spec)) || !(a.ubar_out = adj_alloc(c, spec)) ||
+      !(a.final_state = adj_alloc(c, spec)) || !(a.tmp = adj_alloc(c, spec)) || !(a.Wb = adj_alloc(c, 2 * wide)) ||
+      !(a.Pb = adj_alloc(c, 3 * wide)) || !(a.etab = adj_alloc(c, plane))) {
+    for (void* p : a.mem) cudaFree(p);
+    a = gf_ctx::Adjoint{};
+    return fail(c, GF_ERR_NOMEM, "adjoint buffers");
+  }
+  // unused padding columns of the accumulators stay zero
+  for (void* p : {a.ub, a.n1acc, a.xaacc, a.x1acc, a.ubar_in, a.ubar_out, a.tmp})
+    GF_CUDA(c, cudaMemsetAsync(p, 0, spec, c->stream));
+  GF_CUDA(c, cudaMemsetAsync(a.Wb, 0, 2 * wide, c->stream));
+  GF_CUDA(c, cudaMemsetAsync(a.Pb, 0, 3 * wide, c->stream));
+  a.ck_t.assign(a.nseg, 0.0);
+  a.ck_step.assign(a.nseg, 0);
+  a.ready = true;
+  return GF_OK;
+}
+
+extern "C" int gf_adjoint_forward(gf_ctx* c) {
+  if (!c) return GF_ERR_ARG;
+  auto& a = c->adj;
+  if (!a.ready) return fail(c, GF_ERR_STATE, "call gf_adjoint_setup first");
+  const size_t spec = c->g.bs_spec * c->cb;
+  for (int64_t k = 0; k < a.nsteps; k += a.every) {
+    const int seg = (int)(k / a.every);
+    GF_CUDA(c, cudaMemcpyAsync((char*)a.ckpt + seg * spec, c->sol, spec, cudaMemcpyDeviceToDevice, c->stream));
+    a.ck_t[seg] = c->t;
+    a.ck_step[seg] = c->step;
+    if (int r = gf_step(c, std::min<int64_t>(a.every, a.nsteps - k))) return r;
+  }
+  GF_CUDA(c, cudaMemcpyAsync(a.final_state, c->sol, spec, cudaMemcpyDeviceToDevice, c->stream));
+  a.t_end = c->t;
+  a.step_end = c->step;
+  a.forward_done = true;
+  return GF_OK;
+}
+
+static AdjArgs adj_args(gf_ctx* c) {
+  auto& d = c->adj;
+  AdjArgs a{};
+  a.filtered = c->filtered;
+  a.cplx = c->cplxL;
+  a.e = c->etd[0]; a.e2 = c->etd[1]; a.zeta = c->etd[2]; a.alpha = c->etd[3]; a.beta = c->etd[4]; a.gamma = c->etd[5];
+  a.filt = c->filt;
+  a.ub = d.ub; a.n1acc = d.n1acc; a.xaacc = d.xaacc; a.x1acc = d.x1acc;
+  a.ubar_in = d.ubar_in; a.ubar_out = d.ubar_out; a.Wb = d.Wb; a.Pb = d.Pb; a.etab = d.etab;
+  a.U = (c->cfg.module == GF_SINGLELAYERQG) ? c->cfg.U : 0.0;
+  split_hl(a.U, &a.U_f, &a.U_l);
+  return a;
+}
+
+// The reverse sweep from the cotangent in adj.ubar_in (internal layout) to adj.ubar_out
+// and adj.etab; the state and clock are the forward pass's result again afterwards.
+static int adjoint_reverse(gf_ctx* c) {
+  auto& d = c->adj;
+  const Geom& g = c->g;
+  const size_t spec = g.bs_spec * c->cb, plane = (size_t)g.ny * g.nx * c->rb;
+  const double dt = c->cfg.dt;
+  GF_CUDA(c, cudaMemsetAsync(d.etab, 0, plane, c->stream));
+  AdjArgs a = adj_args(c);
+  const Bufs b = Bufs{c->twid, nullptr, nullptr};
+  a.stage = 5;
+  GF_CUDA(c, DISPATCH(c, launch_adj_col, g, c->m, a, b, c->stream));
+  c->launches++;
+  for (int seg = d.nseg - 1; seg >= 0; --seg) {
+    const int64_t k0 = (int64_t)seg * d.every;
+    const int cnt = (int)std::min<int64_t>(d.every, d.nsteps - k0);
+    // recompute the segment, keeping every stage's physical fields
+    GF_CUDA(c, cudaMemcpyAsync(c->sol, (char*)d.ckpt + seg * spec, spec, cudaMemcpyDeviceToDevice, c->stream));
+    c->t = d.ck_t[seg];
+    c->step = d.ck_step[seg];
+    if (int r = upload_clock(c)) return r;
+    c->W_valid = false;
+    for (int i = 0; i < cnt; ++i) {
+      if (int r = ensure_W(c)) return r;
+      for (int stg = 1; stg <= 4; ++stg) {
+        const double ts = c->t + (stg == 1 ? 0.0 : stg == 4 ? dt : 0.5 * dt);
+        StepArgs s = stage_args(c, stg, ts);
+        s.clk = c->dclk;
+        c->row_phys = (char*)d.phys + ((size_t)i * 4 + stg - 1) * 3 * plane;
+        const int r = launch_stage(c, s, 1);
+        c->row_phys = nullptr;
+        if (r) return r;
+      }
+      advance_clock_kernel<<<1, 32, 0, c->stream>>>(c->dclk, dt, c->cfg.forcing_omega, c->cfg.forcing_phase,
+                                                    c->cfg.forcing_kind == GF_FORCING_HARMONIC, c->nstages);
+      GF_CUDA(c, cudaGetLastError());
+      c->launches++;
+      host_advance(c);
+    }
+    // transposed stages, last step first
+    for (int i = cnt - 1; i >= 0; --i) {
+      for (int r = 4; r >= 1; --r) {
+        a.stage = r;
+        a.head = (r == 1) && !(seg == 0 && i == 0);
+        a.phys = (char*)d.phys + ((size_t)i * 4 + r - 1) * 3 * plane;
+        GF_CUDA(c, DISPATCH(c, launch_adj_row, g, a, b, c->stream));
+        GF_CUDA(c, DISPATCH(c, launch_adj_col, g, c->m, a, b, c->stream));
+        c->launches += 2;
+      }
+    }
+  }
+  GF_CUDA(c, cudaMemcpyAsync(c->sol, d.final_state, spec, cudaMemcpyDeviceToDevice, c->stream));
+  c->t = d.t_end;
+  c->step = d.step_end;
+  c->W_valid = false;
+  return upload_clock(c);
+}
+
+extern "C" int gf_adjoint_backward(gf_ctx* c, const void* sol_bar, void* sol0_bar, void* eta_bar, int where) {
+  if (!c || !sol_bar) return GF_ERR_ARG;
+  auto& d = c->adj;
+  if (!d.forward_done) return fail(c, GF_ERR_STATE, "run gf_adjoint_forward first");
+  if (eta_bar && c->cfg.module != GF_SINGLELAYERQG) return fail(c, GF_ERR_ARG, "TwoDNavierStokes has no topography");
+  if (int r = copy_spec_in(c, d.ubar_in, sol_bar, where)) return r;
+  if (int r = adjoint_reverse(c)) return r;
+  if (sol0_bar)
+    if (int r = copy_spec_out(c, sol0_bar, d.ubar_out, where)) return r;
+  if (eta_bar)
+    if (int r = copy_phys_out(c, eta_bar, d.etab, where)) return r;
+  if (where == GF_HOST) GF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GF_OK;
+}
+
+extern "C" int gf_grad(gf_ctx* c, int loss_kind, void* dq0, void* deta, double* loss, int where) {
+  if (!c) return GF_ERR_ARG;
+  if (loss_kind != GF_LOSS_KINETIC_ENERGY) return fail(c, GF_ERR_ARG, "unknown loss");
+  auto& d = c->adj;
+  if (!d.ready) return fail(c, GF_ERR_STATE, "call gf_adjoint_setup first");
+  if (deta && c->cfg.module != GF_SINGLELAYERQG) return fail(c, GF_ERR_ARG, "TwoDNavierStokes has no topography");
+  if (int r = gf_adjoint_forward(c)) return r;
+  // loss: SingleLayerQG.kinetic_energy / TwoDNavierStokes.energy of the final state
+  if (loss) {
+    const int32_t id = 0;
+    if (int r = gf_diagnostics(c, &id, 1, loss)) return r;
+  }
+  GF_CUDA(c, DISPATCH(c, launch_adj_spec, c->g, c->m, c->sol, d.ubar_in, 0, c->stream));
+  if (int r = adjoint_reverse(c)) return r;
+  if (dq0) {  // gradient with respect to q0 in set_q!(prob, q0): rfft^T of the dealiased cotangent
+    GF_CUDA(c, DISPATCH(c, launch_adj_spec, c->g, c->m, d.ubar_out, d.tmp, 1, c->stream));
+    const size_t pf = (size_t)c->g.ny * c->g.nx * c->rb;
+    void* ph = (char*)c->phys + 3 * pf;
+    if (int r = inv_transform(c, d.tmp, SF_RAW, 0, ph)) return r;
+    if (int r = copy_phys_out(c, dq0, ph, where)) return r;
+  }
+  if (deta)
+    if (int r = copy_phys_out(c, deta, d.etab, where)) return r;
+  if (where == GF_HOST) GF_CUDA(c, cudaStreamSynchronize(c->stream));
   return GF_OK;
 }

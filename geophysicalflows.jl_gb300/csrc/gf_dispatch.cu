@@ -111,6 +111,67 @@ cudaError_t launch_spec_apply(const Geom& g, const ModArgs& m, const void* in, v
   return cudaGetLastError();
 }
 
+template <class T>
+cudaError_t launch_adj_row(const Geom& g, const AdjArgs& a, const Bufs& b, cudaStream_t st) {
+  switch (g.nx) {
+    case 32: return launch_adj_row_n<T, 32>(g, a, b, st);
+    case 64: return launch_adj_row_n<T, 64>(g, a, b, st);
+    case 128: return launch_adj_row_n<T, 128>(g, a, b, st);
+    case 256: return launch_adj_row_n<T, 256>(g, a, b, st);
+    case 512: return launch_adj_row_n<T, 512>(g, a, b, st);
+    case 1024: return launch_adj_row_n<T, 1024>(g, a, b, st);
+    case 2048: return launch_adj_row_n<T, 2048>(g, a, b, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <class T>
+cudaError_t launch_adj_col(const Geom& g, const ModArgs& m, const AdjArgs& a, const Bufs& b, cudaStream_t st) {
+  switch (g.ny) {
+    case 32: return launch_adj_col_n<T, 32>(g, m, a, b, st);
+    case 64: return launch_adj_col_n<T, 64>(g, m, a, b, st);
+    case 128: return launch_adj_col_n<T, 128>(g, m, a, b, st);
+    case 256: return launch_adj_col_n<T, 256>(g, m, a, b, st);
+    case 512: return launch_adj_col_n<T, 512>(g, m, a, b, st);
+    case 1024: return launch_adj_col_n<T, 1024>(g, m, a, b, st);
+    case 2048: return launch_adj_col_n<T, 2048>(g, m, a, b, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// op 0: out = w K^2 f^2 in / (nx ny)^2, the gradient of the kinetic energy
+//       sum_full K^2 |f in|^2 / (2 (nx ny)^2) with respect to in (real (Re, Im) pairs);
+// op 1: out = M in nx ny / w, so that the normalised c2r of out is rfft^T(M in), the
+//       gradient with respect to the physical field whose rfft (dealiased) is the state.
+// w = 2 on interior kr columns, 1 on kr = 0 and Nyquist; f the PV-inversion factor.
+template <class T>
+__global__ void adj_spec_kernel(Geom g, ModArgs m, const cplx<T>* in, cplx<T>* out, int op) {
+  const size_t n = (size_t)g.ny * g.nkr;
+  const T dky = sel<T>(g.dky, g.dky_f, g.dky_l), dkx = sel<T>(g.dkx, g.dkx_f, g.dkx_l);
+  const T ell2 = sel<T>(m.ell_inv2, m.ell_inv2_f, m.ell_inv2_l), inv_n = sel<T>(g.inv_nxny, g.inv_nxny_f, g.inv_nxny_l);
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const int kr = (int)(e % g.nkr), j = (int)(e / g.nkr);
+    const size_t ti = (size_t)j * g.ldk + kr;
+    const bool edge = (kr == 0) || (2 * kr == g.nx);
+    const cplx<T> x = in[ti];
+    if (op == 0) {
+      const T krT = T(kr) * dkx, lv = T(lidx(g, j)) * dky;
+      const T K2 = krT * krT + lv * lv;
+      const T f = psi_factor<T>(m.psi_kind, K2, ell2, m.mult, ti);
+      const T w = edge ? T(1) : T(2);
+      out[ti] = ((w * K2 * f * f) * inv_n * inv_n) * x;
+    } else {
+      const T nn = T((double)g.nx * (double)g.ny);
+      out[ti] = kept(g, kr, j) ? ((edge ? T(1) : T(0.5)) * nn) * x : czero<T>();
+    }
+  }
+}
+
+template <class T>
+cudaError_t launch_adj_spec(const Geom& g, const ModArgs& m, const void* in, void* out, int op, cudaStream_t st) {
+  adj_spec_kernel<T><<<256, 256, 0, st>>>(g, m, static_cast<const cplx<T>*>(in), static_cast<cplx<T>*>(out), op);
+  return cudaGetLastError();
+}
 
 #define GF_INST_DISPATCH(T)                                                                                    \
   template cudaError_t launch_row<T>(const Geom&, const ModArgs&, const Bufs&, cudaStream_t);                   \
@@ -123,7 +184,10 @@ cudaError_t launch_spec_apply(const Geom& g, const ModArgs& m, const void* in, v
   template cudaError_t launch_diag<T>(const Geom&, const ModArgs&, const void*, const void*, const void*,       \
                                       uint32_t, double*, int, cudaStream_t);                                   \
   template cudaError_t launch_mask_inplace<T>(const Geom&, void*, cudaStream_t);                                \
-  template cudaError_t launch_spec_apply<T>(const Geom&, const ModArgs&, const void*, void*, int, cudaStream_t);
+  template cudaError_t launch_spec_apply<T>(const Geom&, const ModArgs&, const void*, void*, int, cudaStream_t); \
+  template cudaError_t launch_adj_row<T>(const Geom&, const AdjArgs&, const Bufs&, cudaStream_t);               \
+  template cudaError_t launch_adj_col<T>(const Geom&, const ModArgs&, const AdjArgs&, const Bufs&, cudaStream_t); \
+  template cudaError_t launch_adj_spec<T>(const Geom&, const ModArgs&, const void*, void*, int, cudaStream_t);
 
 GF_INST_DISPATCH(float)
 GF_INST_DISPATCH(double)

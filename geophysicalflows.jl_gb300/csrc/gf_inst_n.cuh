@@ -1,6 +1,6 @@
 // Per-size launchers: block shapes for one FFT length NN and precision T, and the launch.
 #pragma once
-#include "gf_kernels.cuh"
+#include "gf_adjoint.cuh"
 #include "gf_launch.cuh"
 
 namespace gf {
@@ -90,6 +90,32 @@ cudaError_t launch_col_fwd_n(const Geom& g, const Bufs& b, int nf, void* out, in
   return cudaGetLastError();
 }
 
+template <class T, int NN>
+cudaError_t launch_adj_row_n(const Geom& g, const AdjArgs& a, const Bufs& b, cudaStream_t st) {
+  cudaError_t err;
+  const size_t e = sizeof(cplx<T>);
+  const int B = pick_B(NN, RADIX<T>, e, 3, g.ny / 2, 1);
+  const size_t sm = (size_t)B * 3 * row_stride<T>(NN, NN / RADIX<T>) * e;
+  auto k = adj_row_kernel<T, NN, RADIX<T>>;
+  if ((err = set_smem(k, sm)) != cudaSuccess) return err;
+  k<<<g.ny / 2 / B, B * (NN / RADIX<T>), sm, st>>>(g, a, b, B);
+  return cudaGetLastError();
+}
+
+template <class T, int NN>
+cudaError_t launch_adj_col_n(const Geom& g, const ModArgs& m, const AdjArgs& a, const Bufs& b, cudaStream_t st) {
+  cudaError_t err;
+  const size_t e = sizeof(cplx<T>);
+  const int C = pick_C(NN, RADIX<T>, g.nkr, [&](int c) { return adj_col_smem(c, col_stride<T>(NN, c), e); }, 1);
+  Geom g2 = g;
+  g2.cs = col_stride<T>(NN, C);
+  const size_t sm = adj_col_smem(C, g2.cs, e);
+  auto k = adj_col_kernel<T, NN, RADIX<T>>;
+  if ((err = set_smem(k, sm)) != cudaSuccess) return err;
+  k<<<(g.nkr + C - 1) / C, C * (NN / RADIX<T>), sm, st>>>(g2, m, a, b, C);
+  return cudaGetLastError();
+}
+
 #define GF_INST_N(T, NN)                                                                                       \
   template cudaError_t launch_row_n<T, NN>(const Geom&, const ModArgs&, const Bufs&, cudaStream_t);             \
   template cudaError_t launch_col_n<T, NN>(const Geom&, const ModArgs&, const StepArgs&, const Bufs&,           \
@@ -98,6 +124,9 @@ cudaError_t launch_col_fwd_n(const Geom& g, const Bufs& b, int nf, void* out, in
                                                cudaStream_t);                                                  \
   template cudaError_t launch_row_c2r_n<T, NN>(const Geom&, const Bufs&, int, void*, cudaStream_t);             \
   template cudaError_t launch_row_r2c_n<T, NN>(const Geom&, const Bufs&, int, const void*, cudaStream_t);       \
-  template cudaError_t launch_col_fwd_n<T, NN>(const Geom&, const Bufs&, int, void*, int, cudaStream_t);
+  template cudaError_t launch_col_fwd_n<T, NN>(const Geom&, const Bufs&, int, void*, int, cudaStream_t);        \
+  template cudaError_t launch_adj_row_n<T, NN>(const Geom&, const AdjArgs&, const Bufs&, cudaStream_t);         \
+  template cudaError_t launch_adj_col_n<T, NN>(const Geom&, const ModArgs&, const AdjArgs&, const Bufs&,        \
+                                               cudaStream_t);
 
 }  // namespace gf

@@ -102,9 +102,25 @@ inline void split_hl(double d, float* h, float* l) {
 }
 
 struct Bufs {
-  const void* twid;  // TWN twiddles
-  void* W;           // [3][layer][j][ldw]
-  void* P;           // [3][layer][j][ldk]
+  const void* twid;       // TWN twiddles
+  void* W;                // [3][layer][j][ldw]
+  void* P;                // [3][layer][j][ldk]
+  void* phys = nullptr;   // row kernel: also store (q + eta, u, v) [3][layer][j][nx] (adjoint recompute)
+};
+
+// Arguments of the adjoint kernels (gf_adjoint.cuh).
+struct AdjArgs {
+  int stage;      // 4..1: the forward stage whose calcN! is transposed; 5: start a step from ubar_in
+  int head;       // stage 1: also start the previous step from the result
+  int filtered, cplx;
+  const void *e, *e2, *zeta, *alpha, *beta, *gamma, *filt;
+  void *ub, *n1acc, *xaacc, *x1acc;   // [j][ldk] cotangent accumulators
+  const void* ubar_in;                // stage 5: cotangent of the step's result
+  void* ubar_out;                     // stage 1: cotangent of the step's initial state
+  void *Wb, *Pb;                      // [2][j][ldk] y-inverse (abar, bbar) spectra; [3][j][ldk] products
+  const void* phys;                   // forward (q + eta, u, v) of the stage, [3][j][nx]
+  void* etab;                         // [j][nx] cotangent of eta
+  double U; float U_f, U_l;
 };
 
 // Generic transforms (updatevars!, set_*!, fwdtransform!/invtransform!).
@@ -124,6 +140,12 @@ template <class T> cudaError_t launch_diag(const Geom&, const ModArgs&, const vo
 template <class T> cudaError_t launch_mask_inplace(const Geom&, void* sol, cudaStream_t);
 template <class T> cudaError_t launch_spec_apply(const Geom&, const ModArgs&, const void* in, void* out, int op,
                                                  cudaStream_t);
+
+template <class T> cudaError_t launch_adj_row(const Geom&, const AdjArgs&, const Bufs&, cudaStream_t);
+template <class T> cudaError_t launch_adj_col(const Geom&, const ModArgs&, const AdjArgs&, const Bufs&, cudaStream_t);
+// element-wise adjoint helpers: op 0 kinetic-energy gradient, op 1 rfft^T preparation (see gf_dispatch.cu)
+template <class T> cudaError_t launch_adj_spec(const Geom&, const ModArgs&, const void* in, void* out, int op,
+                                               cudaStream_t);
 
 // message returned by gf_last_error(NULL)
 void set_global_error(const std::string& msg);

@@ -76,5 +76,8 @@ template <class T, int NN> cudaError_t launch_col_inv_n(const Geom&, const ModAr
 template <class T, int NN> cudaError_t launch_row_c2r_n(const Geom&, const Bufs&, int, void*, cudaStream_t);
 template <class T, int NN> cudaError_t launch_row_r2c_n(const Geom&, const Bufs&, int, const void*, cudaStream_t);
 template <class T, int NN> cudaError_t launch_col_fwd_n(const Geom&, const Bufs&, int, void*, int, cudaStream_t);
+template <class T, int NN> cudaError_t launch_adj_row_n(const Geom&, const AdjArgs&, const Bufs&, cudaStream_t);
+template <class T, int NN> cudaError_t launch_adj_col_n(const Geom&, const ModArgs&, const AdjArgs&, const Bufs&,
+                                                        cudaStream_t);
 
 }  // namespace gf

@@ -69,3 +69,8 @@ def energy_work(prob): return _d(prob, 5)
 def enstrophy_work(prob): return _d(prob, 6)
 def energy_drag(prob): return _d(prob, 7)
 def enstrophy_drag(prob): return _d(prob, 8)
+
+
+# library diagnostic ids: stepforward(prob, diags, n) streams these from the device
+for _f, _k in ((kinetic_energy, 0), (energy, 9), (enstrophy, 2)):
+    _f.diag_id = _k

@@ -51,3 +51,8 @@ def buoyancy_work(prob):
     if prob.forcing.kind is None:
         raise TypeError("buoyancy_work needs a forced problem")
     return _d(prob, 4)
+
+
+# library diagnostic ids: stepforward(prob, diags, n) streams these from the device
+for _f, _k in ((kinetic_energy, 0), (buoyancy_variance, 1), (total_3D_energy, 2), (buoyancy_dissipation, 3)):
+    _f.diag_id = _k

@@ -70,3 +70,10 @@ def enstrophy_work(prob):
 def _need_forcing(prob):
     if prob.forcing.kind is None:
         raise TypeError("work diagnostics need a forced problem")
+
+
+# library diagnostic ids: stepforward(prob, diags, n) streams these from the device
+for _f, _k in ((energy, 0), (enstrophy, 1), (palinstrophy, 2), (energy_dissipation_hyperviscosity, 3),
+               (energy_dissipation_hypoviscosity, 4), (enstrophy_dissipation_hyperviscosity, 5),
+               (enstrophy_dissipation_hypoviscosity, 6)):
+    _f.diag_id = _k

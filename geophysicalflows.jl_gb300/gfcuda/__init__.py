@@ -6,6 +6,9 @@ from . import _abi
 from ._abi import load, GFError, GFNotImplemented
 from .core import Diagnostic, Forcing, ensemble_step, stepforward
 from . import TwoDNavierStokes, SingleLayerQG, MultiLayerQG, SurfaceQG
+from . import utils
+from . import adjoint
+from .utils import peakedisotropicspectrum
 
 __all__ = ["load", "GFError", "GFNotImplemented", "Diagnostic", "Forcing", "ensemble_step", "stepforward", "TwoDNavierStokes",
-           "SingleLayerQG", "MultiLayerQG", "SurfaceQG"]
+           "SingleLayerQG", "MultiLayerQG", "SurfaceQG", "utils", "adjoint", "peakedisotropicspectrum"]

@@ -13,13 +13,16 @@ STEPPERS = {"ForwardEuler": 0, "FilteredForwardEuler": 1, "RK4": 2, "FilteredRK4
 F32, F64, DF64 = 0, 1, 2
 FORCING = {None: 0, "static": 1, "harmonic": 2, "stochastic": 3, "stochastic_phase": 4}
 HOST, DEVICE = 0, 1
+LOSS_KINETIC_ENERGY = 0
 FIELD_Q, FIELD_PSI, FIELD_U, FIELD_V = 0, 1, 2, 3
 
 EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_abi_version", "gf_get_dims", "gf_set_state",
            "gf_get_state", "gf_get_clock", "gf_set_clock", "gf_set_physical", "gf_step", "gf_step_diags",
            "gf_calcN", "gf_updatevars", "gf_get_field", "gf_fwdtransform", "gf_invtransform",
            "gf_diagnostics", "gf_set_forcing", "gf_synchronize", "gf_profile_enable", "gf_profile_read",
-           "gf_rfft2_noalloc", "gf_get_batch", "gf_set_graph_steps", "gf_ensemble_step"]
+           "gf_rfft2_noalloc", "gf_get_batch", "gf_set_graph_steps", "gf_ensemble_step",
+           "gf_peakedisotropicspectrum", "gf_get_filter", "gf_adjoint_setup", "gf_adjoint_forward",
+           "gf_adjoint_backward", "gf_grad"]
 
 
 class gf_config(C.Structure):
@@ -82,6 +85,12 @@ def load(path=None):
         "gf_get_batch": ([vp, C.POINTER(i32)], C.c_int),
         "gf_set_graph_steps": ([vp, i32], C.c_int),
         "gf_ensemble_step": ([C.POINTER(vp), i32, i64], C.c_int),
+        "gf_peakedisotropicspectrum": ([vp, C.c_double, C.c_double, vp, i32, C.c_uint64, vp, C.c_int], C.c_int),
+        "gf_get_filter": ([vp, vp], C.c_int),
+        "gf_adjoint_setup": ([vp, i64, i32], C.c_int),
+        "gf_adjoint_forward": ([vp], C.c_int),
+        "gf_adjoint_backward": ([vp, vp, vp, vp, C.c_int], C.c_int),
+        "gf_grad": ([vp, C.c_int, vp, vp, C.POINTER(dbl), C.c_int], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

@@ -1,0 +1,55 @@
+"""Reverse-mode derivative of stepforward! (the host-side counterpart of a
+ChainRulesCore.rrule on stepforward!), over libgfcuda's adjoint entry points.
+
+    loss, dq0, deta = grad(prob, nsteps, checkpoint_every=25)     # final kinetic energy
+    pullback = stepforward_with_pullback(prob, nsteps)           # rrule-style
+    sol0_bar, eta_bar = pullback(sol_bar)
+
+TwoDNavierStokes and SingleLayerQG (constant U) with ETDRK4 or FilteredETDRK4.  The
+gradients are those of the discrete step the library computes, in the Problem's precision.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _abi as A
+
+
+def setup(prob, nsteps, checkpoint_every=25):
+    prob._c(prob._lib.gf_adjoint_setup(prob._ctx, int(nsteps), int(checkpoint_every)))
+    prob._adj_steps = int(nsteps)
+
+
+def grad(prob, nsteps=None, checkpoint_every=25, topography=None):
+    """Step prob forward nsteps from its current state and return (loss, dq0, deta): the
+    final kinetic energy and its gradients with respect to the physical initial field (as
+    given to set_q!/set_zeta!) and to the topographic PV eta (SingleLayerQG; None for
+    TwoDNavierStokes unless topography=True is asked of it)."""
+    if nsteps is not None and getattr(prob, "_adj_steps", None) != int(nsteps):
+        setup(prob, nsteps, checkpoint_every)
+    g = prob.grid
+    dq0 = np.empty((g.ny, g.nx), dtype=prob.T)
+    want_eta = prob.module == "SingleLayerQG" if topography is None else topography
+    deta = np.empty((g.ny, g.nx), dtype=prob.T) if want_eta else None
+    loss = C.c_double()
+    prob._c(prob._lib.gf_grad(prob._ctx, A.LOSS_KINETIC_ENERGY, dq0.ctypes.data,
+                              None if deta is None else deta.ctypes.data, C.byref(loss), A.HOST))
+    return loss.value, dq0, deta
+
+
+def stepforward_with_pullback(prob, nsteps, checkpoint_every=25):
+    """stepforward!(prob, nsteps) keeping checkpoints; returns pullback(sol_bar) ->
+    (sol0_bar, eta_bar), the cotangents of the initial state and (SingleLayerQG) of eta."""
+    setup(prob, nsteps, checkpoint_every)
+    prob._c(prob._lib.gf_adjoint_forward(prob._ctx))
+
+    def pullback(sol_bar):
+        g = prob.grid
+        sb = np.ascontiguousarray(np.broadcast_to(sol_bar, prob.spec_shape), dtype=prob.CT)
+        s0 = np.empty(prob.spec_shape, dtype=prob.CT)
+        eb = np.empty((g.ny, g.nx), dtype=prob.T) if prob.module == "SingleLayerQG" else None
+        prob._c(prob._lib.gf_adjoint_backward(prob._ctx, sb.ctypes.data, s0.ctypes.data,
+                                              None if eb is None else eb.ctypes.data, A.HOST))
+        return s0, eb
+
+    return pullback

@@ -15,6 +15,7 @@ reference's column-major (nx, ny) / (nkr, ny) Julia arrays.
 """
 import ctypes as C
 import math
+import weakref
 
 import numpy as np
 
@@ -36,9 +37,28 @@ class Grid:
         self.invKrsq = np.where(self.Krsq == 0, 0.0, 1.0 / np.where(self.Krsq == 0, 1.0, self.Krsq))
         self.aliased_fraction = aliased_fraction
         self.T = T
+        self._prob = None  # weak reference to the Problem whose context computes on this grid
 
     def gridpoints(self):
         return np.meshgrid(self.x, self.y, indexing="xy")
+
+
+class TimeStepper:
+    """prob.timestepper: the stepper's name and, for the Filtered steppers, its filter
+    ([ny, nx/2+1], FourierFlows makefilter as built by the library)."""
+
+    def __init__(self, prob, name):
+        self._prob, self.name = weakref.ref(prob), name
+
+    @property
+    def filter(self):
+        p = self._prob()
+        out = np.empty((p.grid.ny, p.grid.nkr), dtype=np.float64)
+        code = p._lib.gf_get_filter(p._ctx, out.ctypes.data)
+        if code == A.GF_ERR_STATE:
+            raise AttributeError(f"{self.name} has no filter")
+        p._c(code)
+        return out
 
 
 class Clock:
@@ -128,6 +148,8 @@ class Problem:
         A.check(self._lib, None, self._lib.gf_create(C.byref(cfg), stream, C.byref(self._ctx)))
         self._keep = []
         self.clock = Clock(self, dt)
+        self.timestepper = TimeStepper(self, stepper)
+        self.grid._prob = weakref.ref(self)
         self.vars = Vars(self.field_names)
         if self.forcing.kind in ("static", "harmonic") and self.forcing.Fh is not None:
             self.set_forcing(self.forcing.Fh)
@@ -267,6 +289,21 @@ def stepforward(prob, *args):
         prob._c(prob._lib.gf_step(prob._ctx, n))
         return
     diags = diags if isinstance(diags, (list, tuple)) else [diags]
+    ids = [getattr(d.calc, "diag_id", None) for d in diags]
+    if prob.batch == 1 and all(i is not None for i in ids) and n > 0:
+        # library diagnostics: reduced on the device after every step, one host wait per call
+        idv = np.ascontiguousarray(ids, dtype=np.int32)
+        out = np.empty((n, len(ids)), dtype=np.float64)
+        t, step, dt = prob.clock.t, prob.clock.step, prob.clock.dt
+        prob._c(prob._lib.gf_step_diags(prob._ctx, n, idv.ctypes.data_as(C.POINTER(C.c_int32)), len(ids),
+                                        out.ctypes.data_as(C.POINTER(C.c_double))))
+        for k in range(n):
+            t += dt
+            for j, d in enumerate(diags):
+                d.data.append(float(out[k, j]))
+                d.t.append(t)
+                d.steps.append(step + k + 1)
+        return
     for _ in range(n):
         prob._c(prob._lib.gf_step(prob._ctx, 1))
         for d in diags:

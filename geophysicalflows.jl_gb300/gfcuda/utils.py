@@ -1,0 +1,73 @@
+"""GeophysicalFlows utilities (src/utils.jl) on libgfcuda.
+
+peakedisotropicspectrum runs on the device (gf_peakedisotropicspectrum); ring_forcing_spectrum
+is the host-side set-up the reference's forced examples build before they make a Problem
+(examples/singlelayerqg_betaforced.jl:61-73, examples/twodnavierstokes_stochasticforcing.jl),
+handed to the library through Forcing("stochastic", spectrum=...).
+"""
+import numpy as np
+
+from . import _abi as A
+
+
+def _problem_of(grid_or_prob):
+    p = getattr(grid_or_prob, "_ctx", None) and grid_or_prob
+    if p is None:
+        ref = getattr(grid_or_prob, "_prob", None)
+        p = ref() if ref is not None else None
+    if p is None or not p._ctx:
+        raise ValueError("pass the grid of a live Problem (prob.grid) or the Problem itself")
+    return p
+
+
+def peakedisotropicspectrum(grid, kpeak, E0, mask=None, allones=False, seed=1234):
+    """peakedisotropicspectrum(grid, kpeak, E0; mask, allones) (src/utils.jl:29-54): a random
+    isotropic vorticity field whose streamfunction spectrum peaks at kpeak (in units of
+    2 pi / Lx), with energy E0.  Computed on the device; the random coefficients are Philox
+    draws from `seed` (instance i of a batched Problem uses seed + i).  Returns the physical
+    field, shape (ny, nx) or (batch, ny, nx), in the Problem's real type."""
+    p = _problem_of(grid)
+    g = p.grid
+    m = None
+    if mask is not None:
+        m = np.ascontiguousarray(np.broadcast_to(mask, (g.ny, g.nkr)), dtype=np.float64)
+    out = np.empty(p.phys_shape, dtype=p.T)
+    p._c(p._lib.gf_peakedisotropicspectrum(p._ctx, float(kpeak), float(E0), None if m is None else m.ctypes.data,
+                                           int(bool(allones)), int(seed) & 0xFFFFFFFFFFFFFFFF, out.ctypes.data,
+                                           A.HOST))
+    return out
+
+
+def parsevalsum(fh, grid):
+    """FourierFlows.parsevalsum of a real field's half spectrum fh (ny, nkr): the sum over the
+    full spectrum (interior kr columns counted twice, kr = 0 and, for even nx, the Nyquist
+    column once) times Lx Ly / (nx ny)^2, real part."""
+    w = np.full(grid.nkr, 2.0)
+    w[0] = 1.0
+    if grid.nx % 2 == 0:
+        w[-1] = 1.0
+    return grid.Lx * grid.Ly / (grid.nx * grid.ny) ** 2 * float(np.real(np.sum(np.asarray(fh) * w)))
+
+
+def ring_forcing_spectrum(grid, kf, dkf, eps):
+    """Isotropic Gaussian ring forcing spectrum exp(-(|k| - kf)^2 / (2 dkf^2)) (zero at k = 0),
+    normalised so that white-in-time forcing with this spectrum injects energy at rate eps:
+    eps0 = parsevalsum(spectrum / (2 K^2)) / (Lx Ly) (examples/singlelayerqg_betaforced.jl:61-73).
+    kf, dkf in the grid's wavenumber units (radians per unit length)."""
+    K = np.sqrt(grid.Krsq)
+    spec = np.exp(-(K - kf) ** 2 / (2 * dkf ** 2))
+    spec[grid.Krsq == 0] = 0.0
+    eps0 = parsevalsum(spec * grid.invKrsq / 2, grid) / (grid.Lx * grid.Ly)
+    return spec * (eps / eps0)
+
+
+def random_topography(grid, kmax, amp, seed):
+    """A random topographic PV field: Fourier modes 0 < |k| <= kmax (in units of 2 pi / Lx)
+    with complex-normal coefficients from numpy's seeded generator, scaled so that the
+    field's maximum |eta| is amp; shape (ny, nx)."""
+    rng = np.random.default_rng(seed)
+    K = np.sqrt(grid.Krsq) * grid.Lx / (2 * np.pi)
+    z = rng.standard_normal(grid.Krsq.shape) + 1j * rng.standard_normal(grid.Krsq.shape)
+    eh = np.where((K <= kmax) & (grid.Krsq > 0), z, 0)
+    eta = np.fft.irfft2(eh, s=(grid.ny, grid.nx))
+    return amp * eta / np.max(np.abs(eta))

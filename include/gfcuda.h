@@ -179,6 +179,21 @@ int gf_calcN(gf_ctx* ctx, void* N, void* sol, double t, int where);
 int gf_updatevars(gf_ctx* ctx);
 int gf_get_field(gf_ctx* ctx, int which, void* out, int where);
 
+/* GeophysicalFlows.peakedisotropicspectrum(grid, kpeak, E0; mask, allones) (src/utils.jl:29-54)
+ * on the context's grid (nlayers = 1, Lx = Ly): writes the physical field zeta = irfft(-K^2 psi_hat)
+ * for every ensemble instance ([batch][ny][nx], the context's real type; FP64 for GF_DF64).
+ * psi_hat = mask * z * (K^2 (1 + (K/k0)^4))^(-1/2), k0 = kpeak 2 pi / Lx, z complex normal
+ * (allones: z = 1) drawn with Philox4x32-10, counter (j (nx/2+1) + ik, 0, 0, 0x494E4954) and key
+ * seed + instance; normalised so that sum over the half spectrum of K^2 |psi_hat|^2 / (nx ny)^2 = E0
+ * (the reference's :50).  mask: NULL (ones) or a [ny][nx/2+1] FP64 array in `where` memory.
+ * Julia's randn stream is replaced by Philox; the amplitudes and the normalisation are the
+ * reference's. */
+int gf_peakedisotropicspectrum(gf_ctx* ctx, double kpeak, double E0, const double* mask, int32_t allones,
+                               uint64_t seed, void* zeta, int where);
+/* prob.timestepper.filter of the Filtered steppers (FourierFlows makefilter, order 4, inner 0.65,
+ * outer 1 unless set in gf_config) as [ny][nx/2+1] FP64; GF_ERR_STATE for unfiltered steppers. */
+int gf_get_filter(const gf_ctx* ctx, double* out);
+
 /* MultiLayerQG fwdtransform!/invtransform! (src/multilayerqg.jl:483-493) and the plain
  * rfft/irfft of FourierFlows' rfftplan, applied to nlayers fields at once. */
 int gf_fwdtransform(gf_ctx* ctx, void* fieldh, const void* field, int where);
@@ -208,6 +223,34 @@ int gf_set_forcing(gf_ctx* ctx, const void* data, int where);
 
 /* Block until the context's stream has finished. */
 int gf_synchronize(gf_ctx* ctx);
+
+/* ---- adjoint ----------------------------------------------------------------------------
+ * Reverse-mode derivative of stepforward!(prob, nsteps), the counterpart of a
+ * ChainRulesCore.rrule on stepforward! (the reference has no derivative; its step is
+ * src/singlelayerqg.jl:356-382 / src/twodnavierstokes.jl:253-294 under FourierFlows' ETDRK4).
+ * Supported: TwoDNavierStokes and SingleLayerQG with constant U, stepper ETDRK4 or
+ * FilteredETDRK4, batch = 1.  It is the exact transpose of the discrete step the library
+ * computes (dealiasing, PV inversion, stage combinations), in the context's precision.
+ * Checkpointing: the forward pass keeps the state every checkpoint_every steps; the reverse
+ * pass recomputes one segment at a time from its checkpoint and runs its transposed stages.
+ *
+ * gf_adjoint_setup: allocate for nsteps steps (call again to change them).
+ * gf_adjoint_forward: stepforward!(prob, nsteps) from the current state, keeping checkpoints.
+ * gf_adjoint_backward: given the cotangent sol_bar of the final state (layout of
+ *   gf_get_state), the cotangent of the initial state (sol0_bar, may be NULL) and of the
+ *   topographic PV eta (eta_bar, [ny][nx] physical, SingleLayerQG only, may be NULL).  The
+ *   state and clock are left at the forward pass's result.  Spectral arrays are taken as
+ *   real vectors of (Re, Im) pairs over the stored half spectrum.
+ * gf_grad: gf_adjoint_forward, the loss of the final state (loss_kind
+ *   GF_LOSS_KINETIC_ENERGY: SingleLayerQG.kinetic_energy, src/singlelayerqg.jl:546-553, or
+ *   TwoDNavierStokes.energy, src/twodnavierstokes.jl:374-380) into *loss, and its gradients
+ *   with respect to the physical initial field q0 of set_q!/set_zeta! (dq0, [ny][nx]) and
+ *   to eta (deta), either may be NULL. */
+enum { GF_LOSS_KINETIC_ENERGY = 0 };
+int gf_adjoint_setup(gf_ctx* ctx, int64_t nsteps, int32_t checkpoint_every);
+int gf_adjoint_forward(gf_ctx* ctx);
+int gf_adjoint_backward(gf_ctx* ctx, const void* sol_bar, void* sol0_bar, void* eta_bar, int where);
+int gf_grad(gf_ctx* ctx, int loss_kind, void* dq0, void* deta, double* loss, int where);
 
 /* Kernel timing for benchmarks: while enabled, CUDA events are recorded on the context's
  * stream around every row-pass and column-pass kernel launch.  gf_profile_read waits for the

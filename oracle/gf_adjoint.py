@@ -1,0 +1,198 @@
+"""Oracle (test infrastructure only): FP64 tangent-linear and adjoint of the SingleLayerQG
+ETDRK4 / FilteredETDRK4 step, and the gradient of a final-time kinetic energy with respect to
+the initial PV q0 and the topographic PV eta.
+
+It differentiates the DISCRETE step of the restatement in gf_oracle.py exactly:
+  * calcN! (src/singlelayerqg.jl:356-382, 443-451, constant U): dealias! sol in place,
+    psi_hat = f q_hat (f = -1/K^2 or -1/(K^2 + 1/l^2), src/singlelayerqg.jl:484-490),
+    u_hat = -i l psi_hat, v_hat = i kr psi_hat, q,u,v = irfft2(.), qe = q + eta,
+    N = -i kr rfft2(u qe) - i l rfft2(v qe) - i kr U eta_hat;
+  * the FourierFlows ETDRK4 stage sequence (restated in gf_oracle.TimeStepper.step), in which
+    every calcN! dealiases its input array in place, so that later uses of that array see the
+    dealiased values.
+Inner products: spectral arrays are real vectors of (Re, Im) pairs over the STORED half
+spectrum, <a, b> = Re sum conj(a) b; physical arrays the plain sum.  With them
+  rfft2^T(X) = Re(nx ny ifft2(X placed in the half plane, zero elsewhere)),
+  irfft2^T(x) = w rfft2(x) / (nx ny), w = 2 for interior kr columns, 1 for kr = 0 and Nyquist.
+The loss is SingleLayerQG.kinetic_energy (src/singlelayerqg.jl:546-553): sum over the full
+spectrum of K^2 |psi_hat|^2 / (2 (nx ny)^2).
+"""
+import numpy as np
+
+import gf_oracle as O
+
+
+def _w(grid):
+    w = np.full(grid.nkr, 2.0)
+    w[0] = 1.0
+    if grid.nx % 2 == 0:
+        w[-1] = 1.0
+    return w
+
+
+def rfft2_T(X, grid):
+    """Transpose of the unnormalised r2c transform (half spectrum -> real field)."""
+    full = np.zeros(X.shape[:-1] + (grid.nx,), dtype=np.complex128)
+    full[..., : grid.nkr] = X
+    return np.real(np.fft.ifft2(full, axes=(-2, -1))) * (grid.nx * grid.ny)
+
+
+def irfft2_T(x, grid):
+    """Transpose of the normalised c2r transform (real field -> half spectrum)."""
+    return np.fft.rfft2(x, axes=(-2, -1)) * _w(grid) / (grid.nx * grid.ny)
+
+
+class SLQGAdjoint:
+    """Tangent-linear and adjoint of an oracle SingleLayerQG problem stepped with ETDRK4 or
+    FilteredETDRK4 (constant U; additive forcing does not change the derivative)."""
+
+    def __init__(self, prob):
+        if not prob.U_is_number:
+            raise NotImplementedError("the adjoint supports a constant U")
+        ts = prob.timestepper
+        if ts.kind != "ETDRK4":
+            raise NotImplementedError("the adjoint follows the ETDRK4 stages")
+        self.p, self.g = prob, prob.grid
+        g = self.g
+        self.f = (-g.invKrsq if prob.ell is None else -1.0 / (g.Krsq + 1.0 / prob.ell ** 2))
+        self.mask = np.ones((g.ny, g.nkr))
+        O.dealias(self.mask, g)
+        self.filter = ts.filter if getattr(ts, "filtered", False) else None
+        self.c = dict(e=ts.expLdt, e2=ts.expLdt2, z=ts.zeta, a=ts.alpha, b=ts.beta, g=ts.gamma)
+
+    # -- calcN! without its dealias (the input is already dealiased) and its derivatives
+    def _fields(self, X):
+        g, f = self.g, self.f
+        psih = f * X
+        return O.irfft2(X, g), O.irfft2(-1j * g.l * psih, g), O.irfft2(1j * g.kr * psih, g)
+
+    def N(self, X, eta):
+        g = self.g
+        q, u, v = self._fields(X)
+        qe = q + eta
+        return (-1j * g.kr * O.rfft2(u * qe) - 1j * g.l * O.rfft2(v * qe)
+                - 1j * g.kr * self.p.U * O.rfft2(eta))
+
+    def N_tlm(self, X, eta, dX, deta):
+        g = self.g
+        q, u, v = self._fields(X)
+        dq, du, dv = self._fields(dX)
+        qe, dqe = q + eta, dq + deta
+        return (-1j * g.kr * O.rfft2(du * qe + u * dqe) - 1j * g.l * O.rfft2(dv * qe + v * dqe)
+                - 1j * g.kr * self.p.U * O.rfft2(deta))
+
+    def N_adj(self, X, eta, Nbar):
+        """(Xbar, etabar) = J^T Nbar at (X, eta)."""
+        g = self.g
+        q, u, v = self._fields(X)
+        qe = q + eta
+        abar = rfft2_T(1j * g.kr * Nbar, g)
+        bbar = rfft2_T(1j * g.l * Nbar, g)
+        qbar = abar * u + bbar * v
+        etabar = qbar + self.p.U * abar
+        ub, vb = irfft2_T(abar * qe, g), irfft2_T(bbar * qe, g)
+        Xbar = irfft2_T(qbar, g) + self.f * (1j * g.l * ub - 1j * g.kr * vb)
+        return Xbar, etabar
+
+    # -- one step: forward, tangent-linear, adjoint
+    def step(self, u, eta):
+        c, M = self.c, self.mask
+        X1 = M * u
+        N1 = self.N(X1, eta)
+        XA = M * (c["e2"] * X1 + c["z"] * N1)
+        N2 = self.N(XA, eta)
+        XB = M * (c["e2"] * X1 + c["z"] * N2)
+        N3 = self.N(XB, eta)
+        XC = M * (c["e2"] * XA + c["z"] * (2 * N3 - N1))
+        N4 = self.N(XC, eta)
+        new = c["e"] * X1 + c["a"] * N1 + 2 * c["b"] * (N2 + N3) + c["g"] * N4
+        if self.filter is not None:
+            new = self.filter * new
+        return new, (X1, XA, XB, XC)
+
+    def step_tlm(self, u, eta, du, deta):
+        c, M = self.c, self.mask
+        (X1, XA, XB, XC) = self.step(u, eta)[1]
+        dX1 = M * du
+        dN1 = self.N_tlm(X1, eta, dX1, deta)
+        dXA = M * (c["e2"] * dX1 + c["z"] * dN1)
+        dN2 = self.N_tlm(XA, eta, dXA, deta)
+        dXB = M * (c["e2"] * dX1 + c["z"] * dN2)
+        dN3 = self.N_tlm(XB, eta, dXB, deta)
+        dXC = M * (c["e2"] * dXA + c["z"] * (2 * dN3 - dN1))
+        dN4 = self.N_tlm(XC, eta, dXC, deta)
+        dnew = c["e"] * dX1 + c["a"] * dN1 + 2 * c["b"] * (dN2 + dN3) + c["g"] * dN4
+        if self.filter is not None:
+            dnew = self.filter * dnew
+        return dnew
+
+    def step_adj(self, u, eta, ubar_new):
+        """(ubar, etabar contribution) of one step, the stages taken in reverse."""
+        c, M = self.c, self.mask
+        cj = {k: np.conj(v) for k, v in c.items()}
+        X1, XA, XB, XC = self.step(u, eta)[1]
+        ub = self.filter * ubar_new if self.filter is not None else ubar_new
+        Xb, eb4 = self.N_adj(XC, eta, cj["g"] * ub)
+        Cb = M * Xb
+        N3b = 2 * cj["b"] * ub + 2 * cj["z"] * Cb
+        N1b = cj["a"] * ub - cj["z"] * Cb
+        XAb = cj["e2"] * Cb
+        Xb, eb3 = self.N_adj(XB, eta, N3b)
+        Bb = M * Xb
+        X1b = cj["e"] * ub + cj["e2"] * Bb
+        N2b = 2 * cj["b"] * ub + cj["z"] * Bb
+        Xb, eb2 = self.N_adj(XA, eta, N2b)
+        Ab = M * (XAb + Xb)
+        X1b = X1b + cj["e2"] * Ab
+        N1b = N1b + cj["z"] * Ab
+        Xb, eb1 = self.N_adj(X1, eta, N1b)
+        return M * (X1b + Xb), eb1 + eb2 + eb3 + eb4
+
+    # -- loss and gradients
+    def kinetic_energy(self, sol):
+        g = self.g
+        return float(np.sum(_w(g) * g.Krsq * np.abs(self.f * sol) ** 2)) / (2 * (g.nx * g.ny) ** 2)
+
+    def kinetic_energy_grad(self, sol):
+        g = self.g
+        return _w(g) * g.Krsq * self.f ** 2 * sol / (g.nx * g.ny) ** 2
+
+    def initial_state(self, q0):
+        """set_q! (src/singlelayerqg.jl:519-534): sol = rfft2(q0), dealiased by updatevars!."""
+        return self.mask * O.rfft2(q0)
+
+    def loss(self, q0, eta, nsteps):
+        u = self.initial_state(q0)
+        for _ in range(nsteps):
+            u = self.step(u, eta)[0]
+        return self.kinetic_energy(u)
+
+    def gradient(self, q0, eta, nsteps):
+        """Loss and its gradients with respect to q0 and eta (every step state stored)."""
+        us = [self.initial_state(q0)]
+        for _ in range(nsteps):
+            us.append(self.step(us[-1], eta)[0])
+        ubar = self.kinetic_energy_grad(us[-1])
+        etabar = np.zeros_like(eta)
+        for n in range(nsteps - 1, -1, -1):
+            ubar, eb = self.step_adj(us[n], eta, ubar)
+            etabar += eb
+        return self.kinetic_energy(us[-1]), rfft2_T(self.mask * ubar, self.g), etabar
+
+    def directional_derivative(self, q0, eta, nsteps, dq0, deta):
+        """dL along (dq0, deta) from the tangent-linear model."""
+        u, du = self.initial_state(q0), self.initial_state(dq0)
+        for _ in range(nsteps):
+            du = self.step_tlm(u, eta, du, deta)
+            u = self.step(u, eta)[0]
+        return float(np.sum(np.real(np.conj(self.kinetic_energy_grad(u)) * du)))
+
+
+def random_topography(grid, kmax, amp, seed):
+    """Random Fourier modes |k| <= kmax (in units of 2 pi / Lx) with Philox complex-normal
+    coefficients (tag 0x544F504F), scaled so that the field's maximum |eta| is amp."""
+    K = np.sqrt(grid.Krsq) * grid.Lx / (2 * np.pi)
+    z = O.complex_normal(grid.Krsq.size, seed, 0, 0x544F504F).reshape(grid.Krsq.shape)
+    eh = np.where((K <= kmax) & (grid.Krsq > 0), z, 0)
+    eta = O.irfft2(eh, grid)
+    return amp * eta / np.max(np.abs(eta))

@@ -1,0 +1,169 @@
+"""GPU adjoint of the ETDRK4 step (gf_adjoint_* / gf_grad) against the oracle's discrete
+adjoint (oracle/gf_adjoint.py, itself pinned by finite differences and the tangent-linear
+dot-product identity), against central finite differences of the GPU forward model, and for
+checkpoint-interval invariance."""
+import numpy as np
+import pytest
+
+import gf_adjoint as AD
+import gf_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+gfcuda = pytest.importorskip("gfcuda")
+from gfcuda import SingleLayerQG as SL, TwoDNavierStokes as TD, adjoint  # noqa: E402
+from gfcuda import stepforward  # noqa: E402
+
+
+def rel(a, b):
+    return O.rel_l2(a, b)
+
+
+def slqg_case(n, stepper="ETDRK4", U=0.2, beta=1.0, ell=0.35, dt=0.01):
+    g = O.Grid(n)
+    eta = AD.random_topography(g, 8, 0.1, 7)
+    q0 = O.peakedisotropicspectrum(g, 6, 0.5, seed=1234)
+    kw = dict(nx=n, deformation_radius=ell, eta=eta, dt=dt, stepper=stepper, U=U, beta=beta)
+    return kw, q0, eta
+
+
+def gpu_grad(kw, q0, nsteps, every, T=np.float64, precision=None):
+    p = SL.Problem("GPU", T=T, precision=precision, **kw)
+    SL.set_q(p, q0)
+    loss, dq0, deta = adjoint.grad(p, nsteps, checkpoint_every=every)
+    return p, loss, dq0, deta
+
+
+@pytest.mark.parametrize("stepper,U,beta,ell", [("ETDRK4", 0.2, 1.0, 0.35), ("FilteredETDRK4", 0.0, 0.0, 0.35),
+                                                ("ETDRK4", 0.3, 2.0, np.inf)])
+def test_gradient_matches_oracle_adjoint(stepper, U, beta, ell):
+    n, ns = 64, 12
+    kw, q0, eta = slqg_case(n, stepper, U, beta, ell)
+    p, loss, dq0, deta = gpu_grad(kw, q0, ns, 5)
+    A = AD.SLQGAdjoint(O.SingleLayerQG(**kw))
+    L, gq, ge = A.gradient(q0, eta, ns)
+    assert abs(loss - L) <= 1e-13 * L
+    assert rel(dq0, gq) <= 1e-11
+    assert rel(deta, ge) <= 1e-11
+
+
+@pytest.mark.parametrize("prec,T,tol", [("DF64", np.float64, 1e-10), (None, np.float32, 2e-4)])
+def test_gradient_other_precisions(prec, T, tol):
+    n, ns = 64, 12
+    kw, q0, eta = slqg_case(n)
+    p, loss, dq0, deta = gpu_grad(kw, q0, ns, 4, T=T, precision=prec)
+    L, gq, ge = AD.SLQGAdjoint(O.SingleLayerQG(**kw)).gradient(q0, eta, ns)
+    assert abs(loss - L) <= max(tol, 1e-12) * L
+    assert rel(dq0, gq) <= tol
+    assert rel(deta, ge) <= tol
+
+
+def test_twodns_gradient_and_state_restored():
+    n, ns = 64, 10
+    g = O.Grid(n)
+    z0 = O.peakedisotropicspectrum(g, 6, 0.5, seed=5)
+    kw = dict(nx=n, dt=0.01, nu=1e-3, nnu=1, stepper="ETDRK4")
+    p = TD.Problem("GPU", **kw)
+    TD.set_zeta(p, z0)
+    loss, dq0, deta = adjoint.grad(p, ns, checkpoint_every=3)
+    assert deta is None
+    # TwoDNavierStokes is SingleLayerQG with eta = 0, l = inf, beta = 0 and the same L
+    r = O.SingleLayerQG(nx=n, dt=0.01, nu=1e-3, nnu=1, stepper="ETDRK4")
+    L, gq, _ = AD.SLQGAdjoint(r).gradient(z0, np.zeros((n, n)), ns)
+    assert abs(loss - L) <= 1e-13 * L and rel(dq0, gq) <= 1e-11
+    # the context holds the forward result again, clock included
+    q = TD.Problem("GPU", **kw)
+    TD.set_zeta(q, z0)
+    stepforward(q, ns)
+    assert np.array_equal(p.sol, q.sol)
+    assert p.clock.step == ns and p.clock.t == q.clock.t
+    with pytest.raises(ValueError):
+        adjoint.grad(p, ns, topography=True)
+
+
+def test_checkpoint_interval_does_not_change_the_gradient():
+    kw, q0, eta = slqg_case(64)
+    ref = None
+    for every in (1, 4, 12, 100):
+        _, loss, dq0, deta = gpu_grad(kw, q0, 12, every)
+        if ref is None:
+            ref = (loss, dq0, deta)
+        else:
+            assert loss == ref[0] and np.array_equal(dq0, ref[1]) and np.array_equal(deta, ref[2])
+
+
+def test_pullback_matches_oracle_step_adjoint():
+    kw, q0, eta = slqg_case(64)
+    ns = 6
+    p = SL.Problem("GPU", **kw)
+    SL.set_q(p, q0)
+    pull = adjoint.stepforward_with_pullback(p, ns, checkpoint_every=4)
+    rng = np.random.default_rng(11)
+    sol_bar = np.fft.rfft2(rng.standard_normal((64, 64)))
+    s0, eb = pull(sol_bar)
+    A = AD.SLQGAdjoint(O.SingleLayerQG(**kw))
+    us = [A.initial_state(q0)]
+    for _ in range(ns):
+        us.append(A.step(us[-1], eta)[0])
+    ub, etab = sol_bar, np.zeros_like(eta)
+    for k in range(ns - 1, -1, -1):
+        ub, e = A.step_adj(us[k], eta, ub)
+        etab += e
+    assert rel(s0, ub) <= 1e-11 and rel(eb, etab) <= 1e-11
+    assert rel(p.sol, us[-1]) <= 1e-12
+
+
+def _fd_check(n, ns, every, ndir, seed, richardson=False):
+    kw, q0, eta = slqg_case(n, "ETDRK4", U=0.0, beta=0.0, ell=0.35)
+    _, loss, dq0, deta = gpu_grad(kw, q0, ns, every)
+    rng = np.random.default_rng(seed)
+
+    def L(q, e):
+        k2 = dict(kw)
+        k2["eta"] = e
+        p = SL.Problem("GPU", **k2)
+        SL.set_q(p, q)
+        stepforward(p, ns)
+        return SL.kinetic_energy(p)
+
+    def D(eps, dq, de):
+        return (L(q0 + eps * dq, eta + eps * de) - L(q0 - eps * dq, eta - eps * de)) / (2 * eps)
+
+    eps = 1e-6
+    g = O.Grid(n)
+    for i in range(ndir):
+        if richardson:   # band-limited directions: random Fourier modes |k| <= 8
+            dq = AD.random_topography(g, 8, 1.0, seed + 2 * i)
+            de = AD.random_topography(g, 8, 0.1, seed + 2 * i + 1)
+        else:
+            dq, de = rng.standard_normal(q0.shape), 0.1 * rng.standard_normal(eta.shape)
+        ad = float(np.sum(dq0 * dq) + np.sum(deta * de))
+        d1 = D(eps, dq, de)
+        if richardson:
+            # over 500 steps the flow is nonlinear enough that the O(eps^2) truncation of a
+            # plain central difference reaches ~1e-6 relative (up to 5e-5 along grid-scale
+            # white-noise directions; the FP64 oracle's exact adjoint shows the same); the
+            # eps^2 term is removed with a second difference at 2 eps
+            assert abs(d1 - ad) <= 5e-5 * abs(ad), (d1, ad)
+            fd = (4 * d1 - D(2 * eps, dq, de)) / 3
+        else:
+            fd = d1
+        assert abs(fd - ad) <= 1e-6 * abs(ad), (fd, ad)
+
+
+def test_central_differences_small():
+    _fd_check(64, 20, 5, 4, 1)
+
+
+def test_config3_central_differences_8_directions():
+    """SingleLayerQG 256^2, deformation radius 0.35, topography |k| <= 8 amplitude 0.1,
+    ETDRK4 dt = 0.01, 500 steps, checkpoint every 25, loss = final kinetic energy: central
+    differences (eps = 1e-6, Richardson-extrapolated with 2 eps) along 8 seeded band-limited
+    directions within 1e-6 (FP64)."""
+    _fd_check(256, 500, 25, 8, 2024, richardson=True)
+
+
+def test_config3_central_differences_100_steps():
+    """the same case over 100 steps, where the plain eps = 1e-6 central difference is
+    already within 1e-6"""
+    _fd_check(256, 100, 25, 8, 7)

@@ -1,0 +1,66 @@
+"""peakedisotropicspectrum (src/utils.jl:29-54) on the device against the oracle, and the
+Filtered steppers' filter read back through prob.timestepper.filter."""
+import numpy as np
+import pytest
+
+import gf_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+gfcuda = pytest.importorskip("gfcuda")
+from gfcuda import TwoDNavierStokes as TD, peakedisotropicspectrum  # noqa: E402
+
+
+@pytest.mark.parametrize("T,prec,tol", [(np.float64, None, 1e-13), (np.float64, "DF64", 1e-12),
+                                        (np.float32, None, 2e-6)])
+def test_peakedisotropicspectrum_matches_oracle(T, prec, tol):
+    n = 128
+    p = TD.Problem("GPU", nx=n, dt=0.005, stepper="FilteredRK4", T=T, precision=prec)
+    g = O.Grid(n)
+    filt = O.makefilter(g)
+    assert np.max(np.abs(p.timestepper.filter - filt)) <= 1e-14
+    z = peakedisotropicspectrum(p.grid, 6, 0.5, mask=p.timestepper.filter, seed=1234)
+    zr = O.peakedisotropicspectrum(g, 6, 0.5, mask=filt, seed=1234)
+    assert z.shape == (n, n) and z.dtype == T
+    assert O.rel_l2(z, zr) <= tol
+    # set_zeta! with it gives the requested energy (normalised over the half spectrum, :50)
+    zo = peakedisotropicspectrum(p.grid, 3, 2.0, allones=True)
+    assert O.rel_l2(zo, O.peakedisotropicspectrum(g, 3, 2.0, allones=True)) <= tol
+
+
+def test_peakedisotropicspectrum_rectangle_and_batch():
+    n, B = 64, 3
+    p = TD.Problem("GPU", nx=n, batch=B)
+    z = peakedisotropicspectrum(p.grid, 4, 0.5, seed=77)
+    assert z.shape == (B, n, n)
+    for i in range(B):
+        assert O.rel_l2(z[i], O.peakedisotropicspectrum(O.Grid(n), 4, 0.5, seed=77 + i)) <= 1e-13
+    q = TD.Problem("GPU", nx=n, ny=2 * n, Ly=4 * np.pi)
+    with pytest.raises(ValueError, match="not square"):   # src/utils.jl:30 raises too
+        peakedisotropicspectrum(q.grid, 4, 0.5)
+    r = TD.Problem("GPU", nx=n, stepper="RK4")
+    with pytest.raises(AttributeError):
+        r.timestepper.filter
+
+
+def test_streamed_diagnostics_match_per_step_values():
+    """stepforward!(prob, diags, n): the diagnostics reduced on the device after every step
+    into a ring buffer equal the values read one step at a time, and follow the oracle."""
+    n, ns = 128, 25
+    z0 = O.peakedisotropicspectrum(O.Grid(n), 6, 0.5, seed=3)
+    kw = dict(nx=n, dt=0.005, nu=1e-3, nnu=1, stepper="FilteredRK4")
+    p = TD.Problem("GPU", **kw)
+    TD.set_zeta(p, z0)
+    E, Z = gfcuda.Diagnostic(TD.energy, p), gfcuda.Diagnostic(TD.enstrophy, p)
+    gfcuda.stepforward(p, [E, Z], ns)
+    q = TD.Problem("GPU", **kw)
+    TD.set_zeta(q, z0)
+    r = O.TwoDNavierStokes(nx=n, dt=0.005, nu=1e-3, nnu=1, stepper="FilteredRK4")
+    r.set_zeta(z0)
+    for k in range(1, ns + 1):
+        gfcuda.stepforward(q, 1)
+        r.stepforward(1)
+        assert E[k] == TD.energy(q) and Z[k] == TD.enstrophy(q)
+        assert abs(E[k] - r.energy()) <= 1e-12 * r.energy()
+    assert E.steps[-1] == ns and E.t[-1] == q.clock.t == p.clock.t
+    assert np.array_equal(p.sol, q.sol)

@@ -1,0 +1,65 @@
+"""The oracle's tangent-linear and adjoint SingleLayerQG ETDRK4 step (oracle/gf_adjoint.py):
+its forward pass is the oracle's stepforward!, its gradients of the final kinetic energy with
+respect to q0 and the topography match central finite differences (eps = 1e-6) along seeded
+directions, and adjoint and tangent-linear satisfy the dot-product identity."""
+import numpy as np
+import pytest
+
+import gf_adjoint as AD
+import gf_oracle as O
+
+
+def setup(n, stepper, ell=0.35, U=0.0, beta=0.0, nsteps=12):
+    g = O.Grid(n)
+    eta = AD.random_topography(g, 8, 0.1, 7)
+    kw = dict(nx=n, deformation_radius=ell, eta=eta, dt=0.01, stepper=stepper, U=U, beta=beta)
+    p = O.SingleLayerQG(**kw)
+    q0 = O.peakedisotropicspectrum(g, 6, 0.5, seed=1234)
+    return p, AD.SLQGAdjoint(p), q0, eta, kw
+
+
+@pytest.mark.parametrize("stepper,ell,U,beta", [("ETDRK4", 0.35, 0.0, 0.0), ("ETDRK4", np.inf, 0.3, 2.0),
+                                                ("FilteredETDRK4", 0.35, 0.1, 1.0)])
+def test_adjoint_forward_is_stepforward(stepper, ell, U, beta):
+    p, A, q0, eta, kw = setup(32, stepper, ell, U, beta)
+    p.set_q(q0)
+    p.stepforward(12)
+    assert A.loss(q0, eta, 12) == pytest.approx(p.kinetic_energy(), rel=1e-14)
+
+
+@pytest.mark.parametrize("stepper,ell,U,beta", [("ETDRK4", 0.35, 0.0, 0.0), ("ETDRK4", np.inf, 0.3, 2.0),
+                                                ("FilteredETDRK4", 0.35, 0.1, 1.0)])
+def test_gradient_matches_central_differences(stepper, ell, U, beta):
+    """config 3's check in miniature: 8 seeded directions, eps = 1e-6, 1e-6 relative"""
+    p, A, q0, eta, kw = setup(32, stepper, ell, U, beta)
+    ns = 12
+    _, gq, ge = A.gradient(q0, eta, ns)
+    rng = np.random.default_rng(8)
+    for _ in range(8):
+        dq, de = rng.standard_normal(q0.shape), 0.1 * rng.standard_normal(eta.shape)
+        eps = 1e-6
+        fd = (A.loss(q0 + eps * dq, eta + eps * de, ns) - A.loss(q0 - eps * dq, eta - eps * de, ns)) / (2 * eps)
+        ad = np.sum(gq * dq) + np.sum(ge * de)
+        assert abs(fd - ad) <= 1e-6 * abs(ad)
+
+
+def test_dot_product_identity():
+    p, A, q0, eta, kw = setup(32, "ETDRK4", 0.35, 0.2, 1.0)
+    ns = 6
+    rng = np.random.default_rng(3)
+    u = A.initial_state(q0)
+    for _ in range(ns):
+        u = A.step(u, eta)[0]
+    du = A.initial_state(rng.standard_normal(q0.shape))
+    de = rng.standard_normal(eta.shape)
+    ubar = np.fft.rfft2(rng.standard_normal(q0.shape))
+    lhs = np.sum(np.real(np.conj(ubar) * A.step_tlm(u, eta, du, de)))
+    xb, eb = A.step_adj(u, eta, ubar)
+    rhs = np.sum(np.real(np.conj(xb) * du)) + np.sum(eb * de)
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+    # the transforms' transposes
+    x = rng.standard_normal((16, 16))
+    X = np.fft.rfft2(rng.standard_normal((16, 16))) + 0.3j * rng.standard_normal((16, 9))
+    g = O.Grid(16)
+    assert np.sum(np.real(np.conj(X) * O.rfft2(x))) == pytest.approx(np.sum(x * AD.rfft2_T(X, g)), rel=1e-12)
+    assert np.sum(np.real(np.conj(X) * AD.irfft2_T(x, g))) == pytest.approx(np.sum(x * O.irfft2(X, g)), rel=1e-12)
