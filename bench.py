@@ -562,7 +562,8 @@ SINGLE = {"twodns2048_fp32": (HEADLINE, np.float32, None), "twodns2048_fp64": (H
           "twodns2048_df64": (HEADLINE, np.float64, "DF64"), "slqg512_fp32": (CONFIG1, np.float32, None),
           "slqg512_fp64": (CONFIG1, np.float64, None), "slqg512_df64": (CONFIG1, np.float64, "DF64"),
           "mlqg1024x3_fp32": (CONFIG2, np.float32, None), "mlqg1024x3_df64": (CONFIG2, np.float64, "DF64"),
-          "ensemble1536_fp32": (ENSEMBLE, np.float32, None)}
+          "ensemble1536_fp32": (ENSEMBLE, np.float32, None), "adjoint256_fp32": (CONFIG3, np.float32, None),
+          "adjoint256_fp64": (CONFIG3, np.float64, None)}
 
 
 def run_single(args):
@@ -575,6 +576,8 @@ def run_single(args):
     if w is ENSEMBLE:
         r = time_ensemble(args.steps, args.warmup, flush)
         r["pt_steps_per_s"] = r["points"] / (r["ms_per_step"] * 1e-3)
+    elif w is CONFIG3:
+        r = time_adjoint(flush, T, reps=1)
     else:
         r = time_arm(w, T, args.steps, args.warmup, flush, with_e2e=False, precision=prec)
         r.pop("sol")

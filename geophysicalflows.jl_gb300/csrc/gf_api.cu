@@ -10,6 +10,7 @@
 
 #include "gf_fft.cuh"
 #include "gf_internal.h"
+#include "gf_launch.cuh"
 #include "gf_philox.cuh"
 #include "gfcuda.h"
 
@@ -1384,6 +1385,120 @@ extern "C" int gf_step_diags(gf_ctx* c, int64_t nsteps, const int32_t* which, in
   }
   cudaFreeAsync(ring, c->stream);
   return rc;
+}
+
+// ------------------------------------------------------------------------------ autotune
+// Launch-shape autotuner: times the step kernels of this context at every candidate shape
+// -- column kernel: FFT radix (FP32: 4, 8, 16; FP64/df64: 8) x columns per block C; row
+// kernel: radix x row pairs per block B (threads per row = length / radix) -- with CUDA
+// events around each launch, and keeps the fastest.  The state, clock, AB3 history and
+// stochastic-forcing record are restored afterwards; captured graphs are dropped (they
+// are re-captured with the new shapes).  The profiling counters are reset.
+static int set_shape(gf_ctx* c, int Rr, int B, int Rc, int C) {
+  c->g.tuneRr = Rr; c->g.tuneB = B; c->g.tuneRc = Rc; c->g.tuneC = C;
+  drop_graphs(c);
+  return GF_OK;
+}
+
+extern "C" int gf_set_launch_shape(gf_ctx* c, const int32_t* shape) {
+  if (!c || !shape) return GF_ERR_ARG;
+  for (int k = 0; k < 4; ++k) if (shape[k] < 0) return fail(c, GF_ERR_ARG, "launch shape entries must be >= 0");
+  const bool f32 = c->prec == GF_F32;
+  for (int k : {0, 2}) {
+    const int R = shape[k], N = k == 0 ? c->g.nx : c->g.ny;
+    if (R != 0 && R != 8 && !(f32 && f32_radix_built(N, R))) return fail(c, GF_ERR_ARG, "radix not built for this size");
+  }
+  return set_shape(c, shape[0], shape[1], shape[2], shape[3]);
+}
+
+extern "C" int gf_get_launch_shape(const gf_ctx* c, int32_t* shape) {
+  if (!c || !shape) return GF_ERR_ARG;
+  shape[0] = c->g.tuneRr; shape[1] = c->g.tuneB; shape[2] = c->g.tuneRc; shape[3] = c->g.tuneC;
+  return GF_OK;
+}
+
+extern "C" int gf_autotune(gf_ctx* c, int32_t reps, int32_t* shape) {
+  if (!c) return GF_ERR_ARG;
+  if (c->cfg.forcing_kind >= GF_FORCING_STOCHASTIC && !c->fspec) return fail(c, GF_ERR_STATE, "no forcing spectrum");
+  if (reps <= 0) reps = 4;
+  const Geom g0 = c->g;
+  const size_t spec = g0.bs_spec * g0.nb * c->cb;
+  // snapshot of what a step changes
+  std::vector<std::pair<void*, void*>> saved;  // (buffer, copy)
+  auto keep = [&](void* p) -> int {
+    if (!p) return GF_OK;
+    void* q = nullptr;
+    GF_CUDA(c, cudaMallocAsync(&q, spec, c->stream));
+    GF_CUDA(c, cudaMemcpyAsync(q, p, spec, cudaMemcpyDeviceToDevice, c->stream));
+    saved.push_back({p, q});
+    return GF_OK;
+  };
+  int rc = keep(c->sol);
+  if (c->kind == SK_AB3) for (int i = 0; i < 3 && rc == GF_OK; ++i) rc = keep(c->R3[i]);
+  if (c->cfg.forcing_kind >= GF_FORCING_STOCHASTIC && rc == GF_OK) { rc = keep(c->Fh); if (rc == GF_OK) rc = keep(c->prevsol); }
+  const double t0 = c->t, fs0 = c->last_fscale;
+  const int64_t s0 = c->step;
+  const int a0 = c->ab3_out, a1 = c->ab3_m1, a2 = c->ab3_m2;
+  const bool prof0 = c->profiling;
+  auto restore = [&]() {
+    for (auto& pq : saved) cudaMemcpyAsync(pq.first, pq.second, spec, cudaMemcpyDeviceToDevice, c->stream);
+    c->t = t0; c->step = s0; c->last_fscale = fs0;
+    c->ab3_out = a0; c->ab3_m1 = a1; c->ab3_m2 = a2;
+    c->W_valid = false;
+  };
+  // average time of the row (which = 0) or column (1) kernel at the current shape
+  auto measure = [&](int which, double* ms) -> int {
+    restore();
+    if (int r = upload_clock(c)) return r;
+    c->profiling = true;
+    if (int r = one_step(c)) return r;  // warm-up (and kernel attributes)
+    double m2[2]; int64_t n2[2];
+    if (int r = gf_profile_read(c, m2, n2, nullptr)) return r;
+    for (int k = 0; k < reps; ++k)
+      if (int r = one_step(c)) return r;
+    if (int r = gf_profile_read(c, m2, n2, nullptr)) return r;
+    c->profiling = prof0;
+    *ms = m2[which] / std::max<int64_t>(n2[which], 1);
+    return GF_OK;
+  };
+  const bool f32 = c->prec == GF_F32;
+  const int radii[3] = {8, 16, 4};
+  const int unit = 128 / (int)c->cb;  // elements per 128-byte wavefront
+  int bestRc = 0, bestC = 0, bestRr = 0, bestB = 0;
+  double best = 1e30;
+  for (int ri = 0; ri < (f32 ? 3 : 1) && rc == GF_OK; ++ri) {
+    const int R = radii[ri], TPF = g0.ny / R;
+    if (!f32_radix_built(g0.ny, R) || TPF < 1) continue;
+    for (int C = 1; C <= 16 && rc == GF_OK; C *= 2) {
+      const int cs = C > 1 ? g0.ny + std::max(unit / C, 1) : g0.ny;
+      const size_t sm = ((size_t)2 * C * cs + (size_t)g0.nl * g0.ny * C * (g0.nl > 1 ? 2 : 1)) * c->cb;
+      if (C * TPF > 512 || sm > (size_t)SMEM_CAP) continue;
+      set_shape(c, 0, 0, R, C);
+      double ms = 0;
+      rc = measure(1, &ms);
+      if (rc == GF_OK && ms < best) { best = ms; bestRc = R; bestC = C; }
+    }
+  }
+  best = 1e30;
+  for (int ri = 0; ri < (f32 ? 3 : 1) && rc == GF_OK; ++ri) {
+    const int R = radii[ri], TPF = g0.nx / R;
+    if (!f32_radix_built(g0.nx, R) || TPF < 1 || TPF > 256) continue;
+    for (int B = 1; B * TPF <= 256 && rc == GF_OK; B *= 2) {
+      if (!row_shape_ok(g0.nx, R, c->cb, 3, g0.ny / 2, B)) continue;
+      set_shape(c, R, B, bestRc, bestC);
+      double ms = 0;
+      rc = measure(0, &ms);
+      if (rc == GF_OK && ms < best) { best = ms; bestRr = R; bestB = B; }
+    }
+  }
+  c->profiling = prof0;
+  restore();
+  for (auto& pq : saved) cudaFreeAsync(pq.second, c->stream);
+  if (rc != GF_OK) { set_shape(c, g0.tuneRr, g0.tuneB, g0.tuneRc, g0.tuneC); upload_clock(c); return rc; }
+  set_shape(c, bestRr, bestB, bestRc, bestC);
+  if (int r = upload_clock(c)) return r;
+  if (shape) { shape[0] = bestRr; shape[1] = bestB; shape[2] = bestRc; shape[3] = bestC; }
+  return GF_OK;
 }
 
 // ------------------------------------------------------------------------------- adjoint

@@ -3,18 +3,33 @@
 #include "gf_kernels.cuh"
 #include "gf_launch.cuh"
 
+#include <type_traits>
+
 namespace gf {
+
+// FP32: the autotuner's radix (4, 8 or 16) when one was chosen; otherwise RADIX<T>
+#define GF_ROW_CASE(N)                                                                      \
+  case N:                                                                                   \
+    if constexpr (std::is_same<T, float>::value) {                                          \
+      if (g.tuneRr == 16) return launch_row_nr<float, N, 16>(g, m, b, st);                  \
+      if constexpr (N <= 1024)                                                              \
+        if (g.tuneRr == 4) return launch_row_nr<float, N, 4>(g, m, b, st);                  \
+    }                                                                                       \
+    return launch_row_n<T, N>(g, m, b, st);
+#define GF_COL_CASE(N)                                                                      \
+  case N:                                                                                   \
+    if constexpr (std::is_same<T, float>::value) {                                          \
+      if (g.tuneRc == 16) return launch_col_nr<float, N, 16>(g, m, s, b, st);               \
+      if constexpr (N <= 1024)                                                              \
+        if (g.tuneRc == 4) return launch_col_nr<float, N, 4>(g, m, s, b, st);               \
+    }                                                                                       \
+    return launch_col_n<T, N>(g, m, s, b, st);
 
 template <class T>
 cudaError_t launch_row(const Geom& g, const ModArgs& m, const Bufs& b, cudaStream_t st) {
   switch (g.nx) {
-    case 32: return launch_row_n<T, 32>(g, m, b, st);
-    case 64: return launch_row_n<T, 64>(g, m, b, st);
-    case 128: return launch_row_n<T, 128>(g, m, b, st);
-    case 256: return launch_row_n<T, 256>(g, m, b, st);
-    case 512: return launch_row_n<T, 512>(g, m, b, st);
-    case 1024: return launch_row_n<T, 1024>(g, m, b, st);
-    case 2048: return launch_row_n<T, 2048>(g, m, b, st);
+    GF_ROW_CASE(32) GF_ROW_CASE(64) GF_ROW_CASE(128) GF_ROW_CASE(256) GF_ROW_CASE(512) GF_ROW_CASE(1024)
+    GF_ROW_CASE(2048)
     default: return cudaErrorInvalidValue;
   }
 }
@@ -22,13 +37,8 @@ cudaError_t launch_row(const Geom& g, const ModArgs& m, const Bufs& b, cudaStrea
 template <class T>
 cudaError_t launch_col(const Geom& g, const ModArgs& m, const StepArgs& s, const Bufs& b, cudaStream_t st) {
   switch (g.ny) {
-    case 32: return launch_col_n<T, 32>(g, m, s, b, st);
-    case 64: return launch_col_n<T, 64>(g, m, s, b, st);
-    case 128: return launch_col_n<T, 128>(g, m, s, b, st);
-    case 256: return launch_col_n<T, 256>(g, m, s, b, st);
-    case 512: return launch_col_n<T, 512>(g, m, s, b, st);
-    case 1024: return launch_col_n<T, 1024>(g, m, s, b, st);
-    case 2048: return launch_col_n<T, 2048>(g, m, s, b, st);
+    GF_COL_CASE(32) GF_COL_CASE(64) GF_COL_CASE(128) GF_COL_CASE(256) GF_COL_CASE(512) GF_COL_CASE(1024)
+    GF_COL_CASE(2048)
     default: return cudaErrorInvalidValue;
   }
 }

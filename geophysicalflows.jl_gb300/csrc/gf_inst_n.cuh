@@ -5,32 +5,45 @@
 
 namespace gf {
 
-template <class T, int NN>
-cudaError_t launch_row_n(const Geom& g, const ModArgs& m, const Bufs& b, cudaStream_t st) {
-
+// Row kernel with FFT radix R; B row pairs per block from the autotuner when it fits.
+template <class T, int NN, int R>
+cudaError_t launch_row_nr(const Geom& g, const ModArgs& m, const Bufs& b, cudaStream_t st) {
   cudaError_t err = cudaSuccess;
   const size_t e = sizeof(cplx<T>);
-  const int B = pick_B(NN, RADIX<T>, e, 3, g.ny / 2, g.nb);
-  const size_t sm = (size_t)B * 3 * row_stride<T>(NN, NN / RADIX<T>) * e;
-  auto k = row_nl_kernel<T, NN, RADIX<T>>;
+  int B = pick_B(NN, R, e, 3, g.ny / 2, g.nb);
+  if (g.tuneB > 0 && row_shape_ok(NN, R, e, 3, g.ny / 2, g.tuneB)) B = g.tuneB;
+  const size_t sm = (size_t)B * 3 * row_stride<T>(NN, NN / R) * e;
+  auto k = row_nl_kernel<T, NN, R>;
   if ((err = set_smem(k, sm)) != cudaSuccess) return err;
-  k<<<dim3(g.ny / 2 / B, g.nb), B * (NN / RADIX<T>), sm, st>>>(g, m, b, B);
+  k<<<dim3(g.ny / 2 / B, g.nb), B * (NN / R), sm, st>>>(g, m, b, B);
+  return cudaGetLastError();
+}
+
+// Column kernel with FFT radix R; C columns per block from the autotuner when it fits.
+template <class T, int NN, int R>
+cudaError_t launch_col_nr(const Geom& g, const ModArgs& m, const StepArgs& s, const Bufs& b, cudaStream_t st) {
+  cudaError_t err = cudaSuccess;
+  const size_t e = sizeof(cplx<T>);
+  auto smem = [&](int c) { return col_stage_smem(NN, c, col_stride<T>(NN, c), g.nl, e); };
+  int C = pick_C(NN, R, g.nkr, smem, g.nb);
+  if (g.tuneC > 0 && g.tuneC * (NN / R) <= 512 && smem(g.tuneC) <= (size_t)SMEM_CAP) C = g.tuneC;
+  Geom g2 = g;
+  g2.cs = col_stride<T>(NN, C);
+  const size_t sm = smem(C);
+  auto k = col_stage_kernel<T, NN, R>;
+  if ((err = set_smem(k, sm)) != cudaSuccess) return err;
+  k<<<dim3((g.nkr + C - 1) / C, g.nb), C * (NN / R), sm, st>>>(g2, m, s, b, C);
   return cudaGetLastError();
 }
 
 template <class T, int NN>
-cudaError_t launch_col_n(const Geom& g, const ModArgs& m, const StepArgs& s, const Bufs& b, cudaStream_t st) {
+cudaError_t launch_row_n(const Geom& g, const ModArgs& m, const Bufs& b, cudaStream_t st) {
+  return launch_row_nr<T, NN, RADIX<T>>(g, m, b, st);
+}
 
-  cudaError_t err = cudaSuccess;
-  const size_t e = sizeof(cplx<T>);
-  const int C = pick_C(NN, RADIX<T>, g.nkr, [&](int c) { return col_stage_smem(NN, c, col_stride<T>(NN, c), g.nl, e); }, g.nb);
-  Geom g2 = g;
-  g2.cs = col_stride<T>(NN, C);
-  const size_t sm = col_stage_smem(NN, C, g2.cs, g.nl, e);
-  auto k = col_stage_kernel<T, NN, RADIX<T>>;
-  if ((err = set_smem(k, sm)) != cudaSuccess) return err;
-  k<<<dim3((g.nkr + C - 1) / C, g.nb), C * (NN / RADIX<T>), sm, st>>>(g2, m, s, b, C);
-  return cudaGetLastError();
+template <class T, int NN>
+cudaError_t launch_col_n(const Geom& g, const ModArgs& m, const StepArgs& s, const Bufs& b, cudaStream_t st) {
+  return launch_col_nr<T, NN, RADIX<T>>(g, m, s, b, st);
 }
 
 template <class T, int NN>
@@ -115,6 +128,12 @@ cudaError_t launch_adj_col_n(const Geom& g, const ModArgs& m, const AdjArgs& a, 
   k<<<(g.nkr + C - 1) / C, C * (NN / RADIX<T>), sm, st>>>(g2, m, a, b, C);
   return cudaGetLastError();
 }
+
+// the step kernels at another FFT radix (autotuner candidates)
+#define GF_INST_NR(T, NN, R)                                                                                   \
+  template cudaError_t launch_row_nr<T, NN, R>(const Geom&, const ModArgs&, const Bufs&, cudaStream_t);         \
+  template cudaError_t launch_col_nr<T, NN, R>(const Geom&, const ModArgs&, const StepArgs&, const Bufs&,       \
+                                               cudaStream_t);
 
 #define GF_INST_N(T, NN)                                                                                       \
   template cudaError_t launch_row_n<T, NN>(const Geom&, const ModArgs&, const Bufs&, cudaStream_t);             \

@@ -31,6 +31,9 @@ struct Geom {
   // on its own slice; strides (elements) of the per-instance arrays
   int nb;
   size_t bs_spec, bs_w, bs_p, bs_d, bs_phys;
+  // launch shape chosen by gf_autotune (0: the block-shape heuristic): column-kernel columns
+  // per block and FFT radix, row-kernel row pairs per block and FFT radix
+  int tuneC, tuneRc, tuneB, tuneRr;
 };
 
 // Device-resident clock, advanced on the GPU after every step so that a captured graph of

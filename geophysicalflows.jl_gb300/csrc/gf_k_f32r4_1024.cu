@@ -1,0 +1,6 @@
+// FFT-length-1024 FP32 step kernels at radix 4 (autotuner candidates).
+#include "gf_inst_n.cuh"
+
+namespace gf {
+GF_INST_NR(float, 1024, 4)
+}  // namespace gf

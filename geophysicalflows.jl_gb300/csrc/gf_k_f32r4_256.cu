@@ -1,0 +1,6 @@
+// FFT-length-256 FP32 step kernels at radix 4 (autotuner candidates).
+#include "gf_inst_n.cuh"
+
+namespace gf {
+GF_INST_NR(float, 256, 4)
+}  // namespace gf

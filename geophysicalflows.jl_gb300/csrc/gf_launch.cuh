@@ -42,6 +42,12 @@ inline int pick_B(int NX, int R, size_t elem, int nbufs, int npairs, int nb = 1)
   return B;
 }
 
+// Whether B row pairs per block fit the row kernel (threads, shared memory, pair count).
+inline bool row_shape_ok(int NX, int R, size_t elem, int nbufs, int npairs, int B) {
+  const int TPF = NX / R;
+  return B >= 1 && B * TPF <= 256 && (size_t)B * (NX + NX / R) * elem * nbufs <= SMEM_CAP && npairs % B == 0;
+}
+
 // Column stride of the column kernels' work buffers: NY slots, staggered so that the C
 // columns a wavefront touches in the element mapping fall into disjoint banks.
 template <class T>
@@ -70,6 +76,11 @@ constexpr int RADIX = sizeof(T) == 4 ? GF_RADIX_F32 : 8;
 
 // per-size launchers (NN = FFT length along the transformed direction)
 template <class T, int NN> cudaError_t launch_row_n(const Geom&, const ModArgs&, const Bufs&, cudaStream_t);
+template <class T, int NN, int R> cudaError_t launch_row_nr(const Geom&, const ModArgs&, const Bufs&, cudaStream_t);
+template <class T, int NN, int R>
+cudaError_t launch_col_nr(const Geom&, const ModArgs&, const StepArgs&, const Bufs&, cudaStream_t);
+// FFT radices of the FP32 step kernels that the autotuner may pick, per length
+constexpr bool f32_radix_built(int N, int R) { return R == 8 || (R == 16) || (R == 4 && N <= 1024); }
 template <class T, int NN> cudaError_t launch_col_n(const Geom&, const ModArgs&, const StepArgs&, const Bufs&, cudaStream_t);
 template <class T, int NN> cudaError_t launch_col_inv_n(const Geom&, const ModArgs&, const void*, int, int, const Bufs&,
                                                         cudaStream_t);

@@ -22,7 +22,7 @@ EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_abi_version", "gf_get
            "gf_diagnostics", "gf_set_forcing", "gf_synchronize", "gf_profile_enable", "gf_profile_read",
            "gf_rfft2_noalloc", "gf_get_batch", "gf_set_graph_steps", "gf_ensemble_step",
            "gf_peakedisotropicspectrum", "gf_get_filter", "gf_adjoint_setup", "gf_adjoint_forward",
-           "gf_adjoint_backward", "gf_grad"]
+           "gf_adjoint_backward", "gf_grad", "gf_autotune", "gf_set_launch_shape", "gf_get_launch_shape"]
 
 
 class gf_config(C.Structure):
@@ -91,6 +91,9 @@ def load(path=None):
         "gf_adjoint_forward": ([vp], C.c_int),
         "gf_adjoint_backward": ([vp, vp, vp, vp, C.c_int], C.c_int),
         "gf_grad": ([vp, C.c_int, vp, vp, C.POINTER(dbl), C.c_int], C.c_int),
+        "gf_autotune": ([vp, i32, C.POINTER(i32)], C.c_int),
+        "gf_set_launch_shape": ([vp, C.POINTER(i32)], C.c_int),
+        "gf_get_launch_shape": ([vp, C.POINTER(i32)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

@@ -198,6 +198,24 @@ class Problem:
     def set_clock(self, t, step):
         self._c(self._lib.gf_set_clock(self._ctx, float(t), int(step)))
 
+    def autotune(self, reps=4):
+        """Time the step kernels at every candidate launch shape and keep the fastest;
+        returns {row_radix, row_pairs, col_radix, col_columns}."""
+        sh = (C.c_int32 * 4)()
+        self._c(self._lib.gf_autotune(self._ctx, int(reps), sh))
+        return dict(zip(("row_radix", "row_pairs", "col_radix", "col_columns"), list(sh)))
+
+    @property
+    def launch_shape(self):
+        sh = (C.c_int32 * 4)()
+        self._c(self._lib.gf_get_launch_shape(self._ctx, sh))
+        return tuple(sh)
+
+    @launch_shape.setter
+    def launch_shape(self, shape):
+        sh = (C.c_int32 * 4)(*[int(v) for v in shape])
+        self._c(self._lib.gf_set_launch_shape(self._ctx, sh))
+
     def set_graph_steps(self, n):
         """Steps per captured CUDA graph (0: launch kernel by kernel)."""
         self._c(self._lib.gf_set_graph_steps(self._ctx, int(n)))

@@ -224,6 +224,19 @@ int gf_set_forcing(gf_ctx* ctx, const void* data, int where);
 /* Block until the context's stream has finished. */
 int gf_synchronize(gf_ctx* ctx);
 
+/* ---- launch-shape autotuner (no reference counterpart) ----------------------------------
+ * gf_autotune times the step kernels of this context at every candidate launch shape --
+ * column kernel: FFT radix (FP32: 4, 8, 16; otherwise 8) x kr columns per block; row kernel:
+ * radix x row pairs per block (threads per row = length / radix) -- over `reps` steps each
+ * (<= 0: 4) and keeps the fastest.  The state, clock, AB3 history and stochastic-forcing
+ * record are restored; captured graphs are re-captured; the profiling counters are reset.
+ * shape (may be NULL) receives {row radix, row pairs per block, column radix, columns per
+ * block}; 0 entries mean the built-in block-shape rule.  gf_set_launch_shape applies a
+ * shape found earlier (e.g. for another context of the same size). */
+int gf_autotune(gf_ctx* ctx, int32_t reps, int32_t* shape);
+int gf_set_launch_shape(gf_ctx* ctx, const int32_t* shape);
+int gf_get_launch_shape(const gf_ctx* ctx, int32_t* shape);
+
 /* ---- adjoint ----------------------------------------------------------------------------
  * Reverse-mode derivative of stepforward!(prob, nsteps), the counterpart of a
  * ChainRulesCore.rrule on stepforward! (the reference has no derivative; its step is

@@ -112,3 +112,34 @@ def test_batched_slqg_etdrk4_parity():
         r = O.SingleLayerQG(forcing=O.Forcing("stochastic", spectrum=spec, seed=21 + i), **kw)
         r.stepforward(6)
         assert rel(p.sol[i], r.sol) <= 1e-12
+
+
+@pytest.mark.parametrize("T", [np.float32, np.float64])
+@pytest.mark.parametrize("stepper", ["FilteredRK4", "AB3"])
+def test_autotune_keeps_state_and_results(T, stepper):
+    """the autotuner restores state, clock and AB3 history, and every launch shape gives the
+    same step up to rounding (FP32: radices 4, 8, 16 reorder the butterflies)"""
+    n = 128
+    spec = O.ring_forcing_spectrum(O.Grid(n), 8.0, 1.5, 1e-3)
+    kw = dict(nx=n, dt=0.01, nu=1e-4, nnu=1, stepper=stepper, T=T)
+    mk = lambda: TD.Problem("GPU", forcing=Forcing("stochastic", spectrum=spec, seed=3), **kw)
+    p, q = mk(), mk()
+    for r in (p, q):
+        TD.set_zeta(r, zeta0(n, 2))
+        stepforward(r, 5)
+    sol0 = p.sol
+    shape = p.autotune(reps=2)
+    assert np.array_equal(p.sol, sol0) and p.clock.step == 5
+    assert shape["col_radix"] in ((4, 8, 16) if T == np.float32 else (8,))
+    assert p.launch_shape == tuple(shape.values())
+    stepforward(p, 6)
+    stepforward(q, 6)
+    assert rel(p.sol, q.sol) <= (1e-5 if T == np.float32 else 1e-13)
+    for sh in ((16, 1, 16, 1), (4, 2, 4, 4), (8, 4, 8, 2)) if T == np.float32 else ((8, 2, 8, 4),):
+        r = mk()
+        r.launch_shape = sh
+        TD.set_zeta(r, zeta0(n, 2))
+        stepforward(r, 11)
+        assert rel(r.sol, q.sol) <= (1e-5 if T == np.float32 else 1e-13)
+    with pytest.raises(ValueError):
+        p.launch_shape = (3, 1, 8, 1)
