@@ -192,7 +192,7 @@ def _events(n):
     return [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
 
 
-def time_arm(w, T, steps, warmup, flush, with_e2e, precision=None, graph=True):
+def time_arm(w, T, steps, warmup, flush, with_e2e, precision=None, graph=True, tune=True):
     """Run one precision arm: warm-up, K timed steps launched one gf_step at a time (CUDA
     events on the legacy default stream, which orders with the library's blocking stream;
     L2 flushed between steps) with the library's per-kernel event timing on, then K steps
@@ -203,6 +203,7 @@ def time_arm(w, T, steps, warmup, flush, with_e2e, precision=None, graph=True):
     import gfcuda
     prob = make_problem(w, T, precision)
     set_initial_state(prob, w)
+    shape = prob.autotune(reps=3) if tune else None  # the library's launch-shape autotuner
     gfcuda.stepforward(prob, warmup)
     prob.synchronize()
     lib, ctx = prob._lib, prob._ctx
@@ -222,7 +223,7 @@ def time_arm(w, T, steps, warmup, flush, with_e2e, precision=None, graph=True):
     prob._c(lib.gf_profile_read(ctx, ms2, n2, C.byref(nl)))
     lib.gf_profile_enable(ctx, 0)
     res = {"ms_per_step": sum(ms) / steps, "ms_row": ms2[0] / max(n2[0], 1), "ms_col": ms2[1] / max(n2[1], 1),
-           "n_row": n2[0], "n_col": n2[1], "launches": nl.value}
+           "n_row": n2[0], "n_col": n2[1], "launches": nl.value, "launch_shape": shape}
     if graph:
         gfcuda.stepforward(prob, 4)  # captures the graph outside the timed region
         (e0, e1), = _events(1)
@@ -287,6 +288,7 @@ def time_ensemble(steps, warmup, flush):
         probs.append(gfcuda.TwoDNavierStokes.Problem(
             "GPU", nx=n, dt=e["dt"], nu=e["nu"], nnu=e["nnu"], stepper=e["stepper"], T=np.float32, batch=B,
             forcing=gfcuda.Forcing("stochastic", spectrum=spec, seed=1000 * n)))
+    shapes = [p.autotune(reps=3) for p in probs]  # FFT radix and tiles per size class
     gfcuda.ensemble_step(probs, warmup)
     torch.cuda.synchronize()
     ev = _events(steps)
@@ -309,7 +311,8 @@ def time_ensemble(steps, warmup, flush):
     for p in probs:
         p.close()
     pts = sum(n * n * B for n, B in e["classes"])
-    return {"ms_per_step": ms, "ms_per_step_graph": ms_graph, "points": pts, "mean_energy": E}
+    return {"ms_per_step": ms, "ms_per_step_graph": ms_graph, "points": pts, "mean_energy": E,
+            "launch_shapes": shapes}
 
 
 def cpu_baseline(w, seconds=20.0, max_steps=5):
@@ -379,6 +382,8 @@ def time_adjoint(flush, T=np.float32, precision=None, reps=2):
     p = gfcuda.SingleLayerQG.Problem("GPU", nx=w["nx"], deformation_radius=w["ell"], eta=eta, dt=w["dt"],
                                      stepper=w["stepper"], T=T, precision=precision)
     q0 = gfcuda.peakedisotropicspectrum(p.grid, 6, 0.5, seed=1234)
+    gfcuda.SingleLayerQG.set_q(p, q0)
+    p.autotune(reps=3)
     gfcuda.adjoint.setup(p, w["nsteps"], w["every"])
     tdt = torch.float32 if T == np.float32 else torch.float64
     dq0 = torch.empty((w["ny"], w["nx"]), dtype=tdt, device="cuda")
@@ -503,7 +508,7 @@ def run_ours(args):
         "config": {"workload": "TwoDNavierStokes 2048^2 FilteredRK4 dt=5e-4 nu=0, peaked isotropic IC (k0=6, E=0.5)",
                    "nx": w["nx"], "ny": w["ny"], "stepper": w["stepper"], "precision": "FP32 bulk",
                    "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}",
-                   "ms_per_step_graph": msg},
+                   "ms_per_step_graph": msg, "launch_shape": r32["launch_shape"]},
         "roofline": roofline(w, r32, 4, "twodns2048_fp32", peaks, peak_src),
         "cpu_baseline": cpu,
         "e2e": {"value": whole_job(pts, world, e2e_s), "unit": UNIT, "h2d_bytes_per_step": r32["state_bytes"],
@@ -546,7 +551,7 @@ def run_ours(args):
                          "points": ens["points"], "value": ens["points"] / (ens["ms_per_step"] * 1e-3),
                          "value_graph": ens["points"] / (ens["ms_per_step_graph"] * 1e-3),
                          "ms_per_step": ens["ms_per_step"], "ms_per_step_graph": ens["ms_per_step_graph"],
-                         "mean_energy_per_class": ens["mean_energy"]},
+                         "mean_energy_per_class": ens["mean_energy"], "launch_shapes": ens["launch_shapes"]},
         "adjoint_slqg256": {"workload": "gradient of the final kinetic energy w.r.t. q0 and topography: "
                                         "SingleLayerQG 256^2, deformation radius 0.35, topography |k|<=8 amp 0.1, "
                                         "ETDRK4 dt=0.01, 500 steps, checkpoint every 25",
@@ -579,7 +584,7 @@ def run_single(args):
     elif w is CONFIG3:
         r = time_adjoint(flush, T, reps=1)
     else:
-        r = time_arm(w, T, args.steps, args.warmup, flush, with_e2e=False, precision=prec)
+        r = time_arm(w, T, args.steps, args.warmup, flush, with_e2e=False, precision=prec, tune=not args.no_tune)
         r.pop("sol")
         r["pt_steps_per_s"] = points(w) / (r["ms_per_step"] * 1e-3)
     r["workload"] = args.single
@@ -594,6 +599,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--single", choices=sorted(SINGLE), help="time one arm only (profiling mode)")
+    ap.add_argument("--no-tune", action="store_true", help="single mode: built-in block shapes, no autotuner")
     args = ap.parse_args()
     if args.single:
         return run_single(args)

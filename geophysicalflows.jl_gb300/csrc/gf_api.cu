@@ -35,6 +35,7 @@ struct gf_ctx {
   double Hsum = 1, f0 = 1;
   std::vector<double> gprime, Hl;
   std::vector<double> filt_host;  // the Filtered steppers' filter, [ny][nx/2+1]
+  double* Ud = nullptr;           // MultiLayerQG U(y) per layer [nl][ny], FP64 (fluxes)
   // device buffers
   std::vector<void*> allocs;
   void *sol = nullptr, *X = nullptr, *acc = nullptr, *s1 = nullptr, *N1 = nullptr, *R3[3] = {nullptr, nullptr, nullptr};
@@ -455,6 +456,17 @@ static int build(gf_ctx* c, const gf_config* cfg) {
     if (!(c->mult = dalloc(c, tsz * rb))) return fail(c, GF_ERR_NOMEM, "mult");
     if (int r = upload_table(c, c->mult, M, 0)) return r;
     m.mult = c->mult;
+  } else if (k.module == GF_BAROTROPICQGQL) {
+    // L = -mu - nu K^(2 nnu) + i beta kr / K^2 (src/barotropicqgql.jl:168-173)
+    m.psi_kind = PSI_INVK2;
+    m.hasC = 1;
+    m.ql = 1;
+    m.nmu = 0;
+    Lim.assign(nt, 0.0);
+    for (size_t e = 1; e < nt; ++e) {
+      Lre[e] = -k.mu - k.nu * K2pow(e, k.nnu);
+      Lim[e] = k.beta * krv[e % g.nkr] / K2[e];
+    }
   } else if (k.module == GF_SINGLELAYERQG) {
     const bool barotropic = !(k.deformation_radius > 0) || std::isinf(k.deformation_radius);
     m.psi_kind = barotropic ? PSI_INVK2 : PSI_HELMHOLTZ;
@@ -528,6 +540,11 @@ static int build(gf_ctx* c, const gf_config* cfg) {
     if (!(c->U1D = dalloc(c, U.size() * rb)) || !(c->Qy1D = dalloc(c, Qy.size() * rb))) return fail(c, GF_ERR_NOMEM, "U");
     if (int r = upload_real(c, c->U1D, U.data(), U.size())) return r;
     if (int r = upload_real(c, c->Qy1D, Qy.data(), Qy.size())) return r;
+    if (k.module == GF_MULTILAYERQG) {
+      if (!(c->Ud = (double*)dalloc(c, U.size() * 8))) return fail(c, GF_ERR_NOMEM, "U");
+      GF_CUDA(c, cudaMemcpyAsync(c->Ud, U.data(), U.size() * 8, cudaMemcpyHostToDevice, c->stream));
+      GF_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
     m.U1D = c->U1D; m.Qy1D = c->Qy1D;
   }
   c->hasL = 0;
@@ -540,7 +557,7 @@ static int build(gf_ctx* c, const gf_config* cfg) {
   if (!(c->sol = dalloc(c, NB * nsp * cb)) || !(c->W = dalloc(c, NB * Wn * cb)) ||
       !(c->P = dalloc(c, NB * 3 * nsp * cb)) || !(c->D = dalloc(c, NB * tsz * cb)) ||
       !(c->tmp_spec = dalloc(c, NB * nsp * cb)) || !(c->tmp_spec2 = dalloc(c, NB * nsp * cb)) ||
-      !(c->phys = dalloc(c, NB * 4 * g.bs_phys * rb)) || !(c->dclk = (DevClock*)dalloc(c, sizeof(DevClock))))
+      !(c->phys = dalloc(c, NB * (k.module == GF_BAROTROPICQGQL ? 7 : 4) * g.bs_phys * rb)) || !(c->dclk = (DevClock*)dalloc(c, sizeof(DevClock))))
     return fail(c, GF_ERR_NOMEM, "state buffers");
   m.D = c->D;
   if (c->prec == GF_DF64 &&
@@ -703,7 +720,7 @@ extern "C" int gf_create(const gf_config* cfg, void* stream, gf_ctx** out) {
   if (!cfg || !out) return fail(nullptr, GF_ERR_ARG, "null argument");
   *out = nullptr;
   const gf_config& k = *cfg;
-  if (k.module < 0 || k.module > 3) return fail(nullptr, GF_ERR_ARG, "unknown module");
+  if (k.module < 0 || k.module > 4) return fail(nullptr, GF_ERR_ARG, "unknown module");
   if (k.precision != GF_F32 && k.precision != GF_F64 && k.precision != GF_DF64)
     return fail(nullptr, GF_ERR_ARG, "unknown precision");
   if (k.stepper < 0 || k.stepper > 7) return fail(nullptr, GF_ERR_ARG, "unknown stepper");
@@ -858,11 +875,51 @@ extern "C" int gf_synchronize(gf_ctx* c) {
   return GF_OK;
 }
 
+// BarotropicQGQL: sol[0,0] = 0, then the eddy (kr > 0) and zonal-mean (kr = 0) parts
+__global__ void ql_split_kernel(const char* sol, char* eddy, char* mean, int cb, int nkr, int ny, int ldk,
+                                size_t bs, int nb) {
+  const size_t n = (size_t)nb * ny * nkr;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const int kr = (int)(e % nkr);
+    const size_t r = e / nkr;
+    const int j = (int)(r % ny);
+    const size_t ib = r / ny;
+    const size_t off = (ib * bs + (size_t)j * ldk + kr) * cb;
+    const bool k0 = (kr == 0 && j == 0);
+    for (int b = 0; b < cb; ++b) {
+      const char v = k0 ? 0 : sol[off + b];
+      eddy[off + b] = kr == 0 ? 0 : v;
+      mean[off + b] = kr == 0 ? v : 0;
+    }
+  }
+}
+
+// sol[0, 0] = 0 of every instance
+__global__ void zero_k0_kernel(char* sol, int cb, size_t bs, int nb) {
+  const int ib = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ib >= nb) return;
+  for (int b = 0; b < cb; ++b) sol[ib * bs * cb + b] = 0;
+}
+
 extern "C" int gf_updatevars(gf_ctx* c) {
   if (!c) return GF_ERR_ARG;
   const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->g.nb * c->rb;
   GF_CUDA(c, DISPATCH(c, launch_mask_inplace, c->g, c->sol, c->stream));
   c->W_valid = false;
+  if (c->cfg.module == GF_BAROTROPICQGQL) {  // src/barotropicqgql.jl:380-407
+    const Geom& g = c->g;
+    ql_split_kernel<<<256, 256, 0, c->stream>>>((const char*)c->sol, (char*)c->tmp_spec, (char*)c->tmp_spec2,
+                                                (int)c->cb, g.nkr, g.ny, g.ldk, g.bs_spec, g.nb);
+    GF_CUDA(c, cudaGetLastError());
+    zero_k0_kernel<<<(g.nb + 255) / 256, 256, 0, c->stream>>>((char*)c->sol, (int)c->cb, g.bs_spec, g.nb);
+    GF_CUDA(c, cudaGetLastError());
+    const int kinds[4] = {SF_X, SF_PSI, SF_U, SF_V};
+    for (int f = 0; f < 4; ++f)
+      if (int r = inv_transform(c, c->tmp_spec, kinds[f], 0, (char*)c->phys + f * pf)) return r;
+    for (int f = 0; f < 3; ++f)
+      if (int r = inv_transform(c, c->tmp_spec2, kinds[f], 0, (char*)c->phys + (4 + f) * pf)) return r;
+    return GF_OK;
+  }
   const int kinds[4] = {SF_X, SF_PSI, SF_U, SF_V};
   for (int f = 0; f < 4; ++f)
     if (int r = inv_transform(c, c->sol, kinds[f], 0, (char*)c->phys + f * pf)) return r;
@@ -871,7 +928,8 @@ extern "C" int gf_updatevars(gf_ctx* c) {
 
 extern "C" int gf_get_field(gf_ctx* c, int which, void* out, int where) {
   if (!c || !out) return GF_ERR_ARG;
-  if (which < 0 || which > 3) return fail(c, GF_ERR_ARG, "unknown field");
+  const int maxf = c->cfg.module == GF_BAROTROPICQGQL ? 6 : 3;
+  if (which < 0 || which > maxf) return fail(c, GF_ERR_ARG, "unknown field");
   const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->g.nb * c->rb;
   return copy_phys_out(c, out, (char*)c->phys + which * pf, where);
 }
@@ -1288,7 +1346,7 @@ static int diag_mask(gf_ctx* c, const int32_t* which, int32_t nd, uint32_t* mask
       else return fail(c, GF_ERR_ARG, "unknown MultiLayerQG diagnostic");
       continue;
     }
-    const int maxd = mod == GF_TWODNAVIERSTOKES ? 8 : mod == GF_SINGLELAYERQG ? 9 : 4;
+    const int maxd = mod == GF_TWODNAVIERSTOKES ? 8 : mod == GF_SINGLELAYERQG ? 9 : 4;  // SQG, QGQL: 4
     if (d < 0 || d > maxd) return fail(c, GF_ERR_ARG, "unknown diagnostic");
     if (mod == GF_SINGLELAYERQG && d == GF_D_SLQG_ENERGY) { mask |= 3u; continue; }
     if (finite_ell && d >= 3) return fail(c, GF_ERR_NOT_IMPLEMENTED, "not implemented for finite deformation radius");
@@ -1329,7 +1387,7 @@ static void diag_post(const gf_ctx* c, const int32_t* which, int32_t nd, const d
       } else {
         v = h(d) * norm;
         const bool work = (mod == GF_TWODNAVIERSTOKES && (d == 7 || d == 8)) || (mod == GF_SINGLELAYERQG && (d == 5 || d == 6)) ||
-                          (mod == GF_SURFACEQG && d == 4);
+                          (mod == GF_SURFACEQG && d == 4) || (mod == GF_BAROTROPICQGQL && d == 3);
         if (work) v *= fs;
       }
       out[(size_t)ib * nd + i] = v;
@@ -1385,6 +1443,46 @@ extern "C" int gf_step_diags(gf_ctx* c, int64_t nsteps, const int32_t* which, in
   }
   cudaFreeAsync(ring, c->stream);
   return rc;
+}
+
+// ---------------------------------------------------------------------------- fluxes
+// MultiLayerQG.fluxes (src/multilayerqg.jl:977-1022): lateral_j = H_j / V sum U_j v_j du_j/dy
+// dx dy and vertical_{j+1/2} = f0^2 / (g'_j V) sum (U_j - U_{j+1}) v_{j+1} psi_j dx dy,
+// V = Lx Ly sum(H) (one layer: V = Lx Ly, no H factor), after updatevars!; FP64 sums.
+extern "C" int gf_fluxes(gf_ctx* c, double* lateral, double* vertical) {
+  if (!c || !lateral) return GF_ERR_ARG;
+  if (c->cfg.module != GF_MULTILAYERQG) return fail(c, GF_ERR_ARG, "fluxes is a MultiLayerQG diagnostic");
+  const Geom& g = c->g;
+  const int nl = g.nl, NB = g.nb;
+  if (nl > 1 && !vertical) return GF_ERR_ARG;
+  if (int r = gf_updatevars(c)) return r;
+  const size_t pf = (size_t)nl * g.ny * g.nx * NB * c->rb;
+  void* uy = nullptr;
+  GF_CUDA(c, cudaMallocAsync(&uy, pf, c->stream));
+  int rc = inv_transform(c, c->sol, SF_UY, 0, uy);
+  if (rc == GF_OK) {
+    const cudaError_t e = DISPATCH(c, launch_flux, g, (const char*)c->phys + 3 * pf, uy, (const char*)c->phys + pf,
+                                   c->Ud, c->dpart, c->diag_blocks, c->stream);
+    if (e != cudaSuccess) rc = fail(c, GF_ERR_CUDA, cudaGetErrorString(e));
+  }
+  if (rc == GF_OK) {
+    diag_finish<<<NB, 256, 0, c->stream>>>(c->dpart, c->diag_blocks, (1u << (2 * nl - 1)) - 1, c->dout);
+    c->launches += 2;
+  }
+  cudaFreeAsync(uy, c->stream);
+  if (rc != GF_OK) return rc;
+  std::vector<double> hv((size_t)NDIAG * NB);
+  GF_CUDA(c, cudaMemcpyAsync(hv.data(), c->dout, hv.size() * 8, cudaMemcpyDeviceToHost, c->stream));
+  GF_CUDA(c, cudaStreamSynchronize(c->stream));
+  const double dxdy = (c->cfg.Lx / g.nx) * (c->cfg.Ly / g.ny);
+  const double V = c->cfg.Lx * c->cfg.Ly * (nl > 1 ? c->Hsum : 1.0);
+  for (int ib = 0; ib < NB; ++ib) {
+    auto h = [&](int q) { return hv[(size_t)q * NB + ib]; };
+    for (int L = 0; L < nl; ++L) lateral[(size_t)ib * nl + L] = (nl > 1 ? c->Hl[L] : 1.0) * h(L) * dxdy / V;
+    for (int L = 0; L < nl - 1; ++L)
+      vertical[(size_t)ib * (nl - 1) + L] = c->f0 * c->f0 / c->gprime[L] * h(nl + L) * dxdy / V;
+  }
+  return GF_OK;
 }
 
 // ------------------------------------------------------------------------------ autotune

@@ -183,6 +183,51 @@ cudaError_t launch_adj_spec(const Geom& g, const ModArgs& m, const void* in, voi
   return cudaGetLastError();
 }
 
+template <class T> __device__ __forceinline__ double to_double(T x) { return (double)x; }
+template <> __device__ __forceinline__ double to_double<df64>(df64 x) { return (double)x.hi + (double)x.lo; }
+
+// Partial sums of the MultiLayerQG fluxes per block and instance (blockIdx.y): slot L < nl
+// sum U_L v_L uy_L, slot nl + L sum (U_L - U_{L+1}) v_{L+1} psi_L; physical fields
+// [instance][layer][j][i], U [layer][j] in FP64.
+template <class T>
+__global__ void __launch_bounds__(256) flux_kernel(Geom g, const T* __restrict__ v, const T* __restrict__ uy,
+                                                   const T* __restrict__ psi, const double* __restrict__ U,
+                                                   double* partial) {
+  __shared__ double red[256];
+  const int ib = blockIdx.y, nl = g.nl, nq = 2 * nl - 1;
+  const size_t np = (size_t)g.ny * g.nx, off = (size_t)ib * nl * np;
+  for (int q = 0; q < nq; ++q) {
+    const bool lat = q < nl;
+    const int L = lat ? q : q - nl;
+    double s = 0, comp = 0;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < np; e += (size_t)gridDim.x * blockDim.x) {
+      const int j = (int)(e / g.nx);
+      const double x = lat ? U[(size_t)L * g.ny + j] * to_double(v[off + L * np + e]) * to_double(uy[off + L * np + e])
+                           : (U[(size_t)L * g.ny + j] - U[(size_t)(L + 1) * g.ny + j]) *
+                                 to_double(v[off + (L + 1) * np + e]) * to_double(psi[off + L * np + e]);
+      const double t = s + x;
+      comp += (fabs(s) >= fabs(x)) ? (s - t) + x : (x - t) + s;
+      s = t;
+    }
+    red[threadIdx.x] = s + comp;
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+      if ((int)threadIdx.x < st) red[threadIdx.x] += red[threadIdx.x + st];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[((size_t)q * gridDim.y + ib) * gridDim.x + blockIdx.x] = red[0];
+    __syncthreads();
+  }
+}
+
+template <class T>
+cudaError_t launch_flux(const Geom& g, const void* v, const void* uy, const void* psi, const double* U, double* partial,
+                        int nblocks, cudaStream_t st) {
+  flux_kernel<T><<<dim3(nblocks, g.nb), 256, 0, st>>>(g, static_cast<const T*>(v), static_cast<const T*>(uy),
+                                                      static_cast<const T*>(psi), U, partial);
+  return cudaGetLastError();
+}
+
 #define GF_INST_DISPATCH(T)                                                                                    \
   template cudaError_t launch_row<T>(const Geom&, const ModArgs&, const Bufs&, cudaStream_t);                   \
   template cudaError_t launch_col<T>(const Geom&, const ModArgs&, const StepArgs&, const Bufs&, cudaStream_t);  \
@@ -197,7 +242,9 @@ cudaError_t launch_adj_spec(const Geom& g, const ModArgs& m, const void* in, voi
   template cudaError_t launch_spec_apply<T>(const Geom&, const ModArgs&, const void*, void*, int, cudaStream_t); \
   template cudaError_t launch_adj_row<T>(const Geom&, const AdjArgs&, const Bufs&, cudaStream_t);               \
   template cudaError_t launch_adj_col<T>(const Geom&, const ModArgs&, const AdjArgs&, const Bufs&, cudaStream_t); \
-  template cudaError_t launch_adj_spec<T>(const Geom&, const ModArgs&, const void*, void*, int, cudaStream_t);
+  template cudaError_t launch_adj_spec<T>(const Geom&, const ModArgs&, const void*, void*, int, cudaStream_t);      \
+  template cudaError_t launch_flux<T>(const Geom&, const void*, const void*, const void*, const double*, double*,   \
+                                      int, cudaStream_t);
 
 GF_INST_DISPATCH(float)
 GF_INST_DISPATCH(double)

@@ -10,7 +10,7 @@ namespace gf {
 struct df64;
 template <class T> struct cplx;
 
-enum Module { MOD_TWODNS = 0, MOD_SLQG = 1, MOD_MLQG = 2, MOD_SQG = 3 };
+enum Module { MOD_TWODNS = 0, MOD_SLQG = 1, MOD_MLQG = 2, MOD_SQG = 3, MOD_QGQL = 4 };
 enum StepKind { SK_FE = 0, SK_RK4 = 1, SK_ETDRK4 = 2, SK_AB3 = 3, SK_NOUT = 4 /* write N to acc (calcN!) */ };
 enum PsiKind { PSI_INVK2 = 0, PSI_HELMHOLTZ = 1, PSI_TABLE = 2, PSI_EIGEN = 3 };
 enum ForceKind { FK_NONE = 0, FK_STATIC = 1, FK_HARMONIC = 2, FK_STOCH = 3, FK_STOCH_PHASE = 4 };
@@ -56,6 +56,7 @@ struct ModArgs {
   double lam[MAXL], V[MAXL * MAXL], Vinv[MAXL * MAXL];
   // physical-space products
   int hasB, hasC, linear;
+  int ql;  // BarotropicQGQL: products (U z' + u' Z, v' Z, v' z'), N by kr column (zonal mean / eddies)
   const void* eta;       // real [j][i] or null: q' = q + eta
   const void* U1D;       // real [layer][j] or null: u' = u + U
   const void* Qy1D;      // real [layer][j] or null
@@ -149,6 +150,10 @@ template <class T> cudaError_t launch_adj_col(const Geom&, const ModArgs&, const
 // element-wise adjoint helpers: op 0 kinetic-energy gradient, op 1 rfft^T preparation (see gf_dispatch.cu)
 template <class T> cudaError_t launch_adj_spec(const Geom&, const ModArgs&, const void* in, void* out, int op,
                                                cudaStream_t);
+
+// MultiLayerQG fluxes: per-block partial sums (gf_dispatch.cu)
+template <class T> cudaError_t launch_flux(const Geom&, const void* v, const void* uy, const void* psi, const double* U,
+                                           double* partial, int nblocks, cudaStream_t);
 
 // message returned by gf_last_error(NULL)
 void set_global_error(const std::string& msg);

@@ -177,7 +177,9 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? GF_MINBLOCKS_F32 : 1)
         cplx<T> d;
         if (slot == 0) d = krT * mul_mi(v);                          // -i kr A
         else if (slot == 1) d = (T(lidx(g, j)) * dky) * mul_mi(v);   // -i l B
+        else if (m.ql) d = (T(lidx(g, j)) * dky) * mul_mi(v);        // -i l C (zonal mean)
         else d = czero<T>() - v;                                     // -C
+        if (m.ql && ((kr == 0) != (slot == 2))) d = czero<T>();      // mean: C only; eddies: A, B
         XL[j * C] = (f == 0) ? d : XL[j * C] + d;
       }
       __syncthreads();  // Fb is the target of the prefetch issued in the next iteration
@@ -458,10 +460,19 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) row_nl_kernel(Geo
         ph[2 * fs + ia] = v.x; ph[2 * fs + ia + NX] = v.y;
       }
       const cplx<T> au = m.linear ? Up : u;
-      const cplx<T> A = mk<T>(au.x * q.x, au.y * q.y);
-      const cplx<T> Bv = mk<T>(v.x * q.x, v.y * q.y);
+      cplx<T> A = mk<T>(au.x * q.x, au.y * q.y);
+      cplx<T> Bv = mk<T>(v.x * q.x, v.y * q.y);
       cplx<T> Cv = czero<T>();
-      if (m.hasC) {
+      if (m.ql) {
+        // zonal means Z, U of the two rows (x-constant: the kr = 0 inverse values) and eddies
+        const cplx<T> Z = mk<T>(W[(size_t)j0 * g.ldw].x, W[(size_t)(j0 + 1) * g.ldw].x);
+        const cplx<T>* Wu = W + (size_t)nl * g.ny * g.ldw;
+        const cplx<T> Um = mk<T>(Wu[(size_t)j0 * g.ldw].x, Wu[(size_t)(j0 + 1) * g.ldw].x);
+        const cplx<T> ze = q - Z, ue = u - Um;
+        A = mk<T>(Um.x * ze.x + ue.x * Z.x, Um.y * ze.y + ue.y * Z.y);   // U z' + u' Z
+        Bv = mk<T>(v.x * Z.x, v.y * Z.y);                                 // v' Z
+        Cv = mk<T>(v.x * ze.x, v.y * ze.y);                               // v' z'
+      } else if (m.hasC) {
         cplx<T> Qy = mk<T>(Qa, Qb), Qx = czero<T>();
         if (last && Qy2D) Qy = Qy + mk<T>(Qy2D[(size_t)j0 * NX + x], Qy2D[(size_t)(j0 + 1) * NX + x]);
         if (last && Qx2D) Qx = mk<T>(Qx2D[(size_t)j0 * NX + x], Qx2D[(size_t)(j0 + 1) * NX + x]);
@@ -786,6 +797,12 @@ __global__ void __launch_bounds__(DIAG_BLOCK) diag_kernel(Geom g, ModArgs m, con
       v[6] = wr;
       v[7] = k0 ? 0.0 : mu * iK2 * s2;
       v[8] = k0 ? 0.0 : mu * s2;
+    } else if (m.module == MOD_QGQL) {
+      v[0] = 0.5 * iK2 * s2;
+      v[1] = k0 ? 0.0 : 0.5 * s2;
+      v[2] = k0 ? 0.0 : nu * powi(K2, nnu - 1) * s2;
+      v[3] = iK2 * wr;
+      v[4] = k0 ? 0.0 : mu * iK2 * s2;
     } else {  // SQG
       const double M = to_double(static_cast<const T*>(m.mult)[ti]);
       v[0] = 0.5 * K2 * M * M * s2;

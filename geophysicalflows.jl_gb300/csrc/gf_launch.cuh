@@ -63,7 +63,8 @@ inline cudaError_t set_smem(K kernel, size_t bytes) {
   static_assert(sizeof(K) > 0, "");
   cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   if (e != cudaSuccess) return e;
-  if (bytes > 48 * 1024) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  // the 48 KB default limit covers static + dynamic shared memory: opt in well below it
+  if (bytes > 32 * 1024) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   return cudaSuccess;
 }
 

@@ -69,6 +69,21 @@ def invtransform(prob, fieldh):
     return prob.invtransform(fieldh)
 
 
+def fluxes(prob):
+    """Lateral eddy fluxes per layer and vertical eddy fluxes per interface
+    (src/multilayerqg.jl:977-1022); one layer: the lateral flux only.  Batched problems:
+    arrays with a leading instance axis."""
+    n, B = prob.nlayers, prob.batch
+    lat = np.empty((B, n))
+    ver = np.empty((B, max(n - 1, 1)))
+    prob._c(prob._lib.gf_fluxes(prob._ctx, lat.ctypes.data, ver.ctypes.data))
+    prob._pull_vars()
+    ver = ver[:, : n - 1]
+    if n == 1:
+        return float(lat[0, 0]) if B == 1 else lat[:, 0].copy()
+    return (lat[0].copy(), ver[0].copy()) if B == 1 else (lat, ver)
+
+
 def energies(prob):
     """KE per layer and PE per interface (src/multilayerqg.jl:918-951)."""
     n = prob.nlayers

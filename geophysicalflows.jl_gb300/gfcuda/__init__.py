@@ -5,10 +5,10 @@ Host-side mirror of the reference's module API; every computation runs in libgfc
 from . import _abi
 from ._abi import load, GFError, GFNotImplemented
 from .core import Diagnostic, Forcing, ensemble_step, stepforward
-from . import TwoDNavierStokes, SingleLayerQG, MultiLayerQG, SurfaceQG
+from . import TwoDNavierStokes, SingleLayerQG, MultiLayerQG, SurfaceQG, BarotropicQGQL
 from . import utils
 from . import adjoint
 from .utils import peakedisotropicspectrum
 
 __all__ = ["load", "GFError", "GFNotImplemented", "Diagnostic", "Forcing", "ensemble_step", "stepforward", "TwoDNavierStokes",
-           "SingleLayerQG", "MultiLayerQG", "SurfaceQG", "utils", "adjoint", "peakedisotropicspectrum"]
+           "SingleLayerQG", "MultiLayerQG", "SurfaceQG", "BarotropicQGQL", "utils", "adjoint", "peakedisotropicspectrum"]

@@ -7,7 +7,7 @@ LIBPATH = os.path.join(HERE, "libgfcuda.so")
 
 # enums (include/gfcuda.h)
 GF_OK, GF_ERR_ARG, GF_ERR_UNSUPPORTED, GF_ERR_CUDA, GF_ERR_NOMEM, GF_ERR_STATE, GF_ERR_NOT_IMPLEMENTED = 0, -1, -2, -3, -4, -5, -6
-MODULES = {"TwoDNavierStokes": 0, "SingleLayerQG": 1, "MultiLayerQG": 2, "SurfaceQG": 3}
+MODULES = {"TwoDNavierStokes": 0, "SingleLayerQG": 1, "MultiLayerQG": 2, "SurfaceQG": 3, "BarotropicQGQL": 4}
 STEPPERS = {"ForwardEuler": 0, "FilteredForwardEuler": 1, "RK4": 2, "FilteredRK4": 3,
             "ETDRK4": 4, "FilteredETDRK4": 5, "AB3": 6, "FilteredAB3": 7}
 F32, F64, DF64 = 0, 1, 2
@@ -15,6 +15,7 @@ FORCING = {None: 0, "static": 1, "harmonic": 2, "stochastic": 3, "stochastic_pha
 HOST, DEVICE = 0, 1
 LOSS_KINETIC_ENERGY = 0
 FIELD_Q, FIELD_PSI, FIELD_U, FIELD_V = 0, 1, 2, 3
+FIELD_ZETA_MEAN, FIELD_PSI_MEAN, FIELD_U_MEAN = 4, 5, 6
 
 EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_abi_version", "gf_get_dims", "gf_set_state",
            "gf_get_state", "gf_get_clock", "gf_set_clock", "gf_set_physical", "gf_step", "gf_step_diags",
@@ -22,7 +23,8 @@ EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_abi_version", "gf_get
            "gf_diagnostics", "gf_set_forcing", "gf_synchronize", "gf_profile_enable", "gf_profile_read",
            "gf_rfft2_noalloc", "gf_get_batch", "gf_set_graph_steps", "gf_ensemble_step",
            "gf_peakedisotropicspectrum", "gf_get_filter", "gf_adjoint_setup", "gf_adjoint_forward",
-           "gf_adjoint_backward", "gf_grad", "gf_autotune", "gf_set_launch_shape", "gf_get_launch_shape"]
+           "gf_adjoint_backward", "gf_grad", "gf_autotune", "gf_set_launch_shape", "gf_get_launch_shape",
+           "gf_fluxes"]
 
 
 class gf_config(C.Structure):
@@ -92,6 +94,7 @@ def load(path=None):
         "gf_adjoint_backward": ([vp, vp, vp, vp, C.c_int], C.c_int),
         "gf_grad": ([vp, C.c_int, vp, vp, C.POINTER(dbl), C.c_int], C.c_int),
         "gf_autotune": ([vp, i32, C.POINTER(i32)], C.c_int),
+        "gf_fluxes": ([vp, vp, vp], C.c_int),
         "gf_set_launch_shape": ([vp, C.POINTER(i32)], C.c_int),
         "gf_get_launch_shape": ([vp, C.POINTER(i32)], C.c_int),
     }

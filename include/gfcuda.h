@@ -40,7 +40,11 @@ typedef enum {
   GF_ERR_NOT_IMPLEMENTED = -6 /* the reference raises for this case (e.g. finite deformation radius budgets) */
 } gf_status;
 
-typedef enum { GF_TWODNAVIERSTOKES = 0, GF_SINGLELAYERQG = 1, GF_MULTILAYERQG = 2, GF_SURFACEQG = 3 } gf_module;
+/* GF_BAROTROPICQGQL: the quasi-linear barotropic QG module (src/barotropicqgql.jl): zonal mean
+ * (kr = 0) and eddies (kr > 0) advected quasi-linearly; parameters beta, nu, nnu, mu (linear
+ * drag), eta (kept, unused by the advection as in the reference). */
+typedef enum { GF_TWODNAVIERSTOKES = 0, GF_SINGLELAYERQG = 1, GF_MULTILAYERQG = 2, GF_SURFACEQG = 3,
+               GF_BAROTROPICQGQL = 4 } gf_module;
 
 /* GF_F64: IEEE double throughout.  GF_F32: float bulk (FFTs, products, stage combination);
  * FP64 stays in the setup (ETDRK4 coefficients, inversion factorisation) and in the
@@ -117,7 +121,10 @@ typedef enum {
   GF_FIELD_Q = 0,     /* TwoDNavierStokes zeta / SingleLayerQG, MultiLayerQG q / SurfaceQG b */
   GF_FIELD_PSI = 1,
   GF_FIELD_U = 2,
-  GF_FIELD_V = 3
+  GF_FIELD_V = 3,
+  /* BarotropicQGQL (src/barotropicqgql.jl:380-407): Q/PSI/U/V are the eddy (kr > 0) zeta, psi,
+   * u, v; these are the zonal-mean Zeta, Psi and U */
+  GF_FIELD_ZETA_MEAN = 4, GF_FIELD_PSI_MEAN = 5, GF_FIELD_U_MEAN = 6
 } gf_field;
 
 /* Diagnostic selectors (gf_diagnostics).  Values are the reference functions' values. */
@@ -136,7 +143,10 @@ typedef enum {
   GF_D_SQG_KINETIC_ENERGY = 0, GF_D_SQG_BUOYANCY_VARIANCE = 1, GF_D_SQG_TOTAL_3D_ENERGY = 2,
   GF_D_SQG_BUOYANCY_DISSIPATION = 3, GF_D_SQG_BUOYANCY_WORK = 4,
   /* MultiLayerQG energies (src/multilayerqg.jl:918-951): KE_j = j, PE_{j+1/2} = nlayers + j */
-  GF_D_MLQG_KE0 = 0, GF_D_MLQG_PE0 = 8
+  GF_D_MLQG_KE0 = 0, GF_D_MLQG_PE0 = 8,
+  /* BarotropicQGQL (src/barotropicqgql.jl:433-510) */
+  GF_D_QGQL_ENERGY = 0, GF_D_QGQL_ENSTROPHY = 1, GF_D_QGQL_DISSIPATION = 2, GF_D_QGQL_WORK = 3,
+  GF_D_QGQL_DRAG = 4
 } gf_diag;
 
 /* ---- lifetime ------------------------------------------------------------------------- */
@@ -178,6 +188,12 @@ int gf_calcN(gf_ctx* ctx, void* N, void* sol, double t, int where);
  * compute the physical fields; gf_get_field copies one of them out. */
 int gf_updatevars(gf_ctx* ctx);
 int gf_get_field(gf_ctx* ctx, int which, void* out, int where);
+
+/* MultiLayerQG.fluxes(prob) (src/multilayerqg.jl:977-1022), after updatevars!: the lateral eddy
+ * fluxes H_j / V sum U_j v_j du_j/dy dx dy per layer (lateral[batch][nlayers]) and the vertical
+ * eddy fluxes f0^2 / (g'_{j+1/2} V) sum (U_j - U_{j+1}) v_{j+1} psi_j dx dy per interface
+ * (vertical[batch][nlayers-1], may be NULL for one layer), V = Lx Ly sum(H); FP64 sums. */
+int gf_fluxes(gf_ctx* ctx, double* lateral, double* vertical);
 
 /* GeophysicalFlows.peakedisotropicspectrum(grid, kpeak, E0; mask, allones) (src/utils.jl:29-54)
  * on the context's grid (nlayers = 1, Lx = Ly): writes the physical field zeta = irfft(-K^2 psi_hat)

@@ -466,6 +466,92 @@ class TwoDNavierStokes(Problem):
 # ---------------------------------------------------------------------------------------
 # SingleLayerQG (src/singlelayerqg.jl)
 # ---------------------------------------------------------------------------------------
+class BarotropicQGQL(Problem):
+    """Quasi-linear barotropic QG: src/barotropicqgql.jl:75-110 (Problem), :168-173
+    (Equation), :294-344 (calcN_advection!, calcN!), :380-431 (updatevars!, set_zeta!),
+    :433-510 (diagnostics).  The state is split into the zonal mean (the kr = 0 column, Z)
+    and the eddies (kr > 0, z): N = NZ + Nz with NZ the kr = 0 part of
+    -i kr (u z)^ - i l (v z)^ and Nz the kr > 0 part of -i kr (U z + u Z)^ - i l (v Z)^, where
+    u, v are the eddy velocities and U the mean zonal flow.  The topography is carried in
+    the parameters but does not enter the advection (as in the reference)."""
+
+    def __init__(self, nx=256, ny=None, Lx=2 * np.pi, Ly=None, beta=0.0, eta=None, nu=0.0, nnu=1, mu=0.0,
+                 dt=0.01, stepper="RK4", forcing=None, aliased_fraction=1 / 3):
+        g = Grid(nx, Lx, ny, Ly, aliased_fraction)
+        self.beta, self.nu, self.nnu, self.mu = beta, nu, nnu, mu
+        self.eta = np.zeros((g.ny, g.nx)) if eta is None else np.asarray(eta, dtype=np.float64)
+        L = -mu - nu * _powK(g.Krsq, nnu) + 1j * beta * g.kr * g.invKrsq
+        L = np.asarray(L, dtype=np.complex128)
+        L[0, 0] = 0
+        super().__init__(g, L, self._advection, (g.ny, g.nkr), dt, stepper, forcing)
+
+    @staticmethod
+    def _split(sol):
+        eddy, mean = sol.copy(), sol.copy()
+        eddy[..., :, 0] = 0
+        mean[..., :, 1:] = 0
+        return eddy, mean
+
+    def _advection(self, N, sol, t):
+        g = self.grid
+        dealias(sol, g)
+        zh, Zh = self._split(sol)
+        u = irfft2(1j * g.l * g.invKrsq * zh, g)
+        v = irfft2(-1j * g.kr * g.invKrsq * zh, g)
+        U = irfft2(1j * g.l * g.invKrsq * Zh, g)
+        z, Z = irfft2(zh, g), irfft2(Zh, g)
+        NZ = -1j * g.kr * rfft2(u * z) - 1j * g.l * rfft2(v * z)
+        NZ[:, 1:] = 0
+        Nz = -1j * g.kr * rfft2(U * z + u * Z) - 1j * g.l * rfft2(v * Z)
+        Nz[:, 0] = 0
+        N[...] = NZ + Nz
+
+    def updatevars(self):
+        g, sol = self.grid, self.sol
+        dealias(sol, g)
+        sol[0, 0] = 0
+        zh, Zh = self._split(sol)
+        psih, Psih = -zh * g.invKrsq, -Zh * g.invKrsq
+        self.zeta, self.Zeta = irfft2(zh, g), irfft2(Zh, g)
+        self.psi, self.Psi = irfft2(psih, g), irfft2(Psih, g)
+        self.u, self.v = irfft2(-1j * g.l * psih, g), irfft2(1j * g.kr * psih, g)
+        self.U = irfft2(1j * g.l * Zh * g.invKrsq, g)
+
+    def set_zeta(self, zeta):
+        self.sol[...] = rfft2(zeta)
+        self.sol[0, 0] = 0
+        self.updatevars()
+
+    def _ps(self, a):
+        g = self.grid
+        return parsevalsum(a, g) / (g.Lx * g.Ly)
+
+    def energy(self):
+        g = self.grid
+        return 0.5 * (parsevalsum2(g.kr * g.invKrsq * self.sol, g) + parsevalsum2(g.l * g.invKrsq * self.sol, g)) / (g.Lx * g.Ly)
+
+    def enstrophy(self):
+        g = self.grid
+        a = self.sol.copy()
+        a[0, 0] = 0
+        return 0.5 * parsevalsum2(a, g) / (g.Lx * g.Ly)
+
+    def dissipation(self):
+        with np.errstate(invalid="ignore", divide="ignore"):
+            a = _powK(self.grid.Krsq, self.nnu - 1) * np.abs(self.sol) ** 2
+        a[0, 0] = 0
+        return self.nu * self._ps(a)
+
+    def work(self):
+        s = (self.prevsol + self.sol) / 2 if self.forcing.stochastic else self.sol
+        return self._ps(self.grid.invKrsq * s * np.conj(self.Fh))
+
+    def drag(self):
+        a = self.grid.invKrsq * np.abs(self.sol) ** 2
+        a[0, 0] = 0
+        return self.mu * self._ps(a)
+
+
 class SingleLayerQG(Problem):
     """src/singlelayerqg.jl:91-126 (Problem), :174-207 (Params), :230-252 (Equation),
     :356-432 (calcN_advection!), :484-490 (streamfunctionfrompv!)."""

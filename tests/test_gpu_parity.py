@@ -416,3 +416,48 @@ def test_fp32_twodns_against_fp64_oracle():
     stepforward(p, 100)
     r.stepforward(100)
     assert rel(p.sol, r.sol) <= TOL32
+
+
+@pytest.mark.parametrize("nlayers", [1, 2, 3])
+@pytest.mark.parametrize("prec", [None, "DF64"])
+def test_mlqg_fluxes_gpu(nlayers, prec):
+    """MultiLayerQG.fluxes on the device: the known answers of test/test_multilayerqg.jl:567-655
+    (at 128 x 128) and the oracle on a random state, to 1e-12"""
+    from gfcuda import MultiLayerQG as MLg
+    nx = ny = 128
+    H, b = {1: (None, None), 2: ([0.2, 0.8], [-1.0, -1.2]),
+            3: ([0.2, 0.35, 0.45], [-1.0, -1.2, -1.2 + 1e-9])}[nlayers]
+    g = O.Grid(nx, 2 * np.pi, ny, 2 * np.pi)
+    U = np.zeros((ny, nlayers))
+    U[:, 0] = 1 / np.cosh(g.y / 0.2) ** 2
+    kw = dict(nx=nx, ny=ny, f0=1, H=H, b=b, U=U if nlayers > 1 else U[:, 0])
+    p = MLg.Problem(nlayers, "GPU", precision=prec, **kw)
+    r = O.MultiLayerQG(nlayers, **kw)
+    x, y = g.gridpoints()
+    k0, l0 = 2 * np.pi / g.Lx, 2 * np.pi / g.Ly
+    p1 = np.cos(k0 * x) * np.cos(l0 * y) + np.sin(k0 * x)
+    p2 = np.cos(k0 * x + np.pi / 10) * np.cos(l0 * y)
+    psi = np.stack([p1, p2, p2][:nlayers])
+    MLg.set_psi(p, psi if nlayers > 1 else p1)
+    if nlayers == 1:
+        assert abs(MLg.fluxes(p) - 0.0313134) < 1e-7
+    else:
+        lat, ver = MLg.fluxes(p)
+        assert abs(lat[0] - 0.00626267) < 1e-8 and abs(ver[0] + 0.196539) < 2e-7
+        assert np.all(np.abs(lat[1:]) < 1e-12) and np.all(np.abs(ver[1:]) < 1e-12)
+    if nlayers == 3:
+        # the known-answer configuration has g'_{5/2} = 1e-9 (PV inversion conditioned ~1e9):
+        # compare a random state on a well-conditioned stratification instead
+        kw["b"] = [-1.0, -1.2, -1.3]
+        p = MLg.Problem(nlayers, "GPU", precision=prec, **kw)
+        r = O.MultiLayerQG(nlayers, **kw)
+    rng = np.random.default_rng(5)
+    q = 0.1 * rng.standard_normal((nlayers, ny, nx))
+    MLg.set_q(p, q if nlayers > 1 else q[0])
+    r.set_q(q if nlayers > 1 else q[0])
+    got, ref = MLg.fluxes(p), r.fluxes()
+    if nlayers == 1:
+        assert abs(got - ref) <= 1e-12 * abs(ref)
+    else:
+        for a, c in zip(got, ref):
+            assert np.allclose(a, c, rtol=1e-12, atol=1e-14 * np.max(np.abs(c)))
