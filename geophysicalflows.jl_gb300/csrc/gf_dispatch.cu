@@ -121,16 +121,29 @@ cudaError_t launch_spec_apply(const Geom& g, const ModArgs& m, const void* in, v
   return cudaGetLastError();
 }
 
+#define GF_ADJ_ROW_CASE(N)                                                                  \
+  case N:                                                                                   \
+    if constexpr (std::is_same<T, float>::value) {                                          \
+      if (g.tuneRr == 16) return launch_adj_row_nr<float, N, 16>(g, a, b, st);              \
+      if constexpr (N <= 1024)                                                              \
+        if (g.tuneRr == 4) return launch_adj_row_nr<float, N, 4>(g, a, b, st);              \
+    }                                                                                       \
+    return launch_adj_row_n<T, N>(g, a, b, st);
+#define GF_ADJ_COL_CASE(N)                                                                  \
+  case N:                                                                                   \
+    if constexpr (std::is_same<T, float>::value) {                                          \
+      if (g.tuneRc == 16) return launch_adj_col_nr<float, N, 16>(g, m, a, b, st);           \
+      if constexpr (N <= 1024)                                                              \
+        if (g.tuneRc == 4) return launch_adj_col_nr<float, N, 4>(g, m, a, b, st);           \
+    }                                                                                       \
+    return launch_adj_col_n<T, N>(g, m, a, b, st);
+
+// the adjoint kernels follow the context's tuned radix and tiles (FP32)
 template <class T>
 cudaError_t launch_adj_row(const Geom& g, const AdjArgs& a, const Bufs& b, cudaStream_t st) {
   switch (g.nx) {
-    case 32: return launch_adj_row_n<T, 32>(g, a, b, st);
-    case 64: return launch_adj_row_n<T, 64>(g, a, b, st);
-    case 128: return launch_adj_row_n<T, 128>(g, a, b, st);
-    case 256: return launch_adj_row_n<T, 256>(g, a, b, st);
-    case 512: return launch_adj_row_n<T, 512>(g, a, b, st);
-    case 1024: return launch_adj_row_n<T, 1024>(g, a, b, st);
-    case 2048: return launch_adj_row_n<T, 2048>(g, a, b, st);
+    GF_ADJ_ROW_CASE(32) GF_ADJ_ROW_CASE(64) GF_ADJ_ROW_CASE(128) GF_ADJ_ROW_CASE(256) GF_ADJ_ROW_CASE(512)
+    GF_ADJ_ROW_CASE(1024) GF_ADJ_ROW_CASE(2048)
     default: return cudaErrorInvalidValue;
   }
 }
@@ -138,13 +151,8 @@ cudaError_t launch_adj_row(const Geom& g, const AdjArgs& a, const Bufs& b, cudaS
 template <class T>
 cudaError_t launch_adj_col(const Geom& g, const ModArgs& m, const AdjArgs& a, const Bufs& b, cudaStream_t st) {
   switch (g.ny) {
-    case 32: return launch_adj_col_n<T, 32>(g, m, a, b, st);
-    case 64: return launch_adj_col_n<T, 64>(g, m, a, b, st);
-    case 128: return launch_adj_col_n<T, 128>(g, m, a, b, st);
-    case 256: return launch_adj_col_n<T, 256>(g, m, a, b, st);
-    case 512: return launch_adj_col_n<T, 512>(g, m, a, b, st);
-    case 1024: return launch_adj_col_n<T, 1024>(g, m, a, b, st);
-    case 2048: return launch_adj_col_n<T, 2048>(g, m, a, b, st);
+    GF_ADJ_COL_CASE(32) GF_ADJ_COL_CASE(64) GF_ADJ_COL_CASE(128) GF_ADJ_COL_CASE(256) GF_ADJ_COL_CASE(512)
+    GF_ADJ_COL_CASE(1024) GF_ADJ_COL_CASE(2048)
     default: return cudaErrorInvalidValue;
   }
 }

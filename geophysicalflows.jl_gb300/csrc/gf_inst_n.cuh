@@ -103,37 +103,54 @@ cudaError_t launch_col_fwd_n(const Geom& g, const Bufs& b, int nf, void* out, in
   return cudaGetLastError();
 }
 
-template <class T, int NN>
-cudaError_t launch_adj_row_n(const Geom& g, const AdjArgs& a, const Bufs& b, cudaStream_t st) {
+// Adjoint kernels with FFT radix R; the context's tuned tiles when they fit.
+template <class T, int NN, int R>
+cudaError_t launch_adj_row_nr(const Geom& g, const AdjArgs& a, const Bufs& b, cudaStream_t st) {
   cudaError_t err;
   const size_t e = sizeof(cplx<T>);
-  const int B = pick_B(NN, RADIX<T>, e, 3, g.ny / 2, 1);
-  const size_t sm = (size_t)B * 3 * row_stride<T>(NN, NN / RADIX<T>) * e;
-  auto k = adj_row_kernel<T, NN, RADIX<T>>;
+  int B = pick_B(NN, R, e, 3, g.ny / 2, 1);
+  if (g.tuneB > 0 && row_shape_ok(NN, R, e, 3, g.ny / 2, g.tuneB)) B = g.tuneB;
+  const size_t sm = (size_t)B * 3 * row_stride<T>(NN, NN / R) * e;
+  auto k = adj_row_kernel<T, NN, R>;
   if ((err = set_smem(k, sm)) != cudaSuccess) return err;
-  k<<<g.ny / 2 / B, B * (NN / RADIX<T>), sm, st>>>(g, a, b, B);
+  k<<<g.ny / 2 / B, B * (NN / R), sm, st>>>(g, a, b, B);
+  return cudaGetLastError();
+}
+
+template <class T, int NN, int R>
+cudaError_t launch_adj_col_nr(const Geom& g, const ModArgs& m, const AdjArgs& a, const Bufs& b, cudaStream_t st) {
+  cudaError_t err;
+  const size_t e = sizeof(cplx<T>);
+  auto smem = [&](int c) { return adj_col_smem(c, col_stride<T>(NN, c), e); };
+  int C = pick_C(NN, R, g.nkr, smem, 1);
+  if (g.tuneC > 0 && g.tuneC * (NN / R) <= 512 && smem(g.tuneC) <= (size_t)SMEM_CAP) C = g.tuneC;
+  Geom g2 = g;
+  g2.cs = col_stride<T>(NN, C);
+  const size_t sm = smem(C);
+  auto k = adj_col_kernel<T, NN, R>;
+  if ((err = set_smem(k, sm)) != cudaSuccess) return err;
+  k<<<(g.nkr + C - 1) / C, C * (NN / R), sm, st>>>(g2, m, a, b, C);
   return cudaGetLastError();
 }
 
 template <class T, int NN>
+cudaError_t launch_adj_row_n(const Geom& g, const AdjArgs& a, const Bufs& b, cudaStream_t st) {
+  return launch_adj_row_nr<T, NN, RADIX<T>>(g, a, b, st);
+}
+
+template <class T, int NN>
 cudaError_t launch_adj_col_n(const Geom& g, const ModArgs& m, const AdjArgs& a, const Bufs& b, cudaStream_t st) {
-  cudaError_t err;
-  const size_t e = sizeof(cplx<T>);
-  const int C = pick_C(NN, RADIX<T>, g.nkr, [&](int c) { return adj_col_smem(c, col_stride<T>(NN, c), e); }, 1);
-  Geom g2 = g;
-  g2.cs = col_stride<T>(NN, C);
-  const size_t sm = adj_col_smem(C, g2.cs, e);
-  auto k = adj_col_kernel<T, NN, RADIX<T>>;
-  if ((err = set_smem(k, sm)) != cudaSuccess) return err;
-  k<<<(g.nkr + C - 1) / C, C * (NN / RADIX<T>), sm, st>>>(g2, m, a, b, C);
-  return cudaGetLastError();
+  return launch_adj_col_nr<T, NN, RADIX<T>>(g, m, a, b, st);
 }
 
 // the step kernels at another FFT radix (autotuner candidates)
 #define GF_INST_NR(T, NN, R)                                                                                   \
   template cudaError_t launch_row_nr<T, NN, R>(const Geom&, const ModArgs&, const Bufs&, cudaStream_t);         \
   template cudaError_t launch_col_nr<T, NN, R>(const Geom&, const ModArgs&, const StepArgs&, const Bufs&,       \
-                                               cudaStream_t);
+                                               cudaStream_t);                                                  \
+  template cudaError_t launch_adj_row_nr<T, NN, R>(const Geom&, const AdjArgs&, const Bufs&, cudaStream_t);     \
+  template cudaError_t launch_adj_col_nr<T, NN, R>(const Geom&, const ModArgs&, const AdjArgs&, const Bufs&,    \
+                                                   cudaStream_t);
 
 #define GF_INST_N(T, NN)                                                                                       \
   template cudaError_t launch_row_n<T, NN>(const Geom&, const ModArgs&, const Bufs&, cudaStream_t);             \

@@ -80,6 +80,9 @@ template <class T, int NN> cudaError_t launch_row_n(const Geom&, const ModArgs&,
 template <class T, int NN, int R> cudaError_t launch_row_nr(const Geom&, const ModArgs&, const Bufs&, cudaStream_t);
 template <class T, int NN, int R>
 cudaError_t launch_col_nr(const Geom&, const ModArgs&, const StepArgs&, const Bufs&, cudaStream_t);
+template <class T, int NN, int R> cudaError_t launch_adj_row_nr(const Geom&, const AdjArgs&, const Bufs&, cudaStream_t);
+template <class T, int NN, int R>
+cudaError_t launch_adj_col_nr(const Geom&, const ModArgs&, const AdjArgs&, const Bufs&, cudaStream_t);
 // FFT radices of the FP32 step kernels that the autotuner may pick, per length
 constexpr bool f32_radix_built(int N, int R) { return R == 8 || (R == 16) || (R == 4 && N <= 1024); }
 template <class T, int NN> cudaError_t launch_col_n(const Geom&, const ModArgs&, const StepArgs&, const Bufs&, cudaStream_t);
