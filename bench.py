@@ -273,6 +273,58 @@ def accuracy_100_steps(w, nsteps=100):
             "df64_vs_fp64": relerr(sols["df64"], sols["f64"])}
 
 
+def run_config0(cpu=True):
+    """TwoDNavierStokes decaying 128^2, nu = 0, FilteredRK4 dt = 0.005, 1000 steps from the
+    peaked isotropic state (k0 = 6, E = 0.5), with zeta, energy and enstrophy read back to
+    the host every 100 steps: wall time of the whole run (host outputs included) in IEEE
+    FP64 and FP64-plain (df64), the FP64 CPU restatement on the same run, and the final-state
+    difference from it."""
+    import gfcuda
+    out = {"workload": "TwoDNavierStokes 128^2 decaying, nu=0, FilteredRK4 dt=0.005, 1000 steps, zeta/E/Z "
+                       "to the host every 100 steps"}
+    sols = {}
+    for key, prec in (("fp64", None), ("df64", "DF64")):
+        p = gfcuda.TwoDNavierStokes.Problem("GPU", nx=128, dt=0.005, stepper="FilteredRK4", precision=prec)
+        z0 = gfcuda.peakedisotropicspectrum(p.grid, 6, 0.5, mask=p.timestepper.filter, seed=1234)
+        for rep in range(2):  # the second run is timed
+            gfcuda.TwoDNavierStokes.set_zeta(p, z0)
+            p.set_clock(0.0, 0)
+            p.synchronize()
+            t0 = time.perf_counter()
+            series = []
+            for k in range(10):
+                gfcuda.stepforward(p, 100)
+                E, Z = p.diagnostics([0, 1])
+                p.updatevars()
+                series.append((E, Z, p.vars.zeta))
+            dt = time.perf_counter() - t0
+        # 1000 steps: the total in seconds equals the time per step in milliseconds
+        out[key] = {"s_total": dt, "ms_per_step": dt, "E_final": float(series[-1][0]), "Z_final": float(series[-1][1])}
+        sols[key] = p.sol
+        p.close()
+    if cpu:
+        import gf_oracle as O
+        O.set_fft_workers(os.cpu_count() or 1)
+        try:
+            r = O.TwoDNavierStokes(nx=128, dt=0.005, stepper="FilteredRK4")
+            g = r.grid
+            z0 = O.peakedisotropicspectrum(g, 6, 0.5, mask=O.makefilter(g), seed=1234)
+            r.set_zeta(z0)
+            t0 = time.perf_counter()
+            for k in range(10):
+                r.stepforward(100)
+                r.energy(), r.enstrophy()
+                r.updatevars()
+            dt = time.perf_counter() - t0
+        finally:
+            O.set_fft_workers(None)
+        out["cpu_restatement"] = {"s_total": dt, "cores": os.cpu_count() or 1, "kind": "port"}
+        out["fp64_vs_cpu_rel_l2_after_1000_steps"] = relerr(sols["fp64"], r.sol)
+        out["df64_vs_cpu_rel_l2_after_1000_steps"] = relerr(sols["df64"], r.sol)
+        out["speedup_fp64_vs_cpu"] = dt / out["fp64"]["s_total"]
+    return out
+
+
 def time_ensemble(steps, warmup, flush):
     """The 1536-run ensemble: one batched Problem per size class (instance i of a class
     draws its forcing with seed + i), all stepped by gf_ensemble_step; each class runs on its
@@ -483,6 +535,7 @@ def run_ours(args):
         adj32 = time_adjoint(flush)
         adj64 = time_adjoint(flush, np.float64)
     acc = accuracy_100_steps(w)
+    cfg0 = run_config0(cpu=is_rank0())
     ms, msg, msdf, ms64, e2e_s, e2e_df = reduce_max(dist, [
         r32["ms_per_step"], r32["ms_per_step_graph"], rdf["ms_per_step"], r64["ms_per_step"],
         1e3 * r32["e2e_s_per_step"], 1e3 * rdf["e2e_s_per_step"]])
@@ -552,6 +605,7 @@ def run_ours(args):
                          "value_graph": ens["points"] / (ens["ms_per_step_graph"] * 1e-3),
                          "ms_per_step": ens["ms_per_step"], "ms_per_step_graph": ens["ms_per_step_graph"],
                          "mean_energy_per_class": ens["mean_energy"], "launch_shapes": ens["launch_shapes"]},
+        "twodns128_decaying": cfg0,
         "adjoint_slqg256": {"workload": "gradient of the final kinetic energy w.r.t. q0 and topography: "
                                         "SingleLayerQG 256^2, deformation radius 0.35, topography |k|<=8 amp 0.1, "
                                         "ETDRK4 dt=0.01, 500 steps, checkpoint every 25",

@@ -227,12 +227,93 @@ __device__ __forceinline__ void fft_passes(cplx<T>* buf, int t, const cplx<T>* _
   }
 }
 
+// NF independent length-N Stockham FFTs in lockstep on buffers buf + f * stride: one pair of
+// block barriers per pass for all of them, NF x R independent shared-memory loads in flight
+// per thread, and one twiddle computation shared by the NF butterflies of a thread.
+template <class T, int N, int R, int DIR, int Ns, int NF>
+__device__ __forceinline__ void fft_passes_multi(cplx<T>* buf, int stride, int t, const cplx<T>* __restrict__ tw) {
+  if constexpr (Ns < N) {
+    constexpr int Rp = (N / Ns < R) ? (N / Ns) : R;
+    constexpr int NB = R / Rp;
+    constexpr int TPF = N / R;
+    constexpr int TWS = TWN / (Ns * Rp);
+    cplx<T> v[NF][NB][Rp];
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const int j = t + b * TPF;
+#pragma unroll
+      for (int f = 0; f < NF; ++f)
+#pragma unroll
+        for (int r = 0; r < Rp; ++r) v[f][b][r] = buf[f * stride + swz<T>(j + r * (N / Rp))];
+    }
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const int j = t + b * TPF;
+      if constexpr (Ns > 1) {
+        const int k = j & (Ns - 1);
+        cplx<T> w[Rp];
+        if constexpr (sizeof(T) == 4) {
+          const cplx<T> w1 = twiddle<DIR>(tw, k * TWS);
+          w[1] = w1;
+#pragma unroll
+          for (int r = 2; r < Rp; ++r) w[r] = w[r - 1] * w1;
+        } else {
+#pragma unroll
+          for (int r = 1; r < Rp; ++r) w[r] = twiddle<DIR>(tw, r * k * TWS);
+        }
+#pragma unroll
+        for (int f = 0; f < NF; ++f)
+#pragma unroll
+          for (int r = 1; r < Rp; ++r) v[f][b][r] = v[f][b][r] * w[r];
+      }
+#pragma unroll
+      for (int f = 0; f < NF; ++f) dft<Rp, DIR>(v[f][b]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const int j = t + b * TPF;
+      const int idxD = (j / Ns) * Ns * Rp + (j & (Ns - 1));
+#pragma unroll
+      for (int f = 0; f < NF; ++f)
+#pragma unroll
+        for (int r = 0; r < Rp; ++r) buf[f * stride + swz<T>(idxD + r * Ns)] = v[f][b][r];
+    }
+    __syncthreads();
+    fft_passes_multi<T, N, R, DIR, Ns * Rp, NF>(buf, stride, t, tw);
+  }
+}
+
+// NF in-place FFTs of buffers buf + f * stride (same layout as fft_smem), in lockstep.
+template <class T, int N, int R, int DIR, int NF>
+__device__ __forceinline__ void fft_smem_multi(cplx<T>* buf, int stride, int t, const cplx<T>* __restrict__ tw) {
+  fft_passes_multi<T, N, R, DIR, 1, NF>(buf, stride, t, tw);
+}
+
+// NF FFTs of buffers buf + f * stride: in lockstep when the registers allow (FP32, NF x R <=
+// 24 values per thread), otherwise one after the other.
+template <class T, int N, int R, int DIR, int NF>
+__device__ __forceinline__ void fft_smem_group(cplx<T>* buf, int stride, int t, const cplx<T>* __restrict__ tw);
+
 // In-place length-N FFT (DIR = -1 forward, +1 inverse; both unnormalised) of the swizzled
 // buffer buf (logical element a at buf[swz<T>(a)]) by threads t in [0, N/R).  Every thread
 // of the block must call it (it synchronises the block).
 template <class T, int N, int R, int DIR>
 __device__ __forceinline__ void fft_smem(cplx<T>* buf, int t, const cplx<T>* __restrict__ tw) {
   fft_passes<T, N, R, DIR, 1>(buf, t, tw);
+}
+
+#ifndef GF_FFT_MULTI
+#define GF_FFT_MULTI 1
+#endif
+template <class T, int N, int R, int DIR, int NF>
+__device__ __forceinline__ void fft_smem_group(cplx<T>* buf, int stride, int t, const cplx<T>* __restrict__ tw) {
+  if constexpr (GF_FFT_MULTI && sizeof(T) == 4 && NF * R <= 24 && NF > 1) {
+    fft_smem_multi<T, N, R, DIR, NF>(buf, stride, t, tw);
+  } else {
+#pragma unroll 1
+    for (int f = 0; f < NF; ++f) fft_smem<T, N, R, DIR>(buf + f * stride, t, tw);
+  }
 }
 
 }  // namespace gf

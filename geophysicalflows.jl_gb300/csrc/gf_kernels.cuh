@@ -21,9 +21,13 @@
 #include "gf_philox.cuh"
 #include "gf_internal.h"
 
-// Minimum resident blocks per SM requested for the FP32 step kernels (register budget).
+// Minimum resident blocks per SM requested for the FP32 step kernels (register budget):
+// column kernel (512 threads) and row kernel (256 threads).
 #ifndef GF_MINBLOCKS_F32
-#define GF_MINBLOCKS_F32 2
+#define GF_MINBLOCKS_F32 1
+#endif
+#ifndef GF_ROW_MINBLOCKS_F32
+#define GF_ROW_MINBLOCKS_F32 3
 #endif
 
 namespace gf {
@@ -106,7 +110,8 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? GF_MINBLOCKS_F32 : 1)
   const int nl = g.nl;
   cplx<T>* F0 = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* F1 = F0 + C * cs;
-  cplx<T>* Xs = F1 + C * cs;
+  cplx<T>* F2 = F1 + C * cs;  // one layer: third work buffer (the general path's Xs)
+  cplx<T>* Xs = F2;
   cplx<T>* Ps = Xs + nl * NY * C;
   const int tid = threadIdx.x, c = tid % C, t = tid / C;
   const int cf = tid / TPF, tf = tid % TPF;
@@ -137,11 +142,205 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? GF_MINBLOCKS_F32 : 1)
                                                m.Vinv_l[a - MAXL - MAXL * MAXL]);
   }
 
+  const T U0 = sel<T>(m.U0, m.U0_f, m.U0_l);
+  // per-element stage epilogue: forcing, U eta term, bottom drag, the stepper's stage
+  // combination; returns the next stage's X at (L, j) (zero where dealiased).  kin only.
+  auto epilogue = [&](int L, int j, cplx<T> N) -> cplx<T> {
+    cplx<T> xn = czero<T>();
+    const size_t ti = (size_t)j * g.ldk + kr;       // table index
+    const size_t si = ioff + (size_t)L * lstride + ti;  // state index
+    const bool keep = kept(g, kr, j);
+    if (m.Ueta) N = N - (U0 * krT) * mul_i(static_cast<const cplx<T>*>(m.etah)[ti]);
+    if (m.drag && L == nl - 1) N = N + Dp[ti];
+    cplx<T>* sol = static_cast<cplx<T>*>(s.sol);
+    const cplx<T> solm = keep ? sol[si] : czero<T>();
+    // forcing
+    if (s.fkind == FK_STATIC) {
+      N = N + static_cast<const cplx<T>*>(s.Fh)[si];
+    } else if (s.fkind == FK_HARMONIC) {
+      N = N + fscale * static_cast<const cplx<T>*>(s.Fh)[si];
+    } else if (s.fkind == FK_STOCH || s.fkind == FK_STOCH_PHASE) {
+      cplx<T> Fv;
+      if (s.draw) {
+        const T sp = static_cast<const T*>(s.fspec)[ti];
+        const uint64_t e = (uint64_t)kr + (uint64_t)g.nkr * ((uint64_t)j + (uint64_t)g.ny * L);
+        Fv = czero<T>();
+        const bool zero_mean = (s.fkind == FK_STOCH_PHASE) && kr == 0 && j == 0;
+        if (sp != T(0) && !zero_mean) Fv = sp * draw<T>(e, step, s.seed + ib, s.fkind == FK_STOCH_PHASE);
+        static_cast<cplx<T>*>(s.Fstore)[si] = Fv;
+        static_cast<cplx<T>*>(s.prevsol)[si] = solm;
+      } else {
+        Fv = static_cast<const cplx<T>*>(s.Fh)[si];
+      }
+      N = N + Fv;
+    }
+    auto Lmul = [&](cplx<T> x) { return mulc(ldc<T>(s.Ltab, ti, s.cplxL), x, s.cplxL); };
+    auto finish = [&](cplx<T> v) {
+      if (s.filtered) v = static_cast<const T*>(s.filt)[ti] * v;
+      sol[si] = v;
+      return v;
+    };
+    if (s.kind == SK_NOUT) {
+      static_cast<cplx<T>*>(s.acc)[si] = N;
+    } else if (s.kind == SK_FE) {
+      cplx<T> Rv = N;
+      if (s.hasL) Rv = Rv + Lmul(solm);
+      xn = finish(solm + dt * Rv);
+    } else if (s.kind == SK_RK4) {
+      cplx<T>* X = static_cast<cplx<T>*>(s.X);
+      cplx<T>* acc = static_cast<cplx<T>*>(s.acc);
+      cplx<T> Rv = N;
+      if (s.hasL) Rv = Rv + Lmul(s.stage == 1 ? solm : (keep ? X[si] : czero<T>()));
+      if (s.stage == 1) {
+        acc[si] = T(1.0 / 6.0) * Rv;
+        xn = solm + T(0.5) * dt * Rv;
+      } else if (s.stage < 4) {
+        acc[si] = acc[si] + T(1.0 / 3.0) * Rv;
+        xn = solm + (s.stage == 2 ? T(0.5) * dt : dt) * Rv;
+      } else {
+        xn = finish(solm + dt * (acc[si] + T(1.0 / 6.0) * Rv));
+      }
+      if (s.hasL && s.stage < 4) X[si] = keep ? xn : czero<T>();
+    } else if (s.kind == SK_ETDRK4) {
+      const int cx = s.cplxL;
+      cplx<T>* acc = static_cast<cplx<T>*>(s.acc);
+      if (s.stage == 1) {
+        xn = mulc(ldc<T>(s.e2, ti, cx), solm, cx) + mulc(ldc<T>(s.zeta, ti, cx), N, cx);
+        static_cast<cplx<T>*>(s.s1)[si] = keep ? xn : czero<T>();
+        static_cast<cplx<T>*>(s.N1)[si] = N;
+        acc[si] = mulc(ldc<T>(s.alpha, ti, cx), N, cx);
+      } else if (s.stage == 2) {
+        xn = mulc(ldc<T>(s.e2, ti, cx), solm, cx) + mulc(ldc<T>(s.zeta, ti, cx), N, cx);
+        acc[si] = acc[si] + T(2) * mulc(ldc<T>(s.beta, ti, cx), N, cx);
+      } else if (s.stage == 3) {
+        const cplx<T> s1 = static_cast<const cplx<T>*>(s.s1)[si];
+        const cplx<T> n1 = static_cast<const cplx<T>*>(s.N1)[si];
+        xn = mulc(ldc<T>(s.e2, ti, cx), s1, cx) + mulc(ldc<T>(s.zeta, ti, cx), T(2) * N - n1, cx);
+        acc[si] = acc[si] + T(2) * mulc(ldc<T>(s.beta, ti, cx), N, cx);
+      } else {
+        xn = finish(mulc(ldc<T>(s.e, ti, cx), solm, cx) + acc[si] + mulc(ldc<T>(s.gamma, ti, cx), N, cx));
+      }
+    } else {  // AB3
+      cplx<T> Rv = N;
+      if (s.hasL) Rv = Rv + Lmul(solm);
+      cplx<T> upd;
+      if (ab3_euler) {
+        upd = Rv;
+      } else {
+        const cplx<T> r1 = static_cast<const cplx<T>*>(s.Rm1)[si];
+        const cplx<T> r2 = static_cast<const cplx<T>*>(s.Rm2)[si];
+        upd = T(23.0 / 12.0) * Rv - T(16.0 / 12.0) * r1 + T(5.0 / 12.0) * r2;
+      }
+      static_cast<cplx<T>*>(s.Rout)[si] = Rv;
+      xn = finish(solm + dt * upd);
+    }
+    if (!keep) xn = czero<T>();
+    return xn;
+  };
+  // one product slot's term of N at row j: -i kr A, -i l B, -C (or -i l C of the zonal mean)
+  auto slot_term = [&](int slot, int j, cplx<T> v) -> cplx<T> {
+    cplx<T> d;
+    if (slot == 0) d = krT * mul_mi(v);
+    else if (slot == 1) d = (T(lidx(g, j)) * dky) * mul_mi(v);
+    else if (m.ql) d = (T(lidx(g, j)) * dky) * mul_mi(v);
+    else d = czero<T>() - v;
+    if (m.ql && ((kr == 0) != (slot == 2))) d = czero<T>();  // mean: C only; eddies: A, B
+    return d;
+  };
+  cplx<T>* W = static_cast<cplx<T>*>(b.W) + ib * g.bs_w;
+  const T sc = sel<T>(g.inv_nxny, g.inv_nxny_f, g.inv_nxny_l);
+
+  if (nl == 1 && !m.drag) {
+    // ---- one layer: all product FFTs in lockstep, N and the next X in registers, then the
+    // three inverse FFTs of (q, u, v) in lockstep
+    cplx<T> xr[R];
+    if (s.do_fwd) {
+      const cplx<T>* P = static_cast<const cplx<T>*>(b.P) + ib * g.bs_p;
+      const int nslot = 1 + m.hasB + m.hasC;
+      for (int f = 0; f < nslot; ++f) {  // one cp.async group per product field
+        const cplx<T>* Pf = P + (size_t)f * lstride + kr;
+        cplx<T>* Fc = F0 + (size_t)f * C * cs + c * cs;
+#pragma unroll
+        for (int i = 0; i < R; ++i) {
+          const int j = t + i * TPF;
+          if (kin) cp_async_elem<T>(Fc + swz<T>(j), Pf + (size_t)j * g.ldk);
+          else Fc[swz<T>(j)] = czero<T>();
+        }
+        cp_async_commit();
+      }
+      if constexpr (GF_FFT_MULTI && sizeof(T) == 4 && 3 * R <= 24) {
+        // lockstep FFTs of all fields once every load has landed
+        cp_async_wait<0>();
+        __syncthreads();
+        if (nslot == 3) fft_smem_group<T, NY, R, -1, 3>(F0 + cf * cs, C * cs, tf, tw);
+        else if (nslot == 2) fft_smem_group<T, NY, R, -1, 2>(F0 + cf * cs, C * cs, tf, tw);
+        else fft_smem<T, NY, R, -1>(F0 + cf * cs, tf, tw);
+      } else {
+        // field f's FFT while the later fields' loads are still in flight
+        for (int f = 0; f < nslot; ++f) {
+          const int pending = nslot - 1 - f;
+          if (pending >= 2) cp_async_wait<2>();
+          else if (pending == 1) cp_async_wait<1>();
+          else cp_async_wait<0>();
+          __syncthreads();
+          fft_smem<T, NY, R, -1>(F0 + (size_t)f * C * cs + cf * cs, tf, tw);
+        }
+      }
+#pragma unroll 2
+      for (int i = 0; i < R; ++i) {
+        const int j = t + i * TPF;
+        xr[i] = czero<T>();
+        if (!kin) continue;
+        cplx<T> N = czero<T>();
+        for (int f = 0; f < nslot; ++f) {
+          const int slot = (f == 0) ? 0 : (f == 1 && m.hasB) ? 1 : 2;
+          N = N + slot_term(slot, j, F0[(size_t)f * C * cs + c * cs + swz<T>(j)]);
+        }
+        xr[i] = epilogue(0, j, N);
+      }
+    } else {
+      const cplx<T>* sol = static_cast<const cplx<T>*>(s.sol);
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        const int j = t + i * TPF;
+        xr[i] = (kin && kept(g, kr, j)) ? sol[ioff + (size_t)j * g.ldk + kr] : czero<T>();
+      }
+    }
+    if (!s.do_inv) return;
+    if ((int)blockIdx.x * C >= g.kcut) return;  // whole block aliased: W is never read there
+    // (q, u, v) of the next stage; each thread rewrites only the slots it read above
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int j = t + i * TPF;
+      const T lv = T(lidx(g, j)) * dky;
+      const T K2 = krT * krT + lv * lv;
+      const cplx<T> x = xr[i];
+      const cplx<T> p = psi_factor<T>(m.psi_kind, K2, ell2, m.mult, (size_t)j * g.ldk + (kin ? kr : 0)) * x;
+      F0[c * cs + swz<T>(j)] = sc * x;
+      F1[c * cs + swz<T>(j)] = sc * (lv * mul_mi(p));   // u = -i l psi
+      F2[c * cs + swz<T>(j)] = sc * (krT * mul_i(p));   // v =  i kr psi
+    }
+    __syncthreads();
+    fft_smem_group<T, NY, R, +1, 3>(F0 + cf * cs, C * cs, tf, tw);
+    if (kr < g.kcut) {
+#pragma unroll
+      for (int f = 0; f < 3; ++f) {
+        cplx<T>* Wf = W + (size_t)f * g.ny * g.ldw + kr;
+        const cplx<T>* Fe = F0 + (size_t)f * C * cs + c * cs;
+#pragma unroll
+        for (int i = 0; i < R; ++i) {
+          const int j = t + i * TPF;
+          Wf[(size_t)j * g.ldw] = Fe[swz<T>(j)];
+        }
+      }
+    }
+    return;
+  }
+
   if (s.do_fwd) {
     const cplx<T>* P = static_cast<const cplx<T>*>(b.P) + ib * g.bs_p;
     const int nslot = 1 + m.hasB + m.hasC;
     const int nseq = nl * nslot;
-    const T U0 = sel<T>(m.U0, m.U0_f, m.U0_l);
     // asynchronous copy of product field q = L * nslot + f into work buffer Fb
     auto issue = [&](int q, cplx<T>* Fb) {
       const int L = q / nslot, f = q - L * nslot;
@@ -174,12 +373,7 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? GF_MINBLOCKS_F32 : 1)
       for (int i = 0; i < R; ++i) {
         const int j = t + i * TPF;
         const cplx<T> v = Fc[swz<T>(j)];
-        cplx<T> d;
-        if (slot == 0) d = krT * mul_mi(v);                          // -i kr A
-        else if (slot == 1) d = (T(lidx(g, j)) * dky) * mul_mi(v);   // -i l B
-        else if (m.ql) d = (T(lidx(g, j)) * dky) * mul_mi(v);        // -i l C (zonal mean)
-        else d = czero<T>() - v;                                     // -C
-        if (m.ql && ((kr == 0) != (slot == 2))) d = czero<T>();      // mean: C only; eddies: A, B
+        const cplx<T> d = slot_term(slot, j, v);
         XL[j * C] = (f == 0) ? d : XL[j * C] + d;
       }
       __syncthreads();  // Fb is the target of the prefetch issued in the next iteration
@@ -189,99 +383,7 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? GF_MINBLOCKS_F32 : 1)
 #pragma unroll 2
       for (int i = 0; i < R; ++i) {
         const int j = t + i * TPF;
-        cplx<T> xn = czero<T>();
-        if (kin) {
-          const size_t ti = (size_t)j * g.ldk + kr;       // table index
-          const size_t si = ioff + (size_t)L * lstride + ti;  // state index
-          const bool keep = kept(g, kr, j);
-          cplx<T> N = XL[j * C];
-          if (m.Ueta) N = N - (U0 * krT) * mul_i(static_cast<const cplx<T>*>(m.etah)[ti]);
-          if (m.drag && L == nl - 1) N = N + Dp[ti];
-          cplx<T>* sol = static_cast<cplx<T>*>(s.sol);
-          const cplx<T> solm = keep ? sol[si] : czero<T>();
-          // forcing
-          if (s.fkind == FK_STATIC) {
-            N = N + static_cast<const cplx<T>*>(s.Fh)[si];
-          } else if (s.fkind == FK_HARMONIC) {
-            N = N + fscale * static_cast<const cplx<T>*>(s.Fh)[si];
-          } else if (s.fkind == FK_STOCH || s.fkind == FK_STOCH_PHASE) {
-            cplx<T> Fv;
-            if (s.draw) {
-              const T sp = static_cast<const T*>(s.fspec)[ti];
-              const uint64_t e = (uint64_t)kr + (uint64_t)g.nkr * ((uint64_t)j + (uint64_t)g.ny * L);
-              Fv = czero<T>();
-              const bool zero_mean = (s.fkind == FK_STOCH_PHASE) && kr == 0 && j == 0;
-              if (sp != T(0) && !zero_mean) Fv = sp * draw<T>(e, step, s.seed + ib, s.fkind == FK_STOCH_PHASE);
-              static_cast<cplx<T>*>(s.Fstore)[si] = Fv;
-              static_cast<cplx<T>*>(s.prevsol)[si] = solm;
-            } else {
-              Fv = static_cast<const cplx<T>*>(s.Fh)[si];
-            }
-            N = N + Fv;
-          }
-          auto Lmul = [&](cplx<T> x) { return mulc(ldc<T>(s.Ltab, ti, s.cplxL), x, s.cplxL); };
-          auto finish = [&](cplx<T> v) {
-            if (s.filtered) v = static_cast<const T*>(s.filt)[ti] * v;
-            sol[si] = v;
-            return v;
-          };
-          if (s.kind == SK_NOUT) {
-            static_cast<cplx<T>*>(s.acc)[si] = N;
-          } else if (s.kind == SK_FE) {
-            cplx<T> Rv = N;
-            if (s.hasL) Rv = Rv + Lmul(solm);
-            xn = finish(solm + dt * Rv);
-          } else if (s.kind == SK_RK4) {
-            cplx<T>* X = static_cast<cplx<T>*>(s.X);
-            cplx<T>* acc = static_cast<cplx<T>*>(s.acc);
-            cplx<T> Rv = N;
-            if (s.hasL) Rv = Rv + Lmul(s.stage == 1 ? solm : (keep ? X[si] : czero<T>()));
-            if (s.stage == 1) {
-              acc[si] = T(1.0 / 6.0) * Rv;
-              xn = solm + T(0.5) * dt * Rv;
-            } else if (s.stage < 4) {
-              acc[si] = acc[si] + T(1.0 / 3.0) * Rv;
-              xn = solm + (s.stage == 2 ? T(0.5) * dt : dt) * Rv;
-            } else {
-              xn = finish(solm + dt * (acc[si] + T(1.0 / 6.0) * Rv));
-            }
-            if (s.hasL && s.stage < 4) X[si] = keep ? xn : czero<T>();
-          } else if (s.kind == SK_ETDRK4) {
-            const int cx = s.cplxL;
-            cplx<T>* acc = static_cast<cplx<T>*>(s.acc);
-            if (s.stage == 1) {
-              xn = mulc(ldc<T>(s.e2, ti, cx), solm, cx) + mulc(ldc<T>(s.zeta, ti, cx), N, cx);
-              static_cast<cplx<T>*>(s.s1)[si] = keep ? xn : czero<T>();
-              static_cast<cplx<T>*>(s.N1)[si] = N;
-              acc[si] = mulc(ldc<T>(s.alpha, ti, cx), N, cx);
-            } else if (s.stage == 2) {
-              xn = mulc(ldc<T>(s.e2, ti, cx), solm, cx) + mulc(ldc<T>(s.zeta, ti, cx), N, cx);
-              acc[si] = acc[si] + T(2) * mulc(ldc<T>(s.beta, ti, cx), N, cx);
-            } else if (s.stage == 3) {
-              const cplx<T> s1 = static_cast<const cplx<T>*>(s.s1)[si];
-              const cplx<T> n1 = static_cast<const cplx<T>*>(s.N1)[si];
-              xn = mulc(ldc<T>(s.e2, ti, cx), s1, cx) + mulc(ldc<T>(s.zeta, ti, cx), T(2) * N - n1, cx);
-              acc[si] = acc[si] + T(2) * mulc(ldc<T>(s.beta, ti, cx), N, cx);
-            } else {
-              xn = finish(mulc(ldc<T>(s.e, ti, cx), solm, cx) + acc[si] + mulc(ldc<T>(s.gamma, ti, cx), N, cx));
-            }
-          } else {  // AB3
-            cplx<T> Rv = N;
-            if (s.hasL) Rv = Rv + Lmul(solm);
-            cplx<T> upd;
-            if (ab3_euler) {
-              upd = Rv;
-            } else {
-              const cplx<T> r1 = static_cast<const cplx<T>*>(s.Rm1)[si];
-              const cplx<T> r2 = static_cast<const cplx<T>*>(s.Rm2)[si];
-              upd = T(23.0 / 12.0) * Rv - T(16.0 / 12.0) * r1 + T(5.0 / 12.0) * r2;
-            }
-            static_cast<cplx<T>*>(s.Rout)[si] = Rv;
-            xn = finish(solm + dt * upd);
-          }
-          if (!keep) xn = czero<T>();
-        }
-        XL[j * C] = xn;
+        XL[j * C] = kin ? epilogue(L, j, XL[j * C]) : czero<T>();
       }
     }
   } else {
@@ -330,8 +432,6 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? GF_MINBLOCKS_F32 : 1)
     }
   }
   // y-direction inverse FFT of (q, u, v) for every layer
-  cplx<T>* W = static_cast<cplx<T>*>(b.W) + ib * g.bs_w;
-  const T sc = sel<T>(g.inv_nxny, g.inv_nxny_f, g.inv_nxny_l);
   for (int L = 0; L < nl; ++L) {
     for (int f = 0; f < 3; ++f) {
       cplx<T>* Fb = ((L * 3 + f) & 1) ? F1 : F0;  // alternate so stores of one field overlap the next
@@ -373,7 +473,8 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? GF_MINBLOCKS_F32 : 1)
 
 // shared-memory bytes of col_stage_kernel for C columns with column stride cs
 __host__ __forceinline__ size_t col_stage_smem(int NY, int C, int cs, int nl, size_t elem) {
-  return ((size_t)2 * C * cs + (size_t)nl * NY * C * (nl > 1 ? 2 : 1)) * elem;
+  if (nl == 1) return (size_t)3 * C * cs * elem;  // F0, F1, F2 (cs >= NY: also holds the general path's Xs)
+  return ((size_t)2 * C * cs + (size_t)nl * NY * C * 2) * elem;
 }
 
 // --------------------------------------------------------------------------- row kernel
@@ -409,7 +510,7 @@ __device__ __forceinline__ void unpack_store(const cplx<T>* buf, int k, int NX, 
 }
 
 template <class T, int NX, int R>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) row_nl_kernel(Geom g, ModArgs m, Bufs b, int B) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? GF_ROW_MINBLOCKS_F32 : 1) row_nl_kernel(Geom g, ModArgs m, Bufs b, int B) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int TPF = NX / R;
   constexpr int M = NX / 2;
@@ -439,7 +540,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) row_nl_kernel(Geo
       }
     }
     __syncthreads();
-    for (int f = 0; f < 3; ++f) fft_smem<T, NX, R, +1>(buf + f * PS, t, tw);
+    fft_smem_group<T, NX, R, +1, 3>(buf, PS, t, tw);
     // physical-space products on the packed pairs
     const T Ua = U1D ? U1D[L * g.ny + j0] : T(0), Ub = U1D ? U1D[L * g.ny + j0 + 1] : T(0);
     const T Qa = Qy1D ? Qy1D[L * g.ny + j0] : T(0), Qb = Qy1D ? Qy1D[L * g.ny + j0 + 1] : T(0);
@@ -483,7 +584,9 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) row_nl_kernel(Geo
       else buf[PS + px] = Cv;
     }
     __syncthreads();
-    for (int f = 0; f < nslot; ++f) fft_smem<T, NX, R, -1>(buf + f * PS, t, tw);
+    if (nslot == 2) fft_smem_group<T, NX, R, -1, 2>(buf, PS, t, tw);
+    else if (nslot == 3) fft_smem_group<T, NX, R, -1, 3>(buf, PS, t, tw);
+    else fft_smem<T, NX, R, -1>(buf, t, tw);
     for (int f = 0; f < nslot; ++f) {
       cplx<T>* Pa = P + ((size_t)f * nl + L) * g.ny * g.ldk + (size_t)j0 * g.ldk;
 #pragma unroll
