@@ -192,7 +192,7 @@ def _events(n):
     return [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
 
 
-def time_arm(w, T, steps, warmup, flush, with_e2e, precision=None, graph=True, tune=True):
+def time_arm(w, T, steps, warmup, flush, with_e2e, precision=None, graph=True, tune=True, shape=None):
     """Run one precision arm: warm-up, K timed steps launched one gf_step at a time (CUDA
     events on the legacy default stream, which orders with the library's blocking stream;
     L2 flushed between steps) with the library's per-kernel event timing on, then K steps
@@ -203,7 +203,10 @@ def time_arm(w, T, steps, warmup, flush, with_e2e, precision=None, graph=True, t
     import gfcuda
     prob = make_problem(w, T, precision)
     set_initial_state(prob, w)
-    shape = prob.autotune(reps=3) if tune else None  # the library's launch-shape autotuner
+    if shape is not None:
+        prob.launch_shape = shape
+    elif tune:
+        shape = prob.autotune(reps=3)  # the library's launch-shape autotuner
     gfcuda.stepforward(prob, warmup)
     prob.synchronize()
     lib, ctx = prob._lib, prob._ctx
@@ -235,8 +238,8 @@ def time_arm(w, T, steps, warmup, flush, with_e2e, precision=None, graph=True, t
         res["ms_per_step_graph"] = e0.elapsed_time(e1) / steps
     res["sol"] = prob.sol   # the state after the same number of steps in every arm
     if with_e2e:
-        shape = prob.spec_shape
-        hin = torch.empty(int(np.prod(shape)) * 2, dtype=torch.float32 if T == np.float32 else torch.float64,
+        sshape = prob.spec_shape
+        hin = torch.empty(int(np.prod(sshape)) * 2, dtype=torch.float32 if T == np.float32 else torch.float64,
                           pin_memory=True)
         hout = torch.empty_like(hin, pin_memory=True)
         hin_np, hout_np = hin.numpy(), hout.numpy()
@@ -638,7 +641,9 @@ def run_single(args):
     elif w is CONFIG3:
         r = time_adjoint(flush, T, reps=1)
     else:
-        r = time_arm(w, T, args.steps, args.warmup, flush, with_e2e=False, precision=prec, tune=not args.no_tune)
+        shape = tuple(int(v) for v in args.shape.split(",")) if args.shape else None
+        r = time_arm(w, T, args.steps, args.warmup, flush, with_e2e=False, precision=prec,
+                     tune=not (args.no_tune or shape), shape=shape)
         r.pop("sol")
         r["pt_steps_per_s"] = points(w) / (r["ms_per_step"] * 1e-3)
     r["workload"] = args.single
@@ -654,6 +659,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--single", choices=sorted(SINGLE), help="time one arm only (profiling mode)")
     ap.add_argument("--no-tune", action="store_true", help="single mode: built-in block shapes, no autotuner")
+    ap.add_argument("--shape", help="single mode: launch shape row_radix,row_pairs,col_radix,col_columns "
+                                    "instead of the autotuner (e.g. a shape it chose, for profiling)")
     args = ap.parse_args()
     if args.single:
         return run_single(args)

@@ -1,6 +1,7 @@
 // C ABI of libgfcuda: problem construction, state transfer, the time-step loop and the
 // diagnostics.  The kernels live in gf_kernels.cuh (instantiated by gf_f32.cu/gf_f64.cu);
 // this file holds the host-side orchestration and the FP64 setup kernels.
+#include <atomic>
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -79,6 +80,12 @@ struct gf_ctx {
     int64_t step_end = 0;
   } adj;
   void* row_phys = nullptr;  // forward row kernels also store (q + eta, u, v) here when set
+  // identity and graph generation (an ensemble graph records the members it was built for)
+  uint64_t uid = 0, gen = 0;
+  cudaGraphExec_t egraph = nullptr;                    // ensemble graph held by its first member
+  std::vector<std::pair<uint64_t, uint64_t>> emembers;  // (uid, gen) of its members
+  int eG = 0;
+  cudaEvent_t order_ev = nullptr;  // orders this context's stream with an ensemble graph launch
   std::string err;
 };
 
@@ -743,6 +750,8 @@ extern "C" int gf_create(const gf_config* cfg, void* stream, gf_ctx** out) {
   if (k.forcing_kind < 0 || k.forcing_kind > 4) return fail(nullptr, GF_ERR_ARG, "unknown forcing kind");
   if (k.batch < 0 || k.batch > 65535) return fail(nullptr, GF_ERR_ARG, "batch must be in [0, 65535]");
   gf_ctx* c = new gf_ctx();
+  static std::atomic<uint64_t> next_uid{1};
+  c->uid = next_uid++;
   c->cfg = k;
   c->stream = (cudaStream_t)stream;
   if (!c->stream) {
@@ -771,6 +780,8 @@ extern "C" int gf_destroy(gf_ctx* c) {
   for (auto e : c->ev_free) cudaEventDestroy(e);
   for (auto& u : c->ev_used) { cudaEventDestroy(u.second.first); cudaEventDestroy(u.second.second); }
   for (auto& gx : c->gexec) if (gx) cudaGraphExecDestroy(gx);
+  if (c->egraph) cudaGraphExecDestroy(c->egraph);
+  if (c->order_ev) cudaEventDestroy(c->order_ev);
   for (void* p : c->adj.mem) cudaFree(p);
   if (c->own_stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -1229,6 +1240,8 @@ static int one_step(gf_ctx* c) {
 static void drop_graphs(gf_ctx* c) {
   for (auto& gx : c->gexec)
     if (gx) { cudaGraphExecDestroy(gx); gx = nullptr; }
+  if (c->egraph) { cudaGraphExecDestroy(c->egraph); c->egraph = nullptr; }
+  c->gen++;
 }
 
 // Capture G steps (starting from the current AB3 ring phase) into an executable graph.
@@ -1286,12 +1299,95 @@ extern "C" int gf_step(gf_ctx* c, int64_t nsteps) {
   return GF_OK;
 }
 
-// Several independent problems (e.g. the size classes of an ensemble) stepped together: each
-// context's launches go to its own stream, so the GPU runs them concurrently.
+// Several independent problems (e.g. the size classes of an ensemble) stepped together.
+// When every context replays captured graphs of the same length G (not AB3, profiling off),
+// G steps of all of them are captured as ONE graph on the first context's stream -- the
+// other contexts' streams fork from it and join back, so their kernels run concurrently --
+// and replayed with one launch; otherwise each context steps on its own stream.
+static int ensemble_capture(gf_ctx* const* ctxs, int32_t n, int G) {
+  gf_ctx* o = ctxs[0];
+  std::vector<cudaEvent_t> ev;
+  auto cleanup = [&]() { for (auto e : ev) cudaEventDestroy(e); };
+  for (int32_t i = 0; i < 2 * n; ++i) {
+    cudaEvent_t e;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) { cleanup(); return fail(o, GF_ERR_CUDA, "event"); }
+    ev.push_back(e);
+  }
+  struct Saved { double t, fs; int64_t step, launches; };
+  std::vector<Saved> sv(n);
+  for (int32_t i = 0; i < n; ++i) sv[i] = {ctxs[i]->t, ctxs[i]->last_fscale, ctxs[i]->step, ctxs[i]->launches};
+  cudaError_t e = cudaStreamBeginCapture(o->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) { cleanup(); return fail(o, GF_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e)); }
+  int rc = GF_OK;
+  cudaEventRecord(ev[0], o->stream);
+  for (int32_t i = 1; i < n; ++i) cudaStreamWaitEvent(ctxs[i]->stream, ev[0], 0);   // fork
+  for (int32_t i = 0; i < n && rc == GF_OK; ++i)
+    for (int k = 0; k < G && rc == GF_OK; ++k) {
+      rc = enqueue_step(ctxs[i]);
+      host_advance(ctxs[i]);
+    }
+  for (int32_t i = 1; i < n; ++i) {                                                 // join
+    cudaEventRecord(ev[n + i], ctxs[i]->stream);
+    cudaStreamWaitEvent(o->stream, ev[n + i], 0);
+  }
+  cudaGraph_t graph = nullptr;
+  e = cudaStreamEndCapture(o->stream, &graph);
+  for (int32_t i = 0; i < n; ++i) {
+    ctxs[i]->t = sv[i].t; ctxs[i]->last_fscale = sv[i].fs; ctxs[i]->step = sv[i].step; ctxs[i]->launches = sv[i].launches;
+  }
+  cleanup();
+  if (rc != GF_OK) { if (graph) cudaGraphDestroy(graph); return rc; }
+  if (e != cudaSuccess) return fail(o, GF_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  if (o->egraph) { cudaGraphExecDestroy(o->egraph); o->egraph = nullptr; }
+  e = cudaGraphInstantiate(&o->egraph, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) { o->egraph = nullptr; return fail(o, GF_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e)); }
+  o->emembers.clear();
+  for (int32_t i = 0; i < n; ++i) o->emembers.push_back({ctxs[i]->uid, ctxs[i]->gen});
+  o->eG = G;
+  return GF_OK;
+}
+
 extern "C" int gf_ensemble_step(gf_ctx* const* ctxs, int32_t n, int64_t nsteps) {
   if (!ctxs || n <= 0 || nsteps < 0) return fail(nullptr, GF_ERR_ARG, "gf_ensemble_step: bad arguments");
-  for (int32_t i = 0; i < n; ++i)
+  for (int32_t i = 0; i < n; ++i) {
     if (!ctxs[i]) return fail(nullptr, GF_ERR_ARG, "gf_ensemble_step: null context");
+    for (int32_t k = 0; k < i; ++k)
+      if (ctxs[k] == ctxs[i]) return fail(nullptr, GF_ERR_ARG, "gf_ensemble_step: a context appears twice");
+    if (ctxs[i]->cfg.forcing_kind >= GF_FORCING_STOCHASTIC && !ctxs[i]->fspec)
+      return fail(ctxs[i], GF_ERR_STATE, "no forcing spectrum");
+  }
+  int G = ctxs[0]->graph_steps;
+  bool one_graph = n > 1 && G > 0;
+  for (int32_t i = 0; i < n; ++i)
+    one_graph = one_graph && ctxs[i]->graph_steps == G && ctxs[i]->kind != SK_AB3 && !ctxs[i]->profiling;
+  gf_ctx* o = ctxs[0];
+  while (one_graph && nsteps >= G) {
+    for (int32_t i = 0; i < n; ++i)
+      if (int r = ensure_W(ctxs[i])) { g_create_error = ctxs[i]->err; return r; }
+    bool same = o->egraph && o->eG == G && (int32_t)o->emembers.size() == n;
+    for (int32_t i = 0; same && i < n; ++i)
+      same = o->emembers[i].first == ctxs[i]->uid && o->emembers[i].second == ctxs[i]->gen;
+    if (!same)
+      if (int r = ensemble_capture(ctxs, n, G)) { g_create_error = o->err; return r; }
+    // the graph (on the first stream) waits for the members' earlier work and their streams
+    // wait for the graph, so that later calls on any member are ordered after it
+    for (int32_t i = 0; i < n; ++i)
+      if (!ctxs[i]->order_ev) GF_CUDA(ctxs[i], cudaEventCreateWithFlags(&ctxs[i]->order_ev, cudaEventDisableTiming));
+    for (int32_t i = 1; i < n; ++i) {
+      GF_CUDA(ctxs[i], cudaEventRecord(ctxs[i]->order_ev, ctxs[i]->stream));
+      GF_CUDA(o, cudaStreamWaitEvent(o->stream, ctxs[i]->order_ev, 0));
+    }
+    const cudaError_t e = cudaGraphLaunch(o->egraph, o->stream);
+    if (e != cudaSuccess) return fail(o, GF_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(e));
+    GF_CUDA(o, cudaEventRecord(o->order_ev, o->stream));
+    for (int32_t i = 1; i < n; ++i) GF_CUDA(ctxs[i], cudaStreamWaitEvent(ctxs[i]->stream, o->order_ev, 0));
+    for (int32_t i = 0; i < n; ++i) {
+      for (int k = 0; k < G; ++k) host_advance(ctxs[i]);
+      ctxs[i]->launches += (int64_t)G * (2 * ctxs[i]->nstages + 1);
+    }
+    nsteps -= G;
+  }
   for (int32_t i = 0; i < n; ++i)
     if (int r = gf_step(ctxs[i], nsteps)) {
       g_create_error = ctxs[i]->err;

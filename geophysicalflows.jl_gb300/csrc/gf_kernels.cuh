@@ -24,7 +24,10 @@
 // Minimum resident blocks per SM requested for the FP32 step kernels (register budget):
 // column kernel (512 threads) and row kernel (256 threads).
 #ifndef GF_MINBLOCKS_F32
-#define GF_MINBLOCKS_F32 1
+#define GF_MINBLOCKS_F32 1        // column lengths >= 1024
+#endif
+#ifndef GF_MINBLOCKS_SMALL_F32
+#define GF_MINBLOCKS_SMALL_F32 2  // shorter columns (small grids, ensembles: many small blocks)
 #endif
 #ifndef GF_ROW_MINBLOCKS_F32
 #define GF_ROW_MINBLOCKS_F32 3
@@ -101,7 +104,7 @@ __device__ __forceinline__ void psi_all(const ModArgs& m, int nl, T K2, const cp
 // are prefetched with cp.async into one while the other is transformed), Xs (N, then the
 // next stage X; nl x NY x C interleaved, thread-owned) and, for more than one layer, Ps.
 template <class T, int NY, int R>
-__global__ void __launch_bounds__(512, sizeof(T) == 4 ? GF_MINBLOCKS_F32 : 1)
+__global__ void __launch_bounds__(512, sizeof(T) == 4 ? (NY >= 1024 ? GF_MINBLOCKS_F32 : GF_MINBLOCKS_SMALL_F32) : 1)
     col_stage_kernel(Geom g, ModArgs m, StepArgs s, Bufs b, int C) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T eig[MAXL + 2 * MAXL * MAXL];

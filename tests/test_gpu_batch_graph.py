@@ -143,3 +143,31 @@ def test_autotune_keeps_state_and_results(T, stepper):
         assert rel(r.sol, q.sol) <= (1e-5 if T == np.float32 else 1e-13)
     with pytest.raises(ValueError):
         p.launch_shape = (3, 1, 8, 1)
+
+
+def test_ensemble_graph_ordering_remainders_and_fallback():
+    """one ensemble graph over several contexts: results equal per-context stepping for step
+    counts that are not multiples of the graph length, calls on any member after it see its
+    result, and contexts that cannot share a graph (AB3) step on their own streams"""
+    def make(n, B, stepper, seed):
+        spec = O.ring_forcing_spectrum(O.Grid(n), 8.0, 1.5, 1e-3)
+        return TD.Problem("GPU", nx=n, dt=0.01, nu=1e-4, nnu=1, stepper=stepper, T=np.float32, batch=B,
+                          forcing=Forcing("stochastic", spectrum=spec, seed=seed))
+    for steppers in (("FilteredRK4", "FilteredRK4", "ETDRK4"), ("FilteredRK4", "AB3", "ETDRK4")):
+        probs = [make(n, B, st, 10 * n) for (n, B), st in zip(((64, 3), (128, 2), (32, 5)), steppers)]
+        refs = [make(n, B, st, 10 * n) for (n, B), st in zip(((64, 3), (128, 2), (32, 5)), steppers)]
+        for p, q in zip(probs, refs):
+            z = np.stack([zeta0(p.grid.nx, i) for i in range(p.batch)])
+            TD.set_zeta(p, z)
+            TD.set_zeta(q, z)
+        ensemble_step(probs, 11)           # 2 graph replays + 3 single steps
+        for p in probs[1:]:
+            TD.set_zeta(p, p.invtransform(p.sol))   # work issued on a member's stream after it
+        ensemble_step(probs, 5)
+        for k, q in enumerate(refs):
+            stepforward(q, 11)
+            if k > 0:
+                TD.set_zeta(q, q.invtransform(q.sol))
+            stepforward(q, 5)
+        for p, q in zip(probs, refs):
+            assert rel(p.sol, q.sol) <= 1e-6 and p.clock.step == q.clock.step == 16
