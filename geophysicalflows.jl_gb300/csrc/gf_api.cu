@@ -1299,6 +1299,36 @@ extern "C" int gf_step(gf_ctx* c, int64_t nsteps) {
   return GF_OK;
 }
 
+// stepforward! with an arbitrary host calcF!: before every stage the callback fills F-hat
+// (user layout, the context's element type) for that stage's time, and the library uploads
+// it and runs the stage; each stage waits for the host, so this is the slow, general path.
+extern "C" int gf_step_callback(gf_ctx* c, int64_t nsteps, gf_forcing_fn fn, void* user) {
+  if (!c || nsteps < 0 || !fn) return GF_ERR_ARG;
+  if (c->cfg.forcing_kind != GF_FORCING_STATIC)
+    return fail(c, GF_ERR_STATE, "gf_step_callback needs a context created with forcing_kind = GF_FORCING_STATIC");
+  const Geom& g = c->g;
+  const size_t elems = (size_t)g.nl * g.ny * g.nkr * g.nb;
+  std::vector<char> host(elems * (c->prec == GF_DF64 ? 16 : c->cb));
+  const double dt = c->cfg.dt;
+  for (int64_t k = 0; k < nsteps; ++k) {
+    if (int r = ensure_W(c)) return r;
+    for (int stg = 1; stg <= c->nstages; ++stg) {
+      const double ts = c->t + (c->nstages == 4 ? (stg == 1 ? 0.0 : stg == 4 ? dt : 0.5 * dt) : 0.0);
+      std::memset(host.data(), 0, host.size());
+      if (int r = fn(ts, c->step, stg, host.data(), user)) return fail(c, GF_ERR_ARG, "forcing callback returned " + std::to_string(r));
+      if (int r = copy_spec_in(c, c->Fh, host.data(), GF_HOST)) return r;
+      StepArgs s = stage_args(c, stg, ts);
+      s.clk = c->dclk;
+      if (int r = launch_stage(c, s, 1)) return r;
+    }
+    advance_clock_kernel<<<1, 32, 0, c->stream>>>(c->dclk, dt, c->cfg.forcing_omega, c->cfg.forcing_phase, 0, c->nstages);
+    GF_CUDA(c, cudaGetLastError());
+    c->launches++;
+    host_advance(c);
+  }
+  return GF_OK;
+}
+
 // Several independent problems (e.g. the size classes of an ensemble) stepped together.
 // When every context replays captured graphs of the same length G (not AB3, profiling off),
 // G steps of all of them are captured as ONE graph on the first context's stream -- the

@@ -14,6 +14,8 @@ F32, F64, DF64 = 0, 1, 2
 FORCING = {None: 0, "static": 1, "harmonic": 2, "stochastic": 3, "stochastic_phase": 4}
 HOST, DEVICE = 0, 1
 LOSS_KINETIC_ENERGY = 0
+# int fn(double t, int64_t step, int32_t stage, void* Fh, void* user)
+FORCING_FN = C.CFUNCTYPE(C.c_int, C.c_double, C.c_int64, C.c_int32, C.c_void_p, C.c_void_p)
 FIELD_Q, FIELD_PSI, FIELD_U, FIELD_V = 0, 1, 2, 3
 FIELD_ZETA_MEAN, FIELD_PSI_MEAN, FIELD_U_MEAN = 4, 5, 6
 
@@ -24,7 +26,7 @@ EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_abi_version", "gf_get
            "gf_rfft2_noalloc", "gf_get_batch", "gf_set_graph_steps", "gf_ensemble_step",
            "gf_peakedisotropicspectrum", "gf_get_filter", "gf_adjoint_setup", "gf_adjoint_forward",
            "gf_adjoint_backward", "gf_grad", "gf_autotune", "gf_set_launch_shape", "gf_get_launch_shape",
-           "gf_fluxes"]
+           "gf_fluxes", "gf_step_callback"]
 
 
 class gf_config(C.Structure):
@@ -95,6 +97,7 @@ def load(path=None):
         "gf_grad": ([vp, C.c_int, vp, vp, C.POINTER(dbl), C.c_int], C.c_int),
         "gf_autotune": ([vp, i32, C.POINTER(i32)], C.c_int),
         "gf_fluxes": ([vp, vp, vp], C.c_int),
+        "gf_step_callback": ([vp, i64, FORCING_FN, vp], C.c_int),
         "gf_set_launch_shape": ([vp, C.POINTER(i32)], C.c_int),
         "gf_get_launch_shape": ([vp, C.POINTER(i32)], C.c_int),
     }

@@ -79,12 +79,19 @@ class Clock:
 
 
 class Forcing:
-    """Device-side forms of the reference's calcF! callbacks (see include/gfcuda.h)."""
+    """Device-side forms of the reference's calcF! callbacks (see include/gfcuda.h), or
+    kind="callback" with calcF(Fh, sol, t, clock, vars, params, grid): an arbitrary host
+    calcF! called before every stage with its time (sol is None: the state stays on the
+    device); it fills the half-spectrum Fh in place.  The callback path waits for the host at
+    every stage (the library's gf_step_callback)."""
 
-    def __init__(self, kind=None, Fh=None, spectrum=None, omega=0.0, phase=0.0, seed=0):
-        if kind not in A.FORCING:
+    def __init__(self, kind=None, Fh=None, spectrum=None, omega=0.0, phase=0.0, seed=0, calcF=None):
+        if kind not in A.FORCING and kind != "callback":
             raise ValueError(f"unknown forcing kind {kind}")
+        if kind == "callback" and calcF is None:
+            raise ValueError("kind='callback' needs calcF")
         self.kind, self.Fh, self.spectrum, self.omega, self.phase, self.seed = kind, Fh, spectrum, omega, phase, seed
+        self.calcF = calcF
 
     @property
     def stochastic(self):
@@ -130,7 +137,7 @@ class Problem:
         cfg.stepper = A.STEPPERS[stepper]
         cfg.nx, cfg.ny, cfg.nlayers = nx, ny, nlayers
         cfg.Lx, cfg.Ly, cfg.dt, cfg.aliased_fraction = Lx, Ly, dt, aliased_fraction
-        cfg.forcing_kind = A.FORCING[self.forcing.kind]
+        cfg.forcing_kind = A.FORCING["static" if self.forcing.kind == "callback" else self.forcing.kind]
         cfg.seed = int(self.forcing.seed)
         self.batch = int(batch)
         cfg.batch = self.batch
@@ -303,6 +310,9 @@ def stepforward(prob, *args):
         diags, n = None, int(args[0])
     else:
         diags, n = args[0], int(args[1])
+    if prob.forcing.kind == "callback":
+        _step_callback(prob, n, diags)
+        return
     if not diags:
         prob._c(prob._lib.gf_step(prob._ctx, n))
         return
@@ -324,6 +334,41 @@ def stepforward(prob, *args):
         return
     for _ in range(n):
         prob._c(prob._lib.gf_step(prob._ctx, 1))
+        for d in diags:
+            d.increment()
+
+
+class _StageClock:
+    """clock seen by a callback calcF: t of the stage, the step number and dt"""
+
+    def __init__(self, t, step, dt):
+        self.t, self.step, self.dt = t, step, dt
+
+
+def _step_callback(prob, n, diags=None):
+    g = prob.grid
+    shape = prob.spec_shape
+    nel = int(np.prod(shape))
+    calcF = prob.forcing.calcF
+    err = []
+
+    def fn(t, step, stage, ptr, user):
+        try:
+            Fh = np.ctypeslib.as_array(C.cast(ptr, C.POINTER(C.c_float if prob.T == np.float32 else C.c_double)),
+                                       shape=(2 * nel,)).view(prob.CT).reshape(shape)
+            calcF(Fh, None, t, _StageClock(t, step, prob.clock.dt), prob.vars, getattr(prob, "params", None), g)
+            return 0
+        except Exception as e:  # reported after the library call returns
+            err.append(e)
+            return 1
+
+    cb = A.FORCING_FN(fn)
+    diags = (diags if isinstance(diags, (list, tuple)) else [diags]) if diags else []
+    for _ in range(n if diags else 1):
+        code = prob._lib.gf_step_callback(prob._ctx, 1 if diags else n, cb, None)
+        if err:
+            raise err[0]
+        prob._c(code)
         for d in diags:
             d.increment()
 

@@ -71,3 +71,37 @@ def random_topography(grid, kmax, amp, seed):
     eh = np.where((K <= kmax) & (grid.Krsq > 0), z, 0)
     eta = np.fft.irfft2(eh, s=(grid.ny, grid.nx))
     return amp * eta / np.max(np.abs(eta))
+
+
+def radialspectrum(fh, grid, n=None, m=None, refinement=2):
+    """Azimuthal integral of a half-spectrum array fh (ny, nx/2+1) in the manner of
+    FourierFlows.radialspectrum (called at test/test_utils.jl:9 and in the decaying-turbulence
+    example): fh is extended to the full (Hermitian) plane and centred, interpolated
+    bilinearly on a polar grid of n radii in [0, min(max|k|, max|l|)] and m angles in
+    [-pi, pi), and integrated, F(rho) = rho * sum_theta f(rho, theta) dtheta.  n and m default
+    to refinement * max(nx, ny).  Returns (rho, F).  A host-side post-processing helper."""
+    fh = np.asarray(fh)
+    nx, ny = grid.nx, grid.ny
+    n = refinement * max(nx, ny) if n is None else int(n)
+    m = refinement * max(nx, ny) if m is None else int(m)
+    full = np.zeros((ny, nx), dtype=np.result_type(fh, np.complex128))
+    full[:, : grid.nkr] = fh
+    jj = (-np.arange(ny)) % ny
+    for i in range(1, nx - grid.nkr + 1):      # negative kx from the Hermitian symmetry
+        full[:, nx - i] = np.conj(fh[jj, i])
+    fs = np.fft.fftshift(full)
+    dk, dl = 2 * np.pi / grid.Lx, 2 * np.pi / grid.Ly
+    kmax, lmax = dk * (nx // 2 - 1), dl * (ny // 2 - 1)
+    rho = np.linspace(0.0, min(kmax, lmax), n)
+    theta = -np.pi + 2 * np.pi * np.arange(m) / m
+    kx = rho[:, None] * np.cos(theta)[None, :]
+    ly = rho[:, None] * np.sin(theta)[None, :]
+    # fractional indices into the centred array (index nx//2 is k = 0)
+    fx, fy = kx / dk + nx // 2, ly / dl + ny // 2
+    x0, y0 = np.floor(fx).astype(int), np.floor(fy).astype(int)
+    ax, ay = fx - x0, fy - y0
+    x1, y1 = np.minimum(x0 + 1, nx - 1), np.minimum(y0 + 1, ny - 1)
+    f = ((1 - ax) * (1 - ay) * fs[y0, x0] + ax * (1 - ay) * fs[y0, x1]
+         + (1 - ax) * ay * fs[y1, x0] + ax * ay * fs[y1, x1])
+    F = rho * f.sum(axis=1) * (2 * np.pi / m)
+    return rho, F

@@ -240,6 +240,16 @@ int gf_set_forcing(gf_ctx* ctx, const void* data, int where);
 /* Block until the context's stream has finished. */
 int gf_synchronize(gf_ctx* ctx);
 
+/* stepforward!(prob, nsteps) with an arbitrary host calcF! (calcF!(Fh, sol, t, clock, vars, params,
+ * grid), e.g. examples/singlelayerqg_betaforced.jl:86-90): before every stage the library calls
+ * fn(t_stage, clock.step, stage (1-based), Fh, user); fn fills Fh in the layout of gf_set_forcing
+ * (host memory, the context's element type, zeroed before the call) and returns 0; the library
+ * uploads it and runs the stage with N += Fh.  Each stage waits for the host: this is the slow,
+ * general escape hatch beside the device forcing kinds.  The context must have been created with
+ * forcing_kind = GF_FORCING_STATIC.  A non-zero return from fn stops the call with GF_ERR_ARG. */
+typedef int (*gf_forcing_fn)(double t, int64_t step, int32_t stage, void* Fh, void* user);
+int gf_step_callback(gf_ctx* ctx, int64_t nsteps, gf_forcing_fn fn, void* user);
+
 /* ---- launch-shape autotuner (no reference counterpart) ----------------------------------
  * gf_autotune times the step kernels of this context at every candidate launch shape --
  * column kernel: FFT radix (FP32: 4, 8, 16; otherwise 8) x kr columns per block; row kernel:

@@ -64,3 +64,36 @@ def test_streamed_diagnostics_match_per_step_values():
         assert abs(E[k] - r.energy()) <= 1e-12 * r.energy()
     assert E.steps[-1] == ns and E.t[-1] == q.clock.t == p.clock.t
     assert np.array_equal(p.sol, q.sol)
+
+
+@pytest.mark.parametrize("stepper", ["RK4", "ETDRK4", "AB3"])
+def test_host_calcF_callback_matches_device_harmonic_forcing(stepper):
+    """an arbitrary host calcF! called per stage (gf_step_callback) gives the same steps as the
+    device's harmonic forcing kind F cos(omega t + phase) evaluated at the stage times"""
+    n, dt = 64, 0.01
+    g = O.Grid(n)
+    x, y = g.gridpoints()
+    Fh0 = O.rfft2(0.1 * np.cos(4 * x) * np.cos(5 * y))
+    kw = dict(nx=n, dt=dt, nu=1e-3, nnu=1, stepper=stepper)
+    times = []
+
+    def calcF(Fh, sol, t, clock, vars, params, grid):
+        times.append(t)
+        Fh[...] = Fh0 * np.cos(2.0 * t + 0.3)
+
+    p = TD.Problem("GPU", forcing=gfcuda.Forcing("callback", calcF=calcF), **kw)
+    q = TD.Problem("GPU", forcing=gfcuda.Forcing("harmonic", Fh=Fh0, omega=2.0, phase=0.3), **kw)
+    z = O.peakedisotropicspectrum(g, 4, 0.5, seed=4)
+    TD.set_zeta(p, z)
+    TD.set_zeta(q, z)
+    gfcuda.stepforward(p, 7)
+    gfcuda.stepforward(q, 7)
+    assert O.rel_l2(p.sol, q.sol) <= 1e-14
+    nst = 1 if stepper == "AB3" else 4
+    assert len(times) == 7 * nst and abs(times[1 if nst == 4 else 0] - (0.5 * dt if nst == 4 else 0.0)) < 1e-15
+
+    def bad(Fh, *a):
+        raise RuntimeError("boom")
+    r = TD.Problem("GPU", forcing=gfcuda.Forcing("callback", calcF=bad), **kw)
+    with pytest.raises(RuntimeError, match="boom"):
+        gfcuda.stepforward(r, 1)
