@@ -69,13 +69,17 @@ struct gf_ctx {
   struct Adjoint {
     bool ready = false, forward_done = false;
     int64_t nsteps = 0;
-    int every = 1, nseg = 0;
+    int every = 1, nseg = 0;   // recomputation unit (steps whose forward fields are kept at once), units
+    int snaps = 0;             // state snapshot slots (slot 0: the initial state)
     std::vector<void*> mem;
     void *ckpt = nullptr, *phys = nullptr, *ub = nullptr, *n1acc = nullptr, *xaacc = nullptr, *x1acc = nullptr;
     void *ubar_in = nullptr, *ubar_out = nullptr, *Wb = nullptr, *Pb = nullptr, *etab = nullptr;
     void *final_state = nullptr, *tmp = nullptr;
-    std::vector<double> ck_t;
+    std::vector<double> ck_t;           // per slot
     std::vector<int64_t> ck_step;
+    std::vector<int> split;             // binomial schedule: split[n * snaps + s]
+    std::vector<std::pair<int, int>> spine;  // (unit, slot) snapshots taken by the forward pass
+    int64_t forward_units = 0;          // unit advances the last reverse sweep added (recomputation)
     double t_end = 0;
     int64_t step_end = 0;
   } adj;
@@ -1750,9 +1754,40 @@ static void* adj_alloc(gf_ctx* c, size_t bytes) {
   return p;
 }
 
+// Binomial (Griewank) checkpoint schedule over units of `every` steps: reversing n units whose
+// first state is stored, with s free snapshot slots, costs
+//   C(n, s) = min_{1<=m<n} [ m + C(n - m, s - 1) + C(m, s) ],  C(1, s) = 0,
+//   C(n, 0) = n (n - 1) / 2 (advance from the start for each unit, last first),
+// in unit advances (every unit is also recomputed once with its forward fields kept).  The
+// minimising splits are the binomial schedule; with n - 1 free slots it stores every unit
+// boundary in one forward pass (cost n - 1).
+static int adj_schedule(gf_ctx* c) {
+  auto& a = c->adj;
+  const int U = a.nseg, S = a.snaps;  // s ranges over 0 .. S - 1 free slots
+  a.split.assign((size_t)(U + 1) * S, 0);
+  std::vector<int64_t> cost((size_t)(U + 1) * S, 0);
+  auto C = [&](int n, int sf) -> int64_t& { return cost[(size_t)n * S + sf]; };
+  for (int n = 1; n <= U; ++n)
+    for (int sf = 0; sf < S; ++sf) {
+      if (n == 1) { C(n, sf) = 0; continue; }
+      if (sf == 0) { C(n, sf) = (int64_t)n * (n - 1) / 2; continue; }
+      if (sf >= n - 1) { C(n, sf) = n - 1; a.split[(size_t)n * S + sf] = 1; continue; }
+      int64_t best = -1; int bm = 1;
+      for (int m = 1; m < n; ++m) {
+        const int64_t v = m + C(n - m, sf - 1) + C(m, sf);
+        if (best < 0 || v < best) { best = v; bm = m; }
+      }
+      C(n, sf) = best;
+      a.split[(size_t)n * S + sf] = bm;
+    }
+  return GF_OK;
+}
+
 extern "C" int gf_adjoint_setup(gf_ctx* c, int64_t nsteps, int32_t checkpoint_every) {
   if (!c || nsteps < 1 || checkpoint_every < 1) return GF_ERR_ARG;
   if (int r = adj_check(c)) return r;
+  if ((nsteps + checkpoint_every - 1) / checkpoint_every > 4096)
+    return fail(c, GF_ERR_ARG, "more than 4096 recomputation units: raise checkpoint_every");
   GF_CUDA(c, cudaStreamSynchronize(c->stream));
   auto& a = c->adj;
   for (void* p : a.mem) cudaFree(p);
@@ -1761,9 +1796,10 @@ extern "C" int gf_adjoint_setup(gf_ctx* c, int64_t nsteps, int32_t checkpoint_ev
   a.nsteps = nsteps;
   a.every = (int)std::min<int64_t>(checkpoint_every, nsteps);
   a.nseg = (int)((nsteps + a.every - 1) / a.every);
+  a.snaps = a.nseg;  // one slot per unit boundary: a single forward pass, no recomputation of advances
   const size_t spec = g.bs_spec * c->cb, plane = (size_t)g.ny * g.nx * c->rb;
   const size_t wide = (size_t)g.ny * g.ldk * c->cb;
-  if (!(a.ckpt = adj_alloc(c, a.nseg * spec)) || !(a.phys = adj_alloc(c, (size_t)a.every * 4 * 3 * plane)) ||
+  if (!(a.ckpt = adj_alloc(c, a.snaps * spec)) || !(a.phys = adj_alloc(c, (size_t)a.every * 4 * 3 * plane)) ||
       !(a.ub = adj_alloc(c, spec)) || !(a.n1acc = adj_alloc(c, spec)) || !(a.xaacc = adj_alloc(c, spec)) ||
       !(a.x1acc = adj_alloc(c, spec)) || !(a.ubar_in = adj_alloc(c, spec)) || !(a.ubar_out = adj_alloc(c, spec)) ||
       !(a.final_state = adj_alloc(c, spec)) || !(a.tmp = adj_alloc(c, spec)) || !(a.Wb = adj_alloc(c, 2 * wide)) ||
@@ -1777,24 +1813,83 @@ extern "C" int gf_adjoint_setup(gf_ctx* c, int64_t nsteps, int32_t checkpoint_ev
     GF_CUDA(c, cudaMemsetAsync(p, 0, spec, c->stream));
   GF_CUDA(c, cudaMemsetAsync(a.Wb, 0, 2 * wide, c->stream));
   GF_CUDA(c, cudaMemsetAsync(a.Pb, 0, 3 * wide, c->stream));
-  a.ck_t.assign(a.nseg, 0.0);
-  a.ck_step.assign(a.nseg, 0);
+  a.ck_t.assign(a.snaps, 0.0);
+  a.ck_step.assign(a.snaps, 0);
+  adj_schedule(c);
   a.ready = true;
   return GF_OK;
 }
 
+extern "C" int gf_adjoint_set_snapshots(gf_ctx* c, int32_t snapshots) {
+  if (!c) return GF_ERR_ARG;
+  auto& a = c->adj;
+  if (!a.ready) return fail(c, GF_ERR_STATE, "call gf_adjoint_setup first");
+  if (snapshots < 1) return fail(c, GF_ERR_ARG, "at least one snapshot (the initial state)");
+  snapshots = std::min(snapshots, a.nseg);
+  const size_t spec = c->g.bs_spec * c->cb;
+  void* p = nullptr;
+  if (cudaMalloc(&p, (size_t)snapshots * spec) != cudaSuccess) return fail(c, GF_ERR_NOMEM, "snapshots");
+  GF_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (auto& q : a.mem) if (q == a.ckpt) { cudaFree(q); q = p; }
+  a.ckpt = p;
+  a.snaps = snapshots;
+  a.ck_t.assign(a.snaps, 0.0);
+  a.ck_step.assign(a.snaps, 0);
+  a.forward_done = false;
+  return adj_schedule(c);
+}
+
+extern "C" int gf_adjoint_info(const gf_ctx* c, int32_t* units, int32_t* snapshots, int64_t* unit_advances) {
+  if (!c) return GF_ERR_ARG;
+  if (units) *units = c->adj.nseg;
+  if (snapshots) *snapshots = c->adj.snaps;
+  if (unit_advances) *unit_advances = c->adj.forward_units;
+  return GF_OK;
+}
+
+static int adj_store(gf_ctx* c, int slot) {
+  auto& a = c->adj;
+  const size_t spec = c->g.bs_spec * c->cb;
+  GF_CUDA(c, cudaMemcpyAsync((char*)a.ckpt + slot * spec, c->sol, spec, cudaMemcpyDeviceToDevice, c->stream));
+  a.ck_t[slot] = c->t;
+  a.ck_step[slot] = c->step;
+  return GF_OK;
+}
+
+static int adj_restore(gf_ctx* c, int slot) {
+  auto& a = c->adj;
+  const size_t spec = c->g.bs_spec * c->cb;
+  GF_CUDA(c, cudaMemcpyAsync(c->sol, (char*)a.ckpt + slot * spec, spec, cudaMemcpyDeviceToDevice, c->stream));
+  c->t = a.ck_t[slot];
+  c->step = a.ck_step[slot];
+  c->W_valid = false;
+  return upload_clock(c);
+}
+
+// steps of units [u0, u0 + n)
+static int64_t adj_unit_steps(const gf_ctx* c, int u0, int n) {
+  const auto& a = c->adj;
+  return std::min<int64_t>((int64_t)(u0 + n) * a.every, a.nsteps) - (int64_t)u0 * a.every;
+}
+
+// stepforward!(prob, nsteps) keeping the initial state and the snapshots of the schedule's
+// first descent (the "spine"), so that the reverse sweep starts without recomputation.
 extern "C" int gf_adjoint_forward(gf_ctx* c) {
   if (!c) return GF_ERR_ARG;
   auto& a = c->adj;
   if (!a.ready) return fail(c, GF_ERR_STATE, "call gf_adjoint_setup first");
   const size_t spec = c->g.bs_spec * c->cb;
-  for (int64_t k = 0; k < a.nsteps; k += a.every) {
-    const int seg = (int)(k / a.every);
-    GF_CUDA(c, cudaMemcpyAsync((char*)a.ckpt + seg * spec, c->sol, spec, cudaMemcpyDeviceToDevice, c->stream));
-    a.ck_t[seg] = c->t;
-    a.ck_step[seg] = c->step;
-    if (int r = gf_step(c, std::min<int64_t>(a.every, a.nsteps - k))) return r;
+  a.spine.clear();
+  if (int r = adj_store(c, 0)) return r;
+  int p = 0, n = a.nseg, sf = a.snaps - 1, slot = 1;
+  while (n > 1 && sf > 0) {
+    const int m = a.split[(size_t)n * a.snaps + sf];
+    if (int r = gf_step(c, adj_unit_steps(c, p, m))) return r;
+    p += m; n -= m; sf -= 1;
+    if (int r = adj_store(c, slot)) return r;
+    a.spine.push_back({p, slot++});
   }
+  if (int r = gf_step(c, adj_unit_steps(c, p, n))) return r;
   GF_CUDA(c, cudaMemcpyAsync(a.final_state, c->sol, spec, cudaMemcpyDeviceToDevice, c->stream));
   a.t_end = c->t;
   a.step_end = c->step;
@@ -1818,55 +1913,99 @@ static AdjArgs adj_args(gf_ctx* c) {
 
 // The reverse sweep from the cotangent in adj.ubar_in (internal layout) to adj.ubar_out
 // and adj.etab; the state and clock are the forward pass's result again afterwards.
+// Recompute unit u from the current state with its forward fields kept, then run its
+// transposed stages, last step first.
+static int adj_unit(gf_ctx* c, AdjArgs& a, int u) {
+  auto& d = c->adj;
+  const Geom& g = c->g;
+  const size_t plane = (size_t)g.ny * g.nx * c->rb;
+  const double dt = c->cfg.dt;
+  const Bufs b = Bufs{c->twid, nullptr, nullptr};
+  const int cnt = (int)adj_unit_steps(c, u, 1);
+  for (int i = 0; i < cnt; ++i) {
+    if (int r = ensure_W(c)) return r;
+    for (int stg = 1; stg <= 4; ++stg) {
+      const double ts = c->t + (stg == 1 ? 0.0 : stg == 4 ? dt : 0.5 * dt);
+      StepArgs s = stage_args(c, stg, ts);
+      s.clk = c->dclk;
+      c->row_phys = (char*)d.phys + ((size_t)i * 4 + stg - 1) * 3 * plane;
+      const int r = launch_stage(c, s, 1);
+      c->row_phys = nullptr;
+      if (r) return r;
+    }
+    advance_clock_kernel<<<1, 32, 0, c->stream>>>(c->dclk, dt, c->cfg.forcing_omega, c->cfg.forcing_phase,
+                                                  c->cfg.forcing_kind == GF_FORCING_HARMONIC, c->nstages);
+    GF_CUDA(c, cudaGetLastError());
+    c->launches++;
+    host_advance(c);
+  }
+  for (int i = cnt - 1; i >= 0; --i) {
+    for (int r = 4; r >= 1; --r) {
+      a.stage = r;
+      a.head = (r == 1) && !(u == 0 && i == 0);
+      a.phys = (char*)d.phys + ((size_t)i * 4 + r - 1) * 3 * plane;
+      GF_CUDA(c, DISPATCH(c, launch_adj_row, g, a, b, c->stream));
+      GF_CUDA(c, DISPATCH(c, launch_adj_col, g, c->m, a, b, c->stream));
+      c->launches += 2;
+    }
+  }
+  return GF_OK;
+}
+
+// Reverse units [p, p + n): the state at unit p is in slot sp, sf slots are free.
+static int adj_rev(gf_ctx* c, AdjArgs& a, int p, int n, int sp, int sf, bool spine, std::vector<int>& freeslots,
+                   size_t& spine_i) {
+  auto& d = c->adj;
+  if (n == 1) {
+    if (int r = adj_restore(c, sp)) return r;
+    return adj_unit(c, a, p);
+  }
+  if (sf == 0) {  // no slot left: advance from the start for each unit, last first
+    for (int k = n - 1; k >= 0; --k) {
+      if (int r = adj_restore(c, sp)) return r;
+      if (k > 0) {
+        if (int r = gf_step(c, adj_unit_steps(c, p, k))) return r;
+        d.forward_units += k;
+      }
+      if (int r = adj_unit(c, a, p + k)) return r;
+    }
+    return GF_OK;
+  }
+  const int m = d.split[(size_t)n * d.snaps + sf];
+  int q;
+  if (spine && spine_i < d.spine.size() && d.spine[spine_i].first == p + m) {
+    q = d.spine[spine_i++].second;  // stored by the forward pass
+  } else {
+    if (freeslots.empty()) return fail(c, GF_ERR_STATE, "adjoint schedule ran out of snapshot slots");
+    q = freeslots.back();
+    freeslots.pop_back();
+    if (int r = adj_restore(c, sp)) return r;
+    if (int r = gf_step(c, adj_unit_steps(c, p, m))) return r;
+    d.forward_units += m;
+    if (int r = adj_store(c, q)) return r;
+  }
+  if (int r = adj_rev(c, a, p + m, n - m, q, sf - 1, spine, freeslots, spine_i)) return r;
+  freeslots.push_back(q);
+  return adj_rev(c, a, p, m, sp, sf, false, freeslots, spine_i);
+}
+
+// The reverse sweep from the cotangent in adj.ubar_in (internal layout) to adj.ubar_out
+// and adj.etab; the state and clock are the forward pass's result again afterwards.
 static int adjoint_reverse(gf_ctx* c) {
   auto& d = c->adj;
   const Geom& g = c->g;
   const size_t spec = g.bs_spec * c->cb, plane = (size_t)g.ny * g.nx * c->rb;
-  const double dt = c->cfg.dt;
   GF_CUDA(c, cudaMemsetAsync(d.etab, 0, plane, c->stream));
   AdjArgs a = adj_args(c);
   const Bufs b = Bufs{c->twid, nullptr, nullptr};
   a.stage = 5;
   GF_CUDA(c, DISPATCH(c, launch_adj_col, g, c->m, a, b, c->stream));
   c->launches++;
-  for (int seg = d.nseg - 1; seg >= 0; --seg) {
-    const int64_t k0 = (int64_t)seg * d.every;
-    const int cnt = (int)std::min<int64_t>(d.every, d.nsteps - k0);
-    // recompute the segment, keeping every stage's physical fields
-    GF_CUDA(c, cudaMemcpyAsync(c->sol, (char*)d.ckpt + seg * spec, spec, cudaMemcpyDeviceToDevice, c->stream));
-    c->t = d.ck_t[seg];
-    c->step = d.ck_step[seg];
-    if (int r = upload_clock(c)) return r;
-    c->W_valid = false;
-    for (int i = 0; i < cnt; ++i) {
-      if (int r = ensure_W(c)) return r;
-      for (int stg = 1; stg <= 4; ++stg) {
-        const double ts = c->t + (stg == 1 ? 0.0 : stg == 4 ? dt : 0.5 * dt);
-        StepArgs s = stage_args(c, stg, ts);
-        s.clk = c->dclk;
-        c->row_phys = (char*)d.phys + ((size_t)i * 4 + stg - 1) * 3 * plane;
-        const int r = launch_stage(c, s, 1);
-        c->row_phys = nullptr;
-        if (r) return r;
-      }
-      advance_clock_kernel<<<1, 32, 0, c->stream>>>(c->dclk, dt, c->cfg.forcing_omega, c->cfg.forcing_phase,
-                                                    c->cfg.forcing_kind == GF_FORCING_HARMONIC, c->nstages);
-      GF_CUDA(c, cudaGetLastError());
-      c->launches++;
-      host_advance(c);
-    }
-    // transposed stages, last step first
-    for (int i = cnt - 1; i >= 0; --i) {
-      for (int r = 4; r >= 1; --r) {
-        a.stage = r;
-        a.head = (r == 1) && !(seg == 0 && i == 0);
-        a.phys = (char*)d.phys + ((size_t)i * 4 + r - 1) * 3 * plane;
-        GF_CUDA(c, DISPATCH(c, launch_adj_row, g, a, b, c->stream));
-        GF_CUDA(c, DISPATCH(c, launch_adj_col, g, c->m, a, b, c->stream));
-        c->launches += 2;
-      }
-    }
-  }
+  std::vector<int> freeslots;
+  for (int k = d.snaps - 1; k >= 1 + (int)d.spine.size(); --k) freeslots.push_back(k);
+  size_t spine_i = 0;
+  d.forward_units = 0;  // unit advances the reverse sweep adds to the forward pass
+  if (int r = adj_rev(c, a, 0, d.nseg, 0, d.snaps - 1, true, freeslots, spine_i)) return r;
   GF_CUDA(c, cudaMemcpyAsync(c->sol, d.final_state, spec, cudaMemcpyDeviceToDevice, c->stream));
   c->t = d.t_end;
   c->step = d.step_end;

@@ -15,9 +15,20 @@ import numpy as np
 from . import _abi as A
 
 
-def setup(prob, nsteps, checkpoint_every=25):
+def setup(prob, nsteps, checkpoint_every=25, snapshots=None):
+    """Allocate for nsteps steps recomputed in units of checkpoint_every steps; `snapshots`
+    bounds the stored states (binomial checkpointing; default one per unit)."""
     prob._c(prob._lib.gf_adjoint_setup(prob._ctx, int(nsteps), int(checkpoint_every)))
+    if snapshots is not None:
+        prob._c(prob._lib.gf_adjoint_set_snapshots(prob._ctx, int(snapshots)))
     prob._adj_steps = int(nsteps)
+
+
+def info(prob):
+    """(units, snapshot slots, unit advances the last reverse sweep added to the forward pass)"""
+    u, s, a = C.c_int32(), C.c_int32(), C.c_int64()
+    prob._c(prob._lib.gf_adjoint_info(prob._ctx, C.byref(u), C.byref(s), C.byref(a)))
+    return u.value, s.value, a.value
 
 
 def grad(prob, nsteps=None, checkpoint_every=25, topography=None):

@@ -270,8 +270,8 @@ int gf_get_launch_shape(const gf_ctx* ctx, int32_t* shape);
  * Supported: TwoDNavierStokes and SingleLayerQG with constant U, stepper ETDRK4 or
  * FilteredETDRK4, batch = 1.  It is the exact transpose of the discrete step the library
  * computes (dealiasing, PV inversion, stage combinations), in the context's precision.
- * Checkpointing: the forward pass keeps the state every checkpoint_every steps; the reverse
- * pass recomputes one segment at a time from its checkpoint and runs its transposed stages.
+ * Checkpointing: see gf_adjoint_set_snapshots (binomial schedule over units of
+ * checkpoint_every steps; each unit is recomputed once with its forward fields kept).
  *
  * gf_adjoint_setup: allocate for nsteps steps (call again to change them).
  * gf_adjoint_forward: stepforward!(prob, nsteps) from the current state, keeping checkpoints.
@@ -287,6 +287,16 @@ int gf_get_launch_shape(const gf_ctx* ctx, int32_t* shape);
  *   to eta (deta), either may be NULL. */
 enum { GF_LOSS_KINETIC_ENERGY = 0 };
 int gf_adjoint_setup(gf_ctx* ctx, int64_t nsteps, int32_t checkpoint_every);
+/* Binomial checkpointing (Griewank's schedule) over units of checkpoint_every steps: the
+ * reverse sweep recomputes each unit once with its forward fields kept and reaches unit
+ * starts from at most `snapshots` stored states (slot 0 = the initial state), choosing the
+ * snapshot positions that minimise the unit advances C(n, s) = min_m [m + C(n-m, s-1) + C(m, s)].
+ * The default (one snapshot per unit) needs no advance beyond the forward pass; fewer
+ * snapshots trade memory for recomputation.  Call after gf_adjoint_setup.  gf_adjoint_info
+ * reports the units, the snapshot slots and the unit advances the last reverse sweep added
+ * to the forward pass (0 with one snapshot per unit). */
+int gf_adjoint_set_snapshots(gf_ctx* ctx, int32_t snapshots);
+int gf_adjoint_info(const gf_ctx* ctx, int32_t* units, int32_t* snapshots, int64_t* unit_advances);
 int gf_adjoint_forward(gf_ctx* ctx);
 int gf_adjoint_backward(gf_ctx* ctx, const void* sol_bar, void* sol0_bar, void* eta_bar, int where);
 int gf_grad(gf_ctx* ctx, int loss_kind, void* dq0, void* deta, double* loss, int where);

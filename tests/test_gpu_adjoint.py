@@ -167,3 +167,42 @@ def test_config3_central_differences_100_steps():
     """the same case over 100 steps, where the plain eps = 1e-6 central difference is
     already within 1e-6"""
     _fd_check(256, 100, 25, 8, 7)
+
+
+def _schedule_cost(n, s):
+    """C(n, s) of the binomial schedule, restated independently of the library"""
+    from functools import lru_cache
+
+    @lru_cache(maxsize=None)
+    def C(n, s):
+        if n == 1:
+            return 0
+        if s == 0:
+            return n * (n - 1) // 2
+        return min(m + C(n - m, s - 1) + C(m, s) for m in range(1, n))
+    return C(n, s)
+
+
+def test_binomial_checkpointing_same_gradient_fewer_snapshots():
+    """fewer snapshot slots: the same gradient (bit for bit) with the unit advances of the
+    optimal binomial schedule"""
+    kw, q0, eta = slqg_case(64)
+    ns, every = 24, 2
+    ref = None
+    for snaps in (None, 1, 2, 3, 5):
+        p = SL.Problem("GPU", **kw)
+        SL.set_q(p, q0)
+        adjoint.setup(p, ns, every, snapshots=snaps)
+        loss, dq0, deta = adjoint.grad(p)
+        units, slots, adv = adjoint.info(p)
+        assert units == 12 and slots == (12 if snaps is None else snaps)
+        # the forward pass takes the schedule's first snapshots; the rest is recomputation
+        assert adv <= _schedule_cost(units, slots - 1)
+        if snaps is None:
+            assert adv == 0
+        if snaps == 1:
+            assert adv == units * (units - 1) // 2
+        if ref is None:
+            ref = (loss, dq0, deta)
+        else:
+            assert loss == ref[0] and np.array_equal(dq0, ref[1]) and np.array_equal(deta, ref[2])
