@@ -1699,7 +1699,7 @@ extern "C" int gf_autotune(gf_ctx* c, int32_t reps, int32_t* shape) {
     if (!f32_radix_built(g0.ny, R) || TPF < 1) continue;
     for (int C = 1; C <= 16 && rc == GF_OK; C *= 2) {
       const int cs = C > 1 ? g0.ny + std::max(unit / C, 1) : g0.ny;
-      const size_t sm = ((size_t)2 * C * cs + (size_t)g0.nl * g0.ny * C * (g0.nl > 1 ? 2 : 1)) * c->cb;
+      const size_t sm = col_stage_smem(g0.ny, C, cs, g0.nl, c->cb);
       if (C * TPF > 512 || sm > (size_t)SMEM_CAP) continue;
       set_shape(c, 0, 0, R, C);
       double ms = 0;

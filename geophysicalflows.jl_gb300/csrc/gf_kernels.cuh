@@ -474,11 +474,6 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? (NY >= 1024 ? GF_MINBLOC
   }
 }
 
-// shared-memory bytes of col_stage_kernel for C columns with column stride cs
-__host__ __forceinline__ size_t col_stage_smem(int NY, int C, int cs, int nl, size_t elem) {
-  if (nl == 1) return (size_t)3 * C * cs * elem;  // F0, F1, F2 (cs >= NY: also holds the general path's Xs)
-  return ((size_t)2 * C * cs + (size_t)nl * NY * C * 2) * elem;
-}
 
 // --------------------------------------------------------------------------- row kernel
 // Slots per row-pair buffer: NX, staggered by TPF when several pairs share a wavefront.
