@@ -32,6 +32,9 @@
 #ifndef GF_ROW_MINBLOCKS_F32
 #define GF_ROW_MINBLOCKS_F32 3
 #endif
+#ifndef GF_ROW_MINBLOCKS_WIDE
+#define GF_ROW_MINBLOCKS_WIDE 2   // FP64 and df64 row kernels (128 registers, no spills)
+#endif
 
 namespace gf {
 
@@ -508,7 +511,7 @@ __device__ __forceinline__ void unpack_store(const cplx<T>* buf, int k, int NX, 
 }
 
 template <class T, int NX, int R>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? GF_ROW_MINBLOCKS_F32 : 1) row_nl_kernel(Geom g, ModArgs m, Bufs b, int B) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? GF_ROW_MINBLOCKS_F32 : GF_ROW_MINBLOCKS_WIDE) row_nl_kernel(Geom g, ModArgs m, Bufs b, int B) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int TPF = NX / R;
   constexpr int M = NX / 2;
