@@ -103,9 +103,11 @@ __device__ __forceinline__ void psi_all(const ModArgs& m, int nl, T K2, const cp
 //     global accesses are C-wide contiguous; thread (c, t) owns rows j = t + i (NY/R);
 //   FFT mapping: column cf = tid / TPF, butterfly index tf = tid % TPF, so a warp works on
 //     one column and the swizzled Stockham accesses are conflict-free.
-// Shared memory: two work buffers F0/F1 (C columns of g.cs slots each; the product fields
-// are prefetched with cp.async into one while the other is transformed), Xs (N, then the
-// next stage X; nl x NY x C interleaved, thread-owned) and, for more than one layer, Ps.
+// Shared memory, one layer without bottom drag: three work buffers F0/F1/F2 (C columns of g.cs
+// slots each) for the product and inverse FFTs, N and the next X in registers.  Otherwise:
+// F0/F1 (the product fields prefetched with cp.async into one while the other is
+// transformed) and Xs (N, then the next stage X; nl x NY x C interleaved, thread-owned); the
+// PV inversion of every element is recomputed from Xs where u and v of a layer are formed.
 template <class T, int NY, int R>
 __global__ void __launch_bounds__(512, sizeof(T) == 4 ? (NY >= 1024 ? GF_MINBLOCKS_F32 : GF_MINBLOCKS_SMALL_F32) : 1)
     col_stage_kernel(Geom g, ModArgs m, StepArgs s, Bufs b, int C) {
@@ -118,7 +120,6 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? (NY >= 1024 ? GF_MINBLOC
   cplx<T>* F1 = F0 + C * cs;
   cplx<T>* F2 = F1 + C * cs;  // one layer: third work buffer (the general path's Xs)
   cplx<T>* Xs = F2;
-  cplx<T>* Ps = Xs + nl * NY * C;
   const int tid = threadIdx.x, c = tid % C, t = tid / C;
   const int cf = tid / TPF, tf = tid % TPF;
   const int kr = blockIdx.x * C + c;
@@ -408,25 +409,8 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? (NY >= 1024 ? GF_MINBLOC
   if ((int)blockIdx.x * C >= g.kcut) return;  // whole block aliased: W is never read there
   __syncthreads();  // eig[] filled; F0 free
 
-  // PV inversion for more than one layer (each thread reads back only what it wrote)
-  if (nl > 1) {
-#pragma unroll
-    for (int i = 0; i < R; ++i) {
-      const int j = t + i * TPF;
-      const T lv = T(lidx(g, j)) * dky;
-      const T K2 = krT * krT + lv * lv;
-      cplx<T> X[MAXL], ps[MAXL];
-      for (int L = 0; L < nl; ++L) X[L] = Xs[(L * NY + j) * C + c];
-      if (m.psi_kind == PSI_EIGEN) {
-        psi_eigen<T>(nl, eig, K2, X, ps);
-      } else {
-        const T f = psi_factor<T>(m.psi_kind, K2, ell2, m.mult, (size_t)j * g.ldk + (kin ? kr : 0));
-        for (int L = 0; L < nl; ++L) ps[L] = f * X[L];
-      }
-      for (int L = 0; L < nl; ++L) Ps[(L * NY + j) * C + c] = ps[L];
-      if (m.drag && kin) Dp[(size_t)j * g.ldk + kr] = (muT * K2) * ps[nl - 1];
-    }
-  } else if (m.drag && kin) {
+  // single-layer bottom drag (several layers: in the loop below)
+  if (nl == 1 && m.drag && kin) {
 #pragma unroll
     for (int i = 0; i < R; ++i) {
       const int j = t + i * TPF;
@@ -437,8 +421,10 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? (NY >= 1024 ? GF_MINBLOC
       Dp[ti] = (muT * K2 * f) * Xs[j * C + c];
     }
   }
-  // y-direction inverse FFT of (q, u, v) for every layer
+  // y-direction inverse FFT of (q, u, v) for every layer; psi of layer L from the X of all
+  // layers at the element (several layers: PV inversion), kept in registers for u and v
   for (int L = 0; L < nl; ++L) {
+    cplx<T> preg[R];
     for (int f = 0; f < 3; ++f) {
       cplx<T>* Fb = ((L * 3 + f) & 1) ? F1 : F0;  // alternate so stores of one field overlap the next
       cplx<T>* Fe = Fb + c * cs;
@@ -451,13 +437,25 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? (NY >= 1024 ? GF_MINBLOC
         if (f == 0) {
           v = x;
         } else {
-          cplx<T> p;
-          if (nl > 1) {
-            p = Ps[(L * NY + j) * C + c];
-          } else {
+          if (f == 1) {
             const T K2 = krT * krT + lv * lv;
-            p = psi_factor<T>(m.psi_kind, K2, ell2, m.mult, (size_t)j * g.ldk + (kin ? kr : 0)) * x;
+            const size_t ti = (size_t)j * g.ldk + (kin ? kr : 0);
+            if (nl > 1) {
+              cplx<T> X[MAXL], ps[MAXL];
+              for (int a = 0; a < nl; ++a) X[a] = Xs[(a * NY + j) * C + c];
+              if (m.psi_kind == PSI_EIGEN) {
+                psi_eigen<T>(nl, eig, K2, X, ps);
+              } else {
+                const T fk = psi_factor<T>(m.psi_kind, K2, ell2, m.mult, ti);
+                for (int a = 0; a < nl; ++a) ps[a] = fk * X[a];
+              }
+              preg[i] = ps[L];
+              if (m.drag && kin && L == nl - 1) Dp[ti] = (muT * K2) * ps[nl - 1];
+            } else {
+              preg[i] = psi_factor<T>(m.psi_kind, K2, ell2, m.mult, ti) * x;
+            }
           }
+          const cplx<T> p = preg[i];
           v = (f == 1) ? lv * mul_mi(p)     // u = -i l psi
                        : krT * mul_i(p);    // v =  i kr psi
         }

@@ -45,7 +45,7 @@ inline int pick_B(int NX, int R, size_t elem, int nbufs, int npairs, int nb = 1)
 // shared-memory bytes of col_stage_kernel for C columns with column stride cs
 __host__ __forceinline__ size_t col_stage_smem(int NY, int C, int cs, int nl, size_t elem) {
   if (nl == 1) return (size_t)3 * C * cs * elem;  // F0, F1, F2 (cs >= NY: also holds the general path's Xs)
-  return ((size_t)2 * C * cs + (size_t)nl * NY * C * 2) * elem;
+  return ((size_t)2 * C * cs + (size_t)nl * NY * C) * elem;  // F0, F1, X of every layer
 }
 
 // Whether B row pairs per block fit the row kernel (threads, shared memory, pair count).
