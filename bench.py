@@ -90,6 +90,7 @@ class Clocks:
         try:
             self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
                                        "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+            time.sleep(1.5)  # let the sampler finish starting up before anything is timed
         except OSError:
             self.p = None
         return self
