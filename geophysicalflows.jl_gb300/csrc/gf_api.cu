@@ -1729,6 +1729,70 @@ extern "C" int gf_autotune(gf_ctx* c, int32_t reps, int32_t* shape) {
   return GF_OK;
 }
 
+// Output streaming: every `every` steps the diagnostics `which_diag` are reduced into a
+// device ring and the physical fields `which_field` (updatevars!) are copied into a device
+// ring; the host waits once per ring fill (<= 256 MB of fields), not once per output.
+// diag_out[k][instance][nd]; field_out[k][f][instance][layer][ny][nx] (context real type;
+// FP64 for df64).  Steps after the last output are stepped too.
+extern "C" int gf_step_output(gf_ctx* c, int64_t nsteps, int32_t every, const int32_t* which_diag, int32_t nd,
+                              double* diag_out, const int32_t* which_field, int32_t nf, void* field_out) {
+  if (!c || nsteps < 0 || every < 1 || nd < 0 || nf < 0 || (nd > 0 && (!which_diag || !diag_out)) ||
+      (nf > 0 && (!which_field || !field_out)))
+    return GF_ERR_ARG;
+  uint32_t mask = 0;
+  if (nd > 0)
+    if (int r = diag_mask(c, which_diag, nd, &mask)) return r;
+  const int maxf = c->cfg.module == GF_BAROTROPICQGQL ? 6 : 3;
+  for (int32_t f = 0; f < nf; ++f)
+    if (which_field[f] < 0 || which_field[f] > maxf) return fail(c, GF_ERR_ARG, "unknown field");
+  const int64_t nout = nsteps / every;
+  const Geom& g = c->g;
+  const size_t pf = (size_t)g.nl * g.ny * g.nx * g.nb * c->rb;      // one field, all instances (device)
+  const size_t pfo = (size_t)g.nl * g.ny * g.nx * g.nb * (c->prec == GF_DF64 ? 8 : c->rb);  // at the ABI
+  const size_t dslot = (size_t)NDIAG * g.nb;
+  int64_t cap = nout > 0 ? nout : 1;
+  if (nf > 0) cap = std::max<int64_t>(1, std::min<int64_t>(cap, (int64_t)((256u << 20) / (nf * pf))));
+  double* dring = nullptr;
+  char* fring = nullptr;
+  if (nd > 0) GF_CUDA(c, cudaMallocAsync((void**)&dring, (size_t)cap * dslot * 8, c->stream));
+  if (nf > 0) GF_CUDA(c, cudaMallocAsync((void**)&fring, (size_t)cap * nf * pf, c->stream));
+  std::vector<double> hv(nd > 0 ? (size_t)cap * dslot : 0), fs(cap);
+  int rc = GF_OK;
+  for (int64_t k0 = 0; k0 < nout && rc == GF_OK; k0 += cap) {
+    const int64_t n = std::min<int64_t>(cap, nout - k0);
+    for (int64_t k = 0; k < n && rc == GF_OK; ++k) {
+      rc = gf_step(c, every);
+      if (rc == GF_OK && nd > 0) rc = diag_launch(c, mask, dring + k * dslot);
+      fs[k] = diag_fscale(c);
+      if (rc == GF_OK && nf > 0) {
+        rc = gf_updatevars(c);
+        for (int32_t f = 0; f < nf && rc == GF_OK; ++f)
+          if (cudaMemcpyAsync(fring + ((size_t)k * nf + f) * pf, (char*)c->phys + (size_t)which_field[f] * pf, pf,
+                              cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess)
+            rc = fail(c, GF_ERR_CUDA, "output field copy");
+      }
+    }
+    if (rc != GF_OK) break;
+    if (nd > 0) {
+      if (cudaMemcpyAsync(hv.data(), dring, (size_t)n * dslot * 8, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) {
+        rc = fail(c, GF_ERR_CUDA, "output diagnostics copy");
+        break;
+      }
+    }
+    for (int64_t k = 0; k < n && nf > 0 && rc == GF_OK; ++k)
+      for (int32_t f = 0; f < nf && rc == GF_OK; ++f)
+        rc = copy_phys_out(c, (char*)field_out + ((size_t)(k0 + k) * nf + f) * pfo, fring + ((size_t)k * nf + f) * pf,
+                           GF_HOST);
+    if (rc == GF_OK && cudaStreamSynchronize(c->stream) != cudaSuccess) rc = fail(c, GF_ERR_CUDA, "output sync");
+    for (int64_t k = 0; k < n && nd > 0 && rc == GF_OK; ++k)
+      diag_post(c, which_diag, nd, hv.data() + k * dslot, fs[k], diag_out + (size_t)(k0 + k) * nd * g.nb);
+  }
+  if (dring) cudaFreeAsync(dring, c->stream);
+  if (fring) cudaFreeAsync(fring, c->stream);
+  if (rc == GF_OK && nsteps - nout * every > 0) rc = gf_step(c, nsteps - nout * every);
+  return rc;
+}
+
 // ------------------------------------------------------------------------------- adjoint
 // Reverse-mode derivative of stepforward!(prob, nsteps) for TwoDNavierStokes and
 // SingleLayerQG (constant U) with ETDRK4 / FilteredETDRK4 (the kernels are in gf_adjoint.cuh).

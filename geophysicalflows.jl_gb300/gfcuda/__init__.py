@@ -4,11 +4,11 @@ Host-side mirror of the reference's module API; every computation runs in libgfc
 """
 from . import _abi
 from ._abi import load, GFError, GFNotImplemented
-from .core import Diagnostic, Forcing, ensemble_step, stepforward
+from .core import Diagnostic, Forcing, ensemble_step, stepforward, stepforward_output
 from . import TwoDNavierStokes, SingleLayerQG, MultiLayerQG, SurfaceQG, BarotropicQGQL
 from . import utils
 from . import adjoint
 from .utils import peakedisotropicspectrum
 
-__all__ = ["load", "GFError", "GFNotImplemented", "Diagnostic", "Forcing", "ensemble_step", "stepforward", "TwoDNavierStokes",
+__all__ = ["load", "GFError", "GFNotImplemented", "Diagnostic", "Forcing", "ensemble_step", "stepforward", "stepforward_output", "TwoDNavierStokes",
            "SingleLayerQG", "MultiLayerQG", "SurfaceQG", "BarotropicQGQL", "utils", "adjoint", "peakedisotropicspectrum"]

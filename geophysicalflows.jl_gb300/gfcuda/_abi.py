@@ -26,7 +26,8 @@ EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_abi_version", "gf_get
            "gf_rfft2_noalloc", "gf_get_batch", "gf_set_graph_steps", "gf_ensemble_step",
            "gf_peakedisotropicspectrum", "gf_get_filter", "gf_adjoint_setup", "gf_adjoint_forward",
            "gf_adjoint_backward", "gf_grad", "gf_autotune", "gf_set_launch_shape", "gf_get_launch_shape",
-           "gf_fluxes", "gf_step_callback", "gf_adjoint_set_snapshots", "gf_adjoint_info"]
+           "gf_fluxes", "gf_step_callback", "gf_adjoint_set_snapshots", "gf_adjoint_info",
+           "gf_step_output"]
 
 
 class gf_config(C.Structure):
@@ -99,6 +100,7 @@ def load(path=None):
         "gf_fluxes": ([vp, vp, vp], C.c_int),
         "gf_step_callback": ([vp, i64, FORCING_FN, vp], C.c_int),
         "gf_adjoint_set_snapshots": ([vp, i32], C.c_int),
+        "gf_step_output": ([vp, i64, i32, C.POINTER(i32), i32, C.POINTER(dbl), C.POINTER(i32), i32, vp], C.c_int),
         "gf_adjoint_info": ([vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i64)], C.c_int),
         "gf_set_launch_shape": ([vp, C.POINTER(i32)], C.c_int),
         "gf_get_launch_shape": ([vp, C.POINTER(i32)], C.c_int),

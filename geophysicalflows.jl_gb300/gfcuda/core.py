@@ -373,6 +373,28 @@ def _step_callback(prob, n, diags=None):
             d.increment()
 
 
+def stepforward_output(prob, nsteps, every, diagnostics=(), fields=()):
+    """Step nsteps and record, after every `every` steps, the library diagnostics (ids or
+    module diagnostic functions such as TwoDNavierStokes.energy) and physical fields (names
+    in prob.field_names, e.g. "zeta"), without a host wait per output.  Returns
+    (diag array [nout, (batch,) nd], {field name: array [nout, (batch,) ...]})."""
+    ids = [d if isinstance(d, (int, np.integer)) else d.diag_id for d in diagnostics]
+    names = {v: k for k, v in prob.field_names.items()}
+    fsel = [names[f] for f in fields]
+    nout = int(nsteps) // int(every)
+    shp = prob.phys_shape
+    idv = np.ascontiguousarray(ids, dtype=np.int32)
+    fv = np.ascontiguousarray(fsel, dtype=np.int32)
+    dout = np.empty((nout, prob.batch, len(ids)), dtype=np.float64)
+    fout = np.empty((nout, len(fsel)) + shp, dtype=prob.T)
+    prob._c(prob._lib.gf_step_output(prob._ctx, int(nsteps), int(every), idv.ctypes.data_as(C.POINTER(C.c_int32)),
+                                     len(ids), dout.ctypes.data_as(C.POINTER(C.c_double)),
+                                     fv.ctypes.data_as(C.POINTER(C.c_int32)), len(fsel), fout.ctypes.data))
+    if prob.batch == 1:
+        dout = dout[:, 0]
+    return dout, {f: fout[:, i] for i, f in enumerate(fields)}
+
+
 def ensemble_step(probs, nsteps):
     """Step several problems (e.g. batched problems of different grid sizes) together; each
     runs on its own stream, so they execute concurrently on the GPU."""

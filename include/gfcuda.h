@@ -240,6 +240,16 @@ int gf_set_forcing(gf_ctx* ctx, const void* data, int where);
 /* Block until the context's stream has finished. */
 int gf_synchronize(gf_ctx* ctx);
 
+/* Output streaming (the reference's Diagnostic with freq = every and Output snapshots,
+ * e.g. examples/twodnavierstokes_decaying.jl:90-115): nsteps steps; after every `every` steps
+ * the diagnostics which_diag (gf_diagnostics ids) go to diag_out[k][instance][nd] and the
+ * physical fields which_field (gf_field selectors, after updatevars!) to
+ * field_out[k][f][instance][layer][ny][nx] (host memory, the context's real type; FP64 for
+ * GF_DF64), k = 0 .. nsteps/every - 1.  Diagnostics and fields collect in device rings; the
+ * host waits once per ring fill (<= 256 MB of fields), not once per output.  nd or nf may be 0. */
+int gf_step_output(gf_ctx* ctx, int64_t nsteps, int32_t every, const int32_t* which_diag, int32_t nd,
+                   double* diag_out, const int32_t* which_field, int32_t nf, void* field_out);
+
 /* stepforward!(prob, nsteps) with an arbitrary host calcF! (calcF!(Fh, sol, t, clock, vars, params,
  * grid), e.g. examples/singlelayerqg_betaforced.jl:86-90): before every stage the library calls
  * fn(t_stage, clock.step, stage (1-based), Fh, user); fn fills Fh in the layout of gf_set_forcing

@@ -97,3 +97,24 @@ def test_host_calcF_callback_matches_device_harmonic_forcing(stepper):
     r = TD.Problem("GPU", forcing=gfcuda.Forcing("callback", calcF=bad), **kw)
     with pytest.raises(RuntimeError, match="boom"):
         gfcuda.stepforward(r, 1)
+
+
+@pytest.mark.parametrize("prec", [None, "DF64"])
+def test_output_streaming_matches_stepwise_reads(prec):
+    """gf_step_output: fields and diagnostics every `every` steps equal those read after
+    stepping by hand; trailing steps are stepped too"""
+    n = 64
+    z0 = O.peakedisotropicspectrum(O.Grid(n), 6, 0.5, seed=5)
+    kw = dict(nx=n, dt=0.005, stepper="FilteredRK4", precision=prec)
+    p, q = TD.Problem("GPU", **kw), TD.Problem("GPU", **kw)
+    TD.set_zeta(p, z0)
+    TD.set_zeta(q, z0)
+    d, f = gfcuda.stepforward_output(p, 23, 5, diagnostics=[TD.energy, TD.enstrophy], fields=["zeta", "u"])
+    assert d.shape == (4, 2) and f["zeta"].shape == (4, n, n)
+    for k in range(4):
+        gfcuda.stepforward(q, 5)
+        assert d[k, 0] == TD.energy(q) and d[k, 1] == TD.enstrophy(q)   # before updatevars! dealiases
+        TD.updatevars(q)
+        assert np.array_equal(f["zeta"][k], q.vars.zeta) and np.array_equal(f["u"][k], q.vars.u)
+    gfcuda.stepforward(q, 3)
+    assert p.clock.step == q.clock.step == 23 and np.array_equal(p.sol, q.sol)
