@@ -5,11 +5,14 @@
 Headline workload: TwoDNavierStokes 2048^2, FilteredRK4, nu = 0, peaked isotropic initial
 vorticity (k0 = 6, E = 0.5) -- the configuration the FP32-fused vs FP64-plain target is
 quoted on.  A "step" is one FilteredRK4 time step (4 calcN! stages).  `value` is FP32-fused
-grid-point*steps/s with the state resident in HBM; the FP64-plain arm, its roofline and the
+grid-point*steps/s with the state resident in HBM, timed over stepforward! calls of 10 steps
+(an output interval: the state is looked at after every call, so the last step of each call
+computes every mode and the others only the modes a later step reads); single-step calls
+(every step observed) are timed beside it.  The FP64-plain arm, its roofline and the
 FP32-vs-FP64 error are reported beside it, and so are the other GPU workloads: SingleLayerQG
 512^2 ETDRK4 with stochastic forcing, MultiLayerQG 3 x 1024^2 ETDRK4, and the 1536-run
 TwoDNavierStokes ensemble (1024 x 64^2 + 384 x 128^2 + 128 x 256^2).  L2 is flushed (256 MiB
-write) between timed steps; graph-replayed multi-step timings are reported beside them.
+write) before every timed call; graph-replayed timings of the same calls are reported too.
 `--impl reference` times the FP64 CPU restatement of the reference (oracle/, scipy.fft on all
 host cores) on the same workload.  For N > 1 (torchrun) every rank runs an independent
 replica (the path does not shard) and rank 0 reports the aggregate over the slowest rank.
@@ -34,7 +37,8 @@ for _p in (os.path.join(ROOT, "geophysicalflows.jl_gb300"), os.path.join(ROOT, "
 METRIC = "grid-pt·steps/s FP32-fused vs FP64-plain (≤1e-5 rel L2); adjoint/forward step time"
 UNIT = "grid-pt*steps/s"
 HEADLINE = dict(module="TwoDNavierStokes", nx=2048, ny=2048, stepper="FilteredRK4", dt=5e-4)
-CONFIG1 = dict(module="SingleLayerQG", nx=512, ny=512, stepper="ETDRK4", dt=0.05, beta=10.0, mu=0.01)
+CONFIG1 = dict(module="SingleLayerQG", nx=512, ny=512, stepper="ETDRK4", dt=0.05, beta=10.0, mu=0.01,
+               forcing="stochastic")
 # 3 layers, H = [.2,.3,.5], rho = [4, 5, 5.5] -> b with g' = g (rho_{j+1} - rho_j) / rho_{j+1}, g = 1
 CONFIG2 = dict(module="MultiLayerQG", nx=1024, ny=1024, nlayers=3, stepper="ETDRK4", dt=2.5e-3, f0=1.0, beta=5.0,
                H=[0.2, 0.3, 0.5], b=[-1.0, -1.2, -1.2 - 0.5 / 5.5], U=[1.0, 0.5, 0.0], mu=0.05)
@@ -46,21 +50,64 @@ ENSEMBLE = dict(classes=((64, 1024), (128, 384), (256, 128)), stepper="FilteredR
                 kf=8.0, dkf=1.5, eps=1e-3)
 
 
-def algorithmic_words(module, stepper, nlayers=1, eta=False):
-    """Words per grid point per step of the two-sweep model: per calcN! stage read the stage
-    input (1), write k column-pass intermediates, read them in the row pass (k), write m
-    products, read them in the column pass (m), write N (1), read a physical parameter arrays;
-    plus C stage-combination sweeps per step (RK4 16, ETDRK4 23).  Returns (per step, row
-    kernel per launch, column kernel per launch)."""
-    k, m, a = 3, 2, 0
-    if module == "MultiLayerQG":
-        m = 3
-    if module == "SingleLayerQG" and eta:
-        a = 1
-    C = 23 if "ETDRK4" in stepper else 16
-    row = k + m + a
-    col = 2 + k + m + C / 4
-    return 4 * (row + col), row, col
+def dealias_geometry(nx, ny):
+    """Kept spectral columns and rows of the 2/3 rule (FourierFlows TwoDGrid with
+    aliased_fraction = 1/3): kr < kcut and l outside the aliased band."""
+    nkr = nx // 2 + 1
+    lo, hi = (1 - 1 / 3) / 2, (1 + 1 / 3) / 2
+    kcut = min(int(math.floor(lo * nx)), nkr)
+    lA, lB = int(math.floor(lo * ny)), int(math.ceil(hi * ny)) - 1
+    return nkr, kcut, ny - (lB - lA + 1)
+
+
+def launch_bytes(w, cb, observed):
+    """Bytes one row-kernel and one column-kernel launch must move -- every element of every
+    array the launch reads or writes, once -- averaged over the stages of a step.  `cb` is
+    the complex element size.  An observed step forms all nkr columns of the products and
+    updates every mode of the state; an unobserved one (every step of a stepforward! call
+    but the last) forms the products for kr < kcut and updates the kept modes only.  The
+    stage input is read at kept modes only (the dealias of calcN!); the pruned inverse
+    fields W hold kr < kcut."""
+    nx, ny, nl = w["nx"], w["ny"], w.get("nlayers", 1)
+    nkr, kcut, rows = dealias_geometry(nx, ny)
+    rb = cb // 2
+    kept = kcut * rows * nl                       # kept modes, all layers
+    S = nl * nkr * ny if observed else kept       # modes the stage combination runs on
+    kout = nkr if observed else kcut              # product columns formed
+    m = 3 if w["module"] == "MultiLayerQG" else 2
+    Wb = 3 * nl * ny * kcut * cb                  # (q, u, v) after the column pass
+    Pb = m * nl * ny * kout * cb                  # products after the row pass
+    hasL = w.get("nu", 0) > 0 or (w["module"] == "TwoDNavierStokes" and w.get("mu", 0) > 0)
+    tables_cplx = w.get("beta", 0) != 0 and w["module"] == "SingleLayerQG"
+    tb = cb if tables_cplx else rb
+    St = S // nl                                  # table elements ([j][kr], shared by the layers)
+    state = 0.0                                   # bytes of the stage combination, whole step
+    if "RK4" in w["stepper"] and "ETD" not in w["stepper"]:
+        state += (4 * kept + 7 * S) * cb          # sol at kept modes x4; acc w, (r+w) x2, r; sol w
+        if hasL:
+            state += (3 * kept + 3 * S) * cb + 4 * St * rb   # X written x3, read x3 (kept); L table
+        if w["stepper"].startswith("Filtered"):
+            state += St * rb                      # filter, last stage
+    else:                                         # ETDRK4: s1, N1, acc; e2, zeta, alpha/beta, e, gamma
+        state += (3 * kept + 11 * S) * cb + 11 * St * tb
+    if w.get("forcing") == "stochastic":
+        state += 5 * S * cb + St * rb             # draw -> F (w), F read x3, previous state (w); spectrum
+    if w.get("mu", 0) > 0 and w["module"] == "MultiLayerQG":
+        state += 4 * (St * cb + ny * kcut * cb)   # bottom drag term: read (epilogue), write (inverse part)
+    stages = 4
+    return Wb + Pb, Pb + Wb + state / stages
+
+
+CALL_STEPS = 10  # steps per stepforward! call in the timed region (an output interval)
+
+
+def call_bytes(w, cb, call_steps=CALL_STEPS):
+    """Per-launch bytes averaged over the launches of one stepforward! call of call_steps
+    steps (the last one observed)."""
+    ro, co = launch_bytes(w, cb, True)
+    ru, cu = launch_bytes(w, cb, False)
+    f = 1.0 / call_steps
+    return f * ro + (1 - f) * ru, f * co + (1 - f) * cu
 
 
 def is_rank0():
@@ -162,8 +209,9 @@ def make_problem(w, T, precision=None):
 
 
 def set_initial_state(prob, w):
-    """The workload's initial condition, made by the library (peaked isotropic vorticity on the
-    device) or from a seeded generator (MultiLayerQG white noise); SingleLayerQG starts at rest."""
+    """The workload's initial condition at t = 0, made by the library (peaked isotropic
+    vorticity on the device) or from a seeded generator (MultiLayerQG white noise);
+    SingleLayerQG starts at rest."""
     import gfcuda
     if w["module"] == "TwoDNavierStokes":
         z0 = gfcuda.peakedisotropicspectrum(prob.grid, 6, 0.5, mask=prob.timestepper.filter, seed=1234)
@@ -171,6 +219,9 @@ def set_initial_state(prob, w):
     elif w["module"] == "MultiLayerQG":
         q0 = 1e-2 * np.random.default_rng(1234).standard_normal((w["nlayers"], w["ny"], w["nx"]))
         gfcuda.MultiLayerQG.set_q(prob, q0)
+    else:
+        gfcuda.SingleLayerQG.set_q(prob, np.zeros((w["ny"], w["nx"])))
+    prob.set_clock(0.0, 0)
 
 
 def initial_state_oracle(w):
@@ -193,12 +244,17 @@ def _events(n):
     return [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
 
 
-def time_arm(w, T, steps, warmup, flush, with_e2e, precision=None, graph=True, tune=True, shape=None):
-    """Run one precision arm: warm-up, K timed steps launched one gf_step at a time (CUDA
-    events on the legacy default stream, which orders with the library's blocking stream;
-    L2 flushed between steps) with the library's per-kernel event timing on, then K steps
-    replayed from captured multi-step CUDA graphs (one event pair), then optionally the
-    end-to-end timing through the host-buffer API."""
+def time_arm(w, T, steps, warmup, flush, with_e2e, precision=None, graph=True, tune=True, shape=None,
+             call_steps=CALL_STEPS):
+    """Run one precision arm: warm-up, then K timed stepforward! calls of call_steps steps
+    each (CUDA events on the legacy default stream, which orders with the library's
+    blocking stream; L2 flushed before every call) with the library's per-kernel event
+    timing on; then K single-step calls (every step observed, L2 flushed before each); then
+    K calls replayed from captured CUDA graphs of call_steps steps (one event pair); then
+    optionally the end-to-end timing through the host-buffer API.  Every timed leg starts
+    from the initial condition at t = 0 (the SingleLayerQG workload, nu = 0 and no filter,
+    grows to the grid scale and overflows after ~220 steps in the reference algorithm too),
+    so the state returned is the one after K x call_steps steps in every arm."""
     import ctypes as C
     import torch
     import gfcuda
@@ -208,35 +264,47 @@ def time_arm(w, T, steps, warmup, flush, with_e2e, precision=None, graph=True, t
         prob.launch_shape = shape
     elif tune:
         shape = prob.autotune(reps=3)  # the library's launch-shape autotuner
+    prob.set_graph_steps(call_steps)
     gfcuda.stepforward(prob, warmup)
     prob.synchronize()
     lib, ctx = prob._lib, prob._ctx
     ms2 = (C.c_double * 2)()
     n2 = (C.c_int64 * 2)()
     nl = C.c_int64()
-    lib.gf_profile_read(ctx, ms2, n2, C.byref(nl))  # reset counters
-    lib.gf_profile_enable(ctx, 1)
-    ev = _events(steps)
-    for i in range(steps):
-        flush.zero_()
-        ev[i][0].record()
-        prob._c(lib.gf_step(ctx, 1))
-        ev[i][1].record()
-    torch.cuda.synchronize()
-    ms = [a.elapsed_time(b) for a, b in ev]
-    prob._c(lib.gf_profile_read(ctx, ms2, n2, C.byref(nl)))
-    lib.gf_profile_enable(ctx, 0)
-    res = {"ms_per_step": sum(ms) / steps, "ms_row": ms2[0] / max(n2[0], 1), "ms_col": ms2[1] / max(n2[1], 1),
-           "n_row": n2[0], "n_col": n2[1], "launches": nl.value, "launch_shape": shape}
+
+    def timed_calls(nsteps):
+        lib.gf_profile_read(ctx, ms2, n2, C.byref(nl))  # reset counters
+        lib.gf_profile_enable(ctx, 1)                  # (per-kernel events; no graphs)
+        ev = _events(steps)
+        for i in range(steps):
+            flush.zero_()
+            ev[i][0].record()
+            prob._c(lib.gf_step(ctx, nsteps))
+            ev[i][1].record()
+        torch.cuda.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in ev) / (steps * nsteps)
+        prob._c(lib.gf_profile_read(ctx, ms2, n2, C.byref(nl)))
+        lib.gf_profile_enable(ctx, 0)
+        return ms, ms2[0] / max(n2[0], 1), ms2[1] / max(n2[1], 1), nl.value
+
+    set_initial_state(prob, w)
+    ms, mrow, mcol, launches = timed_calls(call_steps)
+    set_initial_state(prob, w)
+    mso, mrowo, mcolo, _ = timed_calls(1)
+    res = {"ms_per_step": ms, "ms_row": mrow, "ms_col": mcol, "launches": launches, "call_steps": call_steps,
+           "ms_per_step_observed": mso, "ms_row_observed": mrowo, "ms_col_observed": mcolo,
+           "launch_shape": shape}
     if graph:
-        gfcuda.stepforward(prob, 4)  # captures the graph outside the timed region
+        gfcuda.stepforward(prob, call_steps)  # captures the graph outside the timed region
+        set_initial_state(prob, w)
+        prob.synchronize()
         (e0, e1), = _events(1)
         flush.zero_()
         e0.record()
-        prob._c(lib.gf_step(ctx, steps))
+        prob._c(lib.gf_step(ctx, steps * call_steps))
         e1.record()
         torch.cuda.synchronize()
-        res["ms_per_step_graph"] = e0.elapsed_time(e1) / steps
+        res["ms_per_step_graph"] = e0.elapsed_time(e1) / (steps * call_steps)
     res["sol"] = prob.sol   # the state after the same number of steps in every arm
     if with_e2e:
         sshape = prob.spec_shape
@@ -329,7 +397,8 @@ def run_config0(cpu=True):
 def time_ensemble(steps, warmup, flush):
     """The 1536-run ensemble: one batched Problem per size class (instance i of a class
     draws its forcing with seed + i), all stepped by gf_ensemble_step; each class runs on its
-    own stream, concurrently.  Per-step timing with L2 flushes, then graph replay."""
+    own stream, concurrently.  Calls of CALL_STEPS steps with L2 flushes before each, then
+    one graph over all classes replayed."""
     import torch
     import gfcuda
     from gfcuda.core import Grid
@@ -342,24 +411,28 @@ def time_ensemble(steps, warmup, flush):
             "GPU", nx=n, dt=e["dt"], nu=e["nu"], nnu=e["nnu"], stepper=e["stepper"], T=np.float32, batch=B,
             forcing=gfcuda.Forcing("stochastic", spectrum=spec, seed=1000 * n)))
     shapes = [p.autotune(reps=3) for p in probs]  # FFT radix and tiles per size class
+    for p in probs:
+        p.set_graph_steps(0)
     gfcuda.ensemble_step(probs, warmup)
     torch.cuda.synchronize()
     ev = _events(steps)
     for i in range(steps):
         flush.zero_()
         ev[i][0].record()
-        gfcuda.ensemble_step(probs, 1)
+        gfcuda.ensemble_step(probs, CALL_STEPS)
         ev[i][1].record()
     torch.cuda.synchronize()
-    ms = sum(a.elapsed_time(b) for a, b in ev) / steps
-    gfcuda.ensemble_step(probs, 4)
+    ms = sum(a.elapsed_time(b) for a, b in ev) / (steps * CALL_STEPS)
+    for p in probs:
+        p.set_graph_steps(CALL_STEPS)
+    gfcuda.ensemble_step(probs, CALL_STEPS)  # captures the ensemble graph
     (e0, e1), = _events(1)
     flush.zero_()
     e0.record()
-    gfcuda.ensemble_step(probs, steps)
+    gfcuda.ensemble_step(probs, steps * CALL_STEPS)
     e1.record()
     torch.cuda.synchronize()
-    ms_graph = e0.elapsed_time(e1) / steps
+    ms_graph = e0.elapsed_time(e1) / (steps * CALL_STEPS)
     E = [float(np.mean(p.diagnostics([0])[:, 0])) for p in probs]
     for p in probs:
         p.close()
@@ -491,18 +564,24 @@ def whole_job(points_per_rank, world, ms_max):
     return world * points_per_rank / (ms_max * 1e-3)
 
 
-def roofline(w, res, wbytes, tag, peaks, peak_src):
-    """HBM roofline of the dominant kernel of an arm: algorithmic bytes per launch of the
-    two-sweep model over the launch duration timed with CUDA events on the library stream."""
-    words, row_w, col_w = algorithmic_words(w["module"], w["stepper"], w.get("nlayers", 1))
+def roofline(w, res, cb, tag, peaks, peak_src):
+    """HBM roofline of the dominant kernel of an arm: the bytes its launches must move
+    (launch_bytes, averaged over the launches of the timed stepforward! calls) over their
+    average duration timed with CUDA events on the library stream; the same for the launches
+    of single observed steps beside it."""
+    row_b, col_b = call_bytes(w, cb, res["call_steps"])
     dom = "col_stage" if res["ms_col"] >= res["ms_row"] else "row_nl"
-    per_launch = (col_w if dom == "col_stage" else row_w) * wbytes * points(w)
+    per_launch = col_b if dom == "col_stage" else row_b
     t = res["ms_col"] if dom == "col_stage" else res["ms_row"]
     ach = per_launch / (t * 1e-3) / 1e9
+    ob = launch_bytes(w, cb, True)[1 if dom == "col_stage" else 0]
+    to = res["ms_col_observed"] if dom == "col_stage" else res["ms_row_observed"]
     return {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": ach / peaks["hbm_gbs"], "peak_source": peak_src, "traffic": ncu_traffic(dom, tag),
             "algorithmic_bytes_per_launch": per_launch, "launch_ms": t, "row_ms": res["ms_row"],
-            "col_ms": res["ms_col"], "step_words_per_pt": words}
+            "col_ms": res["ms_col"], "calls_of_steps": res["call_steps"],
+            "observed_step": {"bytes_per_launch": ob, "launch_ms": to,
+                              "achieved": ob / (to * 1e-3) / 1e9, "frac": ob / (to * 1e-3) / 1e9 / peaks["hbm_gbs"]}}
 
 
 def relerr(a, b):
@@ -536,6 +615,7 @@ def run_ours(args):
         adj32 = time_adjoint(flush)
         adj64 = time_adjoint(flush, np.float64)
     acc = accuracy_100_steps(w)
+    acc1 = accuracy_100_steps(CONFIG1)
     cfg0 = run_config0(cpu=is_rank0())
     ms, msg, msdf, ms64, e2e_s, e2e_df = reduce_max(dist, [
         r32["ms_per_step"], r32["ms_per_step_graph"], rdf["ms_per_step"], r64["ms_per_step"],
@@ -561,9 +641,12 @@ def run_ours(args):
         "data": "synthetic",
         "config": {"workload": "TwoDNavierStokes 2048^2 FilteredRK4 dt=5e-4 nu=0, peaked isotropic IC (k0=6, E=0.5)",
                    "nx": w["nx"], "ny": w["ny"], "stepper": w["stepper"], "precision": "FP32 bulk",
-                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}",
-                   "ms_per_step_graph": msg, "launch_shape": r32["launch_shape"]},
-        "roofline": roofline(w, r32, 4, "twodns2048_fp32", peaks, peak_src),
+                   "l2": f"flushed before every timed stepforward! call of {CALL_STEPS} steps (256 MiB write)",
+                   "parallelism": f"replicas x{world}", "steps_per_call": CALL_STEPS,
+                   "model_steps_timed": args.steps * CALL_STEPS,
+                   "ms_per_step_graph": msg, "launch_shape": r32["launch_shape"],
+                   "ms_per_step_single_step_calls": r32["ms_per_step_observed"]},
+        "roofline": roofline(w, r32, 8, "twodns2048_fp32", peaks, peak_src),
         "cpu_baseline": cpu,
         "e2e": {"value": whole_job(pts, world, e2e_s), "unit": UNIT, "h2d_bytes_per_step": r32["state_bytes"],
                 "d2h_bytes_per_step": r32["state_bytes"]},
@@ -571,18 +654,18 @@ def run_ours(args):
         "clocks": clk.summary(int(os.environ.get("LOCAL_RANK", "0"))),
         "fp64_plain": {"arithmetic": "df64 (double-float pairs, 48-bit significand, FP32 pipes)", "value": vdf,
                        "ms_per_step": msdf, "ms_per_step_graph": rdf["ms_per_step_graph"],
-                       "roofline": roofline(w, rdf, 8, "twodns2048_df64", peaks, peak_src),
+                       "roofline": roofline(w, rdf, 16, "twodns2048_df64", peaks, peak_src),
                        "e2e": {"value": whole_job(pts, world, e2e_df), "unit": UNIT},
                        "rel_l2_vs_ieee_fp64": dferr},
         "fp64_ieee": {"value": v64, "ms_per_step": ms64,
-                      "roofline": roofline(w, r64, 8, "twodns2048_fp64", peaks, peak_src)},
+                      "roofline": roofline(w, r64, 16, "twodns2048_fp64", peaks, peak_src)},
         "fp32_over_fp64": value / vdf,
         "fp32_over_ieee_fp64": value / v64,
         "fp32_vs_fp64_rel_l2": acc["fp32_vs_fp64"],
         "fp32_vs_fp64_steps": acc["steps"],
         "df64_vs_fp64_rel_l2_100_steps": acc["df64_vs_fp64"],
         "fp32_vs_fp64_rel_l2_after_timed_steps": err,
-        "timed_steps_per_arm": args.warmup + 2 * args.steps + 4,
+        "states_compared_after_steps": args.steps * CALL_STEPS,
         "slqg512": {"workload": "SingleLayerQG 512^2 beta=10 mu=0.01 ETDRK4 dt=0.05, stochastic ring forcing "
                                 "kf=14 eps=1e-3, q0=0 (L2-resident: latency, no HBM fraction)",
                     "fp32": c1p / (c32["ms_per_step"] * 1e-3),
@@ -590,15 +673,18 @@ def run_ours(args):
                     "fp64_ieee": c1p / (c64["ms_per_step"] * 1e-3),
                     "ms_per_step_fp32": c32["ms_per_step"], "ms_per_step_graph_fp32": c32["ms_per_step_graph"],
                     "ms_per_step_df64": cdf["ms_per_step"], "ms_per_step_fp64": c64["ms_per_step"],
-                    "fp32_vs_fp64_rel_l2": cerr, "df64_vs_fp64_rel_l2": cdferr},
+                    "fp32_vs_fp64_rel_l2": cerr, "df64_vs_fp64_rel_l2": cdferr,
+                    "states_compared_after_steps": args.steps * CALL_STEPS,
+                    "fp32_vs_fp64_rel_l2_100_steps": acc1["fp32_vs_fp64"],
+                    "df64_vs_fp64_rel_l2_100_steps": acc1["df64_vs_fp64"]},
         "mlqg1024x3": {"workload": "MultiLayerQG 3 layers 1024^2 ETDRK4 dt=2.5e-3, H=[.2,.3,.5], "
                                    "b from rho=[4,5,5.5] (g=1), f0=1, beta=5, U=[1,.5,0], mu=0.05, q0 white noise 1e-2",
                        "points": c2p, "fp32": c2p / (m32["ms_per_step"] * 1e-3),
                        "fp64_plain_df64": c2p / (mdf["ms_per_step"] * 1e-3),
                        "ms_per_step_fp32": m32["ms_per_step"], "ms_per_step_graph_fp32": m32["ms_per_step_graph"],
                        "ms_per_step_df64": mdf["ms_per_step"],
-                       "fp32_vs_df64_rel_l2": merr, "steps_compared": args.warmup + 2 * args.steps + 4,
-                       "roofline_fp32": roofline(CONFIG2, m32, 4, "mlqg1024x3_fp32", peaks, peak_src)},
+                       "fp32_vs_df64_rel_l2": merr, "steps_compared": args.steps * CALL_STEPS,
+                       "roofline_fp32": roofline(CONFIG2, m32, 8, "mlqg1024x3_fp32", peaks, peak_src)},
         "ensemble1536": {"workload": "1536 TwoDNavierStokes runs: 1024 x 64^2 + 384 x 128^2 + 128 x 256^2, "
                                      "FilteredRK4 dt=0.01 nu=1e-4 (nnu=1), per-instance stochastic ring forcing "
                                      "kf=8 eps=1e-3, zeta0=0, FP32, three batched contexts on concurrent streams",
@@ -641,7 +727,7 @@ def run_single(args):
     else:
         shape = tuple(int(v) for v in args.shape.split(",")) if args.shape else None
         r = time_arm(w, T, args.steps, args.warmup, flush, with_e2e=False, precision=prec,
-                     tune=not (args.no_tune or shape), shape=shape)
+                     tune=not (args.no_tune or shape), shape=shape, call_steps=args.call_steps)
         r.pop("sol")
         r["pt_steps_per_s"] = points(w) / (r["ms_per_step"] * 1e-3)
     r["workload"] = args.single
@@ -657,6 +743,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--single", choices=sorted(SINGLE), help="time one arm only (profiling mode)")
     ap.add_argument("--no-tune", action="store_true", help="single mode: built-in block shapes, no autotuner")
+    ap.add_argument("--call-steps", type=int, default=CALL_STEPS, help="single mode: steps per timed call")
     ap.add_argument("--shape", help="single mode: launch shape row_radix,row_pairs,col_radix,col_columns "
                                     "instead of the autotuner (e.g. a shape it chose, for profiling)")
     args = ap.parse_args()

@@ -1151,13 +1151,16 @@ static cudaEvent_t take_event(gf_ctx* c) {
   return e;
 }
 
-// one row (products) and/or column (stage) launch, timed when profiling is on
-static int launch_stage(gf_ctx* c, const StepArgs& s, int with_row) {
+// one row (products) and/or column (stage) launch, timed when profiling is on; `prune`:
+// a stage of an unobserved step (products only for kr < kcut, state only at kept modes)
+static int launch_stage(gf_ctx* c, const StepArgs& s, int with_row, bool prune = false) {
+  Geom g = c->g;
+  if (prune) g.kout = g.kcut;
   for (int which = with_row ? 0 : 1; which < 2; ++which) {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (c->profiling) { e0 = take_event(c); e1 = take_event(c); GF_CUDA(c, cudaEventRecord(e0, c->stream)); }
-    if (which == 0) GF_CUDA(c, DISPATCH(c, launch_row, c->g, c->m, bufs(c), c->stream));
-    else GF_CUDA(c, DISPATCH(c, launch_col, c->g, c->m, s, bufs(c), c->stream));
+    if (which == 0) GF_CUDA(c, DISPATCH(c, launch_row, g, c->m, bufs(c), c->stream));
+    else GF_CUDA(c, DISPATCH(c, launch_col, g, c->m, s, bufs(c), c->stream));
     c->launches++;
     if (c->profiling) { GF_CUDA(c, cudaEventRecord(e1, c->stream)); c->ev_used.push_back({which, {e0, e1}}); }
   }
@@ -1217,15 +1220,24 @@ static void host_advance(gf_ctx* c) {
   c->step += 1;
 }
 
+// Observed and unobserved steps.  Every calcN! starts with dealias!(sol), so the aliased
+// modes of a step's result are never read by a later step: they matter only when the state
+// is looked at (the end of a stepforward! call, diagnostics, output).  A step whose result
+// nobody looks at skips them -- the products' aliased columns and the stage combination at
+// aliased modes -- and leaves exactly the same kept modes.  AB3's aliased modes of a step
+// also use the RHS of the two steps before, so the last three steps of a call are observed.
+static int observed_tail(const gf_ctx* c) { return c->kind == SK_AB3 ? 3 : 1; }
+
 // Launches of one step: the stages (row + column kernels each) and the device-clock advance.
 // W must be valid (the first half of the step's first calcN! done).
-static int enqueue_step(gf_ctx* c) {
+static int enqueue_step(gf_ctx* c, bool observed = true) {
   const double dt = c->cfg.dt;
+  const bool prune = !observed && c->g.kcut < c->g.nkr;
   for (int stg = 1; stg <= c->nstages; ++stg) {
     const double ts = c->t + (c->nstages == 4 ? (stg == 1 ? 0.0 : stg == 4 ? dt : 0.5 * dt) : 0.0);
     StepArgs s = stage_args(c, stg, ts);
     s.clk = c->dclk;
-    if (int r = launch_stage(c, s, 1)) return r;
+    if (int r = launch_stage(c, s, 1, prune)) return r;
   }
   advance_clock_kernel<<<1, 32, 0, c->stream>>>(c->dclk, dt, c->cfg.forcing_omega, c->cfg.forcing_phase,
                                                 c->cfg.forcing_kind == GF_FORCING_HARMONIC, c->nstages);
@@ -1234,9 +1246,9 @@ static int enqueue_step(gf_ctx* c) {
   return GF_OK;
 }
 
-static int one_step(gf_ctx* c) {
+static int one_step(gf_ctx* c, bool observed = true) {
   if (int r = ensure_W(c)) return r;
-  if (int r = enqueue_step(c)) return r;
+  if (int r = enqueue_step(c, observed)) return r;
   host_advance(c);
   return GF_OK;
 }
@@ -1257,7 +1269,7 @@ static int capture_steps(gf_ctx* c, int G, cudaGraphExec_t* out) {
   GF_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   int rc = GF_OK;
   for (int i = 0; i < G && rc == GF_OK; ++i) {
-    rc = enqueue_step(c);
+    rc = enqueue_step(c, i >= G - observed_tail(c));
     host_advance(c);
   }
   cudaGraph_t graph = nullptr;
@@ -1296,7 +1308,7 @@ extern "C" int gf_step(gf_ctx* c, int64_t nsteps) {
       c->launches += (int64_t)G * (2 * c->nstages + 1);
       nsteps -= G;
     } else {
-      if (int r = one_step(c)) return r;
+      if (int r = one_step(c, nsteps <= observed_tail(c))) return r;
       nsteps -= 1;
     }
   }
@@ -1357,7 +1369,7 @@ static int ensemble_capture(gf_ctx* const* ctxs, int32_t n, int G) {
   for (int32_t i = 1; i < n; ++i) cudaStreamWaitEvent(ctxs[i]->stream, ev[0], 0);   // fork
   for (int32_t i = 0; i < n && rc == GF_OK; ++i)
     for (int k = 0; k < G && rc == GF_OK; ++k) {
-      rc = enqueue_step(ctxs[i]);
+      rc = enqueue_step(ctxs[i], k >= G - observed_tail(ctxs[i]));
       host_advance(ctxs[i]);
     }
   for (int32_t i = 1; i < n; ++i) {                                                 // join
@@ -1679,11 +1691,11 @@ extern "C" int gf_autotune(gf_ctx* c, int32_t reps, int32_t* shape) {
     restore();
     if (int r = upload_clock(c)) return r;
     c->profiling = true;
-    if (int r = one_step(c)) return r;  // warm-up (and kernel attributes)
+    if (int r = one_step(c, false)) return r;  // warm-up (and kernel attributes)
     double m2[2]; int64_t n2[2];
     if (int r = gf_profile_read(c, m2, n2, nullptr)) return r;
-    for (int k = 0; k < reps; ++k)
-      if (int r = one_step(c)) return r;
+    for (int k = 0; k < reps; ++k)  // unobserved steps: the bulk of a stepforward! call
+      if (int r = one_step(c, false)) return r;
     if (int r = gf_profile_read(c, m2, n2, nullptr)) return r;
     c->profiling = prof0;
     *ms = m2[which] / std::max<int64_t>(n2[which], 1);
@@ -1697,10 +1709,11 @@ extern "C" int gf_autotune(gf_ctx* c, int32_t reps, int32_t* shape) {
   for (int ri = 0; ri < (f32 ? 3 : 1) && rc == GF_OK; ++ri) {
     const int R = radii[ri], TPF = g0.ny / R;
     if (!f32_radix_built(g0.ny, R) || TPF < 1) continue;
-    for (int C = 1; C <= 16 && rc == GF_OK; C *= 2) {
+    for (const int C : {1, 2, 3, 4, 5, 6, 8, 16}) {
+      if (rc != GF_OK) break;
       const int cs = C > 1 ? g0.ny + std::max(unit / C, 1) : g0.ny;
-      const size_t sm = col_stage_smem(g0.ny, C, cs, g0.nl, c->cb);
-      if (C * TPF > 512 || sm > (size_t)SMEM_CAP) continue;
+      const size_t sm = col_stage_smem(g0.ny, C, cs, g0.nl, c->cb, col_two_buffers(c->m, g0.nl, C * TPF));
+      if (C * TPF > col_max_threads(c->rb, g0.ny, c->m, g0.nl) || sm > (size_t)SMEM_CAP) continue;
       set_shape(c, 0, 0, R, C);
       double ms = 0;
       rc = measure(1, &ms);

@@ -24,15 +24,26 @@ template <class T, int NN, int R>
 cudaError_t launch_col_nr(const Geom& g, const ModArgs& m, const StepArgs& s, const Bufs& b, cudaStream_t st) {
   cudaError_t err = cudaSuccess;
   const size_t e = sizeof(cplx<T>);
-  auto smem = [&](int c) { return col_stage_smem(NN, c, col_stride<T>(NN, c), g.nl, e); };
+  auto smem = [&](int c) {
+    return col_stage_smem(NN, c, col_stride<T>(NN, c), g.nl, e, col_two_buffers(m, g.nl, c * (NN / R)));
+  };
   int C = pick_C(NN, R, g.nkr, smem, g.nb);
-  if (g.tuneC > 0 && g.tuneC * (NN / R) <= 512 && smem(g.tuneC) <= (size_t)SMEM_CAP) C = g.tuneC;
+  if (g.tuneC > 0) {
+    // the tuned columns per block; launches of observed steps (every column, every mode: a
+    // grid of nkr columns) stay within 512-thread blocks
+    const int maxT = g.kout > 0 ? col_max_threads(sizeof(T), NN, m, g.nl) : 512;
+    const int tc = std::min(g.tuneC, maxT / (NN / R));
+    if (tc >= 1 && smem(tc) <= (size_t)SMEM_CAP) C = tc;
+  }
   Geom g2 = g;
   g2.cs = col_stride<T>(NN, C);
   const size_t sm = smem(C);
   auto k = col_stage_kernel<T, NN, R>;
+  if constexpr (sizeof(T) == 4 && NN >= 1024)
+    if (C * (NN / R) > 512) k = col_stage_kernel<T, NN, R, 640>;
   if ((err = set_smem(k, sm)) != cudaSuccess) return err;
-  k<<<dim3((g.nkr + C - 1) / C, g.nb), C * (NN / R), sm, st>>>(g2, m, s, b, C);
+  const int ncols = g.kout > 0 ? g.kout : g.nkr;
+  k<<<dim3((ncols + C - 1) / C, g.nb), C * (NN / R), sm, st>>>(g2, m, s, b, C);
   return cudaGetLastError();
 }
 

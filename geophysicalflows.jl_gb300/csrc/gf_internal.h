@@ -27,6 +27,9 @@ struct Geom {
   float dkx_f, dky_f, inv_nxny_f;  // float copies (the FP32 kernels never touch FP64)
   float dkx_l, dky_l, inv_nxny_l;  // low words: (x_f, x_l) is the df64 value
   int cs;                          // column stride (elements) of the column kernels' buffers
+  // step-kernel launches of an unobserved step: only columns kr < kout of the products are
+  // formed and only the kept modes of the state are updated (0: every column, every mode)
+  int kout;
   // batch of independent instances (an ensemble): instance blockIdx.y of every kernel works
   // on its own slice; strides (elements) of the per-instance arrays
   int nb;

@@ -42,9 +42,23 @@ inline int pick_B(int NX, int R, size_t elem, int nbufs, int npairs, int nb = 1)
   return B;
 }
 
+// Largest column-kernel block: the one-layer path without bottom drag on FP32 columns of
+// >= 1024 points allows 640 threads (e.g. five radix-16 columns of 2048, one block per SM at
+// 96 registers a thread: the wide instantiation), everything else 512.
+inline int col_max_threads(size_t real_bytes, int NY, const ModArgs& m, int nl) {
+  return (real_bytes == 4 && NY >= 1024 && nl == 1 && !m.drag) ? 640 : 512;
+}
+
+// Blocks above 512 threads run the wide instantiation, whose single-layer path without bottom
+// drag and with at most two product fields works in two shared-memory buffers (three
+// otherwise, and in the 512-thread instantiation).
+inline bool col_two_buffers(const ModArgs& m, int nl, int threads) {
+  return threads > 512 && nl == 1 && !m.drag && 1 + m.hasB + m.hasC <= 2;
+}
+
 // shared-memory bytes of col_stage_kernel for C columns with column stride cs
-__host__ __forceinline__ size_t col_stage_smem(int NY, int C, int cs, int nl, size_t elem) {
-  if (nl == 1) return (size_t)3 * C * cs * elem;  // F0, F1, F2 (cs >= NY: also holds the general path's Xs)
+__host__ __forceinline__ size_t col_stage_smem(int NY, int C, int cs, int nl, size_t elem, bool two_buf) {
+  if (nl == 1) return (size_t)(two_buf ? 2 : 3) * C * cs * elem;  // F0, F1 (, F2: also the general path's Xs)
   return ((size_t)2 * C * cs + (size_t)nl * NY * C) * elem;  // F0, F1, X of every layer
 }
 

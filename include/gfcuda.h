@@ -175,7 +175,13 @@ int gf_set_clock(gf_ctx* ctx, double t, int64_t step);
 int gf_set_physical(gf_ctx* ctx, int which, const void* field, int where);
 
 /* ---- the hot path ----------------------------------------------------------------------- */
-/* stepforward!(prob, nsteps) (FourierFlows; calls calcN! 4x per ETDRK4/RK4 step). */
+/* stepforward!(prob, nsteps) (FourierFlows; calls calcN! 4x per ETDRK4/RK4 step).  Every
+ * calcN! starts with dealias!(sol), so the aliased modes of a step's result are read by no
+ * later step: only the last step of the call (AB3: the last three) computes them; the others
+ * form the products for the kept kr columns only and update the kept modes only.  The state
+ * the call leaves (every mode), and the clock, are bit for bit those of nsteps calls of one
+ * step each (to FP32 rounding where the autotuner gave the inner steps wider column blocks
+ * than the last step's, see gf_autotune). */
 int gf_step(gf_ctx* ctx, int64_t nsteps);
 /* stepforward!(prob, diags, nsteps): also records the diagnostics `which[0..nd)` after
  * every step into out[step*nd + d] (host memory, nsteps*nd doubles). */
@@ -267,8 +273,12 @@ int gf_step_callback(gf_ctx* ctx, int64_t nsteps, gf_forcing_fn fn, void* user);
  * (<= 0: 4) and keeps the fastest.  The state, clock, AB3 history and stochastic-forcing
  * record are restored; captured graphs are re-captured; the profiling counters are reset.
  * shape (may be NULL) receives {row radix, row pairs per block, column radix, columns per
- * block}; 0 entries mean the built-in block-shape rule.  gf_set_launch_shape applies a
- * shape found earlier (e.g. for another context of the same size). */
+ * block}; 0 entries mean the built-in block-shape rule.  The candidates are timed on the
+ * steps inside a gf_step call (those that skip the aliased modes); FP32 one-layer problems
+ * without bottom drag with columns of >= 1024 may get blocks of up to 640 threads there,
+ * while the last step of a call keeps blocks of <= 512 threads (the column count capped).
+ * gf_set_launch_shape applies a shape found earlier (e.g. for another context of the same
+ * size). */
 int gf_autotune(gf_ctx* ctx, int32_t reps, int32_t* shape);
 int gf_set_launch_shape(gf_ctx* ctx, const int32_t* shape);
 int gf_get_launch_shape(const gf_ctx* ctx, int32_t* shape);
