@@ -1991,7 +1991,9 @@ static AdjArgs adj_args(gf_ctx* c) {
 // The reverse sweep from the cotangent in adj.ubar_in (internal layout) to adj.ubar_out
 // and adj.etab; the state and clock are the forward pass's result again afterwards.
 // Recompute unit u from the current state with its forward fields kept, then run its
-// transposed stages, last step first.
+// transposed stages, last step first.  The recomputed steps skip the aliased modes: the
+// transposed stages read only the kept forward fields (q + eta, u, v), and the state after
+// the sweep is the stored forward result.
 static int adj_unit(gf_ctx* c, AdjArgs& a, int u) {
   auto& d = c->adj;
   const Geom& g = c->g;
@@ -2006,7 +2008,7 @@ static int adj_unit(gf_ctx* c, AdjArgs& a, int u) {
       StepArgs s = stage_args(c, stg, ts);
       s.clk = c->dclk;
       c->row_phys = (char*)d.phys + ((size_t)i * 4 + stg - 1) * 3 * plane;
-      const int r = launch_stage(c, s, 1);
+      const int r = launch_stage(c, s, 1, c->g.kcut < c->g.nkr);
       c->row_phys = nullptr;
       if (r) return r;
     }
