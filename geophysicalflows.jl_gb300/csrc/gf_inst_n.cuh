@@ -24,9 +24,7 @@ template <class T, int NN, int R>
 cudaError_t launch_col_nr(const Geom& g, const ModArgs& m, const StepArgs& s, const Bufs& b, cudaStream_t st) {
   cudaError_t err = cudaSuccess;
   const size_t e = sizeof(cplx<T>);
-  auto smem = [&](int c) {
-    return col_stage_smem(NN, c, col_stride<T>(NN, c), g.nl, e, col_two_buffers(m, g.nl, c * (NN / R)));
-  };
+  auto smem = [&](int c) { return col_stage_smem(NN, c, col_stride<T>(NN, c), m, g.nl, e, c * (NN / R)); };
   int C = pick_C(NN, R, g.nkr, smem, g.nb);
   if (g.tuneC > 0) {
     // the tuned columns per block; launches of observed steps (every column, every mode: a

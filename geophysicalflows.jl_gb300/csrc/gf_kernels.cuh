@@ -105,10 +105,10 @@ __device__ __forceinline__ void psi_all(const ModArgs& m, int nl, T K2, const cp
 //     one column and the swizzled Stockham accesses are conflict-free.
 // Shared memory, one layer without bottom drag: work buffers F0/F1 (C columns of g.cs slots
 // each; F2 too with three product fields) for the product and inverse FFTs, N and the next X
-// in registers.  Otherwise:
-// F0/F1 (the product fields prefetched with cp.async into one while the other is
-// transformed) and Xs (N, then the next stage X; nl x NY x C interleaved, thread-owned); the
-// PV inversion of every element is recomputed from Xs where u and v of a layer are formed.
+// in registers.  Otherwise: F0/F1/F2 (a layer's product fields, then its (q, u, v), each
+// set transformed in lockstep) and Xs (N, then the next stage X; nl x NY x C interleaved,
+// thread-owned); the PV inversion of every element is recomputed from Xs where u and v of a
+// layer are formed.
 // MAXT: largest block the instantiation is compiled for (register budget); 640 is the wide
 // FP32 variant for five radix-16 columns of 2048 (or radix-8 columns of 1024) per block.
 template <class T, int NY, int R, int MAXT = 512>
@@ -121,8 +121,8 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : sizeof(T) == 4 ? (NY >=
   const int nl = g.nl;
   cplx<T>* F0 = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* F1 = F0 + C * cs;
-  cplx<T>* F2 = F1 + C * cs;  // one layer: third work buffer (the general path's Xs)
-  cplx<T>* Xs = F2;
+  cplx<T>* F2 = F1 + C * cs;  // third work buffer (not in the wide instantiation)
+  cplx<T>* Xs = F2 + C * cs;  // the general path's N / next-X of every layer
   const int tid = threadIdx.x, c = tid % C, t = tid / C;
   const int cf = tid / TPF, tf = tid % TPF;
   const int kr = blockIdx.x * C + c;
@@ -324,44 +324,39 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : sizeof(T) == 4 ? (NY >=
     if (!s.do_inv) return;
     if ((int)blockIdx.x * C >= g.kcut) return;  // whole block aliased: W is never read there
     if constexpr (MAXT > 512) {
-      // the wide instantiation (96 registers), two buffers: q alone (u waiting in F1), then v
-      // and u in lockstep -- psi formed again from the registers for v, dead once v is written
-      auto fill = [&](int which, cplx<T>* Fb) {
+      // the wide instantiation (96 registers), two buffers: q (F0) and u (F1) filled, then the
+      // inverse FFTs of q, u and -- filled into F0 once q is stored, psi formed again from
+      // the registers -- v, one after the other from a single call site (instruction cache)
+#pragma unroll 1
+      for (int k = 0; k < 3; ++k) {
+        if (k != 1) {
 #pragma unroll
-        for (int i = 0; i < R; ++i) {
-          const int j = t + i * TPF;
-          const T lv = T(lidx(g, j)) * dky;
-          const T K2 = krT * krT + lv * lv;
-          const cplx<T> x = xr[i];
-          if (which == 0) {
-            Fb[c * cs + swz<T>(j)] = sc * x;
-            continue;
+          for (int i = 0; i < R; ++i) {
+            const int j = t + i * TPF;
+            const T lv = T(lidx(g, j)) * dky;
+            const T K2 = krT * krT + lv * lv;
+            const cplx<T> x = xr[i];
+            const cplx<T> p = psi_factor<T>(m.psi_kind, K2, ell2, m.mult, (size_t)j * g.ldk + (kin ? kr : 0)) * x;
+            if (k == 0) {
+              F0[c * cs + swz<T>(j)] = sc * x;
+              F1[c * cs + swz<T>(j)] = sc * (lv * mul_mi(p));   // u = -i l psi
+            } else {
+              F0[c * cs + swz<T>(j)] = sc * (krT * mul_i(p));   // v =  i kr psi
+            }
           }
-          const cplx<T> p = psi_factor<T>(m.psi_kind, K2, ell2, m.mult, (size_t)j * g.ldk + (kin ? kr : 0)) * x;
-          Fb[c * cs + swz<T>(j)] = which == 1 ? sc * (lv * mul_mi(p))    // u = -i l psi
-                                              : sc * (krT * mul_i(p));   // v =  i kr psi
         }
-      };
-      auto store = [&](int f, const cplx<T>* Fb) {
-        if (kr >= g.kcut) return;
-        cplx<T>* Wf = W + (size_t)f * g.ny * g.ldw + kr;
+        __syncthreads();  // (k = 2: every thread's reads of q in F0 were before the k = 1 barrier)
+        cplx<T>* Fb = (k == 1) ? F1 : F0;
+        fft_smem<T, NY, R, +1>(Fb + cf * cs, tf, tw);
+        if (kr < g.kcut) {
+          cplx<T>* Wf = W + (size_t)k * g.ny * g.ldw + kr;
 #pragma unroll
-        for (int i = 0; i < R; ++i) {
-          const int j = t + i * TPF;
-          Wf[(size_t)j * g.ldw] = Fb[c * cs + swz<T>(j)];
+          for (int i = 0; i < R; ++i) {
+            const int j = t + i * TPF;
+            Wf[(size_t)j * g.ldw] = Fb[c * cs + swz<T>(j)];
+          }
         }
-      };
-      fill(0, F0);
-      fill(1, F1);
-      __syncthreads();
-      fft_smem<T, NY, R, +1>(F0 + cf * cs, tf, tw);
-      store(0, F0);
-      __syncthreads();  // every thread's reads of F0 done
-      fill(2, F0);
-      __syncthreads();
-      fft_smem_group<T, NY, R, +1, 2>(F0 + cf * cs, C * cs, tf, tw);  // v (F0), u (F1)
-      store(1, F1);
-      store(2, F0);
+      }
     } else {
       // (q, u, v) of the next stage; each thread rewrites only the slots it read above
 #pragma unroll
@@ -394,54 +389,60 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : sizeof(T) == 4 ? (NY >=
   }
 
   if constexpr (MAXT <= 512) {  // several layers or bottom drag (the wide instantiation is one-layer only)
+    // Work buffers F0, F1, F2 and Xs (N, then the next stage's X of every layer: nl x NY x C,
+    // thread-owned).  Per layer: the product fields of the layer in one cp.async group, their
+    // FFTs in lockstep, N and the stage epilogue; then per layer the inverse FFTs of (q, u, v)
+    // in lockstep.
     if (s.do_fwd) {
       const cplx<T>* P = static_cast<const cplx<T>*>(b.P) + ib * g.bs_p;
       const int nslot = 1 + m.hasB + m.hasC;
-      const int nseq = nl * nslot;
-      // asynchronous copy of product field q = L * nslot + f into work buffer Fb
-      auto issue = [&](int q, cplx<T>* Fb) {
-        const int L = q / nslot, f = q - L * nslot;
-        const cplx<T>* Pf = P + ((size_t)f * nl + L) * lstride + kr;
-        cplx<T>* Fc = Fb + c * cs;
+      for (int L = 0; L < nl; ++L) {
+        for (int f = 0; f < nslot; ++f) {  // one cp.async group per field
+          const cplx<T>* Pf = P + ((size_t)f * nl + L) * lstride + kr;
+          cplx<T>* Fc = F0 + (size_t)f * C * cs + c * cs;
   #pragma unroll
-        for (int i = 0; i < R; ++i) {
-          const int j = t + i * TPF;
-          if (kin) cp_async_elem<T>(Fc + swz<T>(j), Pf + (size_t)j * g.ldk);
-          else Fc[swz<T>(j)] = czero<T>();
+          for (int i = 0; i < R; ++i) {
+            const int j = t + i * TPF;
+            if (kin) cp_async_elem<T>(Fc + swz<T>(j), Pf + (size_t)j * g.ldk);
+            else Fc[swz<T>(j)] = czero<T>();
+          }
+          cp_async_commit();
         }
-        cp_async_commit();
-      };
-      issue(0, F0);
-      for (int q = 0; q < nseq; ++q) {
-        cplx<T>* Fb = (q & 1) ? F1 : F0;
-        if (q + 1 < nseq) {
-          issue(q + 1, (q & 1) ? F0 : F1);
-          cp_async_wait<1>();
-        } else {
+        if constexpr (GF_FFT_MULTI && sizeof(T) == 4 && 3 * R <= 24) {
           cp_async_wait<0>();
+          __syncthreads();
+          if (nslot == 3) fft_smem_group<T, NY, R, -1, 3>(F0 + cf * cs, C * cs, tf, tw);
+          else if (nslot == 2) fft_smem_group<T, NY, R, -1, 2>(F0 + cf * cs, C * cs, tf, tw);
+          else fft_smem<T, NY, R, -1>(F0 + cf * cs, tf, tw);
+        } else {
+          // field f's FFT while the later fields' loads are still in flight
+          for (int f = 0; f < nslot; ++f) {
+            const int pending = nslot - 1 - f;
+            if (pending >= 2) cp_async_wait<2>();
+            else if (pending == 1) cp_async_wait<1>();
+            else cp_async_wait<0>();
+            __syncthreads();
+            fft_smem<T, NY, R, -1>(F0 + (size_t)f * C * cs + cf * cs, tf, tw);
+          }
         }
-        __syncthreads();
-        fft_smem<T, NY, R, -1>(Fb + cf * cs, tf, tw);
-        const int L = q / nslot, f = q - L * nslot;
-        const int slot = (f == 0) ? 0 : (f == 1 && m.hasB) ? 1 : 2;
-        cplx<T>* XL = Xs + L * NY * C + c;  // this thread's N / next-X slots: XL[j * C]
-        const cplx<T>* Fc = Fb + c * cs;
-  #pragma unroll
-        for (int i = 0; i < R; ++i) {
-          const int j = t + i * TPF;
-          const cplx<T> v = Fc[swz<T>(j)];
-          const cplx<T> d = slot_term(slot, j, v);
-          XL[j * C] = (f == 0) ? d : XL[j * C] + d;
-        }
-        __syncthreads();  // Fb is the target of the prefetch issued in the next iteration
-        if (f != nslot - 1) continue;
-        // epilogue for layer L: forcing, drag, stage combination (rolled, two elements per
-        // iteration; each thread reads back only the Xs slots it wrote)
+        // N of layer L and the stage epilogue (rolled, two elements per iteration; each
+        // thread writes only its own Xs slots)
+        cplx<T>* XL = Xs + L * NY * C + c;
   #pragma unroll 2
         for (int i = 0; i < R; ++i) {
           const int j = t + i * TPF;
-          XL[j * C] = (kin && (!prune || kept(g, kr, j))) ? epilogue(L, j, XL[j * C]) : czero<T>();
+          cplx<T> xn = czero<T>();
+          if (kin && (!prune || kept(g, kr, j))) {
+            cplx<T> N = czero<T>();
+            for (int f = 0; f < nslot; ++f) {
+              const int slot = (f == 0) ? 0 : (f == 1 && m.hasB) ? 1 : 2;
+              N = N + slot_term(slot, j, F0[(size_t)f * C * cs + c * cs + swz<T>(j)]);
+            }
+            xn = epilogue(L, j, N);
+          }
+          XL[j * C] = xn;
         }
+        __syncthreads();  // the work buffers are the next layer's load targets
       }
     } else {
       const cplx<T>* sol = static_cast<const cplx<T>*>(s.sol);
@@ -457,64 +458,45 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : sizeof(T) == 4 ? (NY >=
     }
     if (!s.do_inv) return;
     if ((int)blockIdx.x * C >= g.kcut) return;  // whole block aliased: W is never read there
-    __syncthreads();  // eig[] filled; F0 free
+    __syncthreads();  // eig[] filled
 
-    // single-layer bottom drag (several layers: in the loop below)
-    if (nl == 1 && m.drag && kin) {
-  #pragma unroll
+    // y-direction inverse FFTs of (q, u, v) of every layer, in lockstep; psi of layer L from
+    // the X of all layers at the element (several layers: PV inversion); the bottom-drag term
+    // of the next stage from the last layer's psi
+    for (int L = 0; L < nl; ++L) {
+  #pragma unroll 2  // rolled: the PV inversion per element is long code (instruction cache)
       for (int i = 0; i < R; ++i) {
         const int j = t + i * TPF;
+        const cplx<T> x = Xs[(L * NY + j) * C + c];
         const T lv = T(lidx(g, j)) * dky;
         const T K2 = krT * krT + lv * lv;
-        const size_t ti = (size_t)j * g.ldk + kr;
-        const T f = psi_factor<T>(m.psi_kind, K2, ell2, m.mult, ti);
-        Dp[ti] = (muT * K2 * f) * Xs[j * C + c];
-      }
-    }
-    // y-direction inverse FFT of (q, u, v) for every layer; psi of layer L from the X of all
-    // layers at the element (several layers: PV inversion), kept in registers for u and v
-    for (int L = 0; L < nl; ++L) {
-      cplx<T> preg[R];
-      for (int f = 0; f < 3; ++f) {
-        cplx<T>* Fb = ((L * 3 + f) & 1) ? F1 : F0;  // alternate so stores of one field overlap the next
-        cplx<T>* Fe = Fb + c * cs;
-  #pragma unroll
-        for (int i = 0; i < R; ++i) {
-          const int j = t + i * TPF;
-          const cplx<T> x = Xs[(L * NY + j) * C + c];
-          const T lv = T(lidx(g, j)) * dky;
-          cplx<T> v;
-          if (f == 0) {
-            v = x;
+        const size_t ti = (size_t)j * g.ldk + (kin ? kr : 0);
+        cplx<T> p;
+        if (nl > 1) {
+          cplx<T> X[MAXL], ps[MAXL];
+          for (int a = 0; a < nl; ++a) X[a] = Xs[(a * NY + j) * C + c];
+          if (m.psi_kind == PSI_EIGEN) {
+            psi_eigen<T>(nl, eig, K2, X, ps);
           } else {
-            if (f == 1) {
-              const T K2 = krT * krT + lv * lv;
-              const size_t ti = (size_t)j * g.ldk + (kin ? kr : 0);
-              if (nl > 1) {
-                cplx<T> X[MAXL], ps[MAXL];
-                for (int a = 0; a < nl; ++a) X[a] = Xs[(a * NY + j) * C + c];
-                if (m.psi_kind == PSI_EIGEN) {
-                  psi_eigen<T>(nl, eig, K2, X, ps);
-                } else {
-                  const T fk = psi_factor<T>(m.psi_kind, K2, ell2, m.mult, ti);
-                  for (int a = 0; a < nl; ++a) ps[a] = fk * X[a];
-                }
-                preg[i] = ps[L];
-                if (m.drag && kin && L == nl - 1) Dp[ti] = (muT * K2) * ps[nl - 1];
-              } else {
-                preg[i] = psi_factor<T>(m.psi_kind, K2, ell2, m.mult, ti) * x;
-              }
-            }
-            const cplx<T> p = preg[i];
-            v = (f == 1) ? lv * mul_mi(p)     // u = -i l psi
-                         : krT * mul_i(p);    // v =  i kr psi
+            const T fk = psi_factor<T>(m.psi_kind, K2, ell2, m.mult, ti);
+            for (int a = 0; a < nl; ++a) ps[a] = fk * X[a];
           }
-          Fe[swz<T>(j)] = sc * v;
+          p = ps[L];
+        } else {
+          p = psi_factor<T>(m.psi_kind, K2, ell2, m.mult, ti) * x;
         }
-        __syncthreads();
-        fft_smem<T, NY, R, +1>(Fb + cf * cs, tf, tw);
-        if (kr < g.kcut) {
+        if (m.drag && kin && L == nl - 1) Dp[ti] = (muT * K2) * p;
+        F0[c * cs + swz<T>(j)] = sc * x;
+        F1[c * cs + swz<T>(j)] = sc * (lv * mul_mi(p));   // u = -i l psi
+        F2[c * cs + swz<T>(j)] = sc * (krT * mul_i(p));   // v =  i kr psi
+      }
+      __syncthreads();
+      fft_smem_group<T, NY, R, +1, 3>(F0 + cf * cs, C * cs, tf, tw);
+      if (kr < g.kcut) {
+  #pragma unroll
+        for (int f = 0; f < 3; ++f) {
           cplx<T>* Wf = W + ((size_t)f * nl + L) * g.ny * g.ldw + kr;
+          const cplx<T>* Fe = F0 + (size_t)f * C * cs + c * cs;
   #pragma unroll
           for (int i = 0; i < R; ++i) {
             const int j = t + i * TPF;
@@ -522,6 +504,7 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : sizeof(T) == 4 ? (NY >=
           }
         }
       }
+      __syncthreads();  // the next layer's fill overwrites the buffers
     }
   }
 }

@@ -56,10 +56,13 @@ inline bool col_two_buffers(const ModArgs& m, int nl, int threads) {
   return threads > 512 && nl == 1 && !m.drag && 1 + m.hasB + m.hasC <= 2;
 }
 
-// shared-memory bytes of col_stage_kernel for C columns with column stride cs
-__host__ __forceinline__ size_t col_stage_smem(int NY, int C, int cs, int nl, size_t elem, bool two_buf) {
-  if (nl == 1) return (size_t)(two_buf ? 2 : 3) * C * cs * elem;  // F0, F1 (, F2: also the general path's Xs)
-  return ((size_t)2 * C * cs + (size_t)nl * NY * C) * elem;  // F0, F1, X of every layer
+// shared-memory bytes of col_stage_kernel for C columns with column stride cs and `threads`
+// threads: one layer without bottom drag F0, F1 (, F2); otherwise F0, F1, F2 and the X of
+// every layer
+__host__ __forceinline__ size_t col_stage_smem(int NY, int C, int cs, const ModArgs& m, int nl, size_t elem,
+                                               int threads) {
+  if (nl == 1 && !m.drag) return (size_t)(col_two_buffers(m, nl, threads) ? 2 : 3) * C * cs * elem;
+  return ((size_t)3 * C * cs + (size_t)nl * NY * C) * elem;
 }
 
 // Whether B row pairs per block fit the row kernel (threads, shared memory, pair count).
