@@ -35,8 +35,20 @@
 #ifndef GF_ROW_MINBLOCKS_WIDE
 #define GF_ROW_MINBLOCKS_WIDE 2   // FP64 and df64 row kernels (128 registers, no spills)
 #endif
+// Elements per iteration of the column kernel's stage-epilogue loops (code size: the
+// epilogue covers every stepper and forcing kind)
+#ifndef GF_EPI_UNROLL
+#define GF_EPI_UNROLL 1
+#endif
+// Elements per iteration of the wide column path's (q, u, v) fill loop
+#ifndef GF_FILL_UNROLL
+#define GF_FILL_UNROLL 16
+#endif
 
 namespace gf {
+
+constexpr int EPI_UNROLL = GF_EPI_UNROLL;
+constexpr int FILL_UNROLL = GF_FILL_UNROLL;
 
 // ------------------------------------------------------------------------------ helpers
 __device__ __forceinline__ bool kept(const Geom& g, int kr, int j) { return kr < g.kcut && (j < g.lA || j > g.lB); }
@@ -301,7 +313,7 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : sizeof(T) == 4 ? (NY >=
           fft_smem<T, NY, R, -1>(F0 + (size_t)f * C * cs + cf * cs, tf, tw);
         }
       }
-#pragma unroll 2
+#pragma unroll (EPI_UNROLL)
       for (int i = 0; i < R; ++i) {
         const int j = t + i * TPF;
         xr[i] = czero<T>();
@@ -330,7 +342,7 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : sizeof(T) == 4 ? (NY >=
 #pragma unroll 1
       for (int k = 0; k < 3; ++k) {
         if (k != 1) {
-#pragma unroll
+#pragma unroll (FILL_UNROLL)
           for (int i = 0; i < R; ++i) {
             const int j = t + i * TPF;
             const T lv = T(lidx(g, j)) * dky;
@@ -425,10 +437,10 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : sizeof(T) == 4 ? (NY >=
             fft_smem<T, NY, R, -1>(F0 + (size_t)f * C * cs + cf * cs, tf, tw);
           }
         }
-        // N of layer L and the stage epilogue (rolled, two elements per iteration; each
-        // thread writes only its own Xs slots)
+        // N of layer L and the stage epilogue (rolled: GF_EPI_UNROLL elements per iteration;
+        // each thread writes only its own Xs slots)
         cplx<T>* XL = Xs + L * NY * C + c;
-  #pragma unroll 2
+  #pragma unroll (EPI_UNROLL)
         for (int i = 0; i < R; ++i) {
           const int j = t + i * TPF;
           cplx<T> xn = czero<T>();
