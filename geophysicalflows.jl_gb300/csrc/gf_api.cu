@@ -48,7 +48,7 @@ struct gf_ctx {
   void *phys = nullptr;     // [4][nl][ny][nx] physical fields from updatevars!
   void *tmp_spec = nullptr; // [nl][ny][ldk] scratch spectral array
   void *tmp_spec2 = nullptr;
-  void *stage = nullptr;    // df64 contexts: double staging for spectral/physical transfers
+  void *stage = nullptr;    // staging for host transfers (contiguous copy, re-pitched / df64-converted on the device)
   double *dpart = nullptr, *dout = nullptr;
   int diag_blocks = 0;
   int ab3_out = 0, ab3_m1 = 1, ab3_m2 = 2;
@@ -202,6 +202,17 @@ __global__ void add_scalar_kernel(T* a, size_t n, double v) {
   const T tv = T(v);
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     a[i] = a[i] + tv;
+}
+
+// `rows` rows of `w` 8-byte words from one row stride to another (in words): the pitch
+// conversion between a contiguous host-transfer staging buffer and the padded layout
+__global__ void repack_kernel(const uint64_t* __restrict__ src, size_t ss, uint64_t* __restrict__ dst, size_t ds,
+                              size_t rows, size_t w) {
+  const size_t n = rows * w;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = e / w, k = e - r * w;
+    dst[r * ds + k] = src[r * ss + k];
+  }
 }
 
 // double <-> df64 copies of `rows` rows of `w` reals with their own row strides (in reals)
@@ -571,9 +582,8 @@ static int build(gf_ctx* c, const gf_config* cfg) {
       !(c->phys = dalloc(c, NB * (k.module == GF_BAROTROPICQGQL ? 7 : 4) * g.bs_phys * rb)) || !(c->dclk = (DevClock*)dalloc(c, sizeof(DevClock))))
     return fail(c, GF_ERR_NOMEM, "state buffers");
   m.D = c->D;
-  if (c->prec == GF_DF64 &&
-      !(c->stage = dalloc(c, NB * std::max(nsp * cb, g.bs_phys * rb))))
-    return fail(c, GF_ERR_NOMEM, "df64 staging");
+  if (!(c->stage = dalloc(c, NB * std::max(nsp * cb, g.bs_phys * rb))))  // host-transfer staging
+    return fail(c, GF_ERR_NOMEM, "staging");
   if (c->kind == SK_RK4) {
     if (!(c->acc = dalloc(c, NB * nsp * cb))) return fail(c, GF_ERR_NOMEM, "acc");
     if (c->hasL && !(c->X = dalloc(c, NB * nsp * cb))) return fail(c, GF_ERR_NOMEM, "X");
@@ -811,14 +821,28 @@ static int convert_launch(gf_ctx* c, bool to_df, const void* src, size_t ss, voi
   return GF_OK;
 }
 
-// caller spectral array (Julia layout, row stride nkr) -> internal array (row stride ldk)
+static int repack_launch(gf_ctx* c, const void* src, size_t ss, void* dst, size_t ds, size_t rows, size_t w) {
+  const int nb = (int)std::min<size_t>((rows * w + 255) / 256, 4096);
+  repack_kernel<<<nb, 256, 0, c->stream>>>((const uint64_t*)src, ss, (uint64_t*)dst, ds, rows, w);
+  GF_CUDA(c, cudaGetLastError());
+  return GF_OK;
+}
+
+// caller spectral array (Julia layout, row stride nkr) -> internal array (row stride ldk).
+// Host arrays travel as one contiguous copy through the staging buffer and are re-pitched on
+// the device (a pitched host copy of thousands of short rows is several times slower).
 static int copy_spec_in(gf_ctx* c, void* dst, const void* src, int where) {
   const Geom& g = c->g;
   const cudaMemcpyKind kind = where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  const size_t rows = (size_t)g.ny * g.nl * g.nb;
   if (c->prec == GF_DF64) {
     GF_CUDA(c, cudaMemcpyAsync(c->stage, src, (size_t)g.nkr * g.ny * g.nl * g.nb * 16, kind, c->stream));
     if (int r = convert_launch(c, true, c->stage, 2 * (size_t)g.nkr, dst, 2 * (size_t)g.ldk,
                                (size_t)g.ny * g.nl * g.nb, 2 * (size_t)g.nkr)) return r;
+  } else if (where == GF_HOST) {
+    const size_t wpe = c->cb / 8;  // 8-byte words per complex element
+    GF_CUDA(c, cudaMemcpyAsync(c->stage, src, rows * g.nkr * c->cb, kind, c->stream));
+    if (int r = repack_launch(c, c->stage, wpe * g.nkr, dst, wpe * g.ldk, rows, wpe * g.nkr)) return r;
   } else {
     GF_CUDA(c, cudaMemcpy2DAsync(dst, g.ldk * c->cb, src, g.nkr * c->cb, g.nkr * c->cb, (size_t)g.ny * g.nl * g.nb,
                                  kind, c->stream));
@@ -829,10 +853,15 @@ static int copy_spec_in(gf_ctx* c, void* dst, const void* src, int where) {
 static int copy_spec_out(gf_ctx* c, void* dst, const void* src, int where) {
   const Geom& g = c->g;
   const cudaMemcpyKind kind = where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  const size_t rows = (size_t)g.ny * g.nl * g.nb;
   if (c->prec == GF_DF64) {
     if (int r = convert_launch(c, false, src, 2 * (size_t)g.ldk, c->stage, 2 * (size_t)g.nkr,
                                (size_t)g.ny * g.nl * g.nb, 2 * (size_t)g.nkr)) return r;
     GF_CUDA(c, cudaMemcpyAsync(dst, c->stage, (size_t)g.nkr * g.ny * g.nl * g.nb * 16, kind, c->stream));
+  } else if (where == GF_HOST) {
+    const size_t wpe = c->cb / 8;
+    if (int r = repack_launch(c, src, wpe * g.ldk, c->stage, wpe * g.nkr, rows, wpe * g.nkr)) return r;
+    GF_CUDA(c, cudaMemcpyAsync(dst, c->stage, rows * g.nkr * c->cb, kind, c->stream));
   } else {
     GF_CUDA(c, cudaMemcpy2DAsync(dst, g.nkr * c->cb, src, g.ldk * c->cb, g.nkr * c->cb, (size_t)g.ny * g.nl * g.nb,
                                  kind, c->stream));
