@@ -23,6 +23,13 @@
 namespace gf {
 
 constexpr int TWN = 4096;  // twiddle table length (largest supported transform)
+__host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n / 2); }
+
+// FP64 / df64 FFTs: full radix passes from one run-time loop body (1) or each inlined at its
+// stride (0).
+#ifndef GF_FFT_LOOP
+#define GF_FFT_LOOP 1
+#endif
 
 // ---------------------------------------------------------------------------------------
 // df64: a double-word ("double-float") number hi + lo with |lo| <= ulp(hi)/2, giving a
@@ -227,6 +234,51 @@ __device__ __forceinline__ void fft_passes(cplx<T>* buf, int t, const cplx<T>* _
   }
 }
 
+// Number of full radix-R passes of a length-N transform (R^p <= N) and the stride after them.
+template <int N, int R> __host__ __device__ constexpr int full_passes() { int p = 0; for (int s = R; s <= N; s *= R) ++p; return p; }
+template <int N, int R> __host__ __device__ constexpr int full_stride() { int s = 1; for (int p = 0; p < full_passes<N, R>(); ++p) s *= R; return s; }
+
+// One full radix-R pass at a run-time stride Ns = R^p (2^lg): the same arithmetic as
+// fft_passes at that Ns, but one body serves every full pass (code size: the step kernels
+// are bound by instruction fetch when every pass is inlined separately).
+template <class T, int N, int R, int DIR, int NF>
+__device__ __forceinline__ void fft_pass_dyn(cplx<T>* buf, int stride, int t, const cplx<T>* __restrict__ tw,
+                                             int Ns, int lg) {
+  constexpr int TWR = TWN / R;  // TWS = TWN / (Ns R) = TWR >> lg
+  cplx<T> v[NF][R];
+#pragma unroll
+  for (int f = 0; f < NF; ++f)
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[f][r] = buf[f * stride + swz<T>(t + r * (N / R))];
+  const int k = t & (Ns - 1);
+  if (Ns > 1) {
+    const int tws = TWR >> lg;
+    cplx<T> w[R];
+    if constexpr (sizeof(T) == 4) {
+      const cplx<T> w1 = twiddle<DIR>(tw, k * tws);
+      w[1] = w1;
+#pragma unroll
+      for (int r = 2; r < R; ++r) w[r] = w[r - 1] * w1;
+    } else {
+#pragma unroll
+      for (int r = 1; r < R; ++r) w[r] = twiddle<DIR>(tw, r * k * tws);
+    }
+#pragma unroll
+    for (int f = 0; f < NF; ++f)
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[f][r] = v[f][r] * w[r];
+  }
+#pragma unroll
+  for (int f = 0; f < NF; ++f) dft<R, DIR>(v[f]);
+  __syncthreads();
+  const int idxD = ((t >> lg) << lg) * R + k;
+#pragma unroll
+  for (int f = 0; f < NF; ++f)
+#pragma unroll
+    for (int r = 0; r < R; ++r) buf[f * stride + swz<T>(idxD + r * Ns)] = v[f][r];
+  __syncthreads();
+}
+
 // NF independent length-N Stockham FFTs in lockstep on buffers buf + f * stride: one pair of
 // block barriers per pass for all of them, NF x R independent shared-memory loads in flight
 // per thread, and one twiddle computation shared by the NF butterflies of a thread.
@@ -287,7 +339,15 @@ __device__ __forceinline__ void fft_passes_multi(cplx<T>* buf, int stride, int t
 // NF in-place FFTs of buffers buf + f * stride (same layout as fft_smem), in lockstep.
 template <class T, int N, int R, int DIR, int NF>
 __device__ __forceinline__ void fft_smem_multi(cplx<T>* buf, int stride, int t, const cplx<T>* __restrict__ tw) {
-  fft_passes_multi<T, N, R, DIR, 1, NF>(buf, stride, t, tw);
+  if constexpr (GF_FFT_LOOP && sizeof(T) == 8) {
+    int lg = 0;
+#pragma unroll 1
+    for (int Ns = 1; Ns < full_stride<N, R>(); Ns *= R, lg += ilog2(R))
+      fft_pass_dyn<T, N, R, DIR, NF>(buf, stride, t, tw, Ns, lg);
+    fft_passes_multi<T, N, R, DIR, full_stride<N, R>(), NF>(buf, stride, t, tw);
+  } else {
+    fft_passes_multi<T, N, R, DIR, 1, NF>(buf, stride, t, tw);
+  }
 }
 
 // NF FFTs of buffers buf + f * stride: in lockstep when the registers allow (FP32, NF x R <=
@@ -297,10 +357,19 @@ __device__ __forceinline__ void fft_smem_group(cplx<T>* buf, int stride, int t, 
 
 // In-place length-N FFT (DIR = -1 forward, +1 inverse; both unnormalised) of the swizzled
 // buffer buf (logical element a at buf[swz<T>(a)]) by threads t in [0, N/R).  Every thread
-// of the block must call it (it synchronises the block).
+// of the block must call it (it synchronises the block).  In FP64 and df64 the full radix-R
+// passes run from one loop body and the remaining smaller-radix pass after them (their
+// butterflies are long code); FP32 inlines every pass at its stride (measured faster).
 template <class T, int N, int R, int DIR>
 __device__ __forceinline__ void fft_smem(cplx<T>* buf, int t, const cplx<T>* __restrict__ tw) {
-  fft_passes<T, N, R, DIR, 1>(buf, t, tw);
+  if constexpr (GF_FFT_LOOP && sizeof(T) == 8) {
+    int lg = 0;
+#pragma unroll 1
+    for (int Ns = 1; Ns < full_stride<N, R>(); Ns *= R, lg += ilog2(R)) fft_pass_dyn<T, N, R, DIR, 1>(buf, 0, t, tw, Ns, lg);
+    fft_passes<T, N, R, DIR, full_stride<N, R>()>(buf, t, tw);
+  } else {
+    fft_passes<T, N, R, DIR, 1>(buf, t, tw);
+  }
 }
 
 #ifndef GF_FFT_MULTI
