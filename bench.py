@@ -98,6 +98,30 @@ def launch_bytes(w, cb, observed):
     return Wb + Pb, Pb + Wb + state / stages
 
 
+def algorithmic_bytes(w, word):
+    """Bytes per step of the two-sweep reference model of a pseudospectral step: per calcN!
+    stage read the stage input (1 word/pt), write and read k inverse-transformed fields,
+    write and read m products, write N (1), read a physical parameter arrays, plus C
+    stage-combination sweeps per step (RK4 / FilteredRK4 16, ETDRK4 23); `word` = 4 (FP32)
+    or 8 (FP64).  It counts every mode in every step (no pruning, no L2 reuse), so it is an
+    upper figure beside launch_bytes."""
+    k, m, a = 3, 2, 0
+    if w["module"] == "MultiLayerQG":
+        m = 3
+    if w["module"] == "SingleLayerQG" and w.get("eta"):
+        a = 1
+    C = 23 if "ETDRK4" in w["stepper"] else 16
+    return word * points(w) * (4 * (2 + 2 * k + 2 * m + a) + C)
+
+
+def step_roofline(w, ms_per_step, word, peaks):
+    """The whole step against HBM with the two-sweep model's bytes (algorithmic_bytes)."""
+    b = algorithmic_bytes(w, word)
+    ach = b / (ms_per_step * 1e-3) / 1e9
+    return {"model": "two-sweep words/pt*step", "bytes_per_step": b, "achieved": ach, "unit": "GB/s",
+            "frac": ach / peaks["hbm_gbs"]}
+
+
 CALL_STEPS = 10  # steps per stepforward! call in the timed region (an output interval)
 
 
@@ -647,6 +671,7 @@ def run_ours(args):
                    "ms_per_step_graph": msg, "launch_shape": r32["launch_shape"],
                    "ms_per_step_single_step_calls": r32["ms_per_step_observed"]},
         "roofline": roofline(w, r32, 8, "twodns2048_fp32", peaks, peak_src),
+        "roofline_step_two_sweep": step_roofline(w, ms, 4, peaks),
         "cpu_baseline": cpu,
         "e2e": {"value": whole_job(pts, world, e2e_s), "unit": UNIT, "h2d_bytes_per_step": r32["state_bytes"],
                 "d2h_bytes_per_step": r32["state_bytes"]},
@@ -655,10 +680,12 @@ def run_ours(args):
         "fp64_plain": {"arithmetic": "df64 (double-float pairs, 48-bit significand, FP32 pipes)", "value": vdf,
                        "ms_per_step": msdf, "ms_per_step_graph": rdf["ms_per_step_graph"],
                        "roofline": roofline(w, rdf, 16, "twodns2048_df64", peaks, peak_src),
+                       "roofline_step_two_sweep": step_roofline(w, msdf, 8, peaks),
                        "e2e": {"value": whole_job(pts, world, e2e_df), "unit": UNIT},
                        "rel_l2_vs_ieee_fp64": dferr},
         "fp64_ieee": {"value": v64, "ms_per_step": ms64,
-                      "roofline": roofline(w, r64, 16, "twodns2048_fp64", peaks, peak_src)},
+                      "roofline": roofline(w, r64, 16, "twodns2048_fp64", peaks, peak_src),
+                      "roofline_step_two_sweep": step_roofline(w, ms64, 8, peaks)},
         "fp32_over_fp64": value / vdf,
         "fp32_over_ieee_fp64": value / v64,
         "fp32_vs_fp64_rel_l2": acc["fp32_vs_fp64"],
