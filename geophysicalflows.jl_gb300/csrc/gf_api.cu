@@ -40,6 +40,7 @@ struct gf_ctx {
   // device buffers
   std::vector<void*> allocs;
   void *sol = nullptr, *X = nullptr, *acc = nullptr, *s1 = nullptr, *N1 = nullptr, *R3[3] = {nullptr, nullptr, nullptr};
+  void* Xg = nullptr;       // several layers: the next stage's X between the two column launches
   void *W = nullptr, *P = nullptr, *D = nullptr, *twid = nullptr;
   void *Ltab = nullptr, *filt = nullptr, *etd[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   void *mult = nullptr, *eta = nullptr, *U1D = nullptr, *Qy1D = nullptr, *Qx2D = nullptr, *Qy2D = nullptr,
@@ -584,6 +585,7 @@ static int build(gf_ctx* c, const gf_config* cfg) {
   m.D = c->D;
   if (!(c->stage = dalloc(c, NB * std::max(nsp * cb, g.bs_phys * rb))))  // host-transfer staging
     return fail(c, GF_ERR_NOMEM, "staging");
+  if (g.nl > 1 && !(c->Xg = dalloc(c, NB * nsp * cb))) return fail(c, GF_ERR_NOMEM, "layer X");
   if (c->kind == SK_RK4) {
     if (!(c->acc = dalloc(c, NB * nsp * cb))) return fail(c, GF_ERR_NOMEM, "acc");
     if (c->hasL && !(c->X = dalloc(c, NB * nsp * cb))) return fail(c, GF_ERR_NOMEM, "X");
@@ -1159,7 +1161,7 @@ static StepArgs stage_args(gf_ctx* c, int stage, double tstage) {
   s.dt = c->cfg.dt;
   s.Ltab = c->Ltab; s.filt = c->filt;
   s.e = c->etd[0]; s.e2 = c->etd[1]; s.zeta = c->etd[2]; s.alpha = c->etd[3]; s.beta = c->etd[4]; s.gamma = c->etd[5];
-  s.sol = c->sol; s.X = c->X; s.acc = c->acc; s.s1 = c->s1; s.N1 = c->N1;
+  s.sol = c->sol; s.X = c->X; s.acc = c->acc; s.s1 = c->s1; s.N1 = c->N1; s.Xg = c->Xg;
   if (c->kind == SK_AB3) { s.Rout = c->R3[c->ab3_out]; s.Rm1 = c->R3[c->ab3_m1]; s.Rm2 = c->R3[c->ab3_m2]; }
   s.fkind = c->cfg.forcing_kind;
   s.Fh = c->Fh;

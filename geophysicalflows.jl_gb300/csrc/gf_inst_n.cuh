@@ -41,7 +41,26 @@ cudaError_t launch_col_nr(const Geom& g, const ModArgs& m, const StepArgs& s, co
     if (C * (NN / R) > 512) k = col_stage_kernel<T, NN, R, 640>;
   if ((err = set_smem(k, sm)) != cudaSuccess) return err;
   const int ncols = g.kout > 0 ? g.kout : g.nkr;
-  k<<<dim3((ncols + C - 1) / C, g.nb), C * (NN / R), sm, st>>>(g2, m, s, b, C);
+  if (g.nl == 1) {
+    k<<<dim3((ncols + C - 1) / C, g.nb), C * (NN / R), sm, st>>>(g2, m, s, b, C);
+    return cudaGetLastError();
+  }
+  // several layers: one launch for the forward half (every (column block, layer)), one for
+  // the inverse half (column blocks below kcut, every layer)
+  StepArgs sf = s;
+  sf.layer_split = 1;
+  if (s.do_fwd) {
+    sf.do_inv = 0;
+    k<<<dim3((ncols + C - 1) / C, g.nb, g.nl), C * (NN / R), sm, st>>>(g2, m, sf, b, C);
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+  }
+  if (s.do_inv) {
+    StepArgs si = sf;
+    si.do_fwd = 0;
+    si.do_inv = 1;
+    if (s.do_fwd) si.sol = s.Xg;
+    k<<<dim3((std::min(ncols, g.kcut) + C - 1) / C, g.nb, g.nl), C * (NN / R), sm, st>>>(g2, m, si, b, C);
+  }
   return cudaGetLastError();
 }
 

@@ -94,6 +94,10 @@ struct StepArgs {
   uint64_t seed, step;
   float dt_f, fscale_f, dt_l, fscale_l;
   const DevClock* clk;  // if set, step / fscale / AB3 start-up come from the device clock
+  // several layers: column stage as two launches over (column block, layer) -- see the
+  // column kernel; Xg holds the next stage's X of every layer between them
+  int layer_split;
+  void* Xg;
 };
 
 // value of a host-prepared scalar (double d, its float rounding h and the remainder l) in

@@ -405,10 +405,17 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : sizeof(T) == 4 ? (NY >=
     // thread-owned).  Per layer: the product fields of the layer in one cp.async group, their
     // FFTs in lockstep, N and the stage epilogue; then per layer the inverse FFTs of (q, u, v)
     // in lockstep.
+    // Layer split (several layers, s.layer_split): one block per (column block, layer L =
+    // blockIdx.z) and two launches per stage -- the forward launch writes the next stage's X
+    // of its layer to s.Xg; the inverse launch (do_fwd = 0, s.sol = s.Xg) reads the X of
+    // every layer at each element from there for the PV inversion of its layer.  Three times
+    // the blocks, and no Xs in shared memory.
+    const bool split = s.layer_split;
+    const int L0 = split ? (int)blockIdx.z : 0, L1 = split ? L0 + 1 : nl;
     if (s.do_fwd) {
       const cplx<T>* P = static_cast<const cplx<T>*>(b.P) + ib * g.bs_p;
       const int nslot = 1 + m.hasB + m.hasC;
-      for (int L = 0; L < nl; ++L) {
+      for (int L = L0; L < L1; ++L) {
         for (int f = 0; f < nslot; ++f) {  // one cp.async group per field
           const cplx<T>* Pf = P + ((size_t)f * nl + L) * lstride + kr;
           cplx<T>* Fc = F0 + (size_t)f * C * cs + c * cs;
@@ -452,11 +459,12 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : sizeof(T) == 4 ? (NY >=
             }
             xn = epilogue(L, j, N);
           }
-          XL[j * C] = xn;
+          if (!split) XL[j * C] = xn;
+          else if (kin) static_cast<cplx<T>*>(s.Xg)[ioff + (size_t)L * lstride + (size_t)j * g.ldk + kr] = xn;
         }
         __syncthreads();  // the work buffers are the next layer's load targets
       }
-    } else {
+    } else if (!split) {
       const cplx<T>* sol = static_cast<const cplx<T>*>(s.sol);
       for (int L = 0; L < nl; ++L) {
   #pragma unroll
@@ -475,18 +483,25 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : sizeof(T) == 4 ? (NY >=
     // y-direction inverse FFTs of (q, u, v) of every layer, in lockstep; psi of layer L from
     // the X of all layers at the element (several layers: PV inversion); the bottom-drag term
     // of the next stage from the last layer's psi
-    for (int L = 0; L < nl; ++L) {
+    const cplx<T>* Xsrc = static_cast<const cplx<T>*>(s.sol) + ioff;  // layer split: X of every layer
+    for (int L = L0; L < L1; ++L) {
   #pragma unroll 2  // rolled: the PV inversion per element is long code (instruction cache)
       for (int i = 0; i < R; ++i) {
         const int j = t + i * TPF;
-        const cplx<T> x = Xs[(L * NY + j) * C + c];
+        const bool xin = kin && kept(g, kr, j);
+        // X of layer a at this element
+        auto Xat = [&](int a) -> cplx<T> {
+          if (!split) return Xs[(a * NY + j) * C + c];
+          return xin ? Xsrc[(size_t)a * lstride + (size_t)j * g.ldk + kr] : czero<T>();
+        };
+        const cplx<T> x = Xat(L);
         const T lv = T(lidx(g, j)) * dky;
         const T K2 = krT * krT + lv * lv;
         const size_t ti = (size_t)j * g.ldk + (kin ? kr : 0);
         cplx<T> p;
         if (nl > 1) {
           cplx<T> X[MAXL], ps[MAXL];
-          for (int a = 0; a < nl; ++a) X[a] = Xs[(a * NY + j) * C + c];
+          for (int a = 0; a < nl; ++a) X[a] = Xat(a);
           if (m.psi_kind == PSI_EIGEN) {
             psi_eigen<T>(nl, eig, K2, X, ps);
           } else {

@@ -62,6 +62,7 @@ inline bool col_two_buffers(const ModArgs& m, int nl, int threads) {
 __host__ __forceinline__ size_t col_stage_smem(int NY, int C, int cs, const ModArgs& m, int nl, size_t elem,
                                                int threads) {
   if (nl == 1 && !m.drag) return (size_t)(col_two_buffers(m, nl, threads) ? 2 : 3) * C * cs * elem;
+  if (nl > 1) return (size_t)3 * C * cs * elem;  // layer split: X of every layer in global memory
   return ((size_t)3 * C * cs + (size_t)nl * NY * C) * elem;
 }
 
