@@ -94,6 +94,8 @@ def launch_bytes(w, cb, observed):
         state += 5 * S * cb + St * rb             # draw -> F (w), F read x3, previous state (w); spectrum
     if w.get("mu", 0) > 0 and w["module"] == "MultiLayerQG":
         state += 4 * (St * cb + ny * kcut * cb)   # bottom drag term: read (epilogue), write (inverse part)
+    if nl > 1:
+        state += 4 * (nl * ny * kout + kept) * cb  # next-stage X between the two column launches
     stages = 4
     return Wb + Pb, Pb + Wb + state / stages
 
