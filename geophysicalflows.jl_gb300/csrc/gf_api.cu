@@ -63,7 +63,8 @@ struct gf_ctx {
   // device clock and graph replay of multi-step sequences
   DevClock* dclk = nullptr;
   int graph_steps = 4;
-  cudaGraphExec_t gexec[3] = {nullptr, nullptr, nullptr};
+  // captured step sequences [AB3 ring phase][0: every step unobserved, 1: the last observed]
+  cudaGraphExec_t gexec[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
   bool own_stream = false;
   // adjoint (gf_adjoint_setup): checkpoints, the recomputed forward fields of one segment,
   // and the cotangent arrays; freed by gf_destroy or a new set-up
@@ -87,7 +88,7 @@ struct gf_ctx {
   void* row_phys = nullptr;  // forward row kernels also store (q + eta, u, v) here when set
   // identity and graph generation (an ensemble graph records the members it was built for)
   uint64_t uid = 0, gen = 0;
-  cudaGraphExec_t egraph = nullptr;                    // ensemble graph held by its first member
+  cudaGraphExec_t egraph[2] = {nullptr, nullptr};      // ensemble graphs held by the first member (as gexec)
   std::vector<std::pair<uint64_t, uint64_t>> emembers;  // (uid, gen) of its members
   int eG = 0;
   cudaEvent_t order_ev = nullptr;  // orders this context's stream with an ensemble graph launch
@@ -795,8 +796,9 @@ extern "C" int gf_destroy(gf_ctx* c) {
   for (void* p : c->allocs) cudaFree(p);
   for (auto e : c->ev_free) cudaEventDestroy(e);
   for (auto& u : c->ev_used) { cudaEventDestroy(u.second.first); cudaEventDestroy(u.second.second); }
-  for (auto& gx : c->gexec) if (gx) cudaGraphExecDestroy(gx);
-  if (c->egraph) cudaGraphExecDestroy(c->egraph);
+  for (auto& ph : c->gexec)
+    for (auto& gx : ph) if (gx) cudaGraphExecDestroy(gx);
+  for (auto& gx : c->egraph) if (gx) cudaGraphExecDestroy(gx);
   if (c->order_ev) cudaEventDestroy(c->order_ev);
   for (void* p : c->adj.mem) cudaFree(p);
   if (c->own_stream) cudaStreamDestroy(c->stream);
@@ -1284,15 +1286,23 @@ static int one_step(gf_ctx* c, bool observed = true) {
   return GF_OK;
 }
 
-static void drop_graphs(gf_ctx* c) {
-  for (auto& gx : c->gexec)
+static void drop_ensemble_graphs(gf_ctx* c) {
+  for (auto& gx : c->egraph)
     if (gx) { cudaGraphExecDestroy(gx); gx = nullptr; }
-  if (c->egraph) { cudaGraphExecDestroy(c->egraph); c->egraph = nullptr; }
+}
+
+static void drop_graphs(gf_ctx* c) {
+  for (auto& ph : c->gexec)
+    for (auto& gx : ph)
+      if (gx) { cudaGraphExecDestroy(gx); gx = nullptr; }
+  drop_ensemble_graphs(c);
   c->gen++;
 }
 
-// Capture G steps (starting from the current AB3 ring phase) into an executable graph.
-static int capture_steps(gf_ctx* c, int G, cudaGraphExec_t* out) {
+// Capture G steps (starting from the current AB3 ring phase) into an executable graph; with
+// last_observed the last step (AB3: three) computes the aliased modes, otherwise none does
+// (a replay followed by further steps of the same call).
+static int capture_steps(gf_ctx* c, int G, cudaGraphExec_t* out, bool last_observed) {
   const double t0 = c->t;
   const int64_t s0 = c->step, l0 = c->launches;
   const int r0 = c->ab3_out, r1 = c->ab3_m1, r2 = c->ab3_m2;
@@ -1300,7 +1310,7 @@ static int capture_steps(gf_ctx* c, int G, cudaGraphExec_t* out) {
   GF_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   int rc = GF_OK;
   for (int i = 0; i < G && rc == GF_OK; ++i) {
-    rc = enqueue_step(c, i >= G - observed_tail(c));
+    rc = enqueue_step(c, last_observed && i >= G - observed_tail(c));
     host_advance(c);
   }
   cudaGraph_t graph = nullptr;
@@ -1332,9 +1342,10 @@ extern "C" int gf_step(gf_ctx* c, int64_t nsteps) {
     if (G > 0 && nsteps >= G && !c->profiling) {
       if (int r = ensure_W(c)) return r;
       const int phase = (c->kind == SK_AB3) ? c->ab3_out : 0;
-      if (!c->gexec[phase])
-        if (int r = capture_steps(c, G, &c->gexec[phase])) return r;
-      GF_CUDA(c, cudaGraphLaunch(c->gexec[phase], c->stream));
+      const int obs = nsteps - G < observed_tail(c);  // replay holds some of the call's last steps
+      if (!c->gexec[phase][obs])
+        if (int r = capture_steps(c, G, &c->gexec[phase][obs], obs)) return r;
+      GF_CUDA(c, cudaGraphLaunch(c->gexec[phase][obs], c->stream));
       for (int i = 0; i < G; ++i) host_advance(c);
       c->launches += (int64_t)G * (2 * c->nstages + 1);
       nsteps -= G;
@@ -1381,7 +1392,7 @@ extern "C" int gf_step_callback(gf_ctx* c, int64_t nsteps, gf_forcing_fn fn, voi
 // G steps of all of them are captured as ONE graph on the first context's stream -- the
 // other contexts' streams fork from it and join back, so their kernels run concurrently --
 // and replayed with one launch; otherwise each context steps on its own stream.
-static int ensemble_capture(gf_ctx* const* ctxs, int32_t n, int G) {
+static int ensemble_capture(gf_ctx* const* ctxs, int32_t n, int G, int obs) {
   gf_ctx* o = ctxs[0];
   std::vector<cudaEvent_t> ev;
   auto cleanup = [&]() { for (auto e : ev) cudaEventDestroy(e); };
@@ -1400,7 +1411,7 @@ static int ensemble_capture(gf_ctx* const* ctxs, int32_t n, int G) {
   for (int32_t i = 1; i < n; ++i) cudaStreamWaitEvent(ctxs[i]->stream, ev[0], 0);   // fork
   for (int32_t i = 0; i < n && rc == GF_OK; ++i)
     for (int k = 0; k < G && rc == GF_OK; ++k) {
-      rc = enqueue_step(ctxs[i], k >= G - observed_tail(ctxs[i]));
+      rc = enqueue_step(ctxs[i], obs && k >= G - observed_tail(ctxs[i]));
       host_advance(ctxs[i]);
     }
   for (int32_t i = 1; i < n; ++i) {                                                 // join
@@ -1415,10 +1426,15 @@ static int ensemble_capture(gf_ctx* const* ctxs, int32_t n, int G) {
   cleanup();
   if (rc != GF_OK) { if (graph) cudaGraphDestroy(graph); return rc; }
   if (e != cudaSuccess) return fail(o, GF_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-  if (o->egraph) { cudaGraphExecDestroy(o->egraph); o->egraph = nullptr; }
-  e = cudaGraphInstantiate(&o->egraph, graph, 0);
+  // a new membership or graph length invalidates both kinds
+  bool same = o->eG == G && (int32_t)o->emembers.size() == n;
+  for (int32_t i = 0; same && i < n; ++i)
+    same = o->emembers[i].first == ctxs[i]->uid && o->emembers[i].second == ctxs[i]->gen;
+  if (!same) drop_ensemble_graphs(o);
+  if (o->egraph[obs]) { cudaGraphExecDestroy(o->egraph[obs]); o->egraph[obs] = nullptr; }
+  e = cudaGraphInstantiate(&o->egraph[obs], graph, 0);
   cudaGraphDestroy(graph);
-  if (e != cudaSuccess) { o->egraph = nullptr; return fail(o, GF_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e)); }
+  if (e != cudaSuccess) { o->egraph[obs] = nullptr; return fail(o, GF_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e)); }
   o->emembers.clear();
   for (int32_t i = 0; i < n; ++i) o->emembers.push_back({ctxs[i]->uid, ctxs[i]->gen});
   o->eG = G;
@@ -1442,11 +1458,12 @@ extern "C" int gf_ensemble_step(gf_ctx* const* ctxs, int32_t n, int64_t nsteps) 
   while (one_graph && nsteps >= G) {
     for (int32_t i = 0; i < n; ++i)
       if (int r = ensure_W(ctxs[i])) { g_create_error = ctxs[i]->err; return r; }
-    bool same = o->egraph && o->eG == G && (int32_t)o->emembers.size() == n;
+    const int obs = nsteps - G < 1;  // the replay holds the call's last step
+    bool same = o->egraph[obs] && o->eG == G && (int32_t)o->emembers.size() == n;
     for (int32_t i = 0; same && i < n; ++i)
       same = o->emembers[i].first == ctxs[i]->uid && o->emembers[i].second == ctxs[i]->gen;
     if (!same)
-      if (int r = ensemble_capture(ctxs, n, G)) { g_create_error = o->err; return r; }
+      if (int r = ensemble_capture(ctxs, n, G, obs)) { g_create_error = o->err; return r; }
     // the graph (on the first stream) waits for the members' earlier work and their streams
     // wait for the graph, so that later calls on any member are ordered after it
     for (int32_t i = 0; i < n; ++i)
@@ -1455,7 +1472,7 @@ extern "C" int gf_ensemble_step(gf_ctx* const* ctxs, int32_t n, int64_t nsteps) 
       GF_CUDA(ctxs[i], cudaEventRecord(ctxs[i]->order_ev, ctxs[i]->stream));
       GF_CUDA(o, cudaStreamWaitEvent(o->stream, ctxs[i]->order_ev, 0));
     }
-    const cudaError_t e = cudaGraphLaunch(o->egraph, o->stream);
+    const cudaError_t e = cudaGraphLaunch(o->egraph[obs], o->stream);
     if (e != cudaSuccess) return fail(o, GF_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(e));
     GF_CUDA(o, cudaEventRecord(o->order_ev, o->stream));
     for (int32_t i = 1; i < n; ++i) GF_CUDA(ctxs[i], cudaStreamWaitEvent(ctxs[i]->stream, o->order_ev, 0));

@@ -102,6 +102,29 @@ def test_surfaceqg_and_qgql():
     same(p, q)
 
 
+@pytest.mark.parametrize("stepper", ["FilteredRK4", "ETDRK4", "AB3"])
+@pytest.mark.parametrize("nsteps", [8, 12, 13])
+def test_graph_replays_of_a_long_call(stepper, nsteps):
+    """calls longer than the graph: replays followed by more steps of the same call capture
+    every step unobserved, the replay that ends the call its last step (AB3: three)
+    observed; the result equals single-step calls bit for bit"""
+    n = 128
+    spec = O.ring_forcing_spectrum(O.Grid(n), 8.0, 1.5, 1e-3)
+    make = lambda: TD.Problem("GPU", nx=n, dt=0.005, nu=1e-4, nnu=1, stepper=stepper, T=np.float32,
+                              forcing=Forcing("stochastic", spectrum=spec, seed=7))
+    p, q = make(), make()
+    for r in (p, q):
+        TD.set_zeta(r, zeta0(n, 4))
+    p.set_graph_steps(4)
+    q.set_graph_steps(0)
+    stepforward(p, nsteps)
+    stepforward(p, nsteps)        # the captured graphs replayed again
+    for _ in range(2 * nsteps):
+        stepforward(q, 1)
+    same(p, q)
+    assert TD.energy_work(p) == TD.energy_work(q)
+
+
 @pytest.mark.parametrize("shape", [(8, 1, 8, 5), (8, 1, 16, 5)])
 def test_wide_column_blocks(shape):
     """FP32 columns of 1024 with five columns per block (640 threads: the wide instantiation,
