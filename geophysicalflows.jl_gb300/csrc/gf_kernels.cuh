@@ -40,6 +40,11 @@
 #ifndef GF_EPI_UNROLL
 #define GF_EPI_UNROLL 1
 #endif
+// Column kernel, one layer: prefetch the stage input and accumulator of the element this many
+// iterations ahead in the epilogue loop (0: off)
+#ifndef GF_EPI_PREFETCH
+#define GF_EPI_PREFETCH 1
+#endif
 // Elements per iteration of the wide column path's (q, u, v) fill loop
 #ifndef GF_FILL_UNROLL
 #define GF_FILL_UNROLL 16
@@ -316,6 +321,14 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : sizeof(T) == 4 ? (NY >=
 #pragma unroll (EPI_UNROLL)
       for (int i = 0; i < R; ++i) {
         const int j = t + i * TPF;
+        constexpr int PF = MAXT > 512 ? 0 : GF_EPI_PREFETCH;  // measured: helps 512-thread blocks only
+        if constexpr (PF > 0) {
+          if (kin && i + PF < R) {  // the state of a later element towards L1
+            const size_t sn = ioff + (size_t)(j + PF * TPF) * g.ldk + kr;
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(static_cast<const cplx<T>*>(s.sol) + sn));
+            if (s.acc) asm volatile("prefetch.global.L1 [%0];" ::"l"(static_cast<const cplx<T>*>(s.acc) + sn));
+          }
+        }
         xr[i] = czero<T>();
         if (!kin || (prune && !kept(g, kr, j))) continue;
         cplx<T> N = czero<T>();
@@ -450,6 +463,13 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : sizeof(T) == 4 ? (NY >=
   #pragma unroll (EPI_UNROLL)
         for (int i = 0; i < R; ++i) {
           const int j = t + i * TPF;
+          if constexpr (GF_EPI_PREFETCH > 0 && sizeof(T) == 8) {  // measured: FP32 is better without
+            if (kin && i + GF_EPI_PREFETCH < R) {  // the state of a later element towards L1
+              const size_t sn = ioff + (size_t)L * lstride + (size_t)(j + GF_EPI_PREFETCH * TPF) * g.ldk + kr;
+              asm volatile("prefetch.global.L1 [%0];" ::"l"(static_cast<const cplx<T>*>(s.sol) + sn));
+              if (s.acc) asm volatile("prefetch.global.L1 [%0];" ::"l"(static_cast<const cplx<T>*>(s.acc) + sn));
+            }
+          }
           cplx<T> xn = czero<T>();
           if (kin && (!prune || kept(g, kr, j))) {
             cplx<T> N = czero<T>();
