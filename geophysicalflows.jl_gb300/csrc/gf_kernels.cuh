@@ -504,6 +504,23 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : sizeof(T) == 4 ? (NY >=
     // the X of all layers at the element (several layers: PV inversion); the bottom-drag term
     // of the next stage from the last layer's psi
     const cplx<T>* Xsrc = static_cast<const cplx<T>*>(s.sol) + ioff;  // layer split: X of every layer
+    // layer split with up to three layers: the X of every layer staged into F0..F2 with
+    // cp.async (all loads in flight); each thread later reads and overwrites only its own
+    // elements there, so no barrier is needed before the fill
+    const bool staged = split && nl <= 3;
+    if (staged) {
+      for (int a = 0; a < nl; ++a) {
+        cplx<T>* Fa = F0 + (size_t)a * C * cs + c * cs;
+  #pragma unroll
+        for (int i = 0; i < R; ++i) {
+          const int j = t + i * TPF;
+          if (kin && kept(g, kr, j)) cp_async_elem<T>(Fa + swz<T>(j), Xsrc + (size_t)a * lstride + (size_t)j * g.ldk + kr);
+          else Fa[swz<T>(j)] = czero<T>();
+        }
+      }
+      cp_async_commit();
+      cp_async_wait<0>();
+    }
     for (int L = L0; L < L1; ++L) {
   #pragma unroll 2  // rolled: the PV inversion per element is long code (instruction cache)
       for (int i = 0; i < R; ++i) {
@@ -512,6 +529,7 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : sizeof(T) == 4 ? (NY >=
         // X of layer a at this element
         auto Xat = [&](int a) -> cplx<T> {
           if (!split) return Xs[(a * NY + j) * C + c];
+          if (staged) return F0[(size_t)a * C * cs + c * cs + swz<T>(j)];
           return xin ? Xsrc[(size_t)a * lstride + (size_t)j * g.ldk + kr] : czero<T>();
         };
         const cplx<T> x = Xat(L);
