@@ -62,6 +62,22 @@ def test_twodns_one_call_equals_single_steps(stepper, T, prec):
     assert np.count_nonzero(p.sol[aliased]) > 0.5 * np.count_nonzero(aliased)
 
 
+@pytest.mark.parametrize("nx,ny,Lx,Ly", [(128, 64, 2 * np.pi, np.pi), (64, 256, 3.0, 7.0)])
+def test_rectangular_grids(nx, ny, Lx, Ly):
+    """kcut and the aliased l band of a rectangular grid (the launch grid of unobserved steps
+    covers the kept columns only)"""
+    make = lambda: TD.Problem("GPU", nx=nx, ny=ny, Lx=Lx, Ly=Ly, dt=0.002, nu=1e-4, nnu=1,
+                              stepper="FilteredRK4", T=np.float64)
+    rng = np.random.default_rng(3)
+    z0 = rng.standard_normal((ny, nx))
+    p, q = pair(make, lambda r: TD.set_zeta(r, z0))
+    same(p, q)
+    r = O.TwoDNavierStokes(nx=nx, ny=ny, Lx=Lx, Ly=Ly, dt=0.002, nu=1e-4, nnu=1, stepper="FilteredRK4")
+    r.set_zeta(z0)
+    r.stepforward(N_STEPS)
+    assert O.rel_l2(p.sol, r.sol) <= 1e-12
+
+
 @pytest.mark.parametrize("graph_steps", [0, 4])
 def test_slqg_topography_stochastic_etdrk4(graph_steps):
     n = 128
@@ -88,6 +104,25 @@ def test_mlqg_three_layers_drag(prec):
     same(p, q)
     for a, b in zip(ML.energies(p), ML.energies(q)):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("nl", [4, 5])
+def test_mlqg_more_than_three_layers(nl):
+    """beyond three layers the inverse column launch reads the layers' X from global memory
+    (no staging into its three work buffers): oracle parity and one call = single steps"""
+    n = 64
+    H = list(np.linspace(0.1, 0.3, nl))
+    b = list(-1.0 - 0.15 * np.arange(nl))
+    U = list(np.linspace(1.0, 0.0, nl))
+    kw = dict(nx=n, f0=1.0, beta=5.0, H=H, b=b, U=U, mu=0.05, dt=2.5e-3, stepper="ETDRK4")
+    rng = np.random.default_rng(nl)
+    q0 = 1e-2 * rng.standard_normal((nl, n, n))
+    p, q = pair(lambda: ML.Problem(nl, "GPU", **kw), lambda r: ML.set_q(r, q0))
+    same(p, q)
+    r = O.MultiLayerQG(nl, **kw)
+    r.set_q(q0)
+    r.stepforward(N_STEPS)
+    assert O.rel_l2(p.sol, r.sol) <= 1e-11
 
 
 def test_surfaceqg_and_qgql():
