@@ -1760,7 +1760,7 @@ extern "C" int gf_autotune(gf_ctx* c, int32_t reps, int32_t* shape) {
     for (const int C : {1, 2, 3, 4, 5, 6, 8, 16}) {
       if (rc != GF_OK) break;
       const int cs = C > 1 ? g0.ny + std::max(unit / C, 1) : g0.ny;
-      const size_t sm = col_stage_smem(g0.ny, C, cs, c->m, g0.nl, c->cb, C * TPF);
+      const size_t sm = col_stage_smem(g0.ny, C, cs, c->m, g0.nl, c->cb, C * TPF, c->prec == GF_DF64);
       if (C * TPF > col_max_threads(c->rb, g0.ny, c->m, g0.nl) || sm > (size_t)SMEM_CAP) continue;
       set_shape(c, 0, 0, R, C);
       double ms = 0;

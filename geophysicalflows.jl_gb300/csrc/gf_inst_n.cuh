@@ -1,5 +1,6 @@
 // Per-size launchers: block shapes for one FFT length NN and precision T, and the launch.
 #pragma once
+#include <type_traits>
 #include "gf_adjoint.cuh"
 #include "gf_launch.cuh"
 
@@ -24,7 +25,8 @@ template <class T, int NN, int R>
 cudaError_t launch_col_nr(const Geom& g, const ModArgs& m, const StepArgs& s, const Bufs& b, cudaStream_t st) {
   cudaError_t err = cudaSuccess;
   const size_t e = sizeof(cplx<T>);
-  auto smem = [&](int c) { return col_stage_smem(NN, c, col_stride<T>(NN, c), m, g.nl, e, c * (NN / R)); };
+  constexpr bool is_df64 = std::is_same<T, df64>::value;
+  auto smem = [&](int c) { return col_stage_smem(NN, c, col_stride<T>(NN, c), m, g.nl, e, c * (NN / R), is_df64); };
   int C = pick_C(NN, R, g.nkr, smem, g.nb);
   if (g.tuneC > 0) {
     // the tuned columns per block; launches of observed steps (every column, every mode: a
@@ -37,8 +39,11 @@ cudaError_t launch_col_nr(const Geom& g, const ModArgs& m, const StepArgs& s, co
   g2.cs = col_stride<T>(NN, C);
   const size_t sm = smem(C);
   auto k = col_stage_kernel<T, NN, R>;
+  const int variant = col_variant(is_df64, NN, m, g.nl, C * (NN / R));
   if constexpr (sizeof(T) == 4 && NN >= 1024)
-    if (C * (NN / R) > 512) k = col_stage_kernel<T, NN, R, 640>;
+    if (variant == 640) k = col_stage_kernel<T, NN, R, 640>;
+  if constexpr (is_df64 && NN >= 1024)
+    if (variant == 256) k = col_stage_kernel<T, NN, R, 256>;
   if ((err = set_smem(k, sm)) != cudaSuccess) return err;
   const int ncols = g.kout > 0 ? g.kout : g.nkr;
   if (g.nl == 1) {

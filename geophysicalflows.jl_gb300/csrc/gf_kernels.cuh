@@ -35,6 +35,9 @@
 #ifndef GF_ROW_MINBLOCKS_WIDE
 #define GF_ROW_MINBLOCKS_WIDE 2   // FP64 and df64 row kernels (128 registers, no spills)
 #endif
+#ifndef GF_MINBLOCKS_WIDE_COL
+#define GF_MINBLOCKS_WIDE_COL 1   // FP64 and df64 column kernels
+#endif
 // Elements per iteration of the column kernel's stage-epilogue loops (code size: the
 // epilogue covers every stepper and forcing kind)
 #ifndef GF_EPI_UNROLL
@@ -127,9 +130,11 @@ __device__ __forceinline__ void psi_all(const ModArgs& m, int nl, T K2, const cp
 // thread-owned); the PV inversion of every element is recomputed from Xs where u and v of a
 // layer are formed.
 // MAXT: largest block the instantiation is compiled for (register budget); 640 is the wide
-// FP32 variant for five radix-16 columns of 2048 (or radix-8 columns of 1024) per block.
+// FP32 variant for five radix-16 columns of 2048 (or radix-8 columns of 1024) per block, 256
+// the narrow FP64 / df64 variant (one radix-8 column of 2048, three blocks per SM); both run
+// the one-layer path only, with the two-buffer inverse pass.
 template <class T, int NY, int R, int MAXT = 512>
-__global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : sizeof(T) == 4 ? (NY >= 1024 ? GF_MINBLOCKS_F32 : GF_MINBLOCKS_SMALL_F32) : 1)
+__global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : MAXT < 512 ? 3 : sizeof(T) == 4 ? (NY >= 1024 ? GF_MINBLOCKS_F32 : GF_MINBLOCKS_SMALL_F32) : GF_MINBLOCKS_WIDE_COL)
     col_stage_kernel(Geom g, ModArgs m, StepArgs s, Bufs b, int C) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T eig[MAXL + 2 * MAXL * MAXL];
@@ -321,7 +326,7 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : sizeof(T) == 4 ? (NY >=
 #pragma unroll (EPI_UNROLL)
       for (int i = 0; i < R; ++i) {
         const int j = t + i * TPF;
-        constexpr int PF = MAXT > 512 ? 0 : GF_EPI_PREFETCH;  // measured: helps 512-thread blocks only
+        constexpr int PF = MAXT > 512 ? 0 : GF_EPI_PREFETCH;  // measured: slower in the wide blocks
         if constexpr (PF > 0) {
           if (kin && i + PF < R) {  // the state of a later element towards L1
             const size_t sn = ioff + (size_t)(j + PF * TPF) * g.ldk + kr;
@@ -348,8 +353,8 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : sizeof(T) == 4 ? (NY >=
     }
     if (!s.do_inv) return;
     if ((int)blockIdx.x * C >= g.kcut) return;  // whole block aliased: W is never read there
-    if constexpr (MAXT > 512) {
-      // the wide instantiation (96 registers), two buffers: q (F0) and u (F1) filled, then the
+    if constexpr (MAXT != 512) {
+      // the wide and narrow instantiations, two buffers: q (F0) and u (F1) filled, then the
       // inverse FFTs of q, u and -- filled into F0 once q is stored, psi formed again from
       // the registers -- v, one after the other from a single call site (instruction cache)
 #pragma unroll 1
@@ -413,7 +418,7 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : sizeof(T) == 4 ? (NY >=
     return;
   }
 
-  if constexpr (MAXT <= 512) {  // several layers or bottom drag (the wide instantiation is one-layer only)
+  if constexpr (MAXT == 512) {  // several layers or bottom drag (the wide and narrow instantiations are one-layer only)
     // Work buffers F0, F1, F2 and Xs (N, then the next stage's X of every layer: nl x NY x C,
     // thread-owned).  Per layer: the product fields of the layer in one cp.async group, their
     // FFTs in lockstep, N and the stage epilogue; then per layer the inverse FFTs of (q, u, v)

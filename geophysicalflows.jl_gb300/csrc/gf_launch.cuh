@@ -49,19 +49,30 @@ inline int col_max_threads(size_t real_bytes, int NY, const ModArgs& m, int nl) 
   return (real_bytes == 4 && NY >= 1024 && nl == 1 && !m.drag) ? 640 : 512;
 }
 
-// Blocks above 512 threads run the wide instantiation, whose single-layer path without bottom
-// drag and with at most two product fields works in two shared-memory buffers (three
-// otherwise, and in the 512-thread instantiation).
-inline bool col_two_buffers(const ModArgs& m, int nl, int threads) {
-  return threads > 512 && nl == 1 && !m.drag && 1 + m.hasB + m.hasC <= 2;
+// The column-kernel instantiation (its MAXT) a launch of `threads` threads runs: 640, the
+// wide FP32 one-layer instantiation above 512 threads; 256, the narrow df64 one (one layer,
+// no bottom drag, two product fields, columns >= 1024, at most 256 threads: three blocks per
+// SM at 80 registers in two shared-memory buffers; IEEE FP64 is ALU-bound and measured slower
+// there); 512 otherwise.
+inline int col_variant(bool df64, int NY, const ModArgs& m, int nl, int threads) {
+  if (threads > 512) return 640;
+  if (df64 && NY >= 1024 && threads <= 256 && nl == 1 && !m.drag && 1 + m.hasB + m.hasC <= 2) return 256;
+  return 512;
+}
+
+// The wide and narrow instantiations run the one-layer path without bottom drag and with at
+// most two product fields in two shared-memory buffers (three otherwise, and in the
+// 512-thread instantiation).
+inline bool col_two_buffers(const ModArgs& m, int nl, int threads, bool df64, int NY) {
+  return col_variant(df64, NY, m, nl, threads) != 512 && nl == 1 && !m.drag && 1 + m.hasB + m.hasC <= 2;
 }
 
 // shared-memory bytes of col_stage_kernel for C columns with column stride cs and `threads`
-// threads: one layer without bottom drag F0, F1 (, F2); otherwise F0, F1, F2 and the X of
-// every layer
+// threads (elem: complex element bytes): one layer without bottom drag F0, F1 (, F2);
+// otherwise F0, F1, F2 and the X of every layer
 __host__ __forceinline__ size_t col_stage_smem(int NY, int C, int cs, const ModArgs& m, int nl, size_t elem,
-                                               int threads) {
-  if (nl == 1 && !m.drag) return (size_t)(col_two_buffers(m, nl, threads) ? 2 : 3) * C * cs * elem;
+                                               int threads, bool df64) {
+  if (nl == 1 && !m.drag) return (size_t)(col_two_buffers(m, nl, threads, df64, NY) ? 2 : 3) * C * cs * elem;
   if (nl > 1) return (size_t)3 * C * cs * elem;  // layer split: X of every layer in global memory
   return ((size_t)3 * C * cs + (size_t)nl * NY * C) * elem;
 }

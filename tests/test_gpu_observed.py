@@ -182,6 +182,28 @@ def test_wide_column_blocks(shape):
     assert O.rel_l2(p.sol, r.sol) <= 1e-5
 
 
+@pytest.mark.parametrize("prec", [None, "DF64"])
+def test_narrow_column_blocks(prec):
+    """FP64 and df64 columns of 1024, one column per block (df64: the narrow 256-thread
+    instantiation with three blocks per SM and two shared-memory buffers) in observed and
+    unobserved steps: one call equals single steps bit for bit, and the FP64 oracle"""
+    n = 1024
+    make = lambda: TD.Problem("GPU", nx=n, dt=0.001, nu=1e-4, nnu=1, stepper="FilteredRK4", T=np.float64,
+                              precision=prec)
+    rng = np.random.default_rng(6)
+    z = 0.5 * np.fft.irfft2(np.fft.rfft2(rng.standard_normal((n, n))) * O.Grid(n).dealias_mask(), s=(n, n))
+
+    def init(r):
+        r.launch_shape = (8, 1, 8, 1)
+        TD.set_zeta(r, z)
+    p, q = pair(make, init)
+    same(p, q)
+    r = O.TwoDNavierStokes(nx=n, dt=0.001, nu=1e-4, nnu=1, stepper="FilteredRK4")
+    r.set_zeta(z)
+    r.stepforward(N_STEPS)
+    assert O.rel_l2(p.sol, r.sol) <= 1e-12
+
+
 def test_batched_and_ensemble_graph():
     """a batched context and one ensemble graph over two contexts (graph of 4 steps: the
     last step of every replay observed)"""
