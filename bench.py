@@ -511,7 +511,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "TwoDNavierStokes 2048^2 FilteredRK4 dt=5e-4 nu=0, peaked isotropic IC",
+            "config": {"workload": "TwoDNavierStokes 2048^2 FilteredRK4 dt=5e-4 nu=0, peaked isotropic IC (k0=6, E=0.5)",
                        "nx": w["nx"], "ny": w["ny"], "stepper": w["stepper"]},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": f"{args.steps} steps after {args.warmup} warm-up, FP64 restatement of the "
