@@ -13,8 +13,13 @@ cudaError_t launch_row_nr(const Geom& g, const ModArgs& m, const Bufs& b, cudaSt
   const size_t e = sizeof(cplx<T>);
   int B = pick_B(NN, R, e, 3, g.ny / 2, g.nb);
   if (g.tuneB > 0 && row_shape_ok(NN, R, e, 3, g.ny / 2, g.tuneB)) B = g.tuneB;
-  const size_t sm = (size_t)B * 3 * row_stride<T>(NN, NN / R) * e;
+  // df64 rows of >= 1024 with the two products (u q', v q') only: the two-buffer
+  // instantiation, three blocks per SM
+  const bool two = std::is_same<T, df64>::value && NN >= 1024 && m.hasB && !m.hasC && !m.ql && B * (NN / R) <= 256;
+  const size_t sm = (size_t)B * (two ? 2 : 3) * row_stride<T>(NN, NN / R) * e;
   auto k = row_nl_kernel<T, NN, R>;
+  if constexpr (std::is_same<T, df64>::value && NN >= 1024)
+    if (two) k = row_nl_kernel<T, NN, R, true>;
   if ((err = set_smem(k, sm)) != cudaSuccess) return err;
   k<<<dim3(g.ny / 2 / B, g.nb), B * (NN / R), sm, st>>>(g, m, b, B);
   return cudaGetLastError();

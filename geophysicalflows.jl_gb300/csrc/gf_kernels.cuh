@@ -612,15 +612,19 @@ __device__ __forceinline__ void unpack_store(const cplx<T>* buf, int k, int NX, 
   Pb[k] = mk<T>(T(0.5) * (z.y + w.y), T(0.5) * (w.x - z.x));
 }
 
-template <class T, int NX, int R>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? GF_ROW_MINBLOCKS_F32 : GF_ROW_MINBLOCKS_WIDE) row_nl_kernel(Geom g, ModArgs m, Bufs b, int B) {
+// TWO: products (u q', v q') only, in two buffers per row pair -- q, then u with the first
+// product, then v with the second, one c2r and one r2c call site -- so that three df64 blocks
+// (80 registers, 64 KB at 2048) fit on an SM instead of two.
+template <class T, int NX, int R, bool TWO = false>
+__global__ void __launch_bounds__(256, TWO ? 3 : sizeof(T) == 4 ? GF_ROW_MINBLOCKS_F32 : GF_ROW_MINBLOCKS_WIDE)
+    row_nl_kernel(Geom g, ModArgs m, Bufs b, int B) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int TPF = NX / R;
   constexpr int M = NX / 2;
   constexpr int PS = row_stride<T>(NX, NX / R);
   const int tid = threadIdx.x, bp = tid / TPF, t = tid % TPF;
   const int j0 = 2 * (blockIdx.x * B + bp);
-  cplx<T>* buf = reinterpret_cast<cplx<T>*>(smem_raw) + (size_t)bp * 3 * PS;
+  cplx<T>* buf = reinterpret_cast<cplx<T>*>(smem_raw) + (size_t)bp * (TWO ? 2 : 3) * PS;
   const cplx<T>* tw = static_cast<const cplx<T>*>(b.twid);
   const cplx<T>* W = static_cast<const cplx<T>*>(b.W) + blockIdx.y * g.bs_w;
   cplx<T>* P = static_cast<cplx<T>*>(b.P) + blockIdx.y * g.bs_p;
@@ -633,6 +637,54 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? GF_ROW_MINBLOCKS_F32 : G
   const int nslot = 1 + m.hasB + m.hasC;
   const int kout = g.kout > 0 ? g.kout : g.nkr;  // columns of the products formed
   for (int L = 0; L < nl; ++L) {
+    if constexpr (TWO) {
+      const cplx<T> Up = mk<T>(U1D ? U1D[L * g.ny + j0] : T(0), U1D ? U1D[L * g.ny + j0 + 1] : T(0));
+#pragma unroll 1
+      for (int f = 0; f < 3; ++f) {
+        cplx<T>* dst = f == 0 ? buf : buf + PS;
+        const cplx<T>* Wa = W + ((size_t)f * nl + L) * g.ny * g.ldw + (size_t)j0 * g.ldw;
+#pragma unroll
+        for (int i = 0; i < R; ++i) {
+          const int k = t + i * TPF;
+          dst[swz<T>(k)] = packed_spec<T>(Wa, Wa + g.ldw, k, NX, g.kcut);
+        }
+        __syncthreads();
+        fft_smem<T, NX, R, +1>(dst, t, tw);
+        if (f == 0) continue;
+        // f = 1: q' = q (+ eta) kept in buf, A = (U + u) q' (or U q' when linear);
+        // f = 2: B = v q'.  Each thread rewrites only its own elements.
+#pragma unroll
+        for (int i = 0; i < R; ++i) {
+          const int x = t + i * TPF;
+          const int px = swz<T>(x);
+          cplx<T> q = buf[px], w = buf[PS + px];
+          const size_t ia = (size_t)j0 * NX + x, fs = (size_t)nl * g.ny * NX;
+          T* ph = b.phys ? static_cast<T*>(b.phys) + (size_t)L * g.ny * NX : nullptr;
+          if (f == 1) {
+            if (eta) q = q + mk<T>(eta[(size_t)j0 * NX + x], eta[(size_t)(j0 + 1) * NX + x]);
+            buf[px] = q;
+            const cplx<T> u = w + Up;
+            if (ph) { ph[ia] = q.x; ph[ia + NX] = q.y; ph[fs + ia] = u.x; ph[fs + ia + NX] = u.y; }
+            const cplx<T> au = m.linear ? Up : u;
+            w = mk<T>(au.x * q.x, au.y * q.y);
+          } else {
+            if (ph) { ph[2 * fs + ia] = w.x; ph[2 * fs + ia + NX] = w.y; }
+            w = mk<T>(w.x * q.x, w.y * q.y);
+          }
+          buf[PS + px] = w;
+        }
+        __syncthreads();
+        fft_smem<T, NX, R, -1>(buf + PS, t, tw);
+        cplx<T>* Pa = P + ((size_t)(f - 1) * nl + L) * g.ny * g.ldk + (size_t)j0 * g.ldk;
+#pragma unroll
+        for (int i = 0; i < R; ++i) {
+          const int k = t + i * TPF;
+          if (k <= M && k < kout) unpack_store<T>(buf + PS, k, NX, Pa, Pa + g.ldk);
+        }
+        __syncthreads();
+      }
+      continue;
+    }
     for (int f = 0; f < 3; ++f) {
       const cplx<T>* Wf = W + ((size_t)f * nl + L) * g.ny * g.ldw;
       const cplx<T>* Wa = Wf + (size_t)j0 * g.ldw;

@@ -204,6 +204,26 @@ def test_narrow_column_blocks(prec):
     assert O.rel_l2(p.sol, r.sol) <= 1e-12
 
 
+def test_df64_two_buffer_rows_with_topography():
+    """df64 rows of 1024 with topography: the two-buffer row instantiation forms q + eta once
+    and keeps it for both products; it matches the IEEE FP64 path"""
+    n = 1024
+    g = O.Grid(n)
+    x, y = g.gridpoints()
+    eta = 0.2 * np.cos(3 * x) * np.sin(2 * y)
+    rng = np.random.default_rng(2)
+    q0 = 0.1 * np.fft.irfft2(np.fft.rfft2(rng.standard_normal((n, n))) * g.dealias_mask(), s=(n, n))
+    sols = []
+    for prec in ("DF64", None):
+        p = SL.Problem("GPU", nx=n, beta=10.0, mu=0.01, U=0.3, eta=eta, deformation_radius=1.2, dt=0.002,
+                       stepper="ETDRK4", T=np.float64, precision=prec)
+        p.launch_shape = (8, 1, 8, 1)
+        SL.set_q(p, q0)
+        stepforward(p, N_STEPS)
+        sols.append(p.sol)
+    assert O.rel_l2(sols[0], sols[1]) <= 1e-12
+
+
 def test_batched_and_ensemble_graph():
     """a batched context and one ensemble graph over two contexts (graph of 4 steps: the
     last step of every replay observed)"""
