@@ -125,6 +125,24 @@ def test_mlqg_more_than_three_layers(nl):
     assert O.rel_l2(p.sol, r.sol) <= 1e-11
 
 
+def test_mlqg_batched_layer_split():
+    """a batched three-layer context (instance = blockIdx.y, layer = blockIdx.z of the split
+    column launches) equals independent runs bit for bit"""
+    n, nl, B = 64, 3, 2
+    kw = dict(nx=n, f0=1.0, beta=5.0, H=[0.2, 0.3, 0.5], b=[-1.0, -1.2, -1.290909], U=[1.0, 0.5, 0.0], mu=0.05,
+              dt=2.5e-3, stepper="ETDRK4")
+    rng = np.random.default_rng(8)
+    q0 = 1e-2 * rng.standard_normal((B, nl, n, n))
+    pb = ML.Problem(nl, "GPU", batch=B, **kw)
+    ML.set_q(pb, q0)
+    stepforward(pb, N_STEPS)
+    for i in range(B):
+        p = ML.Problem(nl, "GPU", **kw)
+        ML.set_q(p, q0[i])
+        stepforward(p, N_STEPS)
+        assert np.array_equal(pb.sol[i], p.sol)
+
+
 def test_surfaceqg_and_qgql():
     n = 128
     rng = np.random.default_rng(9)
