@@ -37,14 +37,14 @@ for _p in (os.path.join(ROOT, "geophysicalflows.jl_gb300"), os.path.join(ROOT, "
 METRIC = "grid-pt·steps/s FP32-fused vs FP64-plain (≤1e-5 rel L2); adjoint/forward step time"
 UNIT = "grid-pt*steps/s"
 HEADLINE = dict(module="TwoDNavierStokes", nx=2048, ny=2048, stepper="FilteredRK4", dt=5e-4)
-CONFIG1 = dict(module="SingleLayerQG", nx=512, ny=512, stepper="ETDRK4", dt=0.05, beta=10.0, mu=0.01,
+SLQG512 = dict(module="SingleLayerQG", nx=512, ny=512, stepper="ETDRK4", dt=0.05, beta=10.0, mu=0.01,
                forcing="stochastic")
 # 3 layers, H = [.2,.3,.5], rho = [4, 5, 5.5] -> b with g' = g (rho_{j+1} - rho_j) / rho_{j+1}, g = 1
-CONFIG2 = dict(module="MultiLayerQG", nx=1024, ny=1024, nlayers=3, stepper="ETDRK4", dt=2.5e-3, f0=1.0, beta=5.0,
+MLQG1024X3 = dict(module="MultiLayerQG", nx=1024, ny=1024, nlayers=3, stepper="ETDRK4", dt=2.5e-3, f0=1.0, beta=5.0,
                H=[0.2, 0.3, 0.5], b=[-1.0, -1.2, -1.2 - 0.5 / 5.5], U=[1.0, 0.5, 0.0], mu=0.05)
 # gradient of the final kinetic energy: SingleLayerQG 256^2, deformation radius 0.35,
 # topography |k| <= 8 amplitude 0.1, ETDRK4 dt = 0.01, 500 steps, checkpoint every 25
-CONFIG3 = dict(module="SingleLayerQG", nx=256, ny=256, stepper="ETDRK4", dt=0.01, ell=0.35, nsteps=500, every=25)
+ADJOINT256 = dict(module="SingleLayerQG", nx=256, ny=256, stepper="ETDRK4", dt=0.01, ell=0.35, nsteps=500, every=25)
 # 1536 independent TwoDNavierStokes runs in three batched size classes (size, instances)
 ENSEMBLE = dict(classes=((64, 1024), (128, 384), (256, 128)), stepper="FilteredRK4", dt=0.01, nu=1e-4, nnu=1,
                 kf=8.0, dkf=1.5, eps=1e-3)
@@ -371,7 +371,7 @@ def accuracy_100_steps(w, nsteps=100):
             "df64_vs_fp64": relerr(sols["df64"], sols["f64"])}
 
 
-def run_config0(cpu=True):
+def run_decaying128(cpu=True):
     """TwoDNavierStokes decaying 128^2, nu = 0, FilteredRK4 dt = 0.005, 1000 steps from the
     peaked isotropic state (k0 = 6, E = 0.5), with zeta, energy and enstrophy read back to
     the host every 100 steps: wall time of the whole run (host outputs included) in IEEE
@@ -528,7 +528,7 @@ def time_adjoint(flush, T=np.float32, precision=None, reps=2):
     import torch
     import gfcuda
     from gfcuda.core import Grid
-    w = CONFIG3
+    w = ADJOINT256
     g = Grid(w["nx"], w["ny"], 2 * np.pi, 2 * np.pi, 1 / 3, np.float64)
     eta = gfcuda.utils.random_topography(g, 8, 0.1, seed=3)
     p = gfcuda.SingleLayerQG.Problem("GPU", nx=w["nx"], deformation_radius=w["ell"], eta=eta, dt=w["dt"],
@@ -632,17 +632,17 @@ def run_ours(args):
         r32 = time_arm(w, np.float32, args.steps, args.warmup, flush, with_e2e=True)
         rdf = time_arm(w, np.float64, args.steps, args.warmup, flush, with_e2e=True, precision="DF64")
         r64 = time_arm(w, np.float64, args.steps, args.warmup, flush, with_e2e=False)
-        c32 = time_arm(CONFIG1, np.float32, args.steps, args.warmup, flush, with_e2e=False)
-        cdf = time_arm(CONFIG1, np.float64, args.steps, args.warmup, flush, with_e2e=False, precision="DF64")
-        c64 = time_arm(CONFIG1, np.float64, args.steps, args.warmup, flush, with_e2e=False)
-        m32 = time_arm(CONFIG2, np.float32, args.steps, args.warmup, flush, with_e2e=False)
-        mdf = time_arm(CONFIG2, np.float64, args.steps, args.warmup, flush, with_e2e=False, precision="DF64")
+        c32 = time_arm(SLQG512, np.float32, args.steps, args.warmup, flush, with_e2e=False)
+        cdf = time_arm(SLQG512, np.float64, args.steps, args.warmup, flush, with_e2e=False, precision="DF64")
+        c64 = time_arm(SLQG512, np.float64, args.steps, args.warmup, flush, with_e2e=False)
+        m32 = time_arm(MLQG1024X3, np.float32, args.steps, args.warmup, flush, with_e2e=False)
+        mdf = time_arm(MLQG1024X3, np.float64, args.steps, args.warmup, flush, with_e2e=False, precision="DF64")
         ens = time_ensemble(args.steps, args.warmup, flush)
         adj32 = time_adjoint(flush)
         adj64 = time_adjoint(flush, np.float64)
     acc = accuracy_100_steps(w)
-    acc1 = accuracy_100_steps(CONFIG1)
-    cfg0 = run_config0(cpu=is_rank0())
+    acc1 = accuracy_100_steps(SLQG512)
+    dec128 = run_decaying128(cpu=is_rank0())
     ms, msg, msdf, ms64, e2e_s, e2e_df = reduce_max(dist, [
         r32["ms_per_step"], r32["ms_per_step_graph"], rdf["ms_per_step"], r64["ms_per_step"],
         1e3 * r32["e2e_s_per_step"], 1e3 * rdf["e2e_s_per_step"]])
@@ -660,7 +660,7 @@ def run_ours(args):
     cdferr = relerr(cdf["sol"], c64["sol"])
     merr = relerr(m32["sol"], mdf["sol"])
     cpu = cpu_baseline(w)
-    c1p, c2p = points(CONFIG1), points(CONFIG2)
+    c1p, c2p = points(SLQG512), points(MLQG1024X3)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -713,7 +713,7 @@ def run_ours(args):
                        "ms_per_step_fp32": m32["ms_per_step"], "ms_per_step_graph_fp32": m32["ms_per_step_graph"],
                        "ms_per_step_df64": mdf["ms_per_step"],
                        "fp32_vs_df64_rel_l2": merr, "steps_compared": args.steps * CALL_STEPS,
-                       "roofline_fp32": roofline(CONFIG2, m32, 8, "mlqg1024x3_fp32", peaks, peak_src)},
+                       "roofline_fp32": roofline(MLQG1024X3, m32, 8, "mlqg1024x3_fp32", peaks, peak_src)},
         "ensemble1536": {"workload": "1536 TwoDNavierStokes runs: 1024 x 64^2 + 384 x 128^2 + 128 x 256^2, "
                                      "FilteredRK4 dt=0.01 nu=1e-4 (nnu=1), per-instance stochastic ring forcing "
                                      "kf=8 eps=1e-3, zeta0=0, FP32, three batched contexts on concurrent streams",
@@ -721,7 +721,7 @@ def run_ours(args):
                          "value_graph": ens["points"] / (ens["ms_per_step_graph"] * 1e-3),
                          "ms_per_step": ens["ms_per_step"], "ms_per_step_graph": ens["ms_per_step_graph"],
                          "mean_energy_per_class": ens["mean_energy"], "launch_shapes": ens["launch_shapes"]},
-        "twodns128_decaying": cfg0,
+        "twodns128_decaying": dec128,
         "adjoint_slqg256": {"workload": "gradient of the final kinetic energy w.r.t. q0 and topography: "
                                         "SingleLayerQG 256^2, deformation radius 0.35, topography |k|<=8 amp 0.1, "
                                         "ETDRK4 dt=0.01, 500 steps, checkpoint every 25",
@@ -734,11 +734,11 @@ def run_ours(args):
 
 
 SINGLE = {"twodns2048_fp32": (HEADLINE, np.float32, None), "twodns2048_fp64": (HEADLINE, np.float64, None),
-          "twodns2048_df64": (HEADLINE, np.float64, "DF64"), "slqg512_fp32": (CONFIG1, np.float32, None),
-          "slqg512_fp64": (CONFIG1, np.float64, None), "slqg512_df64": (CONFIG1, np.float64, "DF64"),
-          "mlqg1024x3_fp32": (CONFIG2, np.float32, None), "mlqg1024x3_df64": (CONFIG2, np.float64, "DF64"),
-          "ensemble1536_fp32": (ENSEMBLE, np.float32, None), "adjoint256_fp32": (CONFIG3, np.float32, None),
-          "adjoint256_fp64": (CONFIG3, np.float64, None)}
+          "twodns2048_df64": (HEADLINE, np.float64, "DF64"), "slqg512_fp32": (SLQG512, np.float32, None),
+          "slqg512_fp64": (SLQG512, np.float64, None), "slqg512_df64": (SLQG512, np.float64, "DF64"),
+          "mlqg1024x3_fp32": (MLQG1024X3, np.float32, None), "mlqg1024x3_df64": (MLQG1024X3, np.float64, "DF64"),
+          "ensemble1536_fp32": (ENSEMBLE, np.float32, None), "adjoint256_fp32": (ADJOINT256, np.float32, None),
+          "adjoint256_fp64": (ADJOINT256, np.float64, None)}
 
 
 def run_single(args):
@@ -751,7 +751,7 @@ def run_single(args):
     if w is ENSEMBLE:
         r = time_ensemble(args.steps, args.warmup, flush)
         r["pt_steps_per_s"] = r["points"] / (r["ms_per_step"] * 1e-3)
-    elif w is CONFIG3:
+    elif w is ADJOINT256:
         r = time_adjoint(flush, T, reps=1)
     else:
         shape = tuple(int(v) for v in args.shape.split(",")) if args.shape else None

@@ -27,11 +27,11 @@ def test_kept_geometry_matches_the_dealias_mask(nx, ny):
 def test_two_sweep_words_per_point():
     assert bench.algorithmic_bytes(bench.HEADLINE, 4) == 256 * bench.points(bench.HEADLINE)
     assert bench.algorithmic_bytes(bench.HEADLINE, 8) == 512 * bench.points(bench.HEADLINE)
-    assert bench.algorithmic_bytes(bench.CONFIG1, 4) == 284 * bench.points(bench.CONFIG1)
-    assert bench.algorithmic_bytes(bench.CONFIG2, 4) == 316 * bench.points(bench.CONFIG2)
+    assert bench.algorithmic_bytes(bench.SLQG512, 4) == 284 * bench.points(bench.SLQG512)
+    assert bench.algorithmic_bytes(bench.MLQG1024X3, 4) == 316 * bench.points(bench.MLQG1024X3)
 
 
-@pytest.mark.parametrize("w", [bench.HEADLINE, bench.CONFIG1, bench.CONFIG2])
+@pytest.mark.parametrize("w", [bench.HEADLINE, bench.SLQG512, bench.MLQG1024X3])
 @pytest.mark.parametrize("cb", [8, 16])
 def test_unobserved_launches_move_fewer_bytes(w, cb):
     ro, co = bench.launch_bytes(w, cb, True)

@@ -155,7 +155,7 @@ def test_central_differences_small():
     _fd_check(64, 20, 5, 4, 1)
 
 
-def test_config3_central_differences_8_directions():
+def test_adjoint_slqg256_central_differences_8_directions():
     """SingleLayerQG 256^2, deformation radius 0.35, topography |k| <= 8 amplitude 0.1,
     ETDRK4 dt = 0.01, 500 steps, checkpoint every 25, loss = final kinetic energy: central
     differences (eps = 1e-6, Richardson-extrapolated with 2 eps) along 8 seeded band-limited
@@ -163,7 +163,7 @@ def test_config3_central_differences_8_directions():
     _fd_check(256, 500, 25, 8, 2024, richardson=True)
 
 
-def test_config3_central_differences_100_steps():
+def test_adjoint_slqg256_central_differences_100_steps():
     """the same case over 100 steps, where the plain eps = 1e-6 central difference is
     already within 1e-6"""
     _fd_check(256, 100, 25, 8, 7)

@@ -88,7 +88,7 @@ def test_graph_matches_oracle_with_harmonic_forcing():
 
 
 def test_ensemble_step_three_size_classes():
-    """configs[4] shape in miniature: three batched size classes stepped by one call"""
+    """the 1536-run ensemble in miniature: three batched size classes stepped by one call"""
     probs, refs = [], []
     for n, B in ((64, 4), (128, 2), (256, 1)):
         spec = O.ring_forcing_spectrum(O.Grid(n), 8.0, 1.5, 1e-3)

@@ -69,7 +69,7 @@ def test_df64_filteredrk4_single_step_parity(n):
         assert rel(p.sol, r.sol) <= TOL
 
 
-def test_df64_config0_100_steps():
+def test_df64_decaying_128_100_steps():
     n, dt = 128, 0.005
     r = O.TwoDNavierStokes(nx=n, dt=dt, stepper="FilteredRK4")
     z0 = ic(n, r.timestepper.filter)

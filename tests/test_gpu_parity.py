@@ -77,7 +77,7 @@ def test_calcN_matches_oracle(module):
 
 
 # ------------------------------------------------------------------------------ 2DNS config 0
-def _cfg0_ic(n, filt):
+def _peaked_ic(n, filt):
     g = O.Grid(n)
     return O.peakedisotropicspectrum(g, 6, 0.5, mask=filt, seed=1234)
 
@@ -85,7 +85,7 @@ def _cfg0_ic(n, filt):
 def test_twodns_filteredrk4_single_step_parity():
     n, dt = 128, 0.005
     r = O.TwoDNavierStokes(nx=n, dt=dt, stepper="FilteredRK4")
-    r.set_zeta(_cfg0_ic(n, r.timestepper.filter))
+    r.set_zeta(_peaked_ic(n, r.timestepper.filter))
     r.stepforward(20)  # a developed state
     p = TD.Problem("GPU", nx=n, dt=dt, stepper="FilteredRK4")
     for _ in range(3):
@@ -96,11 +96,11 @@ def test_twodns_filteredrk4_single_step_parity():
         assert rel(p.sol, r.sol) <= TOL64
 
 
-def test_twodns_config0_parity_100_steps():
-    """configs[0]: 128^2 FP64 FilteredRK4 dt=0.005 nu=0, peaked isotropic IC (k0=6, E=0.5)"""
+def test_twodns_decaying_128_parity_100_steps():
+    """The decaying 128^2 workload: FP64 FilteredRK4 dt=0.005 nu=0, peaked isotropic IC (k0=6, E=0.5)"""
     n, dt = 128, 0.005
     r = O.TwoDNavierStokes(nx=n, dt=dt, stepper="FilteredRK4")
-    z0 = _cfg0_ic(n, r.timestepper.filter)
+    z0 = _peaked_ic(n, r.timestepper.filter)
     r.set_zeta(z0)
     p = TD.Problem("GPU", nx=n, dt=dt, stepper="FilteredRK4")
     TD.set_zeta(p, z0)
@@ -391,8 +391,9 @@ def test_twodns_stochastic_energy_budget_gpu():
 
 
 # ------------------------------------------------------------------------------ FP32
-def test_fp32_slqg_config1_shape_against_fp64_oracle():
-    """configs[1] physics (beta=10, mu=0.01, ETDRK4 dt=0.05, stochastic ring forcing at kf=14)
+def test_fp32_slqg_beta_forced_against_fp64_oracle():
+    """The beta-plane forced SingleLayerQG physics (beta=10, mu=0.01, ETDRK4 dt=0.05,
+    stochastic ring forcing at kf=14)
     at 256^2 for 100 steps: FP32 bulk vs the FP64 oracle."""
     n, dt = 256, 0.05
     g = O.Grid(n)
@@ -409,7 +410,7 @@ def test_fp32_slqg_config1_shape_against_fp64_oracle():
 def test_fp32_twodns_against_fp64_oracle():
     n, dt = 256, 0.005
     r = O.TwoDNavierStokes(nx=n, dt=dt, stepper="FilteredRK4")
-    z0 = _cfg0_ic(n, r.timestepper.filter)
+    z0 = _peaked_ic(n, r.timestepper.filter)
     r.set_zeta(z0)
     p = TD.Problem("GPU", nx=n, dt=dt, stepper="FilteredRK4", T=np.float32)
     TD.set_zeta(p, z0)
