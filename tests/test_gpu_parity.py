@@ -76,7 +76,7 @@ def test_calcN_matches_oracle(module):
     assert rel(sol_gpu, s_ref) <= 1e-15
 
 
-# ------------------------------------------------------------------------------ 2DNS config 0
+# ---------------------------------------------------------------- 2DNS decaying 128^2 workload
 def _peaked_ic(n, filt):
     g = O.Grid(n)
     return O.peakedisotropicspectrum(g, 6, 0.5, mask=filt, seed=1234)

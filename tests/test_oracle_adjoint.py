@@ -30,7 +30,7 @@ def test_adjoint_forward_is_stepforward(stepper, ell, U, beta):
 @pytest.mark.parametrize("stepper,ell,U,beta", [("ETDRK4", 0.35, 0.0, 0.0), ("ETDRK4", np.inf, 0.3, 2.0),
                                                 ("FilteredETDRK4", 0.35, 0.1, 1.0)])
 def test_gradient_matches_central_differences(stepper, ell, U, beta):
-    """config 3's check in miniature: 8 seeded directions, eps = 1e-6, 1e-6 relative"""
+    """the SingleLayerQG 256^2 adjoint check in miniature: 8 seeded directions, eps = 1e-6, 1e-6 relative"""
     p, A, q0, eta, kw = setup(32, stepper, ell, U, beta)
     ns = 12
     _, gq, ge = A.gradient(q0, eta, ns)
