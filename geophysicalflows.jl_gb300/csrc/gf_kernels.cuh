@@ -288,8 +288,10 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : MAXT < 512 ? 3 : sizeof
   const T sc = sel<T>(g.inv_nxny, g.inv_nxny_f, g.inv_nxny_l);
 
   if (nl == 1 && !m.drag) {
-    // ---- one layer: all product FFTs in lockstep, N and the next X in registers, then the
-    // three inverse FFTs of (q, u, v) in lockstep
+    // ---- one layer: the product FFTs (in lockstep where the registers allow), N and the
+    // next X in registers, then the three inverse FFTs of (q, u, v) -- in lockstep from three
+    // buffers, or from two in the wide and narrow instantiations (which the host launches
+    // for one layer without bottom drag only)
     cplx<T> xr[R];
     if (s.do_fwd) {
       const cplx<T>* P = static_cast<const cplx<T>*>(b.P) + ib * g.bs_p;
