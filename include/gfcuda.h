@@ -230,8 +230,11 @@ int gf_get_batch(const gf_ctx* ctx, int32_t* batch);
  * gf_step replays a CUDA graph of `steps` captured time steps (the step counter, time and
  * harmonic-forcing phases live on the GPU, so one graph serves every later step); AB3
  * problems always use graphs of 3 steps (their right-hand-side ring has period 3).
- * steps = 0 launches kernel by kernel.  Default 4.  No counterpart in the reference
- * (its steps are launched broadcast by broadcast). */
+ * steps = 0 launches kernel by kernel.  Default 4.  Two sequences are captured per ring
+ * phase: every step unobserved (replayed while more steps of the call follow) and the last
+ * step (AB3: three) computing the aliased modes (the replay that ends the call), so a long
+ * call pays for one observed step.  No counterpart in the reference (its steps are
+ * launched broadcast by broadcast). */
 int gf_set_graph_steps(gf_ctx* ctx, int32_t steps);
 /* Steps n contexts (e.g. one batched context per grid size of an ensemble) by nsteps each;
  * every context runs on its own stream, so the size classes execute concurrently.
