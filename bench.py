@@ -4,11 +4,12 @@
 
 Headline workload: TwoDNavierStokes 2048^2, FilteredRK4, nu = 0, peaked isotropic initial
 vorticity (k0 = 6, E = 0.5) -- the configuration the FP32-fused vs FP64-plain target is
-quoted on.  A "step" is one FilteredRK4 time step (4 calcN! stages).  `value` is FP32-fused
-grid-point*steps/s with the state resident in HBM, timed over stepforward! calls of 10 steps
-(an output interval: the state is looked at after every call, so the last step of each call
-computes every mode and the others only the modes a later step reads); single-step calls
-(every step observed) are timed beside it.  The FP64-plain arm, its roofline and the
+quoted on.  A "step" is one FilteredRK4 time step (4 calcN! stages); --steps K and --warmup W
+count these model steps.  `value` is FP32-fused grid-point*steps/s with the state resident in
+HBM, timed over exactly K steps run as stepforward! calls of 10 steps (an output interval: the
+state is looked at after every call, so the last step of each call computes every mode and
+the others only the modes a later step reads); single-step calls (every step observed) are
+timed beside it (`value_single_step_calls`).  The FP64-plain arm, its roofline and the
 FP32-vs-FP64 error are reported beside it, and so are the other GPU workloads: SingleLayerQG
 512^2 ETDRK4 with stochastic forcing, MultiLayerQG 3 x 1024^2 ETDRK4, and the 1536-run
 TwoDNavierStokes ensemble (1024 x 64^2 + 384 x 128^2 + 128 x 256^2).  L2 is flushed (256 MiB
@@ -114,6 +115,22 @@ def algorithmic_bytes(w, word):
         a = 1
     C = 23 if "ETDRK4" in w["stepper"] else 16
     return word * points(w) * (4 * (2 + 2 * k + 2 * m + a) + C)
+
+
+def model_launch_bytes(w, word):
+    """The two-sweep model's bytes (algorithmic_bytes) split between the two kernels of a
+    stage: the row kernel reads the k inverse-transformed fields and the a parameter arrays
+    and writes the m products (k + m + a words/pt); the column kernel reads the m products
+    and the stage input, writes the k inverse fields of the next stage and N, and carries the
+    stage combination (m + 1 + k + 1 + C/4 words/pt).  Returns (row, column) bytes per launch."""
+    k, m, a = 3, 2, 0
+    if w["module"] == "MultiLayerQG":
+        m = 3
+    if w["module"] == "SingleLayerQG" and w.get("eta"):
+        a = 1
+    C = 23 if "ETDRK4" in w["stepper"] else 16
+    n = word * points(w)
+    return n * (k + m + a), n * (m + 1 + k + 1 + C / 4)
 
 
 def step_roofline(w, ms_per_step, word, peaks):
@@ -270,17 +287,27 @@ def _events(n):
     return [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
 
 
+def call_plan(steps, call_steps):
+    """stepforward! calls covering exactly `steps` model steps: calls of call_steps steps,
+    the last one shorter when call_steps does not divide steps."""
+    calls = [call_steps] * (steps // call_steps)
+    if steps % call_steps:
+        calls.append(steps % call_steps)
+    return calls
+
+
 def time_arm(w, T, steps, warmup, flush, with_e2e, precision=None, graph=True, tune=True, shape=None,
              call_steps=CALL_STEPS):
-    """Run one precision arm: warm-up, then K timed stepforward! calls of call_steps steps
-    each (CUDA events on the legacy default stream, which orders with the library's
-    blocking stream; L2 flushed before every call) with the library's per-kernel event
-    timing on; then K single-step calls (every step observed, L2 flushed before each); then
-    K calls replayed from captured CUDA graphs of call_steps steps (one event pair); then
-    optionally the end-to-end timing through the host-buffer API.  Every timed leg starts
-    from the initial condition at t = 0 (the SingleLayerQG workload, nu = 0 and no filter,
-    grows to the grid scale and overflows after ~220 steps in the reference algorithm too),
-    so the state returned is the one after K x call_steps steps in every arm."""
+    """Run one precision arm: `warmup` model steps, then exactly `steps` timed model steps as
+    stepforward! calls of call_steps steps each (CUDA events on the legacy default stream,
+    which orders with the library's blocking stream; L2 flushed before every call) with the
+    library's per-kernel event timing on; then `steps` single-step calls (every step
+    observed, L2 flushed before each); then one call of `steps` steps replayed from captured
+    CUDA graphs of call_steps steps (one event pair); then optionally the end-to-end timing
+    through the host-buffer API (`steps` single-step calls).  Every timed leg starts from the
+    initial condition at t = 0 (the SingleLayerQG workload, nu = 0 and no filter, grows to the
+    grid scale and overflows after ~220 steps in the reference algorithm too), so the state
+    returned is the one after `steps` steps in every arm."""
     import ctypes as C
     import torch
     import gfcuda
@@ -298,28 +325,28 @@ def time_arm(w, T, steps, warmup, flush, with_e2e, precision=None, graph=True, t
     n2 = (C.c_int64 * 2)()
     nl = C.c_int64()
 
-    def timed_calls(nsteps):
+    def timed_calls(calls):
         lib.gf_profile_read(ctx, ms2, n2, C.byref(nl))  # reset counters
         lib.gf_profile_enable(ctx, 1)                  # (per-kernel events; no graphs)
-        ev = _events(steps)
-        for i in range(steps):
+        ev = _events(len(calls))
+        for i, nsteps in enumerate(calls):
             flush.zero_()
             ev[i][0].record()
             prob._c(lib.gf_step(ctx, nsteps))
             ev[i][1].record()
         torch.cuda.synchronize()
-        ms = sum(a.elapsed_time(b) for a, b in ev) / (steps * nsteps)
+        ms = sum(a.elapsed_time(b) for a, b in ev) / sum(calls)
         prob._c(lib.gf_profile_read(ctx, ms2, n2, C.byref(nl)))
         lib.gf_profile_enable(ctx, 0)
         return ms, ms2[0] / max(n2[0], 1), ms2[1] / max(n2[1], 1), nl.value
 
     set_initial_state(prob, w)
-    ms, mrow, mcol, launches = timed_calls(call_steps)
+    ms, mrow, mcol, launches = timed_calls(call_plan(steps, call_steps))
     set_initial_state(prob, w)
-    mso, mrowo, mcolo, _ = timed_calls(1)
+    mso, mrowo, mcolo, _ = timed_calls([1] * steps)
     res = {"ms_per_step": ms, "ms_row": mrow, "ms_col": mcol, "launches": launches, "call_steps": call_steps,
            "ms_per_step_observed": mso, "ms_row_observed": mrowo, "ms_col_observed": mcolo,
-           "launch_shape": shape}
+           "launch_shape": shape, "steps": steps}
     if graph:
         gfcuda.stepforward(prob, call_steps)  # captures the graph outside the timed region
         set_initial_state(prob, w)
@@ -327,10 +354,10 @@ def time_arm(w, T, steps, warmup, flush, with_e2e, precision=None, graph=True, t
         (e0, e1), = _events(1)
         flush.zero_()
         e0.record()
-        prob._c(lib.gf_step(ctx, steps * call_steps))
+        prob._c(lib.gf_step(ctx, steps))
         e1.record()
         torch.cuda.synchronize()
-        res["ms_per_step_graph"] = e0.elapsed_time(e1) / (steps * call_steps)
+        res["ms_per_step_graph"] = e0.elapsed_time(e1) / steps
     res["sol"] = prob.sol   # the state after the same number of steps in every arm
     if with_e2e:
         sshape = prob.spec_shape
@@ -423,8 +450,9 @@ def run_decaying128(cpu=True):
 def time_ensemble(steps, warmup, flush):
     """The 1536-run ensemble: one batched Problem per size class (instance i of a class
     draws its forcing with seed + i), all stepped by gf_ensemble_step; each class runs on its
-    own stream, concurrently.  Calls of CALL_STEPS steps with L2 flushes before each, then
-    one graph over all classes replayed."""
+    own stream, concurrently.  `warmup` model steps, then exactly `steps` timed model steps
+    as calls of CALL_STEPS steps with L2 flushes before each, then the same steps from one
+    graph over all classes replayed."""
     import torch
     import gfcuda
     from gfcuda.core import Grid
@@ -441,24 +469,25 @@ def time_ensemble(steps, warmup, flush):
         p.set_graph_steps(0)
     gfcuda.ensemble_step(probs, warmup)
     torch.cuda.synchronize()
-    ev = _events(steps)
-    for i in range(steps):
+    calls = call_plan(steps, CALL_STEPS)
+    ev = _events(len(calls))
+    for i, nsteps in enumerate(calls):
         flush.zero_()
         ev[i][0].record()
-        gfcuda.ensemble_step(probs, CALL_STEPS)
+        gfcuda.ensemble_step(probs, nsteps)
         ev[i][1].record()
     torch.cuda.synchronize()
-    ms = sum(a.elapsed_time(b) for a, b in ev) / (steps * CALL_STEPS)
+    ms = sum(a.elapsed_time(b) for a, b in ev) / steps
     for p in probs:
         p.set_graph_steps(CALL_STEPS)
     gfcuda.ensemble_step(probs, CALL_STEPS)  # captures the ensemble graph
     (e0, e1), = _events(1)
     flush.zero_()
     e0.record()
-    gfcuda.ensemble_step(probs, steps * CALL_STEPS)
+    gfcuda.ensemble_step(probs, steps)
     e1.record()
     torch.cuda.synchronize()
-    ms_graph = e0.elapsed_time(e1) / (steps * CALL_STEPS)
+    ms_graph = e0.elapsed_time(e1) / steps
     E = [float(np.mean(p.diagnostics([0])[:, 0])) for p in probs]
     for p in probs:
         p.close()
@@ -591,23 +620,31 @@ def whole_job(points_per_rank, world, ms_max):
 
 
 def roofline(w, res, cb, tag, peaks, peak_src):
-    """HBM roofline of the dominant kernel of an arm: the bytes its launches must move
-    (launch_bytes, averaged over the launches of the timed stepforward! calls) over their
-    average duration timed with CUDA events on the library stream; the same for the launches
-    of single observed steps beside it."""
+    """HBM roofline of the dominant kernel of an arm: its share of the two-sweep model's
+    bytes per launch (model_launch_bytes, every mode of every array once, word = half the
+    complex element size) over the average duration of its launches in the timed
+    stepforward! calls, timed with CUDA events on the library stream.  Beside it the exact
+    byte count of what the launches touch (launch_bytes: pruned columns and modes, averaged
+    over the launches of a call) and the same figures for single observed steps."""
     row_b, col_b = call_bytes(w, cb, res["call_steps"])
     dom = "col_stage" if res["ms_col"] >= res["ms_row"] else "row_nl"
-    per_launch = col_b if dom == "col_stage" else row_b
+    ix = 1 if dom == "col_stage" else 0
+    model = model_launch_bytes(w, cb // 2)[ix]
+    exact = col_b if dom == "col_stage" else row_b
     t = res["ms_col"] if dom == "col_stage" else res["ms_row"]
-    ach = per_launch / (t * 1e-3) / 1e9
-    ob = launch_bytes(w, cb, True)[1 if dom == "col_stage" else 0]
+    ach = model / (t * 1e-3) / 1e9
+    ach_exact = exact / (t * 1e-3) / 1e9
+    ob = launch_bytes(w, cb, True)[ix]
     to = res["ms_col_observed"] if dom == "col_stage" else res["ms_row_observed"]
     return {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": ach / peaks["hbm_gbs"], "peak_source": peak_src, "traffic": ncu_traffic(dom, tag),
-            "algorithmic_bytes_per_launch": per_launch, "launch_ms": t, "row_ms": res["ms_row"],
-            "col_ms": res["ms_col"], "calls_of_steps": res["call_steps"],
-            "observed_step": {"bytes_per_launch": ob, "launch_ms": to,
-                              "achieved": ob / (to * 1e-3) / 1e9, "frac": ob / (to * 1e-3) / 1e9 / peaks["hbm_gbs"]}}
+            "algorithmic_bytes_per_launch": model, "bytes_model": "two-sweep words/pt per kernel",
+            "launch_ms": t, "row_ms": res["ms_row"], "col_ms": res["ms_col"], "calls_of_steps": res["call_steps"],
+            "exact_bytes_per_launch": exact, "achieved_exact": ach_exact, "frac_exact": ach_exact / peaks["hbm_gbs"],
+            "observed_step": {"model_bytes_per_launch": model, "exact_bytes_per_launch": ob, "launch_ms": to,
+                              "achieved": model / (to * 1e-3) / 1e9,
+                              "frac": model / (to * 1e-3) / 1e9 / peaks["hbm_gbs"],
+                              "frac_exact": ob / (to * 1e-3) / 1e9 / peaks["hbm_gbs"]}}
 
 
 def relerr(a, b):
@@ -631,21 +668,25 @@ def run_ours(args):
     with Clocks() as clk:
         r32 = time_arm(w, np.float32, args.steps, args.warmup, flush, with_e2e=True)
         rdf = time_arm(w, np.float64, args.steps, args.warmup, flush, with_e2e=True, precision="DF64")
-        r64 = time_arm(w, np.float64, args.steps, args.warmup, flush, with_e2e=False)
-        c32 = time_arm(SLQG512, np.float32, args.steps, args.warmup, flush, with_e2e=False)
-        cdf = time_arm(SLQG512, np.float64, args.steps, args.warmup, flush, with_e2e=False, precision="DF64")
-        c64 = time_arm(SLQG512, np.float64, args.steps, args.warmup, flush, with_e2e=False)
-        m32 = time_arm(MLQG1024X3, np.float32, args.steps, args.warmup, flush, with_e2e=False)
-        mdf = time_arm(MLQG1024X3, np.float64, args.steps, args.warmup, flush, with_e2e=False, precision="DF64")
-        ens = time_ensemble(args.steps, args.warmup, flush)
+        r64 = time_arm(w, np.float64, args.steps, args.warmup, flush, with_e2e=True)
+        # the workloads beside the headline: at most 200 steps per timed leg (the SingleLayerQG
+        # workload as specified overflows after ~220 steps from rest)
+        ks = min(args.steps, 200)
+        c32 = time_arm(SLQG512, np.float32, ks, args.warmup, flush, with_e2e=False)
+        cdf = time_arm(SLQG512, np.float64, ks, args.warmup, flush, with_e2e=False, precision="DF64")
+        c64 = time_arm(SLQG512, np.float64, ks, args.warmup, flush, with_e2e=False)
+        m32 = time_arm(MLQG1024X3, np.float32, ks, args.warmup, flush, with_e2e=False)
+        mdf = time_arm(MLQG1024X3, np.float64, ks, args.warmup, flush, with_e2e=False, precision="DF64")
+        ens = time_ensemble(ks, args.warmup, flush)
         adj32 = time_adjoint(flush)
         adj64 = time_adjoint(flush, np.float64)
     acc = accuracy_100_steps(w)
     acc1 = accuracy_100_steps(SLQG512)
     dec128 = run_decaying128(cpu=is_rank0())
-    ms, msg, msdf, ms64, e2e_s, e2e_df = reduce_max(dist, [
+    ms, msg, msdf, ms64, e2e_s, e2e_df, e2e_64, mso = reduce_max(dist, [
         r32["ms_per_step"], r32["ms_per_step_graph"], rdf["ms_per_step"], r64["ms_per_step"],
-        1e3 * r32["e2e_s_per_step"], 1e3 * rdf["e2e_s_per_step"]])
+        1e3 * r32["e2e_s_per_step"], 1e3 * rdf["e2e_s_per_step"], 1e3 * r64["e2e_s_per_step"],
+        r32["ms_per_step_observed"]])
     if dist:
         dist.barrier()
     if not is_rank0():
@@ -669,9 +710,9 @@ def run_ours(args):
                    "nx": w["nx"], "ny": w["ny"], "stepper": w["stepper"], "precision": "FP32 bulk",
                    "l2": f"flushed before every timed stepforward! call of {CALL_STEPS} steps (256 MiB write)",
                    "parallelism": f"replicas x{world}", "steps_per_call": CALL_STEPS,
-                   "model_steps_timed": args.steps * CALL_STEPS,
-                   "ms_per_step_graph": msg, "launch_shape": r32["launch_shape"],
-                   "ms_per_step_single_step_calls": r32["ms_per_step_observed"]},
+                   "steps_counted": "model time steps (4 FilteredRK4 stages each), timed as stepforward! "
+                                    f"calls of {CALL_STEPS} steps",
+                   "ms_per_step_graph": msg, "launch_shape": r32["launch_shape"]},
         "roofline": roofline(w, r32, 8, "twodns2048_fp32", peaks, peak_src),
         "roofline_step_two_sweep": step_roofline(w, ms, 4, peaks),
         "cpu_baseline": cpu,
@@ -679,13 +720,19 @@ def run_ours(args):
                 "d2h_bytes_per_step": r32["state_bytes"]},
         "gpu_launches": r32["launches"],
         "clocks": clk.summary(int(os.environ.get("LOCAL_RANK", "0"))),
+        # the same workload, every step its own stepforward!(prob, 1) call (every mode computed)
+        "value_single_step_calls": whole_job(pts, world, mso), "ms_per_step_single_step_calls": mso,
+        # precision-matched arms of the same workload (FP64 inputs and outputs)
+        "value_fp64_plain": vdf, "ms_per_step_fp64_plain": msdf, "e2e_fp64_plain": whole_job(pts, world, e2e_df),
+        "value_fp64_ieee": v64, "ms_per_step_fp64_ieee": ms64, "e2e_fp64_ieee": whole_job(pts, world, e2e_64),
+        "fp32_vs_fp64_rel_l2_100_steps": acc["fp32_vs_fp64"],
         "fp64_plain": {"arithmetic": "df64 (double-float pairs, 48-bit significand, FP32 pipes)", "value": vdf,
                        "ms_per_step": msdf, "ms_per_step_graph": rdf["ms_per_step_graph"],
                        "roofline": roofline(w, rdf, 16, "twodns2048_df64", peaks, peak_src),
                        "roofline_step_two_sweep": step_roofline(w, msdf, 8, peaks),
                        "e2e": {"value": whole_job(pts, world, e2e_df), "unit": UNIT},
                        "rel_l2_vs_ieee_fp64": dferr},
-        "fp64_ieee": {"value": v64, "ms_per_step": ms64,
+        "fp64_ieee": {"value": v64, "ms_per_step": ms64, "e2e": {"value": whole_job(pts, world, e2e_64), "unit": UNIT},
                       "roofline": roofline(w, r64, 16, "twodns2048_fp64", peaks, peak_src),
                       "roofline_step_two_sweep": step_roofline(w, ms64, 8, peaks)},
         "fp32_over_fp64": value / vdf,
@@ -694,7 +741,7 @@ def run_ours(args):
         "fp32_vs_fp64_steps": acc["steps"],
         "df64_vs_fp64_rel_l2_100_steps": acc["df64_vs_fp64"],
         "fp32_vs_fp64_rel_l2_after_timed_steps": err,
-        "states_compared_after_steps": args.steps * CALL_STEPS,
+        "states_compared_after_steps": args.steps,
         "slqg512": {"workload": "SingleLayerQG 512^2 beta=10 mu=0.01 ETDRK4 dt=0.05, stochastic ring forcing "
                                 "kf=14 eps=1e-3, q0=0 (L2-resident: latency, no HBM fraction)",
                     "fp32": c1p / (c32["ms_per_step"] * 1e-3),
@@ -703,7 +750,7 @@ def run_ours(args):
                     "ms_per_step_fp32": c32["ms_per_step"], "ms_per_step_graph_fp32": c32["ms_per_step_graph"],
                     "ms_per_step_df64": cdf["ms_per_step"], "ms_per_step_fp64": c64["ms_per_step"],
                     "fp32_vs_fp64_rel_l2": cerr, "df64_vs_fp64_rel_l2": cdferr,
-                    "states_compared_after_steps": args.steps * CALL_STEPS,
+                    "states_compared_after_steps": ks,
                     "fp32_vs_fp64_rel_l2_100_steps": acc1["fp32_vs_fp64"],
                     "df64_vs_fp64_rel_l2_100_steps": acc1["df64_vs_fp64"]},
         "mlqg1024x3": {"workload": "MultiLayerQG 3 layers 1024^2 ETDRK4 dt=2.5e-3, H=[.2,.3,.5], "
@@ -712,7 +759,7 @@ def run_ours(args):
                        "fp64_plain_df64": c2p / (mdf["ms_per_step"] * 1e-3),
                        "ms_per_step_fp32": m32["ms_per_step"], "ms_per_step_graph_fp32": m32["ms_per_step_graph"],
                        "ms_per_step_df64": mdf["ms_per_step"],
-                       "fp32_vs_df64_rel_l2": merr, "steps_compared": args.steps * CALL_STEPS,
+                       "fp32_vs_df64_rel_l2": merr, "steps_compared": ks,
                        "roofline_fp32": roofline(MLQG1024X3, m32, 8, "mlqg1024x3_fp32", peaks, peak_src)},
         "ensemble1536": {"workload": "1536 TwoDNavierStokes runs: 1024 x 64^2 + 384 x 128^2 + 128 x 256^2, "
                                      "FilteredRK4 dt=0.01 nu=1e-4 (nnu=1), per-instance stochastic ring forcing "
@@ -767,8 +814,8 @@ def run_single(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=200, help="model time steps timed per arm")
+    ap.add_argument("--warmup", type=int, default=20, help="untimed model time steps before them")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--single", choices=sorted(SINGLE), help="time one arm only (profiling mode)")
     ap.add_argument("--no-tune", action="store_true", help="single mode: built-in block shapes, no autotuner")

@@ -12,7 +12,10 @@
 // Limits and rules (also in include/gfcuda.h):
 //   * nx, ny powers of two in [32, GF_NOALLOC_MAX_N]; larger sizes are rejected.
 //   * The first call on a device does the set-up for that device (symbol addresses, twiddle
-//     tables copied in); make that first call before any stream capture.
+//     tables copied in, then a device synchronisation so that the tables are complete for a
+//     kernel on any stream); make that first call before any stream capture.
+//   * At most 64 devices.  A device reset is not supported: the set-up is not redone, so
+//     the reset device's tables would stay unwritten.
 //   * All calls share the scratch array: calls that overlap on the GPU (different streams,
 //     or different host threads without ordering) race and give wrong results.  Every
 //     scratch element a call reads is written earlier in the same call, so nothing has to
@@ -69,6 +72,12 @@ int setup(int dev, DeviceSlot** out) {
     e = cudaMemcpyToSymbol(g_noalloc_tw64, t64, sizeof(t64));
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_noalloc_tw32, t32, sizeof(t32));
     if (e != cudaSuccess) return fail(GF_ERR_CUDA, std::string("cudaMemcpyToSymbol: ") + cudaGetErrorString(e));
+    // A copy from pageable host memory may return before the data reaches the device, and it
+    // is ordered only against the legacy default stream; the kernels go to the caller's
+    // stream, which may be non-blocking.  Wait for the device once here so that no kernel of
+    // any stream can read a partly written table.
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return fail(GF_ERR_CUDA, std::string("cudaDeviceSynchronize: ") + cudaGetErrorString(e));
     s.scratch = scratch;
     s.tw64 = tw64;
     s.tw32 = tw32;
@@ -90,7 +99,10 @@ extern "C" int gf_rfft2_noalloc(const void* field, void* fieldh, int32_t nx, int
     return fail(GF_ERR_UNSUPPORTED, "gf_rfft2_noalloc: nx and ny must be powers of two in [32, GF_NOALLOC_MAX_N = 512]");
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) return fail(GF_ERR_CUDA, "gf_rfft2_noalloc: no current device");
+  if (e != cudaSuccess || dev < 0) return fail(GF_ERR_CUDA, "gf_rfft2_noalloc: no current device");
+  if (dev >= kMaxDevices)
+    return fail(GF_ERR_UNSUPPORTED, "gf_rfft2_noalloc: device ordinal " + std::to_string(dev) +
+                                        " is beyond the supported 64 devices (ordinals 0..63)");
   DeviceSlot* s = nullptr;
   if (int r = setup(dev, &s)) return r;
   gf::Geom g{};

@@ -343,9 +343,12 @@ int gf_profile_read(gf_ctx* ctx, double* ms, int64_t* n, int64_t* launches);
  * loading the library keeps until exit (about 2.2 MB of scratch plus 96 KB of tables).
  * nx, ny: powers of two in [32, GF_NOALLOC_MAX_N]; larger sizes return GF_ERR_UNSUPPORTED.
  * precision: GF_F32 (float in, complex-float out) or GF_F64.  stream: cudaStream_t or NULL.
- * The first call on a device sets that device up (it must be current); make it before any
- * stream capture.  All calls share the scratch: calls that overlap on the GPU race.
- * Errors: gf_last_error(NULL). */
+ * The first call on a device sets that device up (it must be current): it copies the twiddle
+ * tables in and waits for the device before it launches, so the tables are complete whatever
+ * stream the call runs on; make that first call before any stream capture.  At most 64
+ * devices (ordinals 0..63).  A device reset (cudaDeviceReset, CUDA.jl's device_reset!) is not
+ * supported: the tables of the reset device are not copied in again.  All calls share the
+ * scratch: calls that overlap on the GPU race.  Errors: gf_last_error(NULL). */
 #define GF_NOALLOC_MAX_N 512
 int gf_rfft2_noalloc(const void* field, void* fieldh, int32_t nx, int32_t ny, int32_t precision, void* stream);
 

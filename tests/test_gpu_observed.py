@@ -261,28 +261,3 @@ def test_batched_and_ensemble_graph():
     for p, q in zip(probs, refs):
         same(p, q)
 
-
-def test_unobserved_stages_are_cheaper():
-    """a coarse check that pruning is active: the column kernel of a long call (unobserved
-    steps but the last) takes less time per launch than that of single observed steps"""
-    import ctypes as C
-    n = 1024
-    p = TD.Problem("GPU", nx=n, dt=0.005, nu=1e-4, nnu=1, stepper="FilteredRK4", T=np.float32)
-    p.set_graph_steps(0)
-    TD.set_zeta(p, zeta0(n, 1))
-    stepforward(p, 3)
-    lib, ctx = p._lib, p._ctx
-    ms2, n2, nl = (C.c_double * 2)(), (C.c_int64 * 2)(), C.c_int64()
-
-    def col_ms(call_steps, calls):
-        lib.gf_profile_read(ctx, ms2, n2, C.byref(nl))
-        lib.gf_profile_enable(ctx, 1)
-        for _ in range(calls):
-            stepforward(p, call_steps)
-        lib.gf_profile_read(ctx, ms2, n2, C.byref(nl))
-        lib.gf_profile_enable(ctx, 0)
-        return ms2[1] / n2[1]
-
-    full = min(col_ms(1, 16) for _ in range(3))
-    pruned = min(col_ms(16, 1) for _ in range(3))
-    assert pruned < 0.9 * full
