@@ -76,9 +76,7 @@ __global__ void __launch_bounds__(512, 1) adj_col_kernel(Geom g, ModArgs m, AdjA
       }
     }
     __syncthreads();
-#pragma unroll
-    for (int f = 0; f < 3; ++f) fft_smem<T, NY, R, -1>(Fs[f] + cf * cs, tf, tw);
-    __syncthreads();
+    fft_smem_group<T, NY, R, -1, 3>(F0 + cf * cs, C * cs, tf, tw);  // F0, F1, F2 are C * cs apart
 #pragma unroll
     for (int i = 0; i < R; ++i) {
       const int j = t + i * TPF;
@@ -134,21 +132,21 @@ __global__ void __launch_bounds__(512, 1) adj_col_kernel(Geom g, ModArgs m, AdjA
   if (a.stage == 1 && !a.head) out_w = false;
   if (!out_w) return;
 
-  // 3) y-inverse FFT of (i kr Nbar / w, i l Nbar / w) into Wb (every kr column)
+  // 3) y-inverse FFT of (i kr Nbar / w, i l Nbar / w) into Wb (every kr column), both in lockstep
   cplx<T>* Wb = static_cast<cplx<T>*>(a.Wb);
-  for (int f = 0; f < 2; ++f) {
-    cplx<T>* Fb = f ? F1 : F0;
-    cplx<T>* Fe = Fb + c * cs;
 #pragma unroll
-    for (int i = 0; i < R; ++i) {
-      const int j = t + i * TPF;
-      const T mlt = f ? T(lidx(g, j)) * dky : krT;
-      Fe[swz<T>(j)] = (scale_out * mlt) * mul_i(nb[i]);
-    }
-    __syncthreads();
-    fft_smem<T, NY, R, +1>(Fb + cf * cs, tf, tw);
-    if (kin) {
+  for (int i = 0; i < R; ++i) {
+    const int j = t + i * TPF;
+    F0[c * cs + swz<T>(j)] = (scale_out * krT) * mul_i(nb[i]);
+    F1[c * cs + swz<T>(j)] = (scale_out * (T(lidx(g, j)) * dky)) * mul_i(nb[i]);
+  }
+  __syncthreads();
+  fft_smem_group<T, NY, R, +1, 2>(F0 + cf * cs, C * cs, tf, tw);
+  if (kin) {
+#pragma unroll
+    for (int f = 0; f < 2; ++f) {
       cplx<T>* Wf = Wb + (size_t)f * g.ny * g.ldk + kr;
+      const cplx<T>* Fe = F0 + (size_t)f * C * cs + c * cs;
 #pragma unroll
       for (int i = 0; i < R; ++i) {
         const int j = t + i * TPF;
@@ -189,7 +187,7 @@ __global__ void __launch_bounds__(256, 1) adj_row_kernel(Geom g, AdjArgs a, Bufs
     }
   }
   __syncthreads();
-  for (int f = 0; f < 2; ++f) fft_smem<T, NX, R, +1>(buf + f * PS, t, tw);
+  fft_smem_group<T, NX, R, +1, 2>(buf, PS, t, tw);
 #pragma unroll
   for (int i = 0; i < R; ++i) {
     const int x = t + i * TPF;
@@ -207,7 +205,7 @@ __global__ void __launch_bounds__(256, 1) adj_row_kernel(Geom g, AdjArgs a, Bufs
     buf[2 * PS + px] = mk<T>(bb.x * qe.x, bb.y * qe.y);
   }
   __syncthreads();
-  for (int f = 0; f < 3; ++f) fft_smem<T, NX, R, -1>(buf + f * PS, t, tw);
+  fft_smem_group<T, NX, R, -1, 3>(buf, PS, t, tw);
   for (int f = 0; f < 3; ++f) {
     cplx<T>* Pa = Pb + (size_t)f * g.ny * g.ldk + (size_t)j0 * g.ldk;
 #pragma unroll

@@ -84,6 +84,14 @@ struct gf_ctx {
     int64_t forward_units = 0;          // unit advances the last reverse sweep added (recomputation)
     double t_end = 0;
     int64_t step_end = 0;
+    // pipelined reverse sweep: the transposed stages of one unit run on `ts` while the
+    // context stream recomputes the next unit into the other half of `phys` (two units of
+    // forward fields); ev_rec[k] / ev_adj[k] mark the recomputation into / the last read of
+    // half k, ev_sync orders the two streams at the start and end of a sweep
+    cudaStream_t ts = nullptr;
+    cudaEvent_t ev_rec[2] = {nullptr, nullptr}, ev_adj[2] = {nullptr, nullptr}, ev_sync = nullptr;
+    size_t unit_phys = 0;               // bytes of one unit's forward fields
+    int half = 0;                       // half of `phys` the next recomputation writes
   } adj;
   void* row_phys = nullptr;  // forward row kernels also store (q + eta, u, v) here when set
   // identity and graph generation (an ensemble graph records the members it was built for)
@@ -790,6 +798,17 @@ extern "C" int gf_create(const gf_config* cfg, void* stream, gf_ctx** out) {
   return GF_OK;
 }
 
+// Frees the adjoint's buffers, its second stream and its events (after both streams finish).
+static void adj_release(gf_ctx* c) {
+  auto& a = c->adj;
+  if (a.ts) cudaStreamSynchronize(a.ts);
+  for (void* p : a.mem) cudaFree(p);
+  for (cudaEvent_t e : {a.ev_rec[0], a.ev_rec[1], a.ev_adj[0], a.ev_adj[1], a.ev_sync})
+    if (e) cudaEventDestroy(e);
+  if (a.ts) cudaStreamDestroy(a.ts);
+  a = gf_ctx::Adjoint{};
+}
+
 extern "C" int gf_destroy(gf_ctx* c) {
   if (!c) return GF_OK;
   if (c->stream) cudaStreamSynchronize(c->stream); else cudaDeviceSynchronize();
@@ -800,7 +819,7 @@ extern "C" int gf_destroy(gf_ctx* c) {
     for (auto& gx : ph) if (gx) cudaGraphExecDestroy(gx);
   for (auto& gx : c->egraph) if (gx) cudaGraphExecDestroy(gx);
   if (c->order_ev) cudaEventDestroy(c->order_ev);
-  for (void* p : c->adj.mem) cudaFree(p);
+  adj_release(c);
   if (c->own_stream) cudaStreamDestroy(c->stream);
   delete c;
   return GF_OK;
@@ -1915,8 +1934,7 @@ extern "C" int gf_adjoint_setup(gf_ctx* c, int64_t nsteps, int32_t checkpoint_ev
     return fail(c, GF_ERR_ARG, "more than 4096 recomputation units: raise checkpoint_every");
   GF_CUDA(c, cudaStreamSynchronize(c->stream));
   auto& a = c->adj;
-  for (void* p : a.mem) cudaFree(p);
-  a = gf_ctx::Adjoint{};
+  adj_release(c);
   const Geom& g = c->g;
   a.nsteps = nsteps;
   a.every = (int)std::min<int64_t>(checkpoint_every, nsteps);
@@ -1924,13 +1942,25 @@ extern "C" int gf_adjoint_setup(gf_ctx* c, int64_t nsteps, int32_t checkpoint_ev
   a.snaps = a.nseg;  // one slot per unit boundary: a single forward pass, no recomputation of advances
   const size_t spec = g.bs_spec * c->cb, plane = (size_t)g.ny * g.nx * c->rb;
   const size_t wide = (size_t)g.ny * g.ldk * c->cb;
-  if (!(a.ckpt = adj_alloc(c, a.snaps * spec)) || !(a.phys = adj_alloc(c, (size_t)a.every * 4 * 3 * plane)) ||
+  a.unit_phys = (size_t)a.every * 4 * 3 * plane;
+  // the second stream is non-blocking: it is ordered with the context stream by events only,
+  // never implicitly with the legacy default stream
+  if (cudaStreamCreateWithFlags(&a.ts, cudaStreamNonBlocking) != cudaSuccess) {
+    a.ts = nullptr;
+    return fail(c, GF_ERR_CUDA, "adjoint stream");
+  }
+  for (cudaEvent_t* e : {&a.ev_rec[0], &a.ev_rec[1], &a.ev_adj[0], &a.ev_adj[1], &a.ev_sync})
+    if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) {
+      *e = nullptr;
+      adj_release(c);
+      return fail(c, GF_ERR_CUDA, "adjoint events");
+    }
+  if (!(a.ckpt = adj_alloc(c, a.snaps * spec)) || !(a.phys = adj_alloc(c, 2 * a.unit_phys)) ||
       !(a.ub = adj_alloc(c, spec)) || !(a.n1acc = adj_alloc(c, spec)) || !(a.xaacc = adj_alloc(c, spec)) ||
       !(a.x1acc = adj_alloc(c, spec)) || !(a.ubar_in = adj_alloc(c, spec)) || !(a.ubar_out = adj_alloc(c, spec)) ||
       !(a.final_state = adj_alloc(c, spec)) || !(a.tmp = adj_alloc(c, spec)) || !(a.Wb = adj_alloc(c, 2 * wide)) ||
       !(a.Pb = adj_alloc(c, 3 * wide)) || !(a.etab = adj_alloc(c, plane))) {
-    for (void* p : a.mem) cudaFree(p);
-    a = gf_ctx::Adjoint{};
+    adj_release(c);
     return fail(c, GF_ERR_NOMEM, "adjoint buffers");
   }
   // unused padding columns of the accumulators stay zero
@@ -2042,6 +2072,12 @@ static AdjArgs adj_args(gf_ctx* c) {
 // transposed stages, last step first.  The recomputed steps skip the aliased modes: the
 // transposed stages read only the kept forward fields (q + eta, u, v), and the state after
 // the sweep is the stored forward result.
+//
+// Two streams: the recomputation (and every restore and advance before it) runs on the
+// context stream into one half of d.phys, the transposed stages on d.ts from that half.  So
+// the recomputation of the next unit of the sweep overlaps the transposed stages of this
+// one -- they share only read-only tables -- and a recomputation into a half waits for the
+// transposed stages that last read it.
 static int adj_unit(gf_ctx* c, AdjArgs& a, int u) {
   auto& d = c->adj;
   const Geom& g = c->g;
@@ -2049,13 +2085,17 @@ static int adj_unit(gf_ctx* c, AdjArgs& a, int u) {
   const double dt = c->cfg.dt;
   const Bufs b = Bufs{c->twid, nullptr, nullptr};
   const int cnt = (int)adj_unit_steps(c, u, 1);
+  const int k = d.half;
+  d.half ^= 1;
+  char* ph = (char*)d.phys + k * d.unit_phys;
+  GF_CUDA(c, cudaStreamWaitEvent(c->stream, d.ev_adj[k], 0));  // no-op before the half's first use
   for (int i = 0; i < cnt; ++i) {
     if (int r = ensure_W(c)) return r;
     for (int stg = 1; stg <= 4; ++stg) {
       const double ts = c->t + (stg == 1 ? 0.0 : stg == 4 ? dt : 0.5 * dt);
       StepArgs s = stage_args(c, stg, ts);
       s.clk = c->dclk;
-      c->row_phys = (char*)d.phys + ((size_t)i * 4 + stg - 1) * 3 * plane;
+      c->row_phys = ph + ((size_t)i * 4 + stg - 1) * 3 * plane;
       const int r = launch_stage(c, s, 1, c->g.kcut < c->g.nkr);
       c->row_phys = nullptr;
       if (r) return r;
@@ -2066,16 +2106,19 @@ static int adj_unit(gf_ctx* c, AdjArgs& a, int u) {
     c->launches++;
     host_advance(c);
   }
+  GF_CUDA(c, cudaEventRecord(d.ev_rec[k], c->stream));
+  GF_CUDA(c, cudaStreamWaitEvent(d.ts, d.ev_rec[k], 0));
   for (int i = cnt - 1; i >= 0; --i) {
     for (int r = 4; r >= 1; --r) {
       a.stage = r;
       a.head = (r == 1) && !(u == 0 && i == 0);
-      a.phys = (char*)d.phys + ((size_t)i * 4 + r - 1) * 3 * plane;
-      GF_CUDA(c, DISPATCH(c, launch_adj_row, g, a, b, c->stream));
-      GF_CUDA(c, DISPATCH(c, launch_adj_col, g, c->m, a, b, c->stream));
+      a.phys = ph + ((size_t)i * 4 + r - 1) * 3 * plane;
+      GF_CUDA(c, DISPATCH(c, launch_adj_row, g, a, b, d.ts));
+      GF_CUDA(c, DISPATCH(c, launch_adj_col, g, c->m, a, b, d.ts));
       c->launches += 2;
     }
   }
+  GF_CUDA(c, cudaEventRecord(d.ev_adj[k], d.ts));
   return GF_OK;
 }
 
@@ -2125,14 +2168,22 @@ static int adjoint_reverse(gf_ctx* c) {
   GF_CUDA(c, cudaMemsetAsync(d.etab, 0, plane, c->stream));
   AdjArgs a = adj_args(c);
   const Bufs b = Bufs{c->twid, nullptr, nullptr};
+  // the transposed stages (stream d.ts) start after everything the context stream did so far
+  // (the cotangent of the result, the cleared etab)
+  GF_CUDA(c, cudaEventRecord(d.ev_sync, c->stream));
+  GF_CUDA(c, cudaStreamWaitEvent(d.ts, d.ev_sync, 0));
   a.stage = 5;
-  GF_CUDA(c, DISPATCH(c, launch_adj_col, g, c->m, a, b, c->stream));
+  GF_CUDA(c, DISPATCH(c, launch_adj_col, g, c->m, a, b, d.ts));
   c->launches++;
   std::vector<int> freeslots;
   for (int k = d.snaps - 1; k >= 1 + (int)d.spine.size(); --k) freeslots.push_back(k);
   size_t spine_i = 0;
   d.forward_units = 0;  // unit advances the reverse sweep adds to the forward pass
+  d.half = 0;
   if (int r = adj_rev(c, a, 0, d.nseg, 0, d.snaps - 1, true, freeslots, spine_i)) return r;
+  // the context stream continues after the last transposed stage (ubar_out, etab)
+  GF_CUDA(c, cudaEventRecord(d.ev_sync, d.ts));
+  GF_CUDA(c, cudaStreamWaitEvent(c->stream, d.ev_sync, 0));
   GF_CUDA(c, cudaMemcpyAsync(c->sol, d.final_state, spec, cudaMemcpyDeviceToDevice, c->stream));
   c->t = d.t_end;
   c->step = d.step_end;
