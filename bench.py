@@ -297,7 +297,7 @@ def call_plan(steps, call_steps):
 
 
 def time_arm(w, T, steps, warmup, flush, with_e2e, precision=None, graph=True, tune=True, shape=None,
-             call_steps=CALL_STEPS):
+             call_steps=CALL_STEPS, tma=None):
     """Run one precision arm: `warmup` model steps, then exactly `steps` timed model steps as
     stepforward! calls of call_steps steps each (CUDA events on the legacy default stream,
     which orders with the library's blocking stream; L2 flushed before every call) with the
@@ -315,6 +315,8 @@ def time_arm(w, T, steps, warmup, flush, with_e2e, precision=None, graph=True, t
     set_initial_state(prob, w)
     if shape is not None:
         prob.launch_shape = shape
+        if tma is not None:
+            prob.tma_columns = tma
     elif tune:
         shape = prob.autotune(reps=3)  # the library's launch-shape autotuner
     prob.set_graph_steps(call_steps)
@@ -803,7 +805,7 @@ def run_single(args):
     else:
         shape = tuple(int(v) for v in args.shape.split(",")) if args.shape else None
         r = time_arm(w, T, args.steps, args.warmup, flush, with_e2e=False, precision=prec,
-                     tune=not (args.no_tune or shape), shape=shape, call_steps=args.call_steps)
+                     tune=not (args.no_tune or shape), shape=shape, call_steps=args.call_steps, tma=args.tma)
         r.pop("sol")
         r["pt_steps_per_s"] = points(w) / (r["ms_per_step"] * 1e-3)
     r["workload"] = args.single
@@ -822,6 +824,8 @@ def main():
     ap.add_argument("--call-steps", type=int, default=CALL_STEPS, help="single mode: steps per timed call")
     ap.add_argument("--shape", help="single mode: launch shape row_radix,row_pairs,col_radix,col_columns "
                                     "instead of the autotuner (e.g. a shape it chose, for profiling)")
+    ap.add_argument("--tma", type=int, help="single mode with --shape: TMA column stage with this many columns "
+                                             "per block (0: the per-thread-copy column kernel)")
     args = ap.parse_args()
     if args.single:
         return run_single(args)

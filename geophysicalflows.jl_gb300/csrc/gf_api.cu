@@ -1,6 +1,8 @@
 // C ABI of libgfcuda: problem construction, state transfer, the time-step loop and the
 // diagnostics.  The kernels live in gf_kernels.cuh (instantiated by gf_f32.cu/gf_f64.cu);
 // this file holds the host-side orchestration and the FP64 setup kernels.
+#include <cuda.h>
+
 #include <atomic>
 #include <cmath>
 #include <complex>
@@ -94,6 +96,8 @@ struct gf_ctx {
     int half = 0;                       // half of `phys` the next recomputation writes
   } adj;
   void* row_phys = nullptr;  // forward row kernels also store (q + eta, u, v) here when set
+  TmaMaps tma;               // tensor maps of the TMA column stage (one layer)
+  int* derr = nullptr;       // device error flag: a tile-load wait ran out of time
   // identity and graph generation (an ensemble graph records the members it was built for)
   uint64_t uid = 0, gen = 0;
   cudaGraphExec_t egraph[2] = {nullptr, nullptr};      // ensemble graphs held by the first member (as gexec)
@@ -302,7 +306,7 @@ static int upload_table(gf_ctx* c, void* dst, const std::vector<double>& v, int 
   return GF_OK;
 }
 
-static Bufs bufs(gf_ctx* c) { return Bufs{c->twid, c->W, c->P, c->row_phys}; }
+static Bufs bufs(gf_ctx* c) { return Bufs{c->twid, c->W, c->P, c->row_phys, &c->tma, c->derr}; }
 static Geom full_geom(const gf_ctx* c) {
   Geom g = c->g;
   g.kcut = g.nkr; g.lA = 1; g.lB = 0; g.ldw = g.ldk;
@@ -411,6 +415,60 @@ static int inv_transform(gf_ctx* c, const void* src, int kind, int mask, void* o
 extern "C" int gf_abi_version(void) { return GFCUDA_ABI_VERSION; }
 
 extern "C" const char* gf_last_error(const gf_ctx* c) { return c ? c->err.c_str() : g_create_error.c_str(); }
+
+// cuTensorMapEncodeTiled from the driver (through the runtime's entry-point query, so the
+// library links libcudart only); null if the driver does not provide it.
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+// Tensor maps of the TMA column stage (one layer): P and W as 3-D arrays of 32-bit words
+// (x: the words of a row's complex elements; y: field * ny + j; z: instance), boxes of C
+// columns x min(ny, 256) rows for the two candidate column counts (2 and 4 columns of
+// 8-byte elements, 1 and 2 of 16-byte ones: box rows of 16 or 32 bytes).  P's rows span the
+// padded width ldk (loads of columns past nkr read padding the kernel ignores); W's rows are
+// clipped at kcut, so tile stores drop the aliased columns.  Leaves c->tma.ok false if the
+// driver cannot encode them (the cp.async column kernel is used then).
+static void tma_maps(gf_ctx* c) {
+  const EncodeTiledFn fn = encode_tiled();
+  c->tma.ok = false;
+  if (!fn) return;
+  const Geom& g = c->g;
+  const cuuint32_t wpc = (cuuint32_t)(c->cb / 4);
+  const cuuint32_t rows = (cuuint32_t)std::min(g.ny, 256);
+  const cuuint64_t dP[3] = {(cuuint64_t)g.ldk * wpc, (cuuint64_t)3 * g.ny, (cuuint64_t)g.nb};
+  const cuuint64_t sP[2] = {(cuuint64_t)g.ldk * c->cb, (cuuint64_t)g.bs_p * c->cb};
+  const cuuint64_t dW[3] = {(cuuint64_t)g.kcut * wpc, (cuuint64_t)3 * g.ny, (cuuint64_t)g.nb};
+  const cuuint64_t sW[2] = {(cuuint64_t)g.ldw * c->cb, (cuuint64_t)g.bs_w * c->cb};
+  const cuuint32_t es[3] = {1, 1, 1};
+  for (int i = 0; i < 2; ++i) {
+    const int C = (c->cb == 8 ? 2 : 1) << i;
+    c->tma.Cs[i] = C;
+    const cuuint32_t box[3] = {(cuuint32_t)C * wpc, rows, 1};
+    if (fn(reinterpret_cast<CUtensorMap*>(c->tma.p[i]), CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, c->P, dP, sP, box, es,
+           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return;
+    if (fn(reinterpret_cast<CUtensorMap*>(c->tma.w[i]), CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, c->W, dW, sW, box, es,
+           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return;
+  }
+  c->tma.ok = true;
+}
 
 static int build(gf_ctx* c, const gf_config* cfg) {
   const gf_config& k = *cfg;
@@ -595,6 +653,9 @@ static int build(gf_ctx* c, const gf_config* cfg) {
   if (!(c->stage = dalloc(c, NB * std::max(nsp * cb, g.bs_phys * rb))))  // host-transfer staging
     return fail(c, GF_ERR_NOMEM, "staging");
   if (g.nl > 1 && !(c->Xg = dalloc(c, NB * nsp * cb))) return fail(c, GF_ERR_NOMEM, "layer X");
+  if (!(c->derr = (int*)dalloc(c, sizeof(int)))) return fail(c, GF_ERR_NOMEM, "error flag");
+  GF_CUDA(c, cudaMemsetAsync(c->derr, 0, sizeof(int), c->stream));
+  if (g.nl == 1) tma_maps(c);
   if (c->kind == SK_RK4) {
     if (!(c->acc = dalloc(c, NB * nsp * cb))) return fail(c, GF_ERR_NOMEM, "acc");
     if (c->hasL && !(c->X = dalloc(c, NB * nsp * cb))) return fail(c, GF_ERR_NOMEM, "X");
@@ -939,6 +1000,9 @@ extern "C" int gf_set_clock(gf_ctx* c, double t, int64_t step) {
 extern "C" int gf_synchronize(gf_ctx* c) {
   if (!c) return GF_ERR_ARG;
   GF_CUDA(c, cudaStreamSynchronize(c->stream));
+  int flag = 0;
+  GF_CUDA(c, cudaMemcpy(&flag, c->derr, sizeof(int), cudaMemcpyDeviceToHost));
+  if (flag) return fail(c, GF_ERR_CUDA, "a column-stage tile load did not complete within its time limit");
   return GF_OK;
 }
 
@@ -1701,9 +1765,30 @@ extern "C" int gf_fluxes(gf_ctx* c, double* lateral, double* vertical) {
 // events around each launch, and keeps the fastest.  The state, clock, AB3 history and
 // stochastic-forcing record are restored afterwards; captured graphs are dropped (they
 // are re-captured with the new shapes).  The profiling counters are reset.
-static int set_shape(gf_ctx* c, int Rr, int B, int Rc, int C) {
-  c->g.tuneRr = Rr; c->g.tuneB = B; c->g.tuneRc = Rc; c->g.tuneC = C;
+static int set_shape(gf_ctx* c, int Rr, int B, int Rc, int C, int tmaC = 0) {
+  c->g.tuneRr = Rr; c->g.tuneB = B; c->g.tuneRc = Rc; c->g.tuneC = C; c->g.tmaC = tmaC;
   drop_graphs(c);
+  return GF_OK;
+}
+
+// whether the TMA column stage can run this context, and with C columns per block
+static bool tma_eligible(const gf_ctx* c, int C) {
+  return c->tma.ok && c->g.nl == 1 && !c->m.drag && 1 + c->m.hasB + c->m.hasC <= 2 &&
+         (C == c->tma.Cs[0] || C == c->tma.Cs[1]);
+}
+
+extern "C" int gf_set_tma_columns(gf_ctx* c, int32_t C) {
+  if (!c) return GF_ERR_ARG;
+  if (C != 0 && !tma_eligible(c, C))
+    return fail(c, GF_ERR_UNSUPPORTED, "no TMA column stage with this column count for this context");
+  c->g.tmaC = C;
+  drop_graphs(c);
+  return GF_OK;
+}
+
+extern "C" int gf_get_tma_columns(const gf_ctx* c, int32_t* C) {
+  if (!c || !C) return GF_ERR_ARG;
+  *C = c->g.tmaC;
   return GF_OK;
 }
 
@@ -1715,7 +1800,7 @@ extern "C" int gf_set_launch_shape(gf_ctx* c, const int32_t* shape) {
     const int R = shape[k], N = k == 0 ? c->g.nx : c->g.ny;
     if (R != 0 && R != 8 && !(f32 && f32_radix_built(N, R))) return fail(c, GF_ERR_ARG, "radix not built for this size");
   }
-  return set_shape(c, shape[0], shape[1], shape[2], shape[3]);
+  return set_shape(c, shape[0], shape[1], shape[2], shape[3], c->g.tmaC);
 }
 
 extern "C" int gf_get_launch_shape(const gf_ctx* c, int32_t* shape) {
@@ -1771,7 +1856,7 @@ extern "C" int gf_autotune(gf_ctx* c, int32_t reps, int32_t* shape) {
   const bool f32 = c->prec == GF_F32;
   const int radii[3] = {8, 16, 4};
   const int unit = 128 / (int)c->cb;  // elements per 128-byte wavefront
-  int bestRc = 0, bestC = 0, bestRr = 0, bestB = 0;
+  int bestRc = 0, bestC = 0, bestRr = 0, bestB = 0, bestT = 0;
   double best = 1e30;
   for (int ri = 0; ri < (f32 ? 3 : 1) && rc == GF_OK; ++ri) {
     const int R = radii[ri], TPF = g0.ny / R;
@@ -1784,7 +1869,16 @@ extern "C" int gf_autotune(gf_ctx* c, int32_t reps, int32_t* shape) {
       set_shape(c, 0, 0, R, C);
       double ms = 0;
       rc = measure(1, &ms);
-      if (rc == GF_OK && ms < best) { best = ms; bestRc = R; bestC = C; }
+      if (rc == GF_OK && ms < best) { best = ms; bestRc = R; bestC = C; bestT = 0; }
+    }
+    // the TMA column stage at this radix
+    for (int k = 0; k < 2 && rc == GF_OK; ++k) {
+      const int C = c->tma.Cs[k];
+      if (!tma_eligible(c, C) || C * TPF > 1024) continue;
+      set_shape(c, 0, 0, R, 0, C);
+      double ms = 0;
+      rc = measure(1, &ms);
+      if (rc == GF_OK && ms < best) { best = ms; bestRc = R; bestC = 0; bestT = C; }
     }
   }
   best = 1e30;
@@ -1793,7 +1887,7 @@ extern "C" int gf_autotune(gf_ctx* c, int32_t reps, int32_t* shape) {
     if (!f32_radix_built(g0.nx, R) || TPF < 1 || TPF > 256) continue;
     for (int B = 1; B * TPF <= 256 && rc == GF_OK; B *= 2) {
       if (!row_shape_ok(g0.nx, R, c->cb, 3, g0.ny / 2, B)) continue;
-      set_shape(c, R, B, bestRc, bestC);
+      set_shape(c, R, B, bestRc, bestC, bestT);
       double ms = 0;
       rc = measure(0, &ms);
       if (rc == GF_OK && ms < best) { best = ms; bestRr = R; bestB = B; }
@@ -1802,8 +1896,8 @@ extern "C" int gf_autotune(gf_ctx* c, int32_t reps, int32_t* shape) {
   c->profiling = prof0;
   restore();
   for (auto& pq : saved) cudaFreeAsync(pq.second, c->stream);
-  if (rc != GF_OK) { set_shape(c, g0.tuneRr, g0.tuneB, g0.tuneRc, g0.tuneC); upload_clock(c); return rc; }
-  set_shape(c, bestRr, bestB, bestRc, bestC);
+  if (rc != GF_OK) { set_shape(c, g0.tuneRr, g0.tuneB, g0.tuneRc, g0.tuneC, g0.tmaC); upload_clock(c); return rc; }
+  set_shape(c, bestRr, bestB, bestRc, bestC, bestT);
   if (int r = upload_clock(c)) return r;
   if (shape) { shape[0] = bestRr; shape[1] = bestB; shape[2] = bestRc; shape[3] = bestC; }
   return GF_OK;

@@ -3,8 +3,44 @@
 #include <type_traits>
 #include "gf_adjoint.cuh"
 #include "gf_launch.cuh"
+#include "gf_tma.cuh"
 
 namespace gf {
+
+// TMA column stage with C columns per block (tensor-map pair ci of the context).
+template <class T, int NN, int R, int C>
+cudaError_t launch_col_tma_c(const Geom& g, const ModArgs& m, const StepArgs& s, const Bufs& b, cudaStream_t st,
+                             int ci) {
+  cudaError_t err;
+  Geom g2 = g;
+  g2.cs = col_stride<T>(NN, C);
+  const size_t sm = col_tma_smem(C, g2.cs, sizeof(cplx<T>));
+  auto k = col_tma_kernel<T, NN, R, C>;
+  if ((err = set_smem(k, sm)) != cudaSuccess) return err;
+  const int ncols = g.kout > 0 ? g.kout : g.nkr;
+  const CUtensorMap* mp = reinterpret_cast<const CUtensorMap*>(b.tma->p[ci]);
+  const CUtensorMap* mw = reinterpret_cast<const CUtensorMap*>(b.tma->w[ci]);
+  k<<<dim3((ncols + C - 1) / C, g.nb), C * (NN / R), sm, st>>>(g2, m, s, b, *mp, *mw, b.derr);
+  return cudaGetLastError();
+}
+
+// Whether the TMA column stage runs this launch: one layer, no bottom drag, at most two
+// product fields, tensor maps built, and a column count chosen (Geom::tmaC) that has maps.
+// Returns the tensor-map pair index, or -1.
+inline int col_tma_pair(const Geom& g, const ModArgs& m, const Bufs& b) {
+  if (!b.tma || !b.tma->ok || g.tmaC <= 0 || g.nl != 1 || m.drag || 1 + m.hasB + m.hasC > 2) return -1;
+  return g.tmaC == b.tma->Cs[0] ? 0 : g.tmaC == b.tma->Cs[1] ? 1 : -1;
+}
+
+template <class T, int NN, int R>
+cudaError_t launch_col_tma(const Geom& g, const ModArgs& m, const StepArgs& s, const Bufs& b, cudaStream_t st,
+                           int ci) {
+  // the candidate column counts: 2 and 4 columns of 8-byte elements (16- and 32-byte box
+  // rows), 1 and 2 columns of 16-byte elements
+  constexpr int C0 = sizeof(cplx<T>) == 8 ? 2 : 1;
+  if (ci == 0) return launch_col_tma_c<T, NN, R, C0>(g, m, s, b, st, ci);
+  return launch_col_tma_c<T, NN, R, 2 * C0>(g, m, s, b, st, ci);
+}
 
 // Row kernel with FFT radix R; B row pairs per block from the autotuner when it fits.
 template <class T, int NN, int R>
@@ -29,6 +65,7 @@ cudaError_t launch_row_nr(const Geom& g, const ModArgs& m, const Bufs& b, cudaSt
 template <class T, int NN, int R>
 cudaError_t launch_col_nr(const Geom& g, const ModArgs& m, const StepArgs& s, const Bufs& b, cudaStream_t st) {
   cudaError_t err = cudaSuccess;
+  if (const int ci = col_tma_pair(g, m, b); ci >= 0) return launch_col_tma<T, NN, R>(g, m, s, b, st, ci);
   const size_t e = sizeof(cplx<T>);
   constexpr bool is_df64 = std::is_same<T, df64>::value;
   auto smem = [&](int c) { return col_stage_smem(NN, c, col_stride<T>(NN, c), m, g.nl, e, c * (NN / R), is_df64); };

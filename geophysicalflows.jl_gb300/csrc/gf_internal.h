@@ -37,6 +37,8 @@ struct Geom {
   // launch shape chosen by gf_autotune (0: the block-shape heuristic): column-kernel columns
   // per block and FFT radix, row-kernel row pairs per block and FFT radix
   int tuneC, tuneRc, tuneB, tuneRr;
+  // columns per block of the TMA column stage (0: the cp.async column kernel)
+  int tmaC;
 };
 
 // Device-resident clock, advanced on the GPU after every step so that a captured graph of
@@ -112,11 +114,22 @@ inline void split_hl(double d, float* h, float* l) {
   *l = (float)(d - (double)*h);
 }
 
+// Tensor maps (CUtensorMap, 128 bytes each) of P (tile loads) and W (tile stores) for the TMA
+// column stage, one pair per candidate column count Cs[i] of a block.
+struct TmaMaps {
+  alignas(64) unsigned char p[2][128];
+  alignas(64) unsigned char w[2][128];
+  int Cs[2] = {0, 0};
+  bool ok = false;
+};
+
 struct Bufs {
   const void* twid;       // TWN twiddles
   void* W;                // [3][layer][j][ldw]
   void* P;                // [3][layer][j][ldk]
   void* phys = nullptr;   // row kernel: also store (q + eta, u, v) [3][layer][j][nx] (adjoint recompute)
+  const TmaMaps* tma = nullptr;  // host copy of the context's tensor maps (null: no TMA column stage)
+  int* derr = nullptr;           // device error flag (a TMA wait that ran out of time sets it)
 };
 
 // Arguments of the adjoint kernels (gf_adjoint.cuh).

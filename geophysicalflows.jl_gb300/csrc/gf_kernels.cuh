@@ -117,6 +117,163 @@ __device__ __forceinline__ void psi_all(const ModArgs& m, int nl, T K2, const cp
   for (int a = 0; a < nl; ++a) psi[a] = f * X[a];
 }
 
+// ------------------------------------------------------------------- stage epilogue
+// Per-thread constants of a column-kernel thread at column kr (shared by the column kernels).
+template <class T>
+struct EpiCtx {
+  int kr;
+  T krT, dky, dt, U0, fscale;
+  uint64_t step;
+  int ab3_euler;
+  size_t ioff, ib, lstride;
+  int nl;
+  cplx<T>* Dp;
+};
+
+// Per-element stage epilogue at (layer L, row j) of column x.kr: forcing, U eta term, bottom
+// drag, the stepper's stage combination; returns the next stage's X (zero where dealiased).
+// Columns kr < kout only.
+template <class T>
+__device__ __forceinline__ cplx<T> stage_epilogue(const EpiCtx<T>& x, const Geom& g, const ModArgs& m,
+                                                  const StepArgs& s, int L, int j, cplx<T> N) {
+  const int kr = x.kr, nl = x.nl, ab3_euler = x.ab3_euler;
+  const T krT = x.krT, dt = x.dt, U0 = x.U0, fscale = x.fscale;
+  const uint64_t step = x.step;
+  const size_t ioff = x.ioff, ib = x.ib, lstride = x.lstride;
+  cplx<T>* Dp = x.Dp;
+  cplx<T> xn = czero<T>();
+  const size_t ti = (size_t)j * g.ldk + kr;       // table index
+  const size_t si = ioff + (size_t)L * lstride + ti;  // state index
+  const bool keep = kept(g, kr, j);
+  if (m.Ueta) N = N - (U0 * krT) * mul_i(static_cast<const cplx<T>*>(m.etah)[ti]);
+  if (m.drag && L == nl - 1) N = N + Dp[ti];
+  cplx<T>* sol = static_cast<cplx<T>*>(s.sol);
+  const cplx<T> solm = keep ? sol[si] : czero<T>();
+  // forcing
+  if (s.fkind == FK_STATIC) {
+    N = N + static_cast<const cplx<T>*>(s.Fh)[si];
+  } else if (s.fkind == FK_HARMONIC) {
+    N = N + fscale * static_cast<const cplx<T>*>(s.Fh)[si];
+  } else if (s.fkind == FK_STOCH || s.fkind == FK_STOCH_PHASE) {
+    cplx<T> Fv;
+    if (s.draw) {
+      const T sp = static_cast<const T*>(s.fspec)[ti];
+      const uint64_t e = (uint64_t)kr + (uint64_t)g.nkr * ((uint64_t)j + (uint64_t)g.ny * L);
+      Fv = czero<T>();
+      const bool zero_mean = (s.fkind == FK_STOCH_PHASE) && kr == 0 && j == 0;
+      if (sp != T(0) && !zero_mean) Fv = sp * draw<T>(e, step, s.seed + ib, s.fkind == FK_STOCH_PHASE);
+      static_cast<cplx<T>*>(s.Fstore)[si] = Fv;
+      static_cast<cplx<T>*>(s.prevsol)[si] = solm;
+    } else {
+      Fv = static_cast<const cplx<T>*>(s.Fh)[si];
+    }
+    N = N + Fv;
+  }
+  auto Lmul = [&](cplx<T> v) { return mulc(ldc<T>(s.Ltab, ti, s.cplxL), v, s.cplxL); };
+  auto finish = [&](cplx<T> v) {
+    if (s.filtered) v = static_cast<const T*>(s.filt)[ti] * v;
+    sol[si] = v;
+    return v;
+  };
+  if (s.kind == SK_NOUT) {
+    static_cast<cplx<T>*>(s.acc)[si] = N;
+  } else if (s.kind == SK_FE) {
+    cplx<T> Rv = N;
+    if (s.hasL) Rv = Rv + Lmul(solm);
+    xn = finish(solm + dt * Rv);
+  } else if (s.kind == SK_RK4) {
+    cplx<T>* X = static_cast<cplx<T>*>(s.X);
+    cplx<T>* acc = static_cast<cplx<T>*>(s.acc);
+    cplx<T> Rv = N;
+    if (s.hasL) Rv = Rv + Lmul(s.stage == 1 ? solm : (keep ? X[si] : czero<T>()));
+    if (s.stage == 1) {
+      acc[si] = T(1.0 / 6.0) * Rv;
+      xn = solm + T(0.5) * dt * Rv;
+    } else if (s.stage < 4) {
+      acc[si] = acc[si] + T(1.0 / 3.0) * Rv;
+      xn = solm + (s.stage == 2 ? T(0.5) * dt : dt) * Rv;
+    } else {
+      xn = finish(solm + dt * (acc[si] + T(1.0 / 6.0) * Rv));
+    }
+    if (s.hasL && s.stage < 4) X[si] = keep ? xn : czero<T>();
+  } else if (s.kind == SK_ETDRK4) {
+    const int cx = s.cplxL;
+    cplx<T>* acc = static_cast<cplx<T>*>(s.acc);
+    if (s.stage == 1) {
+      xn = mulc(ldc<T>(s.e2, ti, cx), solm, cx) + mulc(ldc<T>(s.zeta, ti, cx), N, cx);
+      static_cast<cplx<T>*>(s.s1)[si] = keep ? xn : czero<T>();
+      static_cast<cplx<T>*>(s.N1)[si] = N;
+      acc[si] = mulc(ldc<T>(s.alpha, ti, cx), N, cx);
+    } else if (s.stage == 2) {
+      xn = mulc(ldc<T>(s.e2, ti, cx), solm, cx) + mulc(ldc<T>(s.zeta, ti, cx), N, cx);
+      acc[si] = acc[si] + T(2) * mulc(ldc<T>(s.beta, ti, cx), N, cx);
+    } else if (s.stage == 3) {
+      const cplx<T> s1 = static_cast<const cplx<T>*>(s.s1)[si];
+      const cplx<T> n1 = static_cast<const cplx<T>*>(s.N1)[si];
+      xn = mulc(ldc<T>(s.e2, ti, cx), s1, cx) + mulc(ldc<T>(s.zeta, ti, cx), T(2) * N - n1, cx);
+      acc[si] = acc[si] + T(2) * mulc(ldc<T>(s.beta, ti, cx), N, cx);
+    } else {
+      xn = finish(mulc(ldc<T>(s.e, ti, cx), solm, cx) + acc[si] + mulc(ldc<T>(s.gamma, ti, cx), N, cx));
+    }
+  } else {  // AB3
+    cplx<T> Rv = N;
+    if (s.hasL) Rv = Rv + Lmul(solm);
+    cplx<T> upd;
+    if (ab3_euler) {
+      upd = Rv;
+    } else {
+      const cplx<T> r1 = static_cast<const cplx<T>*>(s.Rm1)[si];
+      const cplx<T> r2 = static_cast<const cplx<T>*>(s.Rm2)[si];
+      upd = T(23.0 / 12.0) * Rv - T(16.0 / 12.0) * r1 + T(5.0 / 12.0) * r2;
+    }
+    static_cast<cplx<T>*>(s.Rout)[si] = Rv;
+    xn = finish(solm + dt * upd);
+  }
+  if (!keep) xn = czero<T>();
+  return xn;
+}
+
+// One product slot's term of N at row j of column x.kr: -i kr A, -i l B, -C (or -i l C of
+// the zonal mean).
+template <class T>
+__device__ __forceinline__ cplx<T> product_term(const EpiCtx<T>& x, const Geom& g, const ModArgs& m, int slot, int j,
+                                                cplx<T> v) {
+  cplx<T> d;
+  if (slot == 0) d = x.krT * mul_mi(v);
+  else if (slot == 1) d = (T(lidx(g, j)) * x.dky) * mul_mi(v);
+  else if (m.ql) d = (T(lidx(g, j)) * x.dky) * mul_mi(v);
+  else d = czero<T>() - v;
+  if (m.ql && ((x.kr == 0) != (slot == 2))) d = czero<T>();  // mean: C only; eddies: A, B
+  return d;
+}
+
+// The epilogue constants of the column-kernel thread at column kr of instance ib.
+template <class T>
+__device__ __forceinline__ EpiCtx<T> epi_ctx(const Geom& g, const ModArgs& m, const StepArgs& s, int kr, size_t ib) {
+  EpiCtx<T> x;
+  x.kr = kr;
+  x.krT = T(kr) * sel<T>(g.dkx, g.dkx_f, g.dkx_l);
+  x.dky = sel<T>(g.dky, g.dky_f, g.dky_l);
+  x.dt = sel<T>(s.dt, s.dt_f, s.dt_l);
+  x.U0 = sel<T>(m.U0, m.U0_f, m.U0_l);
+  // clock-dependent values: from the device clock when the launch is part of a graph
+  x.step = s.step;
+  x.fscale = sel<T>(s.fscale, s.fscale_f, s.fscale_l);
+  x.ab3_euler = s.ab3_euler;
+  if (s.clk) {
+    x.step = (uint64_t)s.clk->step;
+    const int k = s.stage >= 1 ? s.stage - 1 : 0;
+    x.fscale = sel<T>(s.clk->fs[k], s.clk->fs_f[k], s.clk->fs_l[k]);
+    x.ab3_euler = s.clk->step < 3;
+  }
+  x.ib = ib;
+  x.ioff = ib * g.bs_spec;
+  x.lstride = (size_t)g.ny * g.ldk;
+  x.nl = g.nl;
+  x.Dp = m.D ? static_cast<cplx<T>*>(m.D) + ib * g.bs_d : nullptr;
+  return x;
+}
+
 // ------------------------------------------------------------------------ column kernel
 // Block: C adjacent kr columns x (NY/R) threads per column.  Two thread mappings:
 //   element mapping (global loads/stores, epilogue): c = tid % C, t = tid / C, so a warp's
@@ -180,110 +337,9 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : MAXT < 512 ? 3 : sizeof
   }
 
   const T U0 = sel<T>(m.U0, m.U0_f, m.U0_l);
-  // per-element stage epilogue: forcing, U eta term, bottom drag, the stepper's stage
-  // combination; returns the next stage's X at (L, j) (zero where dealiased).  kin only.
-  auto epilogue = [&](int L, int j, cplx<T> N) -> cplx<T> {
-    cplx<T> xn = czero<T>();
-    const size_t ti = (size_t)j * g.ldk + kr;       // table index
-    const size_t si = ioff + (size_t)L * lstride + ti;  // state index
-    const bool keep = kept(g, kr, j);
-    if (m.Ueta) N = N - (U0 * krT) * mul_i(static_cast<const cplx<T>*>(m.etah)[ti]);
-    if (m.drag && L == nl - 1) N = N + Dp[ti];
-    cplx<T>* sol = static_cast<cplx<T>*>(s.sol);
-    const cplx<T> solm = keep ? sol[si] : czero<T>();
-    // forcing
-    if (s.fkind == FK_STATIC) {
-      N = N + static_cast<const cplx<T>*>(s.Fh)[si];
-    } else if (s.fkind == FK_HARMONIC) {
-      N = N + fscale * static_cast<const cplx<T>*>(s.Fh)[si];
-    } else if (s.fkind == FK_STOCH || s.fkind == FK_STOCH_PHASE) {
-      cplx<T> Fv;
-      if (s.draw) {
-        const T sp = static_cast<const T*>(s.fspec)[ti];
-        const uint64_t e = (uint64_t)kr + (uint64_t)g.nkr * ((uint64_t)j + (uint64_t)g.ny * L);
-        Fv = czero<T>();
-        const bool zero_mean = (s.fkind == FK_STOCH_PHASE) && kr == 0 && j == 0;
-        if (sp != T(0) && !zero_mean) Fv = sp * draw<T>(e, step, s.seed + ib, s.fkind == FK_STOCH_PHASE);
-        static_cast<cplx<T>*>(s.Fstore)[si] = Fv;
-        static_cast<cplx<T>*>(s.prevsol)[si] = solm;
-      } else {
-        Fv = static_cast<const cplx<T>*>(s.Fh)[si];
-      }
-      N = N + Fv;
-    }
-    auto Lmul = [&](cplx<T> x) { return mulc(ldc<T>(s.Ltab, ti, s.cplxL), x, s.cplxL); };
-    auto finish = [&](cplx<T> v) {
-      if (s.filtered) v = static_cast<const T*>(s.filt)[ti] * v;
-      sol[si] = v;
-      return v;
-    };
-    if (s.kind == SK_NOUT) {
-      static_cast<cplx<T>*>(s.acc)[si] = N;
-    } else if (s.kind == SK_FE) {
-      cplx<T> Rv = N;
-      if (s.hasL) Rv = Rv + Lmul(solm);
-      xn = finish(solm + dt * Rv);
-    } else if (s.kind == SK_RK4) {
-      cplx<T>* X = static_cast<cplx<T>*>(s.X);
-      cplx<T>* acc = static_cast<cplx<T>*>(s.acc);
-      cplx<T> Rv = N;
-      if (s.hasL) Rv = Rv + Lmul(s.stage == 1 ? solm : (keep ? X[si] : czero<T>()));
-      if (s.stage == 1) {
-        acc[si] = T(1.0 / 6.0) * Rv;
-        xn = solm + T(0.5) * dt * Rv;
-      } else if (s.stage < 4) {
-        acc[si] = acc[si] + T(1.0 / 3.0) * Rv;
-        xn = solm + (s.stage == 2 ? T(0.5) * dt : dt) * Rv;
-      } else {
-        xn = finish(solm + dt * (acc[si] + T(1.0 / 6.0) * Rv));
-      }
-      if (s.hasL && s.stage < 4) X[si] = keep ? xn : czero<T>();
-    } else if (s.kind == SK_ETDRK4) {
-      const int cx = s.cplxL;
-      cplx<T>* acc = static_cast<cplx<T>*>(s.acc);
-      if (s.stage == 1) {
-        xn = mulc(ldc<T>(s.e2, ti, cx), solm, cx) + mulc(ldc<T>(s.zeta, ti, cx), N, cx);
-        static_cast<cplx<T>*>(s.s1)[si] = keep ? xn : czero<T>();
-        static_cast<cplx<T>*>(s.N1)[si] = N;
-        acc[si] = mulc(ldc<T>(s.alpha, ti, cx), N, cx);
-      } else if (s.stage == 2) {
-        xn = mulc(ldc<T>(s.e2, ti, cx), solm, cx) + mulc(ldc<T>(s.zeta, ti, cx), N, cx);
-        acc[si] = acc[si] + T(2) * mulc(ldc<T>(s.beta, ti, cx), N, cx);
-      } else if (s.stage == 3) {
-        const cplx<T> s1 = static_cast<const cplx<T>*>(s.s1)[si];
-        const cplx<T> n1 = static_cast<const cplx<T>*>(s.N1)[si];
-        xn = mulc(ldc<T>(s.e2, ti, cx), s1, cx) + mulc(ldc<T>(s.zeta, ti, cx), T(2) * N - n1, cx);
-        acc[si] = acc[si] + T(2) * mulc(ldc<T>(s.beta, ti, cx), N, cx);
-      } else {
-        xn = finish(mulc(ldc<T>(s.e, ti, cx), solm, cx) + acc[si] + mulc(ldc<T>(s.gamma, ti, cx), N, cx));
-      }
-    } else {  // AB3
-      cplx<T> Rv = N;
-      if (s.hasL) Rv = Rv + Lmul(solm);
-      cplx<T> upd;
-      if (ab3_euler) {
-        upd = Rv;
-      } else {
-        const cplx<T> r1 = static_cast<const cplx<T>*>(s.Rm1)[si];
-        const cplx<T> r2 = static_cast<const cplx<T>*>(s.Rm2)[si];
-        upd = T(23.0 / 12.0) * Rv - T(16.0 / 12.0) * r1 + T(5.0 / 12.0) * r2;
-      }
-      static_cast<cplx<T>*>(s.Rout)[si] = Rv;
-      xn = finish(solm + dt * upd);
-    }
-    if (!keep) xn = czero<T>();
-    return xn;
-  };
-  // one product slot's term of N at row j: -i kr A, -i l B, -C (or -i l C of the zonal mean)
-  auto slot_term = [&](int slot, int j, cplx<T> v) -> cplx<T> {
-    cplx<T> d;
-    if (slot == 0) d = krT * mul_mi(v);
-    else if (slot == 1) d = (T(lidx(g, j)) * dky) * mul_mi(v);
-    else if (m.ql) d = (T(lidx(g, j)) * dky) * mul_mi(v);
-    else d = czero<T>() - v;
-    if (m.ql && ((kr == 0) != (slot == 2))) d = czero<T>();  // mean: C only; eddies: A, B
-    return d;
-  };
+  const EpiCtx<T> ec{kr, krT, dky, dt, U0, fscale, step, ab3_euler, ioff, ib, lstride, nl, Dp};
+  auto epilogue = [&](int L, int j, cplx<T> N) -> cplx<T> { return stage_epilogue<T>(ec, g, m, s, L, j, N); };
+  auto slot_term = [&](int slot, int j, cplx<T> v) -> cplx<T> { return product_term<T>(ec, g, m, slot, j, v); };
   cplx<T>* W = static_cast<cplx<T>*>(b.W) + ib * g.bs_w;
   const T sc = sel<T>(g.inv_nxny, g.inv_nxny_f, g.inv_nxny_l);
 

@@ -207,10 +207,24 @@ class Problem:
 
     def autotune(self, reps=4):
         """Time the step kernels at every candidate launch shape and keep the fastest;
-        returns {row_radix, row_pairs, col_radix, col_columns}."""
+        returns {row_radix, row_pairs, col_radix, col_columns, tma_columns} (tma_columns > 0:
+        the column stage runs with TMA tile copies, that many columns per block)."""
         sh = (C.c_int32 * 4)()
         self._c(self._lib.gf_autotune(self._ctx, int(reps), sh))
-        return dict(zip(("row_radix", "row_pairs", "col_radix", "col_columns"), list(sh)))
+        d = dict(zip(("row_radix", "row_pairs", "col_radix", "col_columns"), list(sh)))
+        d["tma_columns"] = self.tma_columns
+        return d
+
+    @property
+    def tma_columns(self):
+        """Columns per block of the TMA column stage (0: per-thread-copy column kernel)."""
+        v = C.c_int32()
+        self._c(self._lib.gf_get_tma_columns(self._ctx, C.byref(v)))
+        return v.value
+
+    @tma_columns.setter
+    def tma_columns(self, n):
+        self._c(self._lib.gf_set_tma_columns(self._ctx, int(n)))
 
     @property
     def launch_shape(self):

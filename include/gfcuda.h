@@ -281,10 +281,22 @@ int gf_step_callback(gf_ctx* ctx, int64_t nsteps, gf_forcing_fn fn, void* user);
  * without bottom drag with columns of >= 1024 may get blocks of up to 640 threads there,
  * while the last step of a call keeps blocks of <= 512 threads (the column count capped).
  * gf_set_launch_shape applies a shape found earlier (e.g. for another context of the same
- * size). */
+ * size).  The autotuner also times the TMA column stage (below) at each column radix where
+ * it applies, and selects it (gf_get_tma_columns) when it is the fastest. */
 int gf_autotune(gf_ctx* ctx, int32_t reps, int32_t* shape);
 int gf_set_launch_shape(gf_ctx* ctx, const int32_t* shape);
 int gf_get_launch_shape(const gf_ctx* ctx, int32_t* shape);
+
+/* TMA column stage (no reference counterpart): for one layer without bottom drag and with at
+ * most two nonlinear product fields (TwoDNavierStokes, SurfaceQG, SingleLayerQG without a PV
+ * gradient product), the column half of each stage can load its product tiles and store the
+ * inverse fields with tensor-memory-access tile copies (cp.async.bulk.tensor) instead of
+ * per-thread copies.  C = columns per block: 2 or 4 (GF_F32), 1 or 2 (GF_F64, GF_DF64);
+ * 0 selects the per-thread-copy column kernel.  GF_ERR_UNSUPPORTED if the context cannot use
+ * it with C.  The column radix stays that of the launch shape.  If a tile load does not
+ * arrive within one second the kernel sets an error flag that gf_synchronize reports. */
+int gf_set_tma_columns(gf_ctx* ctx, int32_t C);
+int gf_get_tma_columns(const gf_ctx* ctx, int32_t* C);
 
 /* ---- adjoint ----------------------------------------------------------------------------
  * Reverse-mode derivative of stepforward!(prob, nsteps), the counterpart of a
