@@ -168,11 +168,41 @@ __device__ __forceinline__ void tma_passes(cplx<T>* F, int fstride, int cs, int 
   }
 }
 
+// Stride of the last pass of a length-N transform at radix R (the largest R^p below N).
+template <int N, int R> __host__ __device__ constexpr int last_stride() {
+  int s = 1;
+  while (s * ((N / s < R) ? N / s : R) < N) s *= R;
+  return s;
+}
+
+// The same passes for 8-byte types (FP64, df64), whose butterflies are long code: the first
+// and last passes inlined (they touch the dense layout), the full radix-R passes between them
+// from one run-time loop body (fft_pass_dyn, column-major mapping) for the instruction cache.
+template <class T, int N, int R, int DIR, int NF, int C, bool SRCD, bool DSTD>
+__device__ __forceinline__ void tma_passes_looped(cplx<T>* F, int fstride, int cs, int tid,
+                                                  const cplx<T>* __restrict__ tw) {
+  constexpr int NL = last_stride<N, R>();
+  if constexpr (NL == 1) {
+    tma_pass<T, N, R, DIR, NF, C, 1, SRCD, DSTD>(F, fstride, cs, tid, tw);
+  } else {
+    constexpr int TPF = N / R;
+    tma_pass<T, N, R, DIR, NF, C, 1, SRCD, false>(F, fstride, cs, tid, tw);
+    int lg = ilog2(R);
+#pragma unroll 1
+    for (int Ns = R; Ns < NL; Ns *= R, lg += ilog2(R))
+      fft_pass_dyn<T, N, R, DIR, NF>(F + (tid / TPF) * cs, fstride, tid % TPF, tw, Ns, lg);
+    tma_pass<T, N, R, DIR, NF, C, NL, false, DSTD>(F, fstride, cs, tid, tw);
+  }
+}
+
 // NF FFTs of fields F + f * fstride: in lockstep when the registers allow (FP32, NF x R <= 24
 // values per thread), otherwise one after the other.
 template <class T, int N, int R, int DIR, int NF, int C, bool SRCD, bool DSTD>
 __device__ __forceinline__ void tma_fft(cplx<T>* F, int fstride, int cs, int tid, const cplx<T>* __restrict__ tw) {
-  if constexpr (NF == 1 || (sizeof(T) == 4 && NF * R <= 24)) {
+  if constexpr (sizeof(T) == 8 && GF_FFT_LOOP) {
+#pragma unroll 1
+    for (int f = 0; f < NF; ++f) tma_passes_looped<T, N, R, DIR, 1, C, SRCD, DSTD>(F + f * fstride, 0, cs, tid, tw);
+  } else if constexpr (NF == 1 || (sizeof(T) == 4 && NF * R <= 24)) {
     tma_passes<T, N, R, DIR, NF, C, 1, SRCD, DSTD>(F, fstride, cs, tid, tw);
   } else {
 #pragma unroll 1
@@ -216,11 +246,22 @@ __global__ void __launch_bounds__(C*(NY / R), (C * (NY / R) <= 256) ? 3 : 1)
   const T sc = sel<T>(g.inv_nxny, g.inv_nxny_f, g.inv_nxny_l);
   const int nslot = 1 + m.hasB + m.hasC;  // <= 2 (the host launches this kernel only then)
 
-  cplx<T> xr[R];
   if (__syncthreads_or(tid == 0 && ((smem_u32(F0) | smem_u32(F1)) & 127u) != 0)) {
     if (tid == 0) atomicOr(err, 2);
     return;
   }
+  // The next stage's X at element (c, j) goes straight into the slots of that element: q = X
+  // into F0 and v = i kr psi into F1 (scaled by 1 / (nx ny)), so no per-thread array of X is
+  // kept (with the shared-memory carve-out L1 is small, and such an array would live in local
+  // memory backed by L2).  Each thread reads and writes only its own elements' slots.
+  const T dky = ec.dky, krT = ec.krT;
+  auto fill_qv = [&](int j, cplx<T> x) {
+    const T lv = T(lidx(g, j)) * dky;
+    const T K2 = krT * krT + lv * lv;
+    const cplx<T> p = psi_factor<T>(m.psi_kind, K2, ell2, m.mult, (size_t)j * g.ldk + (kin ? kr : 0)) * x;
+    F0[c * cs + swz<T>(j)] = sc * x;
+    F1[c * cs + swz<T>(j)] = sc * (krT * mul_i(p));   // v = i kr psi
+  };
   if (s.do_fwd) {
     if (tid == 0) {
       mbar_init(&bar, 1);
@@ -246,61 +287,59 @@ __global__ void __launch_bounds__(C*(NY / R), (C * (NY / R) <= 256) ? 3 : 1)
 #pragma unroll 1
     for (int i = 0; i < R; ++i) {
       const int j = t + i * TPF;
-      xr[i] = czero<T>();
-      if (!kin || (prune && !kept(g, kr, j))) continue;
-      cplx<T> N = czero<T>();
-      for (int f = 0; f < nslot; ++f) {
-        const int slot = (f == 0) ? 0 : m.hasB ? 1 : 2;
-        N = N + product_term<T>(ec, g, m, slot, j, F0[f * fstride + c * cs + swz<T>(j)]);
+      cplx<T> xn = czero<T>();
+      if (kin && !(prune && !kept(g, kr, j))) {
+        cplx<T> N = czero<T>();
+        for (int f = 0; f < nslot; ++f) {
+          const int slot = (f == 0) ? 0 : m.hasB ? 1 : 2;
+          N = N + product_term<T>(ec, g, m, slot, j, F0[f * fstride + c * cs + swz<T>(j)]);
+        }
+        xn = stage_epilogue<T>(ec, g, m, s, 0, j, N);
       }
-      xr[i] = stage_epilogue<T>(ec, g, m, s, 0, j, N);
+      fill_qv(j, xn);
     }
   } else {
     const cplx<T>* sol = static_cast<const cplx<T>*>(s.sol);
-#pragma unroll
+#pragma unroll 1
     for (int i = 0; i < R; ++i) {
       const int j = t + i * TPF;
-      xr[i] = (kin && kept(g, kr, j)) ? sol[ec.ioff + (size_t)j * g.ldk + kr] : czero<T>();
+      fill_qv(j, (kin && kept(g, kr, j)) ? sol[ec.ioff + (size_t)j * g.ldk + kr] : czero<T>());
     }
   }
   if (!s.do_inv) return;
   if (kr0 >= g.kcut) return;  // whole block aliased: W is never read there
+  __syncthreads();
 
-  // y-inverse FFTs of the next stage's (q, u, v): q (F0) and u (F1) first, stored by TMA, then
-  // v (F0, psi formed again from the registers).  Each thread fills only the slots it read in
-  // the epilogue, so no barrier is needed before the first fill.
-  const T dky = ec.dky, krT = ec.krT;
+  // y-inverse FFTs of the next stage's (q, u, v): v (F1) first, stored by TMA; then u = -i l
+  // psi formed from the untransformed q in F0 (psi = f q / sc) into F1, and q and u
+  // transformed and stored together.
+  tma_fft<T, NY, R, +1, 1, C, false, true>(F1, fstride, cs, tid, tw);
+  fence_proxy_async_smem();
+  __syncthreads();
+  if (tid == 0) {
+    for (int r0 = 0; r0 < NY; r0 += BR) tma_store_3d(&tmW, kr0 * WPC, 2 * g.ny + r0, z, F1 + r0 * C);
+    bulk_commit();
+    bulk_wait_read();  // F1 is refilled with u below
+  }
+  __syncthreads();
 #pragma unroll 1
-  for (int round = 0; round < 2; ++round) {
-#pragma unroll 4
-    for (int i = 0; i < R; ++i) {
-      const int j = t + i * TPF;
-      const T lv = T(lidx(g, j)) * dky;
-      const T K2 = krT * krT + lv * lv;
-      const cplx<T> x = xr[i];
-      const cplx<T> p = psi_factor<T>(m.psi_kind, K2, ell2, m.mult, (size_t)j * g.ldk + (kin ? kr : 0)) * x;
-      if (round == 0) {
-        F0[c * cs + swz<T>(j)] = sc * x;
-        F1[c * cs + swz<T>(j)] = sc * (lv * mul_mi(p));   // u = -i l psi
-      } else {
-        F0[c * cs + swz<T>(j)] = sc * (krT * mul_i(p));   // v =  i kr psi
-      }
-    }
-    __syncthreads();
-    if (round == 0) tma_fft<T, NY, R, +1, 2, C, false, true>(F0, fstride, cs, tid, tw);
-    else tma_fft<T, NY, R, +1, 1, C, false, true>(F0, fstride, cs, tid, tw);
-    fence_proxy_async_smem();
-    __syncthreads();
-    if (tid == 0) {
-      const int nf = round == 0 ? 2 : 1;
-      for (int f = 0; f < nf; ++f)
-        for (int r0 = 0; r0 < NY; r0 += BR)
-          tma_store_3d(&tmW, kr0 * WPC, (round == 0 ? f : 2) * g.ny + r0, z, F0 + f * fstride + r0 * C);
-      bulk_commit();
-      if (round == 0) bulk_wait_read();  // F0 is refilled with v below
-      else bulk_wait_all();
-    }
-    if (round == 0) __syncthreads();
+  for (int i = 0; i < R; ++i) {
+    const int j = t + i * TPF;
+    const T lv = T(lidx(g, j)) * dky;
+    const T K2 = krT * krT + lv * lv;
+    const cplx<T> p =
+        psi_factor<T>(m.psi_kind, K2, ell2, m.mult, (size_t)j * g.ldk + (kin ? kr : 0)) * F0[c * cs + swz<T>(j)];
+    F1[c * cs + swz<T>(j)] = lv * mul_mi(p);   // u = -i l psi
+  }
+  __syncthreads();
+  tma_fft<T, NY, R, +1, 2, C, false, true>(F0, fstride, cs, tid, tw);
+  fence_proxy_async_smem();
+  __syncthreads();
+  if (tid == 0) {
+    for (int f = 0; f < 2; ++f)
+      for (int r0 = 0; r0 < NY; r0 += BR) tma_store_3d(&tmW, kr0 * WPC, f * g.ny + r0, z, F0 + f * fstride + r0 * C);
+    bulk_commit();
+    bulk_wait_all();
   }
 }
 
