@@ -98,6 +98,7 @@ struct gf_ctx {
   void* row_phys = nullptr;  // forward row kernels also store (q + eta, u, v) here when set
   TmaMaps tma;               // tensor maps of the TMA column stage (one layer)
   int* derr = nullptr;       // device error flag: a tile-load wait ran out of time
+  void *twx = nullptr, *twy = nullptr;  // generic-length twiddle tables (nx and ny entries)
   // identity and graph generation (an ensemble graph records the members it was built for)
   uint64_t uid = 0, gen = 0;
   cudaGraphExec_t egraph[2] = {nullptr, nullptr};      // ensemble graphs held by the first member (as gexec)
@@ -274,6 +275,30 @@ static void* dalloc(gf_ctx* c, size_t bytes) {
 
 static bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
 
+// FFT lengths with compiled-in kernels; every other even length runs the generic-length path
+static bool fixed_length(int n) { return is_pow2(n) && n >= 32 && n <= 2048; }
+
+// Radix plan of a generic length n (product of the radices = n): 16s, then 8, 4, 2 for the
+// power of two, then the odd primes in increasing order.  False if a prime factor exceeds
+// MAXPRIME or the plan has more than MAXP passes.
+static bool radix_plan(int n, int* plan, int* np) {
+  *np = 0;
+  auto push = [&](int r) {
+    if (*np >= MAXP) return false;
+    plan[(*np)++] = r;
+    return true;
+  };
+  while (n % 16 == 0) { if (!push(16)) return false; n /= 16; }
+  for (int r : {8, 4, 2})
+    if (n % r == 0) { if (!push(r)) return false; n /= r; }
+  for (int p = 3; p <= MAXPRIME && n > 1; p += 2)
+    while (n % p == 0) { if (!push(p)) return false; n /= p; }
+  return n == 1;
+}
+
+// Largest generic length: five shared buffers of the length per column block.
+static int max_generic_length(int precision) { return precision == GF_F32 ? 4096 : 2048; }
+
 static size_t nspec(const gf_ctx* c) { return (size_t)c->g.nl * c->g.ny * c->g.ldk; }
 
 // upload a host double array of n values as the context's real type
@@ -306,7 +331,7 @@ static int upload_table(gf_ctx* c, void* dst, const std::vector<double>& v, int 
   return GF_OK;
 }
 
-static Bufs bufs(gf_ctx* c) { return Bufs{c->twid, c->W, c->P, c->row_phys, &c->tma, c->derr}; }
+static Bufs bufs(gf_ctx* c) { return Bufs{c->twid, c->W, c->P, c->row_phys, &c->tma, c->derr, c->twx, c->twy}; }
 static Geom full_geom(const gf_ctx* c) {
   Geom g = c->g;
   g.kcut = g.nkr; g.lA = 1; g.lB = 0; g.ldw = g.ldk;
@@ -514,6 +539,23 @@ static int build(gf_ctx* c, const gf_config* cfg) {
     }
     if (!(c->twid = dalloc(c, 2 * TWN * rb))) return fail(c, GF_ERR_NOMEM, "twiddles");
     if (int r = upload_real(c, c->twid, tw.data(), tw.size())) return r;
+  }
+  // ----- generic-length transforms: radix plans and exp(-2 pi i k / n) tables
+  g.rtx = !fixed_length(k.nx);
+  g.rty = !fixed_length(k.ny);
+  if (g.rtx && !radix_plan(k.nx, g.plx, &g.npx)) return fail(c, GF_ERR_UNSUPPORTED, "nx has no radix plan");
+  if (g.rty && !radix_plan(k.ny, g.ply, &g.npy)) return fail(c, GF_ERR_UNSUPPORTED, "ny has no radix plan");
+  for (int d = 0; d < 2; ++d) {
+    const int n = d == 0 ? k.nx : k.ny;
+    if (!(d == 0 ? g.rtx : g.rty)) continue;
+    std::vector<double> tw(2 * (size_t)n);
+    for (int i = 0; i < n; ++i) {
+      tw[2 * i] = std::cos(2 * M_PI * i / n);
+      tw[2 * i + 1] = -std::sin(2 * M_PI * i / n);
+    }
+    void*& dst = d == 0 ? c->twx : c->twy;
+    if (!(dst = dalloc(c, 2 * (size_t)n * rb))) return fail(c, GF_ERR_NOMEM, "twiddles");
+    if (int r = upload_real(c, dst, tw.data(), tw.size())) return r;
   }
   // ----- wavenumber tables on the host (double)
   std::vector<double> K2((size_t)g.ny * g.nkr), krv(g.nkr), lv(g.ny);
@@ -819,8 +861,14 @@ extern "C" int gf_create(const gf_config* cfg, void* stream, gf_ctx** out) {
   if (k.stepper < 0 || k.stepper > 7) return fail(nullptr, GF_ERR_ARG, "unknown stepper");
   if (k.nx <= 0 || k.ny <= 0 || !(k.Lx > 0) || !(k.Ly > 0) || !(k.dt > 0))
     return fail(nullptr, GF_ERR_ARG, "nx, ny, Lx, Ly and dt must be positive");
-  if (!is_pow2(k.nx) || !is_pow2(k.ny) || k.nx < 32 || k.ny < 32 || k.nx > 2048 || k.ny > 2048)
-    return fail(nullptr, GF_ERR_UNSUPPORTED, "nx and ny must be powers of two in [32, 2048]");
+  for (int n : {k.nx, k.ny}) {
+    if (fixed_length(n)) continue;
+    int plan[MAXP], np = 0;
+    if (n % 2 != 0 || n < 4 || n > max_generic_length(k.precision) || !radix_plan(n, plan, &np))
+      return fail(nullptr, GF_ERR_UNSUPPORTED,
+                  "nx and ny must be even, at least 4, at most 4096 (FP32) or 2048 (FP64, df64), with prime factors "
+                  "no larger than 61");
+  }
   if (!(k.aliased_fraction >= 0) || !(k.aliased_fraction < 1))
     return fail(nullptr, GF_ERR_ARG, "`aliased_fraction` must be less than 1");
   if (k.module == GF_MULTILAYERQG) {
@@ -1773,7 +1821,7 @@ static int set_shape(gf_ctx* c, int Rr, int B, int Rc, int C, int tmaC = 0) {
 
 // whether the TMA column stage can run this context, and with C columns per block
 static bool tma_eligible(const gf_ctx* c, int C) {
-  return c->tma.ok && c->g.nl == 1 && !c->m.drag && 1 + c->m.hasB + c->m.hasC <= 2 &&
+  return c->tma.ok && !c->g.rty && c->g.nl == 1 && !c->m.drag && 1 + c->m.hasB + c->m.hasC <= 2 &&
          (C == c->tma.Cs[0] || C == c->tma.Cs[1]);
 }
 
@@ -1811,6 +1859,10 @@ extern "C" int gf_get_launch_shape(const gf_ctx* c, int32_t* shape) {
 
 extern "C" int gf_autotune(gf_ctx* c, int32_t reps, int32_t* shape) {
   if (!c) return GF_ERR_ARG;
+  if (c->g.rtx || c->g.rty) {  // generic lengths: one launch shape, nothing to tune
+    if (shape) for (int q = 0; q < 4; ++q) shape[q] = 0;
+    return GF_OK;
+  }
   if (c->cfg.forcing_kind >= GF_FORCING_STOCHASTIC && !c->fspec) return fail(c, GF_ERR_STATE, "no forcing spectrum");
   if (reps <= 0) reps = 4;
   const Geom g0 = c->g;
@@ -1977,6 +2029,7 @@ extern "C" int gf_step_output(gf_ctx* c, int64_t nsteps, int32_t every, const in
 // the transposed stages; memory: nsteps / every states + every x 4 x 3 physical fields.
 static int adj_check(gf_ctx* c) {
   const int mod = c->cfg.module;
+  if (c->g.rtx || c->g.rty) return fail(c, GF_ERR_UNSUPPORTED, "the adjoint needs power-of-two nx, ny in [32, 2048]");
   if (mod != GF_TWODNAVIERSTOKES && mod != GF_SINGLELAYERQG)
     return fail(c, GF_ERR_UNSUPPORTED, "the adjoint covers TwoDNavierStokes and SingleLayerQG");
   if (c->kind != SK_ETDRK4) return fail(c, GF_ERR_UNSUPPORTED, "the adjoint follows the ETDRK4 / FilteredETDRK4 stages");

@@ -27,6 +27,7 @@ namespace gf {
 
 template <class T>
 cudaError_t launch_row(const Geom& g, const ModArgs& m, const Bufs& b, cudaStream_t st) {
+  if (g.rtx) return launch_row_rt<T>(g, m, b, st);
   switch (g.nx) {
     GF_ROW_CASE(32) GF_ROW_CASE(64) GF_ROW_CASE(128) GF_ROW_CASE(256) GF_ROW_CASE(512) GF_ROW_CASE(1024)
     GF_ROW_CASE(2048)
@@ -36,6 +37,7 @@ cudaError_t launch_row(const Geom& g, const ModArgs& m, const Bufs& b, cudaStrea
 
 template <class T>
 cudaError_t launch_col(const Geom& g, const ModArgs& m, const StepArgs& s, const Bufs& b, cudaStream_t st) {
+  if (g.rty) return launch_col_rt<T>(g, m, s, b, st);
   switch (g.ny) {
     GF_COL_CASE(32) GF_COL_CASE(64) GF_COL_CASE(128) GF_COL_CASE(256) GF_COL_CASE(512) GF_COL_CASE(1024)
     GF_COL_CASE(2048)
@@ -46,6 +48,7 @@ cudaError_t launch_col(const Geom& g, const ModArgs& m, const StepArgs& s, const
 template <class T>
 cudaError_t launch_col_inv(const Geom& g, const ModArgs& m, const void* src, int kind, int mask, const Bufs& b,
                            cudaStream_t st) {
+  if (g.rty) return launch_col_inv_rt<T>(g, m, src, kind, mask, b, st);
   switch (g.ny) {
     case 32: return launch_col_inv_n<T, 32>(g, m, src, kind, mask, b, st);
     case 64: return launch_col_inv_n<T, 64>(g, m, src, kind, mask, b, st);
@@ -60,6 +63,7 @@ cudaError_t launch_col_inv(const Geom& g, const ModArgs& m, const void* src, int
 
 template <class T>
 cudaError_t launch_row_c2r(const Geom& g, const Bufs& b, int nf, void* out, cudaStream_t st) {
+  if (g.rtx) return launch_row_c2r_rt<T>(g, b, nf, out, st);
   switch (g.nx) {
     case 32: return launch_row_c2r_n<T, 32>(g, b, nf, out, st);
     case 64: return launch_row_c2r_n<T, 64>(g, b, nf, out, st);
@@ -74,6 +78,7 @@ cudaError_t launch_row_c2r(const Geom& g, const Bufs& b, int nf, void* out, cuda
 
 template <class T>
 cudaError_t launch_row_r2c(const Geom& g, const Bufs& b, int nf, const void* in, cudaStream_t st) {
+  if (g.rtx) return launch_row_r2c_rt<T>(g, b, nf, in, st);
   switch (g.nx) {
     case 32: return launch_row_r2c_n<T, 32>(g, b, nf, in, st);
     case 64: return launch_row_r2c_n<T, 64>(g, b, nf, in, st);
@@ -88,6 +93,7 @@ cudaError_t launch_row_r2c(const Geom& g, const Bufs& b, int nf, const void* in,
 
 template <class T>
 cudaError_t launch_col_fwd(const Geom& g, const Bufs& b, int nf, void* out, int zero_mean, cudaStream_t st) {
+  if (g.rty) return launch_col_fwd_rt<T>(g, b, nf, out, zero_mean, st);
   switch (g.ny) {
     case 32: return launch_col_fwd_n<T, 32>(g, b, nf, out, zero_mean, st);
     case 64: return launch_col_fwd_n<T, 64>(g, b, nf, out, zero_mean, st);

@@ -15,6 +15,8 @@ enum StepKind { SK_FE = 0, SK_RK4 = 1, SK_ETDRK4 = 2, SK_AB3 = 3, SK_NOUT = 4 /*
 enum PsiKind { PSI_INVK2 = 0, PSI_HELMHOLTZ = 1, PSI_TABLE = 2, PSI_EIGEN = 3 };
 enum ForceKind { FK_NONE = 0, FK_STATIC = 1, FK_HARMONIC = 2, FK_STOCH = 3, FK_STOCH_PHASE = 4 };
 constexpr int MAXL = 8;  // largest number of layers
+constexpr int MAXP = 16; // passes of a generic-length FFT plan
+constexpr int MAXPRIME = 61;  // largest prime factor of a generic length
 
 // Grid geometry in the internal layout: spectral arrays are [layer][j][kr] with row stride
 // ldk (>= nkr); the pruned inverse intermediates are [field][layer][j][kr < kcut] with row
@@ -39,6 +41,11 @@ struct Geom {
   int tuneC, tuneRc, tuneB, tuneRr;
   // columns per block of the TMA column stage (0: the cp.async column kernel)
   int tmaC;
+  // generic-length transforms (lengths other than the powers of two 32 ... 2048 that have
+  // their own kernels): rtx for the x direction (rows, length nx), rty for y (columns, ny),
+  // with their radix plans (product = the length)
+  int rtx, rty, npx, npy;
+  int plx[MAXP], ply[MAXP];
 };
 
 // Device-resident clock, advanced on the GPU after every step so that a captured graph of
@@ -130,6 +137,8 @@ struct Bufs {
   void* phys = nullptr;   // row kernel: also store (q + eta, u, v) [3][layer][j][nx] (adjoint recompute)
   const TmaMaps* tma = nullptr;  // host copy of the context's tensor maps (null: no TMA column stage)
   int* derr = nullptr;           // device error flag (a TMA wait that ran out of time sets it)
+  const void* twx = nullptr;     // generic-length path: exp(-2 pi i k / nx), k < nx
+  const void* twy = nullptr;     //                      exp(-2 pi i k / ny), k < ny
 };
 
 // Arguments of the adjoint kernels (gf_adjoint.cuh).
@@ -149,6 +158,16 @@ struct AdjArgs {
 
 // Generic transforms (updatevars!, set_*!, fwdtransform!/invtransform!).
 enum SpecField { SF_X = 0, SF_PSI = 1, SF_U = 2, SF_V = 3, SF_UY = 4, SF_RAW = 5, SF_DX = 6, SF_DY = 7 };
+
+// generic-length launchers (gf_rt.cu), used by the dispatchers when Geom::rtx / rty is set
+template <class T> cudaError_t launch_row_rt(const Geom&, const ModArgs&, const Bufs&, cudaStream_t);
+template <class T> cudaError_t launch_col_rt(const Geom&, const ModArgs&, const StepArgs&, const Bufs&, cudaStream_t);
+template <class T> cudaError_t launch_col_inv_rt(const Geom&, const ModArgs&, const void* src, int kind, int mask,
+                                                 const Bufs&, cudaStream_t);
+template <class T> cudaError_t launch_row_c2r_rt(const Geom&, const Bufs&, int nf, void* out, cudaStream_t);
+template <class T> cudaError_t launch_row_r2c_rt(const Geom&, const Bufs&, int nf, const void* in, cudaStream_t);
+template <class T> cudaError_t launch_col_fwd_rt(const Geom&, const Bufs&, int nf, void* out, int zero_mean,
+                                                 cudaStream_t);
 
 template <class T> cudaError_t launch_row(const Geom&, const ModArgs&, const Bufs&, cudaStream_t);
 template <class T> cudaError_t launch_col(const Geom&, const ModArgs&, const StepArgs&, const Bufs&, cudaStream_t);

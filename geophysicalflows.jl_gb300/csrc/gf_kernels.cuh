@@ -670,6 +670,50 @@ __device__ __forceinline__ void unpack_store(const cplx<T>* buf, int k, int NX, 
   Pb[k] = mk<T>(T(0.5) * (z.y + w.y), T(0.5) * (w.x - z.x));
 }
 
+// Physical-space products at column x of the packed row pair (j0, j0 + 1) of layer L (row
+// j0 in the real parts, j0 + 1 in the imaginary parts), from the inverse fields (q, u, v):
+// A = (U + u) q' (U q' when linear), B = v q', C = (U + u) Qx + v Qy (when m.hasC), with
+// q' = q + eta; BarotropicQGQL: (U z' + u' Z, v' Z, v' z') from the zonal means of W.
+// Up / Qyp: the pair's U(y) and Qy(y) values.  Row length NX; also stores (q', U + u, v) for
+// the adjoint when b.phys is set.
+template <class T>
+__device__ __forceinline__ void pair_products(const Geom& g, const ModArgs& m, const Bufs& b, const cplx<T>* W, int L,
+                                              int j0, int x, int NX, cplx<T> Up, cplx<T> Qyp, bool last, cplx<T> q,
+                                              cplx<T> u, cplx<T> v, cplx<T>& A, cplx<T>& Bv, cplx<T>& Cv) {
+  const int nl = g.nl;
+  const T* eta = static_cast<const T*>(m.eta);
+  const T* Qx2D = static_cast<const T*>(m.Qx2D);
+  const T* Qy2D = static_cast<const T*>(m.Qy2D);
+  u = u + Up;
+  if (eta) q = q + mk<T>(eta[(size_t)j0 * NX + x], eta[(size_t)(j0 + 1) * NX + x]);
+  if (b.phys) {  // forward fields (q + eta, u, v) of this stage, kept for the adjoint
+    T* ph = static_cast<T*>(b.phys) + (size_t)L * g.ny * NX;
+    const size_t ia = (size_t)j0 * NX + x, fs = (size_t)nl * g.ny * NX;
+    ph[ia] = q.x; ph[ia + NX] = q.y;
+    ph[fs + ia] = u.x; ph[fs + ia + NX] = u.y;
+    ph[2 * fs + ia] = v.x; ph[2 * fs + ia + NX] = v.y;
+  }
+  const cplx<T> au = m.linear ? Up : u;
+  A = mk<T>(au.x * q.x, au.y * q.y);
+  Bv = mk<T>(v.x * q.x, v.y * q.y);
+  Cv = czero<T>();
+  if (m.ql) {
+    // zonal means Z, U of the two rows (x-constant: the kr = 0 inverse values) and eddies
+    const cplx<T> Z = mk<T>(W[(size_t)j0 * g.ldw].x, W[(size_t)(j0 + 1) * g.ldw].x);
+    const cplx<T>* Wu = W + (size_t)nl * g.ny * g.ldw;
+    const cplx<T> Um = mk<T>(Wu[(size_t)j0 * g.ldw].x, Wu[(size_t)(j0 + 1) * g.ldw].x);
+    const cplx<T> ze = q - Z, ue = u - Um;
+    A = mk<T>(Um.x * ze.x + ue.x * Z.x, Um.y * ze.y + ue.y * Z.y);   // U z' + u' Z
+    Bv = mk<T>(v.x * Z.x, v.y * Z.y);                                 // v' Z
+    Cv = mk<T>(v.x * ze.x, v.y * ze.y);                               // v' z'
+  } else if (m.hasC) {
+    cplx<T> Qy = Qyp, Qx = czero<T>();
+    if (last && Qy2D) Qy = Qy + mk<T>(Qy2D[(size_t)j0 * NX + x], Qy2D[(size_t)(j0 + 1) * NX + x]);
+    if (last && Qx2D) Qx = mk<T>(Qx2D[(size_t)j0 * NX + x], Qx2D[(size_t)(j0 + 1) * NX + x]);
+    Cv = mk<T>(u.x * Qx.x + v.x * Qy.x, u.y * Qx.y + v.y * Qy.y);
+  }
+}
+
 // TWO: products (u q', v q') only, in two buffers per row pair -- q, then u with the first
 // product, then v with the second, one c2r and one r2c call site -- so that three df64 blocks
 // (80 registers, 64 KB at 2048) fit on an SM instead of two.
@@ -763,36 +807,9 @@ __global__ void __launch_bounds__(256, TWO ? 3 : sizeof(T) == 4 ? GF_ROW_MINBLOC
     for (int i = 0; i < R; ++i) {
       const int x = t + i * TPF;
       const int px = swz<T>(x);
-      cplx<T> q = buf[px], u = buf[PS + px], v = buf[2 * PS + px];
-      const cplx<T> Up = mk<T>(Ua, Ub);
-      u = u + Up;
-      if (eta) q = q + mk<T>(eta[(size_t)j0 * NX + x], eta[(size_t)(j0 + 1) * NX + x]);
-      if (b.phys) {  // forward fields (q + eta, u, v) of this stage, kept for the adjoint
-        T* ph = static_cast<T*>(b.phys) + (size_t)L * g.ny * NX;
-        const size_t ia = (size_t)j0 * NX + x, fs = (size_t)nl * g.ny * NX;
-        ph[ia] = q.x; ph[ia + NX] = q.y;
-        ph[fs + ia] = u.x; ph[fs + ia + NX] = u.y;
-        ph[2 * fs + ia] = v.x; ph[2 * fs + ia + NX] = v.y;
-      }
-      const cplx<T> au = m.linear ? Up : u;
-      cplx<T> A = mk<T>(au.x * q.x, au.y * q.y);
-      cplx<T> Bv = mk<T>(v.x * q.x, v.y * q.y);
-      cplx<T> Cv = czero<T>();
-      if (m.ql) {
-        // zonal means Z, U of the two rows (x-constant: the kr = 0 inverse values) and eddies
-        const cplx<T> Z = mk<T>(W[(size_t)j0 * g.ldw].x, W[(size_t)(j0 + 1) * g.ldw].x);
-        const cplx<T>* Wu = W + (size_t)nl * g.ny * g.ldw;
-        const cplx<T> Um = mk<T>(Wu[(size_t)j0 * g.ldw].x, Wu[(size_t)(j0 + 1) * g.ldw].x);
-        const cplx<T> ze = q - Z, ue = u - Um;
-        A = mk<T>(Um.x * ze.x + ue.x * Z.x, Um.y * ze.y + ue.y * Z.y);   // U z' + u' Z
-        Bv = mk<T>(v.x * Z.x, v.y * Z.y);                                 // v' Z
-        Cv = mk<T>(v.x * ze.x, v.y * ze.y);                               // v' z'
-      } else if (m.hasC) {
-        cplx<T> Qy = mk<T>(Qa, Qb), Qx = czero<T>();
-        if (last && Qy2D) Qy = Qy + mk<T>(Qy2D[(size_t)j0 * NX + x], Qy2D[(size_t)(j0 + 1) * NX + x]);
-        if (last && Qx2D) Qx = mk<T>(Qx2D[(size_t)j0 * NX + x], Qx2D[(size_t)(j0 + 1) * NX + x]);
-        Cv = mk<T>(u.x * Qx.x + v.x * Qy.x, u.y * Qx.y + v.y * Qy.y);
-      }
+      cplx<T> A, Bv, Cv;
+      pair_products<T>(g, m, b, W, L, j0, x, NX, mk<T>(Ua, Ub), mk<T>(Qa, Qb), last, buf[px], buf[PS + px],
+                       buf[2 * PS + px], A, Bv, Cv);
       buf[px] = A;
       if (m.hasB) { buf[PS + px] = Bv; if (m.hasC) buf[2 * PS + px] = Cv; }
       else buf[PS + px] = Cv;
@@ -814,6 +831,29 @@ __global__ void __launch_bounds__(256, TWO ? 3 : sizeof(T) == 4 ? GF_ROW_MINBLOC
 }
 
 // ------------------------------------------------------------------ generic transforms
+// Spectral field `kind` of layer L at (kr, j) from the layer values S (instance base, [layer]
+// [j][ldk]): X, psi, u, v, du/dy, d/dx, d/dy or the raw array; `mask`: dealias X first.
+template <class T>
+__device__ __forceinline__ cplx<T> spec_field_value(const Geom& g, const ModArgs& m, const cplx<T>* S, int kind,
+                                                    int mask, int kr, int j, int L, T krT, T dky) {
+  const int nl = g.nl;
+  const size_t lstride = (size_t)g.ny * g.ldk;
+  const size_t ti = (size_t)j * g.ldk + kr;
+  cplx<T> X[MAXL], ps[MAXL];
+  for (int a = 0; a < nl; ++a) X[a] = S[a * lstride + ti];
+  if (mask && !kept(g, kr, j)) for (int a = 0; a < nl; ++a) X[a] = czero<T>();
+  const T lv = T(lidx(g, j)) * dky;
+  if (kind == SF_X || kind == SF_RAW) return X[L];
+  if (kind == SF_DX) return krT * mul_i(X[L]);
+  if (kind == SF_DY) return lv * mul_i(X[L]);
+  psi_all<T>(m, nl, krT * krT + lv * lv, X, ps, ti);
+  const cplx<T> p = ps[L];
+  if (kind == SF_PSI) return p;
+  if (kind == SF_U) return lv * mul_mi(p);   // u = -i l psi
+  if (kind == SF_V) return krT * mul_i(p);   // v =  i kr psi
+  return (lv * lv) * p;                      // du/dy = i l u = l^2 psi
+}
+
 // y-direction inverse FFT of a derived spectral field of every layer into W (full kr
 // range, row stride ldk): kind selects X, psi, u, v, du/dy, d/dx, d/dy or the raw array.
 template <class T, int NY, int R>
@@ -839,29 +879,7 @@ __global__ void __launch_bounds__(512) col_inv_generic(Geom g, ModArgs m, const 
 #pragma unroll
     for (int i = 0; i < R; ++i) {
       const int j = t + i * TPF;
-      cplx<T> v = czero<T>();
-      if (kin) {
-        const size_t ti = (size_t)j * g.ldk + kr;
-        cplx<T> X[MAXL], ps[MAXL];
-        for (int a = 0; a < nl; ++a) X[a] = S[a * lstride + ti];
-        if (mask && !kept(g, kr, j)) for (int a = 0; a < nl; ++a) X[a] = czero<T>();
-        const T lv = T(lidx(g, j)) * dky;
-        if (kind == SF_X || kind == SF_RAW) {
-          v = X[L];
-        } else if (kind == SF_DX) {
-          v = krT * mul_i(X[L]);
-        } else if (kind == SF_DY) {
-          v = lv * mul_i(X[L]);
-        } else {
-          psi_all<T>(m, nl, krT * krT + lv * lv, X, ps, ti);
-          const cplx<T> p = ps[L];
-          if (kind == SF_PSI) v = p;
-          else if (kind == SF_U) v = lv * mul_mi(p);   // u = -i l psi
-          else if (kind == SF_V) v = krT * mul_i(p);   // v =  i kr psi
-          else v = (lv * lv) * p;                     // du/dy = i l u = l^2 psi
-        }
-      }
-      Fc[swz<T>(j)] = sc * v;
+      Fc[swz<T>(j)] = sc * (kin ? spec_field_value<T>(g, m, S, kind, mask, kr, j, L, krT, dky) : czero<T>());
     }
     __syncthreads();
     fft_smem<T, NY, R, +1>(F + cf * cs, tf, tw);

@@ -14,7 +14,13 @@
  *   `where` = GF_HOST (pageable or pinned host memory) or GF_DEVICE (device pointer on the
  *   context's GPU, e.g. from a CuArray).
  * One context = one problem on one stream; a context is not thread-safe, separate
- * contexts are independent.  nx and ny must be powers of two in [32, 2048].
+ * contexts are independent.
+ * Grid sizes: nx and ny even, at least 4, with no prime factor above 61 and at most 4096
+ * (GF_F32) or 2048 (GF_F64, GF_DF64) -- the sizes FourierFlows' TwoDGrid accepts in practice,
+ * e.g. the reference tests' 128 x 126, 64 x 66, 32 x 34 and 16 x 16 (FourierFlows also takes
+ * odd sizes and larger primes; those return GF_ERR_UNSUPPORTED here).  The powers of two 32
+ * ... 2048 run compiled-in FFT lengths (fastest; the TMA column stage, the autotuner and the
+ * adjoint need them); every other length runs a mixed-radix FFT over a run-time radix plan.
  */
 #ifndef GFCUDA_H
 #define GFCUDA_H

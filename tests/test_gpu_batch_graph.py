@@ -131,7 +131,8 @@ def test_autotune_keeps_state_and_results(T, stepper):
     shape = p.autotune(reps=2)
     assert np.array_equal(p.sol, sol0) and p.clock.step == 5
     assert shape["col_radix"] in ((4, 8, 16) if T == np.float32 else (8,))
-    assert p.launch_shape == tuple(shape.values())
+    assert p.launch_shape == tuple(shape[k] for k in ("row_radix", "row_pairs", "col_radix", "col_columns"))
+    assert p.tma_columns == shape["tma_columns"]
     stepforward(p, 6)
     stepforward(q, 6)
     assert rel(p.sol, q.sol) <= (1e-5 if T == np.float32 else 1e-13)

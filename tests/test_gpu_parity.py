@@ -120,7 +120,8 @@ def test_twodns_decaying_128_parity_100_steps():
 
 # ------------------------------------------------------------------------------ reference known answers via GPU
 def test_twodns_energy_enstrophy_palinstrophy_gpu():
-    """test/test_twodnavierstokes.jl:259-317 (ny=128 instead of 126: powers of two only)"""
+    """test/test_twodnavierstokes.jl:259-317 on a square 128 grid (the reference's 128 x 126 grid runs
+    in test_gpu_generic_sizes.py)"""
     nx, Lx, ny, Ly = 128, 2 * np.pi, 128, 3 * np.pi
     p = TD.Problem("GPU", nx=nx, Lx=Lx, ny=ny, Ly=Ly, stepper="ForwardEuler")
     x, y = p.grid.gridpoints()
@@ -271,7 +272,8 @@ def test_slqg_energies_gpu():
 
 # ------------------------------------------------------------------------------ MultiLayerQG
 def test_mlqg_pv_inversion_and_energies_gpu():
-    """test/test_multilayerqg.jl:166-212 and :502-536 (ny=64 instead of 66)"""
+    """test/test_multilayerqg.jl:166-212 and :502-536 on square grids (the reference's 64 x 66 grid
+    runs in test_gpu_generic_sizes.py)"""
     import test_oracle_reference as T
     p = ML.Problem(3, "GPU", nx=128, f0=1, H=[0.25, 0.25, 0.5], b=[-1.0, -1.2, -1.2 - 1 / 6])
     psi, q = T.fields_3layer(O.Grid(128))
@@ -291,7 +293,8 @@ def test_mlqg_pv_inversion_and_energies_gpu():
 
 @pytest.mark.parametrize("nlayers,linear", [(2, False), (3, False), (2, True)])
 def test_mlqg_advection_manufactured_gpu(nlayers, linear):
-    """test/test_multilayerqg.jl:225-494 (ny=64 instead of 66) through the GPU path"""
+    """test/test_multilayerqg.jl:225-494 through the GPU path on a 64 x 64 grid (the reference's
+    64 x 66 grid runs in test_gpu_generic_sizes.py)"""
     import test_oracle_reference as T
     captured = {}
     orig = O.MultiLayerQG
