@@ -59,7 +59,8 @@ def _cfg(**kw):
 
 
 @pytest.mark.parametrize("kw,code", [
-    (dict(nx=100), -2), (dict(nx=4096), -2), (dict(stepper=9), -1), (dict(module=7), -1),
+    (dict(nx=101), -2), (dict(nx=2 * 67), -2), (dict(ny=2), -2), (dict(nx=4096), -2), (dict(nx=8192, precision=0), -2),
+    (dict(stepper=9), -1), (dict(module=7), -1),
     (dict(dt=0.0), -1), (dict(aliased_fraction=1.0), -1), (dict(precision=5), -1),
     (dict(module=2, nlayers=9), -2), (dict(module=0, nlayers=2), -1), (dict(forcing_kind=9), -1),
 ])
