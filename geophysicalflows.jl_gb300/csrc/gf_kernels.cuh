@@ -103,6 +103,23 @@ __device__ __forceinline__ void psi_eigen(int nl, const T* e, T K2, const cplx<T
   }
 }
 
+// Row L of the same inversion: psi_L = sum_q V[L][q] / (lam_q - K^2) sum_r Vinv[q][r] X_r, with
+// the layer values from Xat(r) (zero at K = 0); the same operations in the same order as
+// psi_eigen, without per-layer arrays.
+template <class T, class F>
+__device__ __forceinline__ cplx<T> psi_eigen_row(int nl, const T* e, T K2, int L, F&& Xat) {
+  cplx<T> p = czero<T>();
+  if (K2 == T(0)) return p;
+  const T* V = e + MAXL;
+  const T* Vi = e + MAXL + MAXL * MAXL;
+  for (int q = 0; q < nl; ++q) {
+    cplx<T> s = czero<T>();
+    for (int r = 0; r < nl; ++r) s = s + Vi[q * MAXL + r] * Xat(r);
+    p = p + V[L * MAXL + q] * ((T(1) / (e[q] - K2)) * s);
+  }
+  return p;
+}
+
 // psi for all layers (any module) -- used outside the hot kernels, constants read from m
 template <class T>
 __device__ __forceinline__ void psi_all(const ModArgs& m, int nl, T K2, const cplx<T>* X, cplx<T>* psi, size_t ti) {
@@ -599,20 +616,11 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : MAXT < 512 ? 3 : sizeof
         const T lv = T(lidx(g, j)) * dky;
         const T K2 = krT * krT + lv * lv;
         const size_t ti = (size_t)j * g.ldk + (kin ? kr : 0);
-        cplx<T> p;
-        if (nl > 1) {
-          cplx<T> X[MAXL], ps[MAXL];
-          for (int a = 0; a < nl; ++a) X[a] = Xat(a);
-          if (m.psi_kind == PSI_EIGEN) {
-            psi_eigen<T>(nl, eig, K2, X, ps);
-          } else {
-            const T fk = psi_factor<T>(m.psi_kind, K2, ell2, m.mult, ti);
-            for (int a = 0; a < nl; ++a) ps[a] = fk * X[a];
-          }
-          p = ps[L];
-        } else {
-          p = psi_factor<T>(m.psi_kind, K2, ell2, m.mult, ti) * x;
-        }
+        // psi of layer L only (one row of the inversion, no per-layer arrays: arrays indexed
+        // by the run-time layer count would live in local memory)
+        const cplx<T> p = (nl > 1 && m.psi_kind == PSI_EIGEN)
+                              ? psi_eigen_row<T>(nl, eig, K2, L, Xat)
+                              : psi_factor<T>(m.psi_kind, K2, ell2, m.mult, ti) * x;
         if (m.drag && kin && L == nl - 1) Dp[ti] = (muT * K2) * p;
         F0[c * cs + swz<T>(j)] = sc * x;
         F1[c * cs + swz<T>(j)] = sc * (lv * mul_mi(p));   // u = -i l psi
