@@ -104,6 +104,10 @@ struct gf_ctx {
   cudaGraphExec_t egraph[2] = {nullptr, nullptr};      // ensemble graphs held by the first member (as gexec)
   std::vector<std::pair<uint64_t, uint64_t>> emembers;  // (uid, gen) of its members
   int eG = 0;
+  // ensemble execution when this context leads gf_ensemble_step: 1 the persistent ensemble
+  // kernels where the members allow them, 0 (default, faster on the benchmark ensemble) one
+  // batched context per stream; eMode: the execution the held ensemble graphs were captured with
+  int ens_mode = 0, eMode = -1;
   cudaEvent_t order_ev = nullptr;  // orders this context's stream with an ensemble graph launch
   std::string err;
 };
@@ -1523,8 +1527,78 @@ extern "C" int gf_step_callback(gf_ctx* c, int64_t nsteps, gf_forcing_fn fn, voi
 // G steps of all of them are captured as ONE graph on the first context's stream -- the
 // other contexts' streams fork from it and join back, so their kernels run concurrently --
 // and replayed with one launch; otherwise each context steps on its own stream.
+// Whether the members can step through the persistent ensemble kernels: at most ENS_MAXCLS
+// contexts of one precision and stage count, each one layer without bottom drag on a square
+// grid of 32, 64, 128 or 256 points, no AB3 (its buffer ring rotates per context).
+static bool ens_fusable(gf_ctx* const* ctxs, int32_t n) {
+  if (n < 1 || n > ENS_MAXCLS || ctxs[0]->ens_mode != 1) return false;
+  for (int32_t i = 0; i < n; ++i) {
+    const gf_ctx* c = ctxs[i];
+    if (c->prec != ctxs[0]->prec || c->nstages != ctxs[0]->nstages || c->kind == SK_AB3 || c->g.nl != 1 ||
+        c->m.drag || c->g.nx != c->g.ny || !ens_size_ok(c->g.nx) || c->g.rtx || c->g.rty || c->profiling)
+      return false;
+  }
+  return true;
+}
+
+static size_t ens_cs(const gf_ctx* c, int n) {
+  return c->prec == GF_F32 ? ens_col_stride<float>(n) : c->prec == GF_F64 ? ens_col_stride<double>(n)
+                                                                          : ens_col_stride<df64>(n);
+}
+
+// G steps of every member with one persistent row launch and one persistent column launch per
+// stage on the first member's stream (inside a capture), then the members' clock advances.
+// Steps k >= G - 1 of a replay that ends the call are observed (every column and mode).
+static int enqueue_ens_steps(gf_ctx* const* ctxs, int32_t n, int G, int obs) {
+  gf_ctx* o = ctxs[0];
+  const int nst = o->nstages;
+  for (int k = 0; k < G; ++k) {
+    for (int stg = 1; stg <= nst; ++stg) {
+      EnsArgs ra{}, ca{};
+      ra.ncls = ca.ncls = n;
+      for (int32_t i = 0; i < n; ++i) {
+        gf_ctx* c = ctxs[i];
+        const bool observed = obs && k >= G - observed_tail(c);
+        Geom g = c->g;
+        if (!observed && g.kcut < g.nkr) g.kout = g.kcut;
+        const double dt = c->cfg.dt;
+        const double ts = c->t + (nst == 4 ? (stg == 1 ? 0.0 : stg == 4 ? dt : 0.5 * dt) : 0.0);
+        StepArgs s = stage_args(c, stg, ts);
+        s.clk = c->dclk;
+        const int per = ens_per_block(g.nx);
+        EnsClass& r = ra.c[i];
+        r.g = g; r.m = c->m; r.s = s; r.b = bufs(c); r.n = g.nx; r.per = per;
+        r.nbx = (g.ny / 2) / per; r.nby = g.nb;
+        EnsClass& q = ca.c[i];
+        q = r;
+        q.g.cs = (int)ens_cs(c, g.ny);
+        q.nbx = ((g.kout > 0 ? g.kout : g.nkr) + per - 1) / per;
+        ra.total += r.nbx * r.nby;
+        ca.total += q.nbx * q.nby;
+      }
+      GF_CUDA(o, DISPATCH(o, launch_ens_row, ra, o->stream));
+      GF_CUDA(o, DISPATCH(o, launch_ens_col, ca, o->stream));
+    }
+    for (int32_t i = 0; i < n; ++i) {
+      gf_ctx* c = ctxs[i];
+      advance_clock_kernel<<<1, 32, 0, o->stream>>>(c->dclk, c->cfg.dt, c->cfg.forcing_omega, c->cfg.forcing_phase,
+                                                    c->cfg.forcing_kind == GF_FORCING_HARMONIC, c->nstages);
+      GF_CUDA(o, cudaGetLastError());
+      host_advance(c);
+    }
+  }
+  return GF_OK;
+}
+
+extern "C" int gf_set_ensemble_mode(gf_ctx* c, int32_t mode) {
+  if (!c || (mode != 0 && mode != 1)) return GF_ERR_ARG;
+  c->ens_mode = mode;
+  return GF_OK;
+}
+
 static int ensemble_capture(gf_ctx* const* ctxs, int32_t n, int G, int obs) {
   gf_ctx* o = ctxs[0];
+  const bool fused = ens_fusable(ctxs, n);
   std::vector<cudaEvent_t> ev;
   auto cleanup = [&]() { for (auto e : ev) cudaEventDestroy(e); };
   for (int32_t i = 0; i < 2 * n; ++i) {
@@ -1538,16 +1612,20 @@ static int ensemble_capture(gf_ctx* const* ctxs, int32_t n, int G, int obs) {
   cudaError_t e = cudaStreamBeginCapture(o->stream, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) { cleanup(); return fail(o, GF_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e)); }
   int rc = GF_OK;
-  cudaEventRecord(ev[0], o->stream);
-  for (int32_t i = 1; i < n; ++i) cudaStreamWaitEvent(ctxs[i]->stream, ev[0], 0);   // fork
-  for (int32_t i = 0; i < n && rc == GF_OK; ++i)
-    for (int k = 0; k < G && rc == GF_OK; ++k) {
-      rc = enqueue_step(ctxs[i], obs && k >= G - observed_tail(ctxs[i]));
-      host_advance(ctxs[i]);
+  if (fused) {
+    rc = enqueue_ens_steps(ctxs, n, G, obs);
+  } else {
+    cudaEventRecord(ev[0], o->stream);
+    for (int32_t i = 1; i < n; ++i) cudaStreamWaitEvent(ctxs[i]->stream, ev[0], 0);   // fork
+    for (int32_t i = 0; i < n && rc == GF_OK; ++i)
+      for (int k = 0; k < G && rc == GF_OK; ++k) {
+        rc = enqueue_step(ctxs[i], obs && k >= G - observed_tail(ctxs[i]));
+        host_advance(ctxs[i]);
+      }
+    for (int32_t i = 1; i < n; ++i) {                                                 // join
+      cudaEventRecord(ev[n + i], ctxs[i]->stream);
+      cudaStreamWaitEvent(o->stream, ev[n + i], 0);
     }
-  for (int32_t i = 1; i < n; ++i) {                                                 // join
-    cudaEventRecord(ev[n + i], ctxs[i]->stream);
-    cudaStreamWaitEvent(o->stream, ev[n + i], 0);
   }
   cudaGraph_t graph = nullptr;
   e = cudaStreamEndCapture(o->stream, &graph);
@@ -1557,8 +1635,8 @@ static int ensemble_capture(gf_ctx* const* ctxs, int32_t n, int G, int obs) {
   cleanup();
   if (rc != GF_OK) { if (graph) cudaGraphDestroy(graph); return rc; }
   if (e != cudaSuccess) return fail(o, GF_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-  // a new membership or graph length invalidates both kinds
-  bool same = o->eG == G && (int32_t)o->emembers.size() == n;
+  // a new membership, graph length or execution invalidates both kinds
+  bool same = o->eG == G && o->eMode == (int)fused && (int32_t)o->emembers.size() == n;
   for (int32_t i = 0; same && i < n; ++i)
     same = o->emembers[i].first == ctxs[i]->uid && o->emembers[i].second == ctxs[i]->gen;
   if (!same) drop_ensemble_graphs(o);
@@ -1569,6 +1647,7 @@ static int ensemble_capture(gf_ctx* const* ctxs, int32_t n, int G, int obs) {
   o->emembers.clear();
   for (int32_t i = 0; i < n; ++i) o->emembers.push_back({ctxs[i]->uid, ctxs[i]->gen});
   o->eG = G;
+  o->eMode = (int)fused;
   return GF_OK;
 }
 
@@ -1590,7 +1669,8 @@ extern "C" int gf_ensemble_step(gf_ctx* const* ctxs, int32_t n, int64_t nsteps) 
     for (int32_t i = 0; i < n; ++i)
       if (int r = ensure_W(ctxs[i])) { g_create_error = ctxs[i]->err; return r; }
     const int obs = nsteps - G < 1;  // the replay holds the call's last step
-    bool same = o->egraph[obs] && o->eG == G && (int32_t)o->emembers.size() == n;
+    bool same = o->egraph[obs] && o->eG == G && o->eMode == (int)ens_fusable(ctxs, n) &&
+                (int32_t)o->emembers.size() == n;
     for (int32_t i = 0; same && i < n; ++i)
       same = o->emembers[i].first == ctxs[i]->uid && o->emembers[i].second == ctxs[i]->gen;
     if (!same)

@@ -159,6 +159,31 @@ struct AdjArgs {
 // Generic transforms (updatevars!, set_*!, fwdtransform!/invtransform!).
 enum SpecField { SF_X = 0, SF_PSI = 1, SF_U = 2, SF_V = 3, SF_UY = 4, SF_RAW = 5, SF_DX = 6, SF_DY = 7 };
 
+// Persistent ensemble launch (gf_ens.cu): one row launch and one column launch per stage for
+// several size classes (contexts) at once; each block walks the work list of every class's
+// tiles (class, instance, row-pair block or column block).  Square classes of 32, 64, 128 or
+// 256 points, one layer, no bottom drag.
+constexpr int ENS_MAXCLS = 4;
+constexpr int ENS_THREADS = 128;
+struct EnsClass {
+  Geom g;
+  ModArgs m;
+  StepArgs s;   // column launches
+  Bufs b;
+  int n;        // FFT length (nx = ny)
+  int per;      // row pairs (row launch) or columns (column launch) per block
+  int nbx, nby; // blocks per instance, instances
+};
+struct EnsArgs {
+  int ncls, total;  // classes, work items (sum of nbx * nby)
+  EnsClass c[ENS_MAXCLS];
+};
+bool ens_size_ok(int n);
+int ens_per_block(int n);  // row pairs and columns per block of ENS_THREADS threads
+template <class T> cudaError_t launch_ens_row(const EnsArgs&, cudaStream_t);
+template <class T> cudaError_t launch_ens_col(const EnsArgs&, cudaStream_t);
+template <class T> size_t ens_col_stride(int n);
+
 // generic-length launchers (gf_rt.cu), used by the dispatchers when Geom::rtx / rty is set
 template <class T> cudaError_t launch_row_rt(const Geom&, const ModArgs&, const Bufs&, cudaStream_t);
 template <class T> cudaError_t launch_col_rt(const Geom&, const ModArgs&, const StepArgs&, const Bufs&, cudaStream_t);

@@ -307,11 +307,14 @@ __device__ __forceinline__ EpiCtx<T> epi_ctx(const Geom& g, const ModArgs& m, co
 // FP32 variant for five radix-16 columns of 2048 (or radix-8 columns of 1024) per block, 256
 // the narrow FP64 / df64 variant (one radix-8 column of 2048, three blocks per SM); both run
 // the one-layer path only, with the two-buffer inverse pass.
-template <class T, int NY, int R, int MAXT = 512>
-__global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : MAXT < 512 ? 3 : sizeof(T) == 4 ? (NY >= 1024 ? GF_MINBLOCKS_F32 : GF_MINBLOCKS_SMALL_F32) : GF_MINBLOCKS_WIDE_COL)
-    col_stage_kernel(Geom g, ModArgs m, StepArgs s, Bufs b, int C) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ T eig[MAXL + 2 * MAXL * MAXL];
+// The column kernel's work for block (bx, by, bz) -- column block, instance, layer -- with
+// its shared memory; shared by col_stage_kernel and the persistent ensemble kernel.
+template <class T, int NY, int R, int MAXT = 512, bool ENS = false>
+__device__ __forceinline__ void col_stage_body(const Geom& g, const ModArgs& m, const StepArgs& s, const Bufs& b, int C,
+                                               int ens_bx, int ens_by, unsigned char* smem_raw, T* eig) {
+  // ENS: the block index comes from (ens_bx, ens_by) (persistent ensemble launch, one layer)
+  const int bx = ENS ? ens_bx : (int)blockIdx.x, by = ENS ? ens_by : (int)blockIdx.y;
+  const int bz = ENS ? 0 : (int)blockIdx.z;
   constexpr int TPF = NY / R;
   const int cs = g.cs;
   const int nl = g.nl;
@@ -321,7 +324,7 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : MAXT < 512 ? 3 : sizeof
   cplx<T>* Xs = F2 + C * cs;  // the general path's N / next-X of every layer
   const int tid = threadIdx.x, c = tid % C, t = tid / C;
   const int cf = tid / TPF, tf = tid % TPF;
-  const int kr = blockIdx.x * C + c;
+  const int kr = bx * C + c;
   // unobserved step (kout set): the products exist only for kr < kout = kcut, and the state is
   // updated only at kept modes -- the aliased modes of the state are zeroed by the next
   // stage's dealias before anything reads them, so the step's kept modes (and every later
@@ -330,7 +333,7 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : MAXT < 512 ? 3 : sizeof
   const bool kin = kr < (prune ? g.kout : g.nkr);
   const cplx<T>* tw = static_cast<const cplx<T>*>(b.twid);
   const size_t lstride = (size_t)g.ny * g.ldk;
-  const size_t ib = blockIdx.y;                          // ensemble instance
+  const size_t ib = by;                          // ensemble instance
   const size_t ioff = ib * g.bs_spec;                    // its state arrays
   cplx<T>* Dp = m.D ? static_cast<cplx<T>*>(m.D) + ib * g.bs_d : nullptr;
   const T dky = sel<T>(g.dky, g.dky_f, g.dky_l), krT = T(kr) * sel<T>(g.dkx, g.dkx_f, g.dkx_l);
@@ -427,7 +430,7 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : MAXT < 512 ? 3 : sizeof
       }
     }
     if (!s.do_inv) return;
-    if ((int)blockIdx.x * C >= g.kcut) return;  // whole block aliased: W is never read there
+    if ((int)bx * C >= g.kcut) return;  // whole block aliased: W is never read there
     if constexpr (MAXT != 512) {
       // the wide and narrow instantiations, two buffers: q (F0) and u (F1) filled, then the
       // inverse FFTs of q, u and -- filled into F0 once q is stored, psi formed again from
@@ -499,12 +502,12 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : MAXT < 512 ? 3 : sizeof
     // FFTs in lockstep, N and the stage epilogue; then per layer the inverse FFTs of (q, u, v)
     // in lockstep.
     // Layer split (several layers, s.layer_split): one block per (column block, layer L =
-    // blockIdx.z) and two launches per stage -- the forward launch writes the next stage's X
+    // bz) and two launches per stage -- the forward launch writes the next stage's X
     // of its layer to s.Xg; the inverse launch (do_fwd = 0, s.sol = s.Xg) reads the X of
     // every layer at each element from there for the PV inversion of its layer.  Three times
     // the blocks, and no Xs in shared memory.
     const bool split = s.layer_split;
-    const int L0 = split ? (int)blockIdx.z : 0, L1 = split ? L0 + 1 : nl;
+    const int L0 = split ? bz : 0, L1 = split ? L0 + 1 : nl;
     if (s.do_fwd) {
       const cplx<T>* P = static_cast<const cplx<T>*>(b.P) + ib * g.bs_p;
       const int nslot = 1 + m.hasB + m.hasC;
@@ -577,7 +580,7 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : MAXT < 512 ? 3 : sizeof
       }
     }
     if (!s.do_inv) return;
-    if ((int)blockIdx.x * C >= g.kcut) return;  // whole block aliased: W is never read there
+    if ((int)bx * C >= g.kcut) return;  // whole block aliased: W is never read there
     __syncthreads();  // eig[] filled
 
     // y-direction inverse FFTs of (q, u, v) of every layer, in lockstep; psi of layer L from
@@ -645,6 +648,15 @@ __global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : MAXT < 512 ? 3 : sizeof
   }
 }
 
+
+template <class T, int NY, int R, int MAXT = 512>
+__global__ void __launch_bounds__(MAXT, MAXT > 512 ? 1 : MAXT < 512 ? 3 : sizeof(T) == 4 ? (NY >= 1024 ? GF_MINBLOCKS_F32 : GF_MINBLOCKS_SMALL_F32) : GF_MINBLOCKS_WIDE_COL)
+    col_stage_kernel(const __grid_constant__ Geom g, const __grid_constant__ ModArgs m,
+                     const __grid_constant__ StepArgs s, const __grid_constant__ Bufs b, int C) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ T eig[MAXL + 2 * MAXL * MAXL];
+  col_stage_body<T, NY, R, MAXT>(g, m, s, b, C, 0, 0, smem_raw, eig);
+}
 
 // --------------------------------------------------------------------------- row kernel
 // Slots per row-pair buffer: NX, staggered by TPF when several pairs share a wavefront.
@@ -725,117 +737,28 @@ __device__ __forceinline__ void pair_products(const Geom& g, const ModArgs& m, c
 // TWO: products (u q', v q') only, in two buffers per row pair -- q, then u with the first
 // product, then v with the second, one c2r and one r2c call site -- so that three df64 blocks
 // (80 registers, 64 KB at 2048) fit on an SM instead of two.
+// The row kernel's work for block (ens_bx, ens_by) -- row-pair block, instance -- of the
+// persistent ensemble launch (its arguments through references); row_nl_kernel below runs the
+// same source (gf_row_body.inc) with its own arguments and blockIdx.
+template <class T, int NX, int R, bool TWO = false>
+__device__ __forceinline__ void row_nl_body(const Geom& g, const ModArgs& m, const Bufs& b, int B, unsigned ens_bx,
+                                            unsigned ens_by, unsigned char* smem_raw) {
+#define GF_ROW_BX ens_bx
+#define GF_ROW_BY ens_by
+#include "gf_row_body.inc"
+#undef GF_ROW_BX
+#undef GF_ROW_BY
+}
+
 template <class T, int NX, int R, bool TWO = false>
 __global__ void __launch_bounds__(256, TWO ? 3 : sizeof(T) == 4 ? GF_ROW_MINBLOCKS_F32 : GF_ROW_MINBLOCKS_WIDE)
     row_nl_kernel(Geom g, ModArgs m, Bufs b, int B) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int TPF = NX / R;
-  constexpr int M = NX / 2;
-  constexpr int PS = row_stride<T>(NX, NX / R);
-  const int tid = threadIdx.x, bp = tid / TPF, t = tid % TPF;
-  const int j0 = 2 * (blockIdx.x * B + bp);
-  cplx<T>* buf = reinterpret_cast<cplx<T>*>(smem_raw) + (size_t)bp * (TWO ? 2 : 3) * PS;
-  const cplx<T>* tw = static_cast<const cplx<T>*>(b.twid);
-  const cplx<T>* W = static_cast<const cplx<T>*>(b.W) + blockIdx.y * g.bs_w;
-  cplx<T>* P = static_cast<cplx<T>*>(b.P) + blockIdx.y * g.bs_p;
-  const int nl = g.nl;
-  const T* eta = static_cast<const T*>(m.eta);
-  const T* U1D = static_cast<const T*>(m.U1D);
-  const T* Qy1D = static_cast<const T*>(m.Qy1D);
-  const T* Qx2D = static_cast<const T*>(m.Qx2D);
-  const T* Qy2D = static_cast<const T*>(m.Qy2D);
-  const int nslot = 1 + m.hasB + m.hasC;
-  const int kout = g.kout > 0 ? g.kout : g.nkr;  // columns of the products formed
-  for (int L = 0; L < nl; ++L) {
-    if constexpr (TWO) {
-      const cplx<T> Up = mk<T>(U1D ? U1D[L * g.ny + j0] : T(0), U1D ? U1D[L * g.ny + j0 + 1] : T(0));
-#pragma unroll 1
-      for (int f = 0; f < 3; ++f) {
-        cplx<T>* dst = f == 0 ? buf : buf + PS;
-        const cplx<T>* Wa = W + ((size_t)f * nl + L) * g.ny * g.ldw + (size_t)j0 * g.ldw;
-#pragma unroll
-        for (int i = 0; i < R; ++i) {
-          const int k = t + i * TPF;
-          dst[swz<T>(k)] = packed_spec<T>(Wa, Wa + g.ldw, k, NX, g.kcut);
-        }
-        __syncthreads();
-        fft_smem<T, NX, R, +1>(dst, t, tw);
-        if (f == 0) continue;
-        // f = 1: q' = q (+ eta) kept in buf, A = (U + u) q' (or U q' when linear);
-        // f = 2: B = v q'.  Each thread rewrites only its own elements.
-#pragma unroll
-        for (int i = 0; i < R; ++i) {
-          const int x = t + i * TPF;
-          const int px = swz<T>(x);
-          cplx<T> q = buf[px], w = buf[PS + px];
-          const size_t ia = (size_t)j0 * NX + x, fs = (size_t)nl * g.ny * NX;
-          T* ph = b.phys ? static_cast<T*>(b.phys) + (size_t)L * g.ny * NX : nullptr;
-          if (f == 1) {
-            if (eta) q = q + mk<T>(eta[(size_t)j0 * NX + x], eta[(size_t)(j0 + 1) * NX + x]);
-            buf[px] = q;
-            const cplx<T> u = w + Up;
-            if (ph) { ph[ia] = q.x; ph[ia + NX] = q.y; ph[fs + ia] = u.x; ph[fs + ia + NX] = u.y; }
-            const cplx<T> au = m.linear ? Up : u;
-            w = mk<T>(au.x * q.x, au.y * q.y);
-          } else {
-            if (ph) { ph[2 * fs + ia] = w.x; ph[2 * fs + ia + NX] = w.y; }
-            w = mk<T>(w.x * q.x, w.y * q.y);
-          }
-          buf[PS + px] = w;
-        }
-        __syncthreads();
-        fft_smem<T, NX, R, -1>(buf + PS, t, tw);
-        cplx<T>* Pa = P + ((size_t)(f - 1) * nl + L) * g.ny * g.ldk + (size_t)j0 * g.ldk;
-#pragma unroll
-        for (int i = 0; i < R; ++i) {
-          const int k = t + i * TPF;
-          if (k <= M && k < kout) unpack_store<T>(buf + PS, k, NX, Pa, Pa + g.ldk);
-        }
-        __syncthreads();
-      }
-      continue;
-    }
-    for (int f = 0; f < 3; ++f) {
-      const cplx<T>* Wf = W + ((size_t)f * nl + L) * g.ny * g.ldw;
-      const cplx<T>* Wa = Wf + (size_t)j0 * g.ldw;
-      const cplx<T>* Wb = Wa + g.ldw;
-#pragma unroll
-      for (int i = 0; i < R; ++i) {
-        const int k = t + i * TPF;
-        buf[f * PS + swz<T>(k)] = packed_spec<T>(Wa, Wb, k, NX, g.kcut);
-      }
-    }
-    __syncthreads();
-    fft_smem_group<T, NX, R, +1, 3>(buf, PS, t, tw);
-    // physical-space products on the packed pairs
-    const T Ua = U1D ? U1D[L * g.ny + j0] : T(0), Ub = U1D ? U1D[L * g.ny + j0 + 1] : T(0);
-    const T Qa = Qy1D ? Qy1D[L * g.ny + j0] : T(0), Qb = Qy1D ? Qy1D[L * g.ny + j0 + 1] : T(0);
-    const bool last = (L == nl - 1);
-#pragma unroll
-    for (int i = 0; i < R; ++i) {
-      const int x = t + i * TPF;
-      const int px = swz<T>(x);
-      cplx<T> A, Bv, Cv;
-      pair_products<T>(g, m, b, W, L, j0, x, NX, mk<T>(Ua, Ub), mk<T>(Qa, Qb), last, buf[px], buf[PS + px],
-                       buf[2 * PS + px], A, Bv, Cv);
-      buf[px] = A;
-      if (m.hasB) { buf[PS + px] = Bv; if (m.hasC) buf[2 * PS + px] = Cv; }
-      else buf[PS + px] = Cv;
-    }
-    __syncthreads();
-    if (nslot == 2) fft_smem_group<T, NX, R, -1, 2>(buf, PS, t, tw);
-    else if (nslot == 3) fft_smem_group<T, NX, R, -1, 3>(buf, PS, t, tw);
-    else fft_smem<T, NX, R, -1>(buf, t, tw);
-    for (int f = 0; f < nslot; ++f) {
-      cplx<T>* Pa = P + ((size_t)f * nl + L) * g.ny * g.ldk + (size_t)j0 * g.ldk;
-#pragma unroll
-      for (int i = 0; i < R; ++i) {
-        const int k = t + i * TPF;
-        if (k <= M && k < kout) unpack_store<T>(buf + f * PS, k, NX, Pa, Pa + g.ldk);
-      }
-    }
-    __syncthreads();
-  }
+#define GF_ROW_BX blockIdx.x
+#define GF_ROW_BY blockIdx.y
+#include "gf_row_body.inc"
+#undef GF_ROW_BX
+#undef GF_ROW_BY
 }
 
 // ------------------------------------------------------------------ generic transforms

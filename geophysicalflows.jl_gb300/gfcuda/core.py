@@ -409,10 +409,14 @@ def stepforward_output(prob, nsteps, every, diagnostics=(), fields=()):
     return dout, {f: fout[:, i] for i, f in enumerate(fields)}
 
 
-def ensemble_step(probs, nsteps):
-    """Step several problems (e.g. batched problems of different grid sizes) together; each
-    runs on its own stream, so they execute concurrently on the GPU."""
+def ensemble_step(probs, nsteps, persistent=False):
+    """Step several problems (e.g. batched problems of different grid sizes) together, from
+    one CUDA graph when graphs are on.  persistent=False: each problem runs its own launches
+    on its own stream, concurrently; persistent=True: where the problems allow it (one layer,
+    square 32/64/128/256 grids, one precision, not AB3), every stage of all of them runs in one
+    persistent row launch and one persistent column launch over a work list of all tiles."""
     lib = probs[0]._lib
+    probs[0]._c(lib.gf_set_ensemble_mode(probs[0]._ctx, 1 if persistent else 0))
     arr = (C.c_void_p * len(probs))(*[p._ctx.value for p in probs])
     code = lib.gf_ensemble_step(arr, len(probs), int(nsteps))
     if code != A.GF_OK:

@@ -242,10 +242,20 @@ int gf_get_batch(const gf_ctx* ctx, int32_t* batch);
  * call pays for one observed step.  No counterpart in the reference (its steps are
  * launched broadcast by broadcast). */
 int gf_set_graph_steps(gf_ctx* ctx, int32_t steps);
-/* Steps n contexts (e.g. one batched context per grid size of an ensemble) by nsteps each;
- * every context runs on its own stream, so the size classes execute concurrently.
- * Errors: gf_last_error(NULL). */
+/* Steps n contexts (e.g. one batched context per grid size of an ensemble of independent runs
+ * with uneven grid sizes) by nsteps each.  No counterpart in the reference (its ensembles are
+ * a host loop over Problems).  With graphs on (gf_set_graph_steps > 0) the steps are replayed
+ * from one CUDA graph for all contexts, in one of two executions (gf_set_ensemble_mode on the
+ * first context): 0 (default) each context runs its own tuned launches on its own stream and
+ * the size classes execute concurrently; 1, when the contexts allow it -- at most 4 contexts
+ * of one precision and stepper family (not AB3), each one layer without bottom drag on a
+ * square grid of 32, 64, 128 or 256 points -- every stage of every context runs in ONE
+ * persistent row launch and ONE persistent column launch whose blocks walk the work list of
+ * all contexts' tiles (otherwise mode 0).  Errors: gf_last_error(NULL). */
 int gf_ensemble_step(gf_ctx* const* ctxs, int32_t n, int64_t nsteps);
+/* Ensemble execution when ctx is the first context of gf_ensemble_step: 0 (default) one
+ * context per stream, 1 the persistent ensemble launches.  No counterpart in the reference. */
+int gf_set_ensemble_mode(gf_ctx* ctx, int32_t mode);
 
 /* F-hat for GF_FORCING_STATIC / HARMONIC (same layout as sol), or the forcing spectrum
  * (real, (nkr, ny), the reference's `forcing_spectrum`) for the stochastic kinds.  This is
