@@ -499,6 +499,9 @@ static void tma_maps(gf_ctx* c) {
   c->tma.ok = true;
 }
 
+static bool fp_ctx_ok(const gf_ctx* c);
+static void set_fp(gf_ctx* c, int Rr, int Rc, int C);
+
 static int build(gf_ctx* c, const gf_config* cfg) {
   const gf_config& k = *cfg;
   Geom& g = c->g;
@@ -702,6 +705,9 @@ static int build(gf_ctx* c, const gf_config* cfg) {
   if (!(c->derr = (int*)dalloc(c, sizeof(int)))) return fail(c, GF_ERR_NOMEM, "error flag");
   GF_CUDA(c, cudaMemsetAsync(c->derr, 0, sizeof(int), c->stream));
   if (g.nl == 1) tma_maps(c);
+  // grids whose row pairs (of all instances) do not cover the SMs: the field-parallel kernels
+  if (fp_ctx_ok(c) && (size_t)NB * (g.ny / 2) < (size_t)num_sms()) 
+    set_fp(c, fp_default_row_radix(g.nx), fp_default_col_radix(g.ny), 1);
   if (c->kind == SK_RK4) {
     if (!(c->acc = dalloc(c, NB * nsp * cb))) return fail(c, GF_ERR_NOMEM, "acc");
     if (c->hasL && !(c->X = dalloc(c, NB * nsp * cb))) return fail(c, GF_ERR_NOMEM, "X");
@@ -1888,9 +1894,11 @@ extern "C" int gf_fluxes(gf_ctx* c, double* lateral, double* vertical) {
 
 // ------------------------------------------------------------------------------ autotune
 // Launch-shape autotuner: times the step kernels of this context at every candidate shape
-// -- column kernel: FFT radix (FP32: 4, 8, 16; FP64/df64: 8) x columns per block C; row
-// kernel: radix x row pairs per block B (threads per row = length / radix) -- with CUDA
-// events around each launch, and keeps the fastest.  The state, clock, AB3 history and
+// -- column kernel: FFT radix (FP32: 4, 8, 16; FP64/df64: 8) x columns per block C, the TMA
+// column stage, and on small grids the field-parallel kernel (radix 2, 4, 8 x C); row
+// kernel: radix x row pairs per block B (threads per row = length / radix) and the
+// field-parallel kernel (radix 2, 4, 8) -- with CUDA events around each launch, and keeps
+// the fastest.  The state, clock, AB3 history and
 // stochastic-forcing record are restored afterwards; captured graphs are dropped (they
 // are re-captured with the new shapes).  The profiling counters are reset.
 static int set_shape(gf_ctx* c, int Rr, int B, int Rc, int C, int tmaC = 0) {
@@ -1910,6 +1918,7 @@ extern "C" int gf_set_tma_columns(gf_ctx* c, int32_t C) {
   if (C != 0 && !tma_eligible(c, C))
     return fail(c, GF_ERR_UNSUPPORTED, "no TMA column stage with this column count for this context");
   c->g.tmaC = C;
+  if (C) { c->g.fpRc = 0; c->g.fpC = 0; }  // the TMA stage is a form of the classic column kernel
   drop_graphs(c);
   return GF_OK;
 }
@@ -1917,6 +1926,33 @@ extern "C" int gf_set_tma_columns(gf_ctx* c, int32_t C) {
 extern "C" int gf_get_tma_columns(const gf_ctx* c, int32_t* C) {
   if (!c || !C) return GF_ERR_ARG;
   *C = c->g.tmaC;
+  return GF_OK;
+}
+
+// whether the field-parallel small-grid kernels can run this context
+static bool fp_ctx_ok(const gf_ctx* c) {
+  return !c->g.rtx && !c->g.rty && fp_len_ok(c->g.nx) && fp_len_ok(c->g.ny) && c->g.nl == 1 && !c->m.drag;
+}
+
+static void set_fp(gf_ctx* c, int Rr, int Rc, int C) {
+  c->g.fpR = Rr; c->g.fpRc = Rc; c->g.fpC = Rc ? std::max(C, 1) : 0;
+  drop_graphs(c);
+}
+
+extern "C" int gf_set_field_parallel(gf_ctx* c, int32_t row_radix, int32_t col_radix, int32_t columns) {
+  if (!c || row_radix < 0 || col_radix < 0 || columns < 0) return GF_ERR_ARG;
+  if ((row_radix || col_radix) && !fp_ctx_ok(c))
+    return fail(c, GF_ERR_UNSUPPORTED, "field-parallel kernels: one layer without bottom drag, power-of-two lengths 32 ... 256");
+  if (row_radix && !fp_radix_ok(c->g.nx, row_radix)) return fail(c, GF_ERR_ARG, "field-parallel row radix must be 2, 4 or 8");
+  if (col_radix && (!fp_radix_ok(c->g.ny, col_radix) || !fp_cols_ok(c->g.ny, col_radix, columns ? columns : 1)))
+    return fail(c, GF_ERR_ARG, "field-parallel column radix must be 2, 4 or 8, with 3 x columns x ny / radix <= 384");
+  set_fp(c, row_radix, col_radix, columns);
+  return GF_OK;
+}
+
+extern "C" int gf_get_field_parallel(const gf_ctx* c, int32_t* out) {
+  if (!c || !out) return GF_ERR_ARG;
+  out[0] = c->g.fpR; out[1] = c->g.fpRc; out[2] = c->g.fpC;
   return GF_OK;
 }
 
@@ -1928,6 +1964,7 @@ extern "C" int gf_set_launch_shape(gf_ctx* c, const int32_t* shape) {
     const int R = shape[k], N = k == 0 ? c->g.nx : c->g.ny;
     if (R != 0 && R != 8 && !(f32 && f32_radix_built(N, R))) return fail(c, GF_ERR_ARG, "radix not built for this size");
   }
+  set_fp(c, 0, 0, 0);  // an explicit launch shape runs the classic kernels
   return set_shape(c, shape[0], shape[1], shape[2], shape[3], c->g.tmaC);
 }
 
@@ -1989,6 +2026,9 @@ extern "C" int gf_autotune(gf_ctx* c, int32_t reps, int32_t* shape) {
   const int radii[3] = {8, 16, 4};
   const int unit = 128 / (int)c->cb;  // elements per 128-byte wavefront
   int bestRc = 0, bestC = 0, bestRr = 0, bestB = 0, bestT = 0;
+  int bestFc = 0, bestFC = 0, bestFr = 0;  // field-parallel kernels (radix 0: not chosen)
+  const bool fpok = fp_ctx_ok(c);
+  set_fp(c, 0, 0, 0);
   double best = 1e30;
   for (int ri = 0; ri < (f32 ? 3 : 1) && rc == GF_OK; ++ri) {
     const int R = radii[ri], TPF = g0.ny / R;
@@ -2013,6 +2053,19 @@ extern "C" int gf_autotune(gf_ctx* c, int32_t reps, int32_t* shape) {
       if (rc == GF_OK && ms < best) { best = ms; bestRc = R; bestC = 0; bestT = C; }
     }
   }
+  // the field-parallel column kernel (small grids)
+  for (const int R : {2, 4, 8}) {
+    if (!fpok || rc != GF_OK || !fp_radix_ok(g0.ny, R)) continue;
+    for (const int C : {1, 2, 4}) {
+      if (rc != GF_OK || !fp_cols_ok(g0.ny, R, C)) continue;
+      set_shape(c, 0, 0, 0, 0, 0);
+      set_fp(c, 0, R, C);
+      double ms = 0;
+      rc = measure(1, &ms);
+      if (rc == GF_OK && ms < best) { best = ms; bestFc = R; bestFC = C; }
+    }
+  }
+  set_fp(c, 0, bestFc, bestFC);
   best = 1e30;
   for (int ri = 0; ri < (f32 ? 3 : 1) && rc == GF_OK; ++ri) {
     const int R = radii[ri], TPF = g0.nx / R;
@@ -2025,11 +2078,25 @@ extern "C" int gf_autotune(gf_ctx* c, int32_t reps, int32_t* shape) {
       if (rc == GF_OK && ms < best) { best = ms; bestRr = R; bestB = B; }
     }
   }
+  for (const int R : {2, 4, 8}) {  // the field-parallel row kernel
+    if (!fpok || rc != GF_OK || !fp_radix_ok(g0.nx, R)) continue;
+    set_shape(c, 0, 0, bestRc, bestC, bestT);
+    set_fp(c, R, bestFc, bestFC);
+    double ms = 0;
+    rc = measure(0, &ms);
+    if (rc == GF_OK && ms < best) { best = ms; bestFr = R; }
+  }
   c->profiling = prof0;
   restore();
   for (auto& pq : saved) cudaFreeAsync(pq.second, c->stream);
-  if (rc != GF_OK) { set_shape(c, g0.tuneRr, g0.tuneB, g0.tuneRc, g0.tuneC, g0.tmaC); upload_clock(c); return rc; }
+  if (rc != GF_OK) {
+    set_shape(c, g0.tuneRr, g0.tuneB, g0.tuneRc, g0.tuneC, g0.tmaC);
+    set_fp(c, g0.fpR, g0.fpRc, g0.fpC);
+    upload_clock(c);
+    return rc;
+  }
   set_shape(c, bestRr, bestB, bestRc, bestC, bestT);
+  set_fp(c, bestFr, bestFc, bestFC);
   if (int r = upload_clock(c)) return r;
   if (shape) { shape[0] = bestRr; shape[1] = bestB; shape[2] = bestRc; shape[3] = bestC; }
   return GF_OK;

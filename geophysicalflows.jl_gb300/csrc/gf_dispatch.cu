@@ -28,6 +28,7 @@ namespace gf {
 template <class T>
 cudaError_t launch_row(const Geom& g, const ModArgs& m, const Bufs& b, cudaStream_t st) {
   if (g.rtx) return launch_row_rt<T>(g, m, b, st);
+  if (g.fpR) return launch_row_fp<T>(g, m, b, st);
   switch (g.nx) {
     GF_ROW_CASE(32) GF_ROW_CASE(64) GF_ROW_CASE(128) GF_ROW_CASE(256) GF_ROW_CASE(512) GF_ROW_CASE(1024)
     GF_ROW_CASE(2048)
@@ -38,6 +39,7 @@ cudaError_t launch_row(const Geom& g, const ModArgs& m, const Bufs& b, cudaStrea
 template <class T>
 cudaError_t launch_col(const Geom& g, const ModArgs& m, const StepArgs& s, const Bufs& b, cudaStream_t st) {
   if (g.rty) return launch_col_rt<T>(g, m, s, b, st);
+  if (g.fpRc) return launch_col_fp<T>(g, m, s, b, st);
   switch (g.ny) {
     GF_COL_CASE(32) GF_COL_CASE(64) GF_COL_CASE(128) GF_COL_CASE(256) GF_COL_CASE(512) GF_COL_CASE(1024)
     GF_COL_CASE(2048)

@@ -1,0 +1,7 @@
+// Field-parallel small-grid step kernels (double; lengths 32 ... 256 at radix 2, 4 and 8).
+#include "gf_fpar.cuh"
+
+namespace gf {
+template cudaError_t launch_row_fp<double>(const Geom&, const ModArgs&, const Bufs&, cudaStream_t);
+template cudaError_t launch_col_fp<double>(const Geom&, const ModArgs&, const StepArgs&, const Bufs&, cudaStream_t);
+}  // namespace gf

@@ -27,7 +27,8 @@ EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_abi_version", "gf_get
            "gf_peakedisotropicspectrum", "gf_get_filter", "gf_adjoint_setup", "gf_adjoint_forward",
            "gf_adjoint_backward", "gf_grad", "gf_autotune", "gf_set_launch_shape", "gf_get_launch_shape",
            "gf_fluxes", "gf_step_callback", "gf_adjoint_set_snapshots", "gf_adjoint_info",
-           "gf_step_output", "gf_set_tma_columns", "gf_get_tma_columns", "gf_set_ensemble_mode"]
+           "gf_step_output", "gf_set_tma_columns", "gf_get_tma_columns", "gf_set_ensemble_mode",
+           "gf_set_field_parallel", "gf_get_field_parallel"]
 
 
 class gf_config(C.Structure):
@@ -107,6 +108,8 @@ def load(path=None):
         "gf_set_tma_columns": ([vp, i32], C.c_int),
         "gf_get_tma_columns": ([vp, C.POINTER(i32)], C.c_int),
         "gf_set_ensemble_mode": ([vp, i32], C.c_int),
+        "gf_set_field_parallel": ([vp, i32, i32, i32], C.c_int),
+        "gf_get_field_parallel": ([vp, C.POINTER(i32)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

@@ -207,13 +207,29 @@ class Problem:
 
     def autotune(self, reps=4):
         """Time the step kernels at every candidate launch shape and keep the fastest;
-        returns {row_radix, row_pairs, col_radix, col_columns, tma_columns} (tma_columns > 0:
-        the column stage runs with TMA tile copies, that many columns per block)."""
+        returns {row_radix, row_pairs, col_radix, col_columns, tma_columns, field_parallel}
+        (tma_columns > 0: the column stage runs with TMA tile copies, that many columns per
+        block; field_parallel: (row radix, column radix, columns) of the field-parallel
+        small-grid kernels, radix 0 where the classic kernel runs)."""
         sh = (C.c_int32 * 4)()
         self._c(self._lib.gf_autotune(self._ctx, int(reps), sh))
         d = dict(zip(("row_radix", "row_pairs", "col_radix", "col_columns"), list(sh)))
         d["tma_columns"] = self.tma_columns
+        d["field_parallel"] = self.field_parallel
         return d
+
+    @property
+    def field_parallel(self):
+        """(row radix, column radix, columns per block) of the field-parallel small-grid
+        kernels; radix 0: that half of the stage runs the classic kernel."""
+        v = (C.c_int32 * 3)()
+        self._c(self._lib.gf_get_field_parallel(self._ctx, v))
+        return tuple(v)
+
+    @field_parallel.setter
+    def field_parallel(self, rrc):
+        r, rc, cols = (tuple(rrc) + (0, 0, 0))[:3]
+        self._c(self._lib.gf_set_field_parallel(self._ctx, int(r), int(rc), int(cols)))
 
     @property
     def tma_columns(self):

@@ -297,8 +297,10 @@ int gf_step_callback(gf_ctx* ctx, int64_t nsteps, gf_forcing_fn fn, void* user);
  * without bottom drag with columns of >= 1024 may get blocks of up to 640 threads there,
  * while the last step of a call keeps blocks of <= 512 threads (the column count capped).
  * gf_set_launch_shape applies a shape found earlier (e.g. for another context of the same
- * size).  The autotuner also times the TMA column stage (below) at each column radix where
- * it applies, and selects it (gf_get_tma_columns) when it is the fastest. */
+ * size) and selects the classic kernels for both halves of the stage (the field-parallel
+ * kernels below off).  The autotuner also times the TMA column stage (below) at each column radix where
+ * it applies, and selects it (gf_get_tma_columns) when it is the fastest, and likewise the
+ * field-parallel kernels (below) on grids where they apply (gf_get_field_parallel). */
 int gf_autotune(gf_ctx* ctx, int32_t reps, int32_t* shape);
 int gf_set_launch_shape(gf_ctx* ctx, const int32_t* shape);
 int gf_get_launch_shape(const gf_ctx* ctx, int32_t* shape);
@@ -308,11 +310,25 @@ int gf_get_launch_shape(const gf_ctx* ctx, int32_t* shape);
  * gradient product), the column half of each stage can load its product tiles and store the
  * inverse fields with tensor-memory-access tile copies (cp.async.bulk.tensor) instead of
  * per-thread copies.  C = columns per block: 2 or 4 (GF_F32), 1 or 2 (GF_F64, GF_DF64);
- * 0 selects the per-thread-copy column kernel.  GF_ERR_UNSUPPORTED if the context cannot use
- * it with C.  The column radix stays that of the launch shape.  If a tile load does not
+ * 0 selects the per-thread-copy column kernel; C > 0 also turns the field-parallel column
+ * kernel (below) off.  GF_ERR_UNSUPPORTED if the context cannot use it with C.  The column radix stays that of the launch shape.  If a tile load does not
  * arrive within one second the kernel sets an error flag that gf_synchronize reports. */
 int gf_set_tma_columns(gf_ctx* ctx, int32_t C);
 int gf_get_tma_columns(const gf_ctx* ctx, int32_t* C);
+
+/* Field-parallel small-grid kernels (no reference counterpart): for one layer without bottom
+ * drag and power-of-two nx, ny in 32 ... 256, the row and column halves of each stage can run
+ * with one thread group per field (the three inverse transforms, and the product transforms,
+ * concurrently inside a block) at FFT radix 2, 4 or 8 -- the fast form when the grid has too
+ * few row pairs and columns to occupy the GPU (e.g. one 128^2 run).  row_radix / col_radix 0
+ * select the classic kernel for that half; columns = kr columns per column block (3 x columns
+ * x ny / col_radix <= 384 threads; 0 means 1).  A context whose row pairs, over all instances,
+ * are fewer than the GPU's SMs starts with them (row radix 4; column radix 2 up to ny = 128,
+ * 4 above; one column per block);
+ * gf_autotune times them against the classic kernels.  GF_ERR_UNSUPPORTED for contexts they
+ * cannot run.  gf_get_field_parallel writes {row_radix, col_radix, columns}. */
+int gf_set_field_parallel(gf_ctx* ctx, int32_t row_radix, int32_t col_radix, int32_t columns);
+int gf_get_field_parallel(const gf_ctx* ctx, int32_t* out);
 
 /* ---- adjoint ----------------------------------------------------------------------------
  * Reverse-mode derivative of stepforward!(prob, nsteps), the counterpart of a
