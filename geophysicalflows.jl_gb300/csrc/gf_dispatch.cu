@@ -146,9 +146,11 @@ cudaError_t launch_spec_apply(const Geom& g, const ModArgs& m, const void* in, v
     }                                                                                       \
     return launch_adj_col_n<T, N>(g, m, a, b, st);
 
-// the adjoint kernels follow the context's tuned radix and tiles (FP32)
+// the adjoint kernels follow the context's tuned radix and tiles (FP32), and its
+// field-parallel setting
 template <class T>
 cudaError_t launch_adj_row(const Geom& g, const AdjArgs& a, const Bufs& b, cudaStream_t st) {
+  if (g.fpR) return launch_adj_row_fp<T>(g, a, b, st);
   switch (g.nx) {
     GF_ADJ_ROW_CASE(32) GF_ADJ_ROW_CASE(64) GF_ADJ_ROW_CASE(128) GF_ADJ_ROW_CASE(256) GF_ADJ_ROW_CASE(512)
     GF_ADJ_ROW_CASE(1024) GF_ADJ_ROW_CASE(2048)
@@ -158,6 +160,7 @@ cudaError_t launch_adj_row(const Geom& g, const AdjArgs& a, const Bufs& b, cudaS
 
 template <class T>
 cudaError_t launch_adj_col(const Geom& g, const ModArgs& m, const AdjArgs& a, const Bufs& b, cudaStream_t st) {
+  if (g.fpRc) return launch_adj_col_fp<T>(g, m, a, b, st);
   switch (g.ny) {
     GF_ADJ_COL_CASE(32) GF_ADJ_COL_CASE(64) GF_ADJ_COL_CASE(128) GF_ADJ_COL_CASE(256) GF_ADJ_COL_CASE(512)
     GF_ADJ_COL_CASE(1024) GF_ADJ_COL_CASE(2048)

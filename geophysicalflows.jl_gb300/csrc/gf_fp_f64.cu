@@ -4,4 +4,6 @@
 namespace gf {
 template cudaError_t launch_row_fp<double>(const Geom&, const ModArgs&, const Bufs&, cudaStream_t);
 template cudaError_t launch_col_fp<double>(const Geom&, const ModArgs&, const StepArgs&, const Bufs&, cudaStream_t);
+template cudaError_t launch_adj_row_fp<double>(const Geom&, const AdjArgs&, const Bufs&, cudaStream_t);
+template cudaError_t launch_adj_col_fp<double>(const Geom&, const ModArgs&, const AdjArgs&, const Bufs&, cudaStream_t);
 }  // namespace gf

@@ -19,6 +19,7 @@
 // rounding.  One layer without bottom drag (the column kernel holds the three fields of one
 // layer); lengths 32 ... 256.
 #pragma once
+#include "gf_adjoint.cuh"
 #include "gf_kernels.cuh"
 #include "gf_launch.cuh"
 
@@ -162,6 +163,154 @@ __global__ void __launch_bounds__(FP_MAXT)
   }
 }
 
+// ---- adjoint (the transposed stage of gf_adjoint.cuh), same block structure
+// Row: the x-c2r of (abar, bbar) by groups 0 and 1, the transposed products over all threads,
+// the x-r2c of (qbar, ubar, vbar) by groups 0, 1, 2.
+template <class T, int NX, int R>
+__global__ void __launch_bounds__(FP_MAXT)
+    adj_row_fp_kernel(const __grid_constant__ Geom g, const __grid_constant__ AdjArgs a, const __grid_constant__ Bufs b) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int TPF = NX / R, NT = 3 * TPF;
+  constexpr int PS = row_stride<T>(NX, TPF);
+  const int tid = threadIdx.x, f = tid / TPF, t = tid % TPF;
+  const int j0 = 2 * blockIdx.x;
+  cplx<T>* buf = reinterpret_cast<cplx<T>*>(smem_raw);
+  cplx<T>* mine = buf + f * PS;
+  const cplx<T>* tw = static_cast<const cplx<T>*>(b.twid);
+  const cplx<T>* Wb = static_cast<const cplx<T>*>(a.Wb);
+  cplx<T>* Pb = static_cast<cplx<T>*>(a.Pb);
+  const T* ph = static_cast<const T*>(a.phys);
+  T* etab = static_cast<T*>(a.etab);
+  const size_t np = (size_t)g.ny * NX;
+  const T U = sel<T>(a.U, a.U_f, a.U_l);
+  if (f < 2) {
+    const cplx<T>* Wa = Wb + (size_t)f * g.ny * g.ldk + (size_t)j0 * g.ldk;
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int k = t + i * TPF;
+      mine[swz<T>(k)] = packed_spec<T>(Wa, Wa + g.ldk, k, NX, g.nkr);
+    }
+  }
+  __syncthreads();
+  fft_smem<T, NX, R, +1>(mine, t, tw);  // group 2: a buffer that is overwritten below
+  for (int x = tid; x < NX; x += NT) {
+    const int px = swz<T>(x);
+    const size_t ia = (size_t)j0 * NX + x, ibb = ia + NX;
+    const cplx<T> ab = buf[px], bb = buf[PS + px];
+    const cplx<T> qe = mk<T>(ph[ia], ph[ibb]);
+    const cplx<T> u = mk<T>(ph[np + ia], ph[np + ibb]);
+    const cplx<T> v = mk<T>(ph[2 * np + ia], ph[2 * np + ibb]);
+    const cplx<T> qb = mk<T>(ab.x * u.x + bb.x * v.x, ab.y * u.y + bb.y * v.y);
+    etab[ia] = etab[ia] + (qb.x + U * ab.x);
+    etab[ibb] = etab[ibb] + (qb.y + U * ab.y);
+    buf[px] = qb;
+    buf[PS + px] = mk<T>(ab.x * qe.x, ab.y * qe.y);
+    buf[2 * PS + px] = mk<T>(bb.x * qe.x, bb.y * qe.y);
+  }
+  __syncthreads();
+  fft_smem<T, NX, R, -1>(mine, t, tw);
+  cplx<T>* Pa = Pb + (size_t)f * g.ny * g.ldk + (size_t)j0 * g.ldk;
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int k = t + i * TPF;
+    if (k < g.kcut) unpack_store<T>(mine, k, NX, Pa, Pa + g.ldk);
+  }
+}
+
+// Column: the y-FFTs of the three adjoint products by groups, Xbar and the transposed stage
+// combination element by element over all threads, the y-inverse FFTs of
+// (i kr Nbar / w, i l Nbar / w) by groups 0 and 1 (C columns per block).
+template <class T, int NY, int R>
+__global__ void __launch_bounds__(FP_MAXT)
+    adj_col_fp_kernel(const __grid_constant__ Geom g, const __grid_constant__ ModArgs m,
+                      const __grid_constant__ AdjArgs a, const __grid_constant__ Bufs b, int C) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int TPF = NY / R;
+  const int NT = blockDim.x, CN = C * NY;
+  const int cs = g.cs;
+  cplx<T>* F0 = reinterpret_cast<cplx<T>*>(smem_raw);
+  const int tid = threadIdx.x, cf = tid / TPF, tf = tid % TPF;
+  const int bx = blockIdx.x;
+  const cplx<T>* tw = static_cast<const cplx<T>*>(b.twid);
+  const T dky = sel<T>(g.dky, g.dky_f, g.dky_l), dkx = sel<T>(g.dkx, g.dkx_f, g.dkx_l);
+  const T ell2 = sel<T>(m.ell_inv2, m.ell_inv2_f, m.ell_inv2_l);
+  const T inv_n = sel<T>(g.inv_nxny, g.inv_nxny_f, g.inv_nxny_l);
+  const int cx = a.cplx;
+  const bool fwd = a.stage <= 4 && bx * C < g.kcut;
+  if (fwd) {
+    const cplx<T>* P = static_cast<const cplx<T>*>(a.Pb);
+    const size_t fs = (size_t)g.ny * g.ldk;
+    for (int e = tid; e < 3 * CN; e += NT) {
+      const int f = e / CN, r = e - f * CN, c = r % C, j = r / C, kr = bx * C + c;
+      F0[(size_t)(f * C + c) * cs + swz<T>(j)] = (kr < g.kcut) ? P[f * fs + (size_t)j * g.ldk + kr] : czero<T>();
+    }
+    __syncthreads();
+    fft_smem<T, NY, R, -1>(F0 + (size_t)cf * cs, tf, tw);
+  }
+  const bool out_w = !(a.stage == 1 && !a.head);
+  cplx<T>* ub = static_cast<cplx<T>*>(a.ub);
+  for (int e = tid; e < CN; e += NT) {
+    const int c = e % C, j = e / C, kr = bx * C + c;
+    const bool kin = kr < g.nkr;
+    const T krT = T(kr) * dkx;
+    const bool edge = (kr == 0) || (2 * kr == g.nx);
+    const T scale_in = edge ? inv_n : T(2) * inv_n;  // irfft^T: w / (nx ny)
+    const T scale_out = edge ? T(1) : T(0.5);       // rfft^T via the c2r path: 1 / w
+    const size_t ti = (size_t)j * g.ldk + kr;
+    const bool keep = kin && kept(g, kr, j);
+    cplx<T> xj = czero<T>();
+    if (fwd && keep) {  // Xbar of this stage
+      const T lv = T(lidx(g, j)) * dky;
+      const T K2 = krT * krT + lv * lv;
+      const T f = psi_factor<T>(m.psi_kind, K2, ell2, m.mult, ti);
+      const cplx<T> Q = F0[(size_t)c * cs + swz<T>(j)], Ub = F0[(size_t)(C + c) * cs + swz<T>(j)],
+                    Vb = F0[(size_t)(2 * C + c) * cs + swz<T>(j)];
+      xj = scale_in * (Q + f * (lv * mul_i(Ub) - krT * mul_i(Vb)));
+    }
+    cplx<T> nb = czero<T>();
+    if (kin) {  // transposed stage combination -> the next cotangent
+      auto start = [&](cplx<T> u) {
+        const cplx<T> v = a.filtered ? static_cast<const T*>(a.filt)[ti] * u : u;
+        ub[ti] = v;
+        return mulcj<T>(a.gamma, ti, v, cx);
+      };
+      if (a.stage == 5) {
+        nb = start(static_cast<const cplx<T>*>(a.ubar_in)[ti]);
+      } else if (a.stage == 4) {
+        const cplx<T> u = ub[ti];
+        nb = T(2) * mulcj<T>(a.beta, ti, u, cx) + T(2) * mulcj<T>(a.zeta, ti, xj, cx);
+        static_cast<cplx<T>*>(a.n1acc)[ti] = mulcj<T>(a.alpha, ti, u, cx) - mulcj<T>(a.zeta, ti, xj, cx);
+        static_cast<cplx<T>*>(a.xaacc)[ti] = mulcj<T>(a.e2, ti, xj, cx);
+      } else if (a.stage == 3) {
+        const cplx<T> u = ub[ti];
+        static_cast<cplx<T>*>(a.x1acc)[ti] = mulcj<T>(a.e, ti, u, cx) + mulcj<T>(a.e2, ti, xj, cx);
+        nb = T(2) * mulcj<T>(a.beta, ti, u, cx) + mulcj<T>(a.zeta, ti, xj, cx);
+      } else if (a.stage == 2) {
+        const cplx<T> Ab = keep ? static_cast<const cplx<T>*>(a.xaacc)[ti] + xj : czero<T>();
+        cplx<T>* x1 = static_cast<cplx<T>*>(a.x1acc);
+        x1[ti] = x1[ti] + mulcj<T>(a.e2, ti, Ab, cx);
+        nb = static_cast<const cplx<T>*>(a.n1acc)[ti] + mulcj<T>(a.zeta, ti, Ab, cx);
+      } else {  // stage 1
+        const cplx<T> un = keep ? static_cast<const cplx<T>*>(a.x1acc)[ti] + xj : czero<T>();
+        static_cast<cplx<T>*>(a.ubar_out)[ti] = un;
+        if (a.head) nb = start(un);
+      }
+    }
+    if (out_w) {
+      F0[(size_t)c * cs + swz<T>(j)] = (scale_out * krT) * mul_i(nb);
+      F0[(size_t)(C + c) * cs + swz<T>(j)] = (scale_out * (T(lidx(g, j)) * dky)) * mul_i(nb);
+    }
+  }
+  if (!out_w) return;
+  __syncthreads();
+  fft_smem<T, NY, R, +1>(F0 + (size_t)cf * cs, tf, tw);  // groups of the third field: not stored
+  cplx<T>* Wb = static_cast<cplx<T>*>(a.Wb);
+  for (int e = tid; e < 2 * CN; e += NT) {
+    const int f = e / CN, r = e - f * CN, c = r % C, j = r / C, kr = bx * C + c;
+    if (kr < g.nkr) Wb[(size_t)f * g.ny * g.ldk + (size_t)j * g.ldk + kr] = F0[(size_t)(f * C + c) * cs + swz<T>(j)];
+  }
+}
+
 template <class T, int NN, int R>
 cudaError_t launch_row_fp_nr(const Geom& g, const ModArgs& m, const Bufs& b, cudaStream_t st) {
   const size_t sm = (size_t)3 * row_stride<T>(NN, NN / R) * sizeof(cplx<T>);
@@ -183,6 +332,29 @@ cudaError_t launch_col_fp_nr(const Geom& g, const ModArgs& m, const StepArgs& s,
   if (err != cudaSuccess) return err;
   const int ncols = g.kout > 0 ? g.kout : g.nkr;
   k<<<dim3((ncols + C - 1) / C, g.nb), 3 * C * (NN / R), sm, st>>>(g2, m, s, b, C);
+  return cudaGetLastError();
+}
+
+template <class T, int NN, int R>
+cudaError_t launch_adj_row_fp_nr(const Geom& g, const AdjArgs& a, const Bufs& b, cudaStream_t st) {
+  const size_t sm = (size_t)3 * row_stride<T>(NN, NN / R) * sizeof(cplx<T>);
+  auto k = adj_row_fp_kernel<T, NN, R>;
+  cudaError_t err = set_smem(k, sm);
+  if (err != cudaSuccess) return err;
+  k<<<g.ny / 2, 3 * (NN / R), sm, st>>>(g, a, b);
+  return cudaGetLastError();
+}
+
+template <class T, int NN, int R>
+cudaError_t launch_adj_col_fp_nr(const Geom& g, const ModArgs& m, const AdjArgs& a, const Bufs& b, cudaStream_t st) {
+  const int C = g.fpC > 0 ? g.fpC : 1;
+  Geom g2 = g;
+  g2.cs = col_stride<T>(NN, C);
+  const size_t sm = (size_t)3 * C * g2.cs * sizeof(cplx<T>);
+  auto k = adj_col_fp_kernel<T, NN, R>;
+  cudaError_t err = set_smem(k, sm);
+  if (err != cudaSuccess) return err;
+  k<<<(g.nkr + C - 1) / C, 3 * C * (NN / R), sm, st>>>(g2, m, a, b, C);
   return cudaGetLastError();
 }
 
@@ -212,6 +384,16 @@ cudaError_t launch_row_fp(const Geom& g, const ModArgs& m, const Bufs& b, cudaSt
 template <class T>
 cudaError_t launch_col_fp(const Geom& g, const ModArgs& m, const StepArgs& s, const Bufs& b, cudaStream_t st) {
   GF_FP_SWITCH(launch_col_fp_nr, g.ny, g.fpRc, g, m, s, b, st)
+}
+
+template <class T>
+cudaError_t launch_adj_row_fp(const Geom& g, const AdjArgs& a, const Bufs& b, cudaStream_t st) {
+  GF_FP_SWITCH(launch_adj_row_fp_nr, g.nx, g.fpR, g, a, b, st)
+}
+
+template <class T>
+cudaError_t launch_adj_col_fp(const Geom& g, const ModArgs& m, const AdjArgs& a, const Bufs& b, cudaStream_t st) {
+  GF_FP_SWITCH(launch_adj_col_fp_nr, g.ny, g.fpRc, g, m, a, b, st)
 }
 
 }  // namespace gf

@@ -200,6 +200,9 @@ inline bool fp_radix_ok(int n, int R) { return (R == 2 || R == 4 || R == 8) && 3
 inline bool fp_cols_ok(int n, int R, int C) { return C >= 1 && C <= 8 && 3 * C * (n / R) <= FP_MAXT; }
 template <class T> cudaError_t launch_row_fp(const Geom&, const ModArgs&, const Bufs&, cudaStream_t);
 template <class T> cudaError_t launch_col_fp(const Geom&, const ModArgs&, const StepArgs&, const Bufs&, cudaStream_t);
+template <class T> cudaError_t launch_adj_row_fp(const Geom&, const AdjArgs&, const Bufs&, cudaStream_t);
+template <class T>
+cudaError_t launch_adj_col_fp(const Geom&, const ModArgs&, const AdjArgs&, const Bufs&, cudaStream_t);
 
 // generic-length launchers (gf_rt.cu), used by the dispatchers when Geom::rtx / rty is set
 template <class T> cudaError_t launch_row_rt(const Geom&, const ModArgs&, const Bufs&, cudaStream_t);
