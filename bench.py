@@ -43,6 +43,8 @@ SLQG512 = dict(module="SingleLayerQG", nx=512, ny=512, stepper="ETDRK4", dt=0.05
 # 3 layers, H = [.2,.3,.5], rho = [4, 5, 5.5] -> b with g' = g (rho_{j+1} - rho_j) / rho_{j+1}, g = 1
 MLQG1024X3 = dict(module="MultiLayerQG", nx=1024, ny=1024, nlayers=3, stepper="ETDRK4", dt=2.5e-3, f0=1.0, beta=5.0,
                H=[0.2, 0.3, 0.5], b=[-1.0, -1.2, -1.2 - 0.5 / 5.5], U=[1.0, 0.5, 0.0], mu=0.05)
+# the decaying 128^2 run (nu = 0, FilteredRK4 dt = 0.005, from the peaked isotropic state)
+DECAY128 = dict(module="TwoDNavierStokes", nx=128, ny=128, stepper="FilteredRK4", dt=0.005)
 # gradient of the final kinetic energy: SingleLayerQG 256^2, deformation radius 0.35,
 # topography |k| <= 8 amplitude 0.1, ETDRK4 dt = 0.01, 500 steps, checkpoint every 25
 ADJOINT256 = dict(module="SingleLayerQG", nx=256, ny=256, stepper="ETDRK4", dt=0.01, ell=0.35, nsteps=500, every=25)
@@ -221,17 +223,35 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0}, "fallback"
 
 
-def ncu_traffic(kernel, workload):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary of `workload`
-    (profiles/<kernel>_<workload>.md, line 'traffic_bytes_per_launch: B'), else None."""
+def ncu_figure(kernel, workload, key):
+    """A per-launch figure of `kernel` from the committed ncu summary of `workload`
+    (profiles/<kernel>_<workload>.md, line '<key>: value'), else None."""
     path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
     try:
         for line in open(path):
-            if line.startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":", 1)[1])
-    except OSError:
+            if line.startswith(key + ":"):
+                return float(line.split(":", 1)[1].split()[0])
+    except (OSError, ValueError, IndexError):
         pass
     return None
+
+
+def ncu_traffic(kernel, workload):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from ncu."""
+    return ncu_figure(kernel, workload, "traffic_bytes_per_launch")
+
+
+def compute_roofline(roof, workload):
+    """Issue-rate roofline of a kernel whose arithmetic, not memory, bounds it (df64): the
+    fraction of the SM's instruction-issue slots and of the FMA pipe's cycles it uses (ncu,
+    committed summary), and the HBM fraction it would reach at the full issue rate."""
+    issue = ncu_figure(roof["kernel"], workload, "issue_active_frac")
+    fma = ncu_figure(roof["kernel"], workload, "fma_pipe_active_frac")
+    if issue is None:
+        return None
+    return {"kernel": roof["kernel"], "bound": "issue", "issue_active": issue, "fma_pipe_active": fma,
+            "hbm_frac": roof["frac"], "hbm_frac_at_full_issue": roof["frac"] / issue,
+            "source": f"ncu --set full, profiles/{roof['kernel']}_{workload}.md"}
 
 
 def make_problem(w, T, precision=None):
@@ -714,6 +734,7 @@ def run_ours(args):
     merr = relerr(m32["sol"], mdf["sol"])
     cpu = cpu_baseline(w)
     c1p, c2p = points(SLQG512), points(MLQG1024X3)
+    rf_df = roofline(w, rdf, 16, "twodns2048_df64", peaks, peak_src)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -740,7 +761,8 @@ def run_ours(args):
         "fp32_vs_fp64_rel_l2_100_steps": acc["fp32_vs_fp64"],
         "fp64_plain": {"arithmetic": "df64 (double-float pairs, 48-bit significand, FP32 pipes)", "value": vdf,
                        "ms_per_step": msdf, "ms_per_step_graph": rdf["ms_per_step_graph"],
-                       "roofline": roofline(w, rdf, 16, "twodns2048_df64", peaks, peak_src),
+                       "roofline": rf_df,
+                       "compute_roofline": compute_roofline(rf_df, "twodns2048_df64"),
                        "roofline_step_two_sweep": step_roofline(w, msdf, 8, peaks),
                        "e2e": {"value": whole_job(pts, world, e2e_df), "unit": UNIT},
                        "rel_l2_vs_ieee_fp64": dferr},
@@ -789,6 +811,12 @@ def run_ours(args):
                             "fp32": adj32, "fp64": adj64,
                             "adjoint_over_forward_definition": "(gf_grad time - forward time) / forward time: the "
                             "reverse sweep (segment recomputation + transposed stages) per forward step"},
+        # the same figures at the top level of the line (the small decaying run and the adjoint)
+        "ms_per_step_twodns128_fp64": dec128["fp64"]["ms_per_step"],
+        "ms_per_step_twodns128_df64": dec128["df64"]["ms_per_step"],
+        "speedup_twodns128_fp64_vs_cpu": dec128.get("speedup_fp64_vs_cpu"),
+        "adjoint_grad_over_forward_fp32": adj32["grad_over_forward"],
+        "adjoint_grad_over_forward_fp64": adj64["grad_over_forward"],
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -799,7 +827,8 @@ SINGLE = {"twodns2048_fp32": (HEADLINE, np.float32, None), "twodns2048_fp64": (H
           "slqg512_fp64": (SLQG512, np.float64, None), "slqg512_df64": (SLQG512, np.float64, "DF64"),
           "mlqg1024x3_fp32": (MLQG1024X3, np.float32, None), "mlqg1024x3_df64": (MLQG1024X3, np.float64, "DF64"),
           "ensemble1536_fp32": (ENSEMBLE, np.float32, None), "adjoint256_fp32": (ADJOINT256, np.float32, None),
-          "adjoint256_fp64": (ADJOINT256, np.float64, None)}
+          "adjoint256_fp64": (ADJOINT256, np.float64, None), "twodns128_fp64": (DECAY128, np.float64, None),
+          "twodns128_df64": (DECAY128, np.float64, "DF64")}
 
 
 def run_single(args):
