@@ -1,6 +1,7 @@
-// Adjoint (reverse mode) of the fused ETDRK4 / FilteredETDRK4 step of SingleLayerQG and
-// TwoDNavierStokes (one layer, constant U): the transpose of the discrete step that
-// gf_kernels.cuh computes, stage by stage in reverse, with the same two-kernel structure.
+// Adjoint (reverse mode) of the fused ETDRK4 / FilteredETDRK4 and RK4 / FilteredRK4 steps of
+// SingleLayerQG and TwoDNavierStokes (one layer, constant U): the transpose of the discrete
+// step that gf_kernels.cuh computes, stage by stage in reverse, with the same two-kernel
+// structure (the stage combinations in adj_stage_combine).
 //
 // Forward calcN! at a dealiased stage input X (src/singlelayerqg.jl:356-382, 443-451):
 //   psi = f X, u = irfft(-i l psi), v = irfft(i kr psi), q = irfft(X), qe = q + eta,
@@ -33,6 +34,82 @@ __device__ __forceinline__ cplx<T> mulcj(const void* p, size_t i, cplx<T> x, int
   return mk<T>(c.x * x.x + c.y * x.y, c.x * x.y - c.y * x.x);
 }
 
+// The transposed stage combination at element ti (kr < nkr; keep: a kept mode) given
+// xj = J^T Nbar of this stage's calcN! (zero where not kept): updates the accumulators and
+// returns the Nbar of the next (earlier) stage -- or, at stage 5, of stage 4 from ubar_in.
+// RK4 (a.rk4): RHS_s = N(X_s) + L X_s, so Xbar_s = xj + conj(L) Rbar_s; with ub the filtered
+// cotangent of the step's result and Y_s = M Xbar_s:
+//   stage 5: Rbar4 = dt/6 ub
+//   stage 4: x1acc = ub + Y4;  Rbar3 = dt/3 ub + dt Y4
+//   stage 3: x1acc += Y3;      Rbar2 = dt/3 ub + dt/2 Y3
+//   stage 2: x1acc += Y2;      Rbar1 = dt/6 ub + dt/2 Y2
+//   stage 1: ubar_n = M (x1acc + xj + conj(L) Rbar1)
+// (n1acc holds the current Rbar).  ETDRK4: the combination in the header comment.
+template <class T>
+__device__ __forceinline__ cplx<T> adj_stage_combine(const AdjArgs& a, size_t ti, bool keep, cplx<T> xj) {
+  const int cx = a.cplx;
+  cplx<T>* ub = static_cast<cplx<T>*>(a.ub);
+  cplx<T>* n1 = static_cast<cplx<T>*>(a.n1acc);
+  cplx<T>* x1 = static_cast<cplx<T>*>(a.x1acc);
+  if (a.rk4) {
+    const T dt = sel<T>(a.dt, a.dt_f, a.dt_l);
+    auto start = [&](cplx<T> u) {  // cotangent of a step's result -> stage-4 Rbar
+      const cplx<T> v = a.filtered ? static_cast<const T*>(a.filt)[ti] * u : u;
+      ub[ti] = v;
+      const cplx<T> r = (dt / T(6)) * v;
+      n1[ti] = r;
+      return r;
+    };
+    auto lt = [&](cplx<T> r) { return a.L ? mulcj<T>(a.L, ti, r, cx) : czero<T>(); };
+    if (a.stage == 5) return start(static_cast<const cplx<T>*>(a.ubar_in)[ti]);
+    if (a.stage == 1) {
+      const cplx<T> un = keep ? x1[ti] + xj + lt(n1[ti]) : czero<T>();
+      static_cast<cplx<T>*>(a.ubar_out)[ti] = un;
+      return a.head ? start(un) : czero<T>();
+    }
+    const cplx<T> u = ub[ti];
+    const cplx<T> y = keep ? xj + lt(n1[ti]) : czero<T>();
+    cplx<T> r;
+    if (a.stage == 4) {
+      x1[ti] = u + y;
+      r = (dt / T(3)) * u + dt * y;
+    } else if (a.stage == 3) {
+      x1[ti] = x1[ti] + y;
+      r = (dt / T(3)) * u + (dt / T(2)) * y;
+    } else {
+      x1[ti] = x1[ti] + y;
+      r = (dt / T(6)) * u + (dt / T(2)) * y;
+    }
+    n1[ti] = r;
+    return r;
+  }
+  auto start = [&](cplx<T> u) {  // cotangent of a step's result -> stage-4 Nbar
+    const cplx<T> v = a.filtered ? static_cast<const T*>(a.filt)[ti] * u : u;
+    ub[ti] = v;
+    return mulcj<T>(a.gamma, ti, v, cx);
+  };
+  if (a.stage == 5) return start(static_cast<const cplx<T>*>(a.ubar_in)[ti]);
+  if (a.stage == 4) {
+    const cplx<T> u = ub[ti];
+    n1[ti] = mulcj<T>(a.alpha, ti, u, cx) - mulcj<T>(a.zeta, ti, xj, cx);
+    static_cast<cplx<T>*>(a.xaacc)[ti] = mulcj<T>(a.e2, ti, xj, cx);
+    return T(2) * mulcj<T>(a.beta, ti, u, cx) + T(2) * mulcj<T>(a.zeta, ti, xj, cx);
+  }
+  if (a.stage == 3) {
+    const cplx<T> u = ub[ti];
+    x1[ti] = mulcj<T>(a.e, ti, u, cx) + mulcj<T>(a.e2, ti, xj, cx);
+    return T(2) * mulcj<T>(a.beta, ti, u, cx) + mulcj<T>(a.zeta, ti, xj, cx);
+  }
+  if (a.stage == 2) {
+    const cplx<T> Ab = keep ? static_cast<const cplx<T>*>(a.xaacc)[ti] + xj : czero<T>();
+    x1[ti] = x1[ti] + mulcj<T>(a.e2, ti, Ab, cx);
+    return n1[ti] + mulcj<T>(a.zeta, ti, Ab, cx);
+  }
+  const cplx<T> un = keep ? x1[ti] + xj : czero<T>();  // stage 1
+  static_cast<cplx<T>*>(a.ubar_out)[ti] = un;
+  return a.head ? start(un) : czero<T>();
+}
+
 // Column kernel: y-direction FFT of the three adjoint products of stage a.stage (kr < kcut),
 // the transposed stage combination, and the y-direction inverse FFT of the next cotangent's
 // (i kr Nbar / w, i l Nbar / w) into Wb (all kr).  a.stage = 5: head only (start of a step
@@ -56,7 +133,6 @@ __global__ void __launch_bounds__(512, 1) adj_col_kernel(Geom g, ModArgs m, AdjA
   const bool edge = (kr == 0) || (2 * kr == g.nx);
   const T scale_in = edge ? inv_n : T(2) * inv_n;  // irfft^T: w / (nx ny)
   const T scale_out = edge ? T(1) : T(0.5);       // rfft^T via the c2r path: 1 / w
-  const int cx = a.cplx;
 
   // 1) Xbar of this stage: y-FFT of (qbar, ubar, vbar), combined and masked
   cplx<T> xj[R];
@@ -97,37 +173,7 @@ __global__ void __launch_bounds__(512, 1) adj_col_kernel(Geom g, ModArgs m, AdjA
 #pragma unroll
   for (int i = 0; i < R; ++i) {
     const int j = t + i * TPF;
-    nb[i] = czero<T>();
-    if (!kin) continue;
-    const size_t ti = (size_t)j * g.ldk + kr;
-    const bool keep = kept(g, kr, j);
-    cplx<T>* ub = static_cast<cplx<T>*>(a.ub);
-    auto start = [&](cplx<T> u) {  // cotangent of a step's result -> stage-4 Nbar
-      const cplx<T> v = a.filtered ? static_cast<const T*>(a.filt)[ti] * u : u;
-      ub[ti] = v;
-      return mulcj<T>(a.gamma, ti, v, cx);
-    };
-    if (a.stage == 5) {
-      nb[i] = start(static_cast<const cplx<T>*>(a.ubar_in)[ti]);
-    } else if (a.stage == 4) {
-      const cplx<T> u = ub[ti], Cb = xj[i];
-      nb[i] = T(2) * mulcj<T>(a.beta, ti, u, cx) + T(2) * mulcj<T>(a.zeta, ti, Cb, cx);
-      static_cast<cplx<T>*>(a.n1acc)[ti] = mulcj<T>(a.alpha, ti, u, cx) - mulcj<T>(a.zeta, ti, Cb, cx);
-      static_cast<cplx<T>*>(a.xaacc)[ti] = mulcj<T>(a.e2, ti, Cb, cx);
-    } else if (a.stage == 3) {
-      const cplx<T> u = ub[ti], Bb = xj[i];
-      static_cast<cplx<T>*>(a.x1acc)[ti] = mulcj<T>(a.e, ti, u, cx) + mulcj<T>(a.e2, ti, Bb, cx);
-      nb[i] = T(2) * mulcj<T>(a.beta, ti, u, cx) + mulcj<T>(a.zeta, ti, Bb, cx);
-    } else if (a.stage == 2) {
-      const cplx<T> Ab = keep ? static_cast<const cplx<T>*>(a.xaacc)[ti] + xj[i] : czero<T>();
-      cplx<T>* x1 = static_cast<cplx<T>*>(a.x1acc);
-      x1[ti] = x1[ti] + mulcj<T>(a.e2, ti, Ab, cx);
-      nb[i] = static_cast<const cplx<T>*>(a.n1acc)[ti] + mulcj<T>(a.zeta, ti, Ab, cx);
-    } else {  // stage 1
-      const cplx<T> un = keep ? static_cast<const cplx<T>*>(a.x1acc)[ti] + xj[i] : czero<T>();
-      static_cast<cplx<T>*>(a.ubar_out)[ti] = un;
-      if (a.head) nb[i] = start(un);
-    }
+    nb[i] = kin ? adj_stage_combine<T>(a, (size_t)j * g.ldk + kr, kept(g, kr, j), xj[i]) : czero<T>();
   }
   if (a.stage == 1 && !a.head) out_w = false;
   if (!out_w) return;

@@ -2168,7 +2168,8 @@ extern "C" int gf_step_output(gf_ctx* c, int64_t nsteps, int32_t every, const in
 
 // ------------------------------------------------------------------------------- adjoint
 // Reverse-mode derivative of stepforward!(prob, nsteps) for TwoDNavierStokes and
-// SingleLayerQG (constant U) with ETDRK4 / FilteredETDRK4 (the kernels are in gf_adjoint.cuh).
+// SingleLayerQG (constant U) with ETDRK4 / FilteredETDRK4 or RK4 / FilteredRK4 (the kernels
+// are in gf_adjoint.cuh).
 // Checkpointing: the forward pass stores the state every `every` steps; the reverse pass
 // recomputes one segment at a time from its checkpoint with the fused forward kernels,
 // keeping the physical fields (q + eta, u, v) of all its stages, then runs the transposed
@@ -2179,7 +2180,8 @@ static int adj_check(gf_ctx* c) {
   if (c->g.rtx || c->g.rty) return fail(c, GF_ERR_UNSUPPORTED, "the adjoint needs power-of-two nx, ny in [32, 2048]");
   if (mod != GF_TWODNAVIERSTOKES && mod != GF_SINGLELAYERQG)
     return fail(c, GF_ERR_UNSUPPORTED, "the adjoint covers TwoDNavierStokes and SingleLayerQG");
-  if (c->kind != SK_ETDRK4) return fail(c, GF_ERR_UNSUPPORTED, "the adjoint follows the ETDRK4 / FilteredETDRK4 stages");
+  if (c->kind != SK_ETDRK4 && c->kind != SK_RK4)
+    return fail(c, GF_ERR_UNSUPPORTED, "the adjoint follows the ETDRK4 / FilteredETDRK4 and RK4 / FilteredRK4 stages");
   if (c->g.nb != 1) return fail(c, GF_ERR_UNSUPPORTED, "the adjoint runs one instance (batch = 1)");
   if (c->m.U1D || c->m.hasC || c->m.linear) return fail(c, GF_ERR_UNSUPPORTED, "the adjoint supports a constant U");
   return GF_OK;
@@ -2357,6 +2359,10 @@ static AdjArgs adj_args(gf_ctx* c) {
   a.ubar_in = d.ubar_in; a.ubar_out = d.ubar_out; a.Wb = d.Wb; a.Pb = d.Pb; a.etab = d.etab;
   a.U = (c->cfg.module == GF_SINGLELAYERQG) ? c->cfg.U : 0.0;
   split_hl(a.U, &a.U_f, &a.U_l);
+  a.rk4 = c->kind == SK_RK4;
+  a.L = (c->kind == SK_RK4 && c->hasL) ? c->Ltab : nullptr;
+  a.dt = c->cfg.dt;
+  split_hl(a.dt, &a.dt_f, &a.dt_l);
   return a;
 }
 

@@ -213,7 +213,7 @@ __device__ __forceinline__ int swz(int a) {
   else return a ^ ((a >> 3) & 7);
 }
 // Threads per 128-byte shared-memory wavefront for T's complex element.
-template <class T> constexpr int wave_threads() { return 128 / (int)sizeof(cplx<T>); }
+template <class T> __host__ __device__ constexpr int wave_threads() { return 128 / (int)sizeof(cplx<T>); }
 
 // One radix pass of a length-N Stockham FFT on a swizzled shared-memory buffer.  Threads t in
 // [0, N/R) each do R/Rp butterflies of radix Rp = min(R, N/Ns).  The caller must have

@@ -235,7 +235,6 @@ __global__ void __launch_bounds__(FP_MAXT)
   const T dky = sel<T>(g.dky, g.dky_f, g.dky_l), dkx = sel<T>(g.dkx, g.dkx_f, g.dkx_l);
   const T ell2 = sel<T>(m.ell_inv2, m.ell_inv2_f, m.ell_inv2_l);
   const T inv_n = sel<T>(g.inv_nxny, g.inv_nxny_f, g.inv_nxny_l);
-  const int cx = a.cplx;
   const bool fwd = a.stage <= 4 && bx * C < g.kcut;
   if (fwd) {
     const cplx<T>* P = static_cast<const cplx<T>*>(a.Pb);
@@ -248,7 +247,6 @@ __global__ void __launch_bounds__(FP_MAXT)
     fft_smem<T, NY, R, -1>(F0 + (size_t)cf * cs, tf, tw);
   }
   const bool out_w = !(a.stage == 1 && !a.head);
-  cplx<T>* ub = static_cast<cplx<T>*>(a.ub);
   for (int e = tid; e < CN; e += NT) {
     const int c = e % C, j = e / C, kr = bx * C + c;
     const bool kin = kr < g.nkr;
@@ -267,35 +265,8 @@ __global__ void __launch_bounds__(FP_MAXT)
                     Vb = F0[(size_t)(2 * C + c) * cs + swz<T>(j)];
       xj = scale_in * (Q + f * (lv * mul_i(Ub) - krT * mul_i(Vb)));
     }
-    cplx<T> nb = czero<T>();
-    if (kin) {  // transposed stage combination -> the next cotangent
-      auto start = [&](cplx<T> u) {
-        const cplx<T> v = a.filtered ? static_cast<const T*>(a.filt)[ti] * u : u;
-        ub[ti] = v;
-        return mulcj<T>(a.gamma, ti, v, cx);
-      };
-      if (a.stage == 5) {
-        nb = start(static_cast<const cplx<T>*>(a.ubar_in)[ti]);
-      } else if (a.stage == 4) {
-        const cplx<T> u = ub[ti];
-        nb = T(2) * mulcj<T>(a.beta, ti, u, cx) + T(2) * mulcj<T>(a.zeta, ti, xj, cx);
-        static_cast<cplx<T>*>(a.n1acc)[ti] = mulcj<T>(a.alpha, ti, u, cx) - mulcj<T>(a.zeta, ti, xj, cx);
-        static_cast<cplx<T>*>(a.xaacc)[ti] = mulcj<T>(a.e2, ti, xj, cx);
-      } else if (a.stage == 3) {
-        const cplx<T> u = ub[ti];
-        static_cast<cplx<T>*>(a.x1acc)[ti] = mulcj<T>(a.e, ti, u, cx) + mulcj<T>(a.e2, ti, xj, cx);
-        nb = T(2) * mulcj<T>(a.beta, ti, u, cx) + mulcj<T>(a.zeta, ti, xj, cx);
-      } else if (a.stage == 2) {
-        const cplx<T> Ab = keep ? static_cast<const cplx<T>*>(a.xaacc)[ti] + xj : czero<T>();
-        cplx<T>* x1 = static_cast<cplx<T>*>(a.x1acc);
-        x1[ti] = x1[ti] + mulcj<T>(a.e2, ti, Ab, cx);
-        nb = static_cast<const cplx<T>*>(a.n1acc)[ti] + mulcj<T>(a.zeta, ti, Ab, cx);
-      } else {  // stage 1
-        const cplx<T> un = keep ? static_cast<const cplx<T>*>(a.x1acc)[ti] + xj : czero<T>();
-        static_cast<cplx<T>*>(a.ubar_out)[ti] = un;
-        if (a.head) nb = start(un);
-      }
-    }
+    // transposed stage combination -> the next cotangent
+    const cplx<T> nb = kin ? adj_stage_combine<T>(a, ti, keep, xj) : czero<T>();
     if (out_w) {
       F0[(size_t)c * cs + swz<T>(j)] = (scale_out * krT) * mul_i(nb);
       F0[(size_t)(C + c) * cs + swz<T>(j)] = (scale_out * (T(lidx(g, j)) * dky)) * mul_i(nb);

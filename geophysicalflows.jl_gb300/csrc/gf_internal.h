@@ -157,6 +157,10 @@ struct AdjArgs {
   const void* phys;                   // forward (q + eta, u, v) of the stage, [3][j][nx]
   void* etab;                         // [j][nx] cotangent of eta
   double U; float U_f, U_l;
+  // RK4 / FilteredRK4: the linear operator L ([j][kr], null when the step has none) and dt
+  int rk4;
+  const void* L;
+  double dt; float dt_f, dt_l;
 };
 
 // Generic transforms (updatevars!, set_*!, fwdtransform!/invtransform!).

@@ -1,5 +1,5 @@
 """Oracle (test infrastructure only): FP64 tangent-linear and adjoint of the SingleLayerQG
-ETDRK4 / FilteredETDRK4 step, and the gradient of a final-time kinetic energy with respect to
+ETDRK4 / FilteredETDRK4 and RK4 / FilteredRK4 steps, and the gradient of a final-time kinetic energy with respect to
 the initial PV q0 and the topographic PV eta.
 
 It differentiates the DISCRETE step of the restatement in gf_oracle.py exactly:
@@ -7,9 +7,10 @@ It differentiates the DISCRETE step of the restatement in gf_oracle.py exactly:
     psi_hat = f q_hat (f = -1/K^2 or -1/(K^2 + 1/l^2), src/singlelayerqg.jl:484-490),
     u_hat = -i l psi_hat, v_hat = i kr psi_hat, q,u,v = irfft2(.), qe = q + eta,
     N = -i kr rfft2(u qe) - i l rfft2(v qe) - i kr U eta_hat;
-  * the FourierFlows ETDRK4 stage sequence (restated in gf_oracle.TimeStepper.step), in which
-    every calcN! dealiases its input array in place, so that later uses of that array see the
-    dealiased values.
+  * the FourierFlows ETDRK4 and RK4 stage sequences (restated in gf_oracle.TimeStepper.step),
+    in which every calcN! dealiases its input array in place, so that later uses of that array
+    see the dealiased values (RK4: RHS_s = N(X_s) + L X_s at X_s = M(X1 + c_s dt RHS_{s-1}),
+    X1 = M u, new = X1 + dt (RHS1/6 + RHS2/3 + RHS3/3 + RHS4/6)).
 Inner products: spectral arrays are real vectors of (Re, Im) pairs over the STORED half
 spectrum, <a, b> = Re sum conj(a) b; physical arrays the plain sum.  With them
   rfft2^T(X) = Re(nx ny ifft2(X placed in the half plane, zero elsewhere)),
@@ -43,22 +44,26 @@ def irfft2_T(x, grid):
 
 
 class SLQGAdjoint:
-    """Tangent-linear and adjoint of an oracle SingleLayerQG problem stepped with ETDRK4 or
-    FilteredETDRK4 (constant U; additive forcing does not change the derivative)."""
+    """Tangent-linear and adjoint of an oracle SingleLayerQG problem stepped with ETDRK4,
+    FilteredETDRK4, RK4 or FilteredRK4 (constant U; additive forcing does not change the
+    derivative)."""
 
     def __init__(self, prob):
         if not prob.U_is_number:
             raise NotImplementedError("the adjoint supports a constant U")
         ts = prob.timestepper
-        if ts.kind != "ETDRK4":
-            raise NotImplementedError("the adjoint follows the ETDRK4 stages")
+        if ts.kind not in ("ETDRK4", "RK4"):
+            raise NotImplementedError("the adjoint follows the ETDRK4 and RK4 stages")
+        self.kind = ts.kind
+        self.L, self.dt = prob.L, prob.clock.dt
         self.p, self.g = prob, prob.grid
         g = self.g
         self.f = (-g.invKrsq if prob.ell is None else -1.0 / (g.Krsq + 1.0 / prob.ell ** 2))
         self.mask = np.ones((g.ny, g.nkr))
         O.dealias(self.mask, g)
         self.filter = ts.filter if getattr(ts, "filtered", False) else None
-        self.c = dict(e=ts.expLdt, e2=ts.expLdt2, z=ts.zeta, a=ts.alpha, b=ts.beta, g=ts.gamma)
+        if ts.kind == "ETDRK4":
+            self.c = dict(e=ts.expLdt, e2=ts.expLdt2, z=ts.zeta, a=ts.alpha, b=ts.beta, g=ts.gamma)
 
     # -- calcN! without its dealias (the input is already dealiased) and its derivatives
     def _fields(self, X):
@@ -94,8 +99,63 @@ class SLQGAdjoint:
         Xbar = irfft2_T(qbar, g) + self.f * (1j * g.l * ub - 1j * g.kr * vb)
         return Xbar, etabar
 
+    # -- RK4 (src: FourierFlows RK4 restated in gf_oracle.TimeStepper.step)
+    def _rk4_step(self, u, eta):
+        L, dt, M = self.L, self.dt, self.mask
+        X1 = M * u
+        R1 = self.N(X1, eta) + L * X1
+        X2 = M * (X1 + dt / 2 * R1)
+        R2 = self.N(X2, eta) + L * X2
+        X3 = M * (X1 + dt / 2 * R2)
+        R3 = self.N(X3, eta) + L * X3
+        X4 = M * (X1 + dt * R3)
+        R4 = self.N(X4, eta) + L * X4
+        new = X1 + dt * (R1 / 6 + R2 / 3 + R3 / 3 + R4 / 6)
+        if self.filter is not None:
+            new = self.filter * new
+        return new, (X1, X2, X3, X4)
+
+    def _rk4_tlm(self, u, eta, du, deta):
+        L, dt, M = self.L, self.dt, self.mask
+        X1, X2, X3, X4 = self._rk4_step(u, eta)[1]
+        dX1 = M * du
+        dR1 = self.N_tlm(X1, eta, dX1, deta) + L * dX1
+        dX2 = M * (dX1 + dt / 2 * dR1)
+        dR2 = self.N_tlm(X2, eta, dX2, deta) + L * dX2
+        dX3 = M * (dX1 + dt / 2 * dR2)
+        dR3 = self.N_tlm(X3, eta, dX3, deta) + L * dX3
+        dX4 = M * (dX1 + dt * dR3)
+        dR4 = self.N_tlm(X4, eta, dX4, deta) + L * dX4
+        dnew = dX1 + dt * (dR1 / 6 + dR2 / 3 + dR3 / 3 + dR4 / 6)
+        if self.filter is not None:
+            dnew = self.filter * dnew
+        return dnew
+
+    def _rk4_adj(self, u, eta, ubar_new):
+        """the RK4 stages in reverse: Rbar_s is the cotangent of RHS_s, Y_s = M Xbar_s"""
+        cL, dt, M = np.conj(self.L), self.dt, self.mask
+        X1, X2, X3, X4 = self._rk4_step(u, eta)[1]
+        ub = self.filter * ubar_new if self.filter is not None else ubar_new
+        R4b = dt / 6 * ub
+        Xb, eb4 = self.N_adj(X4, eta, R4b)
+        Y = M * (Xb + cL * R4b)
+        X1b = ub + Y
+        R3b = dt / 3 * ub + dt * Y
+        Xb, eb3 = self.N_adj(X3, eta, R3b)
+        Y = M * (Xb + cL * R3b)
+        X1b = X1b + Y
+        R2b = dt / 3 * ub + dt / 2 * Y
+        Xb, eb2 = self.N_adj(X2, eta, R2b)
+        Y = M * (Xb + cL * R2b)
+        X1b = X1b + Y
+        R1b = dt / 6 * ub + dt / 2 * Y
+        Xb, eb1 = self.N_adj(X1, eta, R1b)
+        return M * (X1b + Xb + cL * R1b), eb1 + eb2 + eb3 + eb4
+
     # -- one step: forward, tangent-linear, adjoint
     def step(self, u, eta):
+        if self.kind == "RK4":
+            return self._rk4_step(u, eta)
         c, M = self.c, self.mask
         X1 = M * u
         N1 = self.N(X1, eta)
@@ -111,6 +171,8 @@ class SLQGAdjoint:
         return new, (X1, XA, XB, XC)
 
     def step_tlm(self, u, eta, du, deta):
+        if self.kind == "RK4":
+            return self._rk4_tlm(u, eta, du, deta)
         c, M = self.c, self.mask
         (X1, XA, XB, XC) = self.step(u, eta)[1]
         dX1 = M * du
@@ -128,6 +190,8 @@ class SLQGAdjoint:
 
     def step_adj(self, u, eta, ubar_new):
         """(ubar, etabar contribution) of one step, the stages taken in reverse."""
+        if self.kind == "RK4":
+            return self._rk4_adj(u, eta, ubar_new)
         c, M = self.c, self.mask
         cj = {k: np.conj(v) for k, v in c.items()}
         X1, XA, XB, XC = self.step(u, eta)[1]

@@ -1,4 +1,4 @@
-"""GPU adjoint of the ETDRK4 step (gf_adjoint_* / gf_grad) against the oracle's discrete
+"""GPU adjoint of the ETDRK4 and RK4 steps (gf_adjoint_* / gf_grad) against the oracle's discrete
 adjoint (oracle/gf_adjoint.py, itself pinned by finite differences and the tangent-linear
 dot-product identity), against central finite differences of the GPU forward model, and for
 checkpoint-interval invariance."""
@@ -35,7 +35,8 @@ def gpu_grad(kw, q0, nsteps, every, T=np.float64, precision=None):
 
 
 @pytest.mark.parametrize("stepper,U,beta,ell", [("ETDRK4", 0.2, 1.0, 0.35), ("FilteredETDRK4", 0.0, 0.0, 0.35),
-                                                ("ETDRK4", 0.3, 2.0, np.inf)])
+                                                ("ETDRK4", 0.3, 2.0, np.inf), ("RK4", 0.2, 1.0, 0.35),
+                                                ("FilteredRK4", 0.0, 2.0, np.inf)])
 def test_gradient_matches_oracle_adjoint(stepper, U, beta, ell):
     n, ns = 64, 12
     kw, q0, eta = slqg_case(n, stepper, U, beta, ell)
@@ -47,10 +48,11 @@ def test_gradient_matches_oracle_adjoint(stepper, U, beta, ell):
     assert rel(deta, ge) <= 1e-11
 
 
+@pytest.mark.parametrize("stepper", ["ETDRK4", "FilteredRK4"])
 @pytest.mark.parametrize("prec,T,tol", [("DF64", np.float64, 1e-10), (None, np.float32, 2e-4)])
-def test_gradient_other_precisions(prec, T, tol):
+def test_gradient_other_precisions(prec, T, tol, stepper):
     n, ns = 64, 12
-    kw, q0, eta = slqg_case(n)
+    kw, q0, eta = slqg_case(n, stepper)
     p, loss, dq0, deta = gpu_grad(kw, q0, ns, 4, T=T, precision=prec)
     L, gq, ge = AD.SLQGAdjoint(O.SingleLayerQG(**kw)).gradient(q0, eta, ns)
     assert abs(loss - L) <= max(tol, 1e-12) * L
@@ -113,8 +115,8 @@ def test_pullback_matches_oracle_step_adjoint():
     assert rel(p.sol, us[-1]) <= 1e-12
 
 
-def _fd_check(n, ns, every, ndir, seed, richardson=False):
-    kw, q0, eta = slqg_case(n, "ETDRK4", U=0.0, beta=0.0, ell=0.35)
+def _fd_check(n, ns, every, ndir, seed, richardson=False, stepper="ETDRK4"):
+    kw, q0, eta = slqg_case(n, stepper, U=0.0, beta=0.0, ell=0.35)
     _, loss, dq0, deta = gpu_grad(kw, q0, ns, every)
     rng = np.random.default_rng(seed)
 
@@ -153,6 +155,46 @@ def _fd_check(n, ns, every, ndir, seed, richardson=False):
 
 def test_central_differences_small():
     _fd_check(64, 20, 5, 4, 1)
+
+
+def test_central_differences_small_filtered_rk4():
+    _fd_check(64, 20, 5, 4, 2, stepper="FilteredRK4")
+
+
+@pytest.mark.parametrize("stepper", ["ETDRK4", "RK4"])
+def test_classic_and_field_parallel_adjoint_kernels_agree(stepper):
+    """the classic adjoint kernels (an explicit launch shape) and the field-parallel ones
+    (the default at 64^2) give the same gradient to rounding, and both match the oracle"""
+    n, ns = 64, 10
+    kw, q0, eta = slqg_case(n, stepper)
+    res = []
+    for classic in (True, False):
+        p = SL.Problem("GPU", **kw)
+        if classic:
+            p.launch_shape = (8, 1, 8, 1)
+        SL.set_q(p, q0)
+        res.append(adjoint.grad(p, ns, checkpoint_every=4))
+        p.close()
+    (l0, g0, e0), (l1, g1, e1) = res
+    assert abs(l1 - l0) <= 1e-13 * l0 and rel(g1, g0) <= 1e-12 and rel(e1, e0) <= 1e-12
+    L, gq, ge = AD.SLQGAdjoint(O.SingleLayerQG(**kw)).gradient(q0, eta, ns)
+    assert rel(g0, gq) <= 1e-11 and rel(e0, ge) <= 1e-11
+
+
+def test_twodns_filtered_rk4_gradient():
+    """TwoDNavierStokes with FilteredRK4 (the decaying run's stepper) and viscosity: the
+    gradient of the final kinetic energy against the oracle's discrete adjoint"""
+    n, ns = 64, 12
+    g = O.Grid(n)
+    z0 = O.peakedisotropicspectrum(g, 6, 0.5, seed=5)
+    kw = dict(nx=n, dt=0.005, nu=1e-3, nnu=1, stepper="FilteredRK4")
+    p = TD.Problem("GPU", T=np.float64, **kw)
+    TD.set_zeta(p, z0)
+    loss, dq0, deta = adjoint.grad(p, ns, checkpoint_every=5)
+    assert deta is None
+    r = O.SingleLayerQG(nx=n, dt=0.005, nu=1e-3, nnu=1, stepper="FilteredRK4")
+    L, gq, _ = AD.SLQGAdjoint(r).gradient(z0, np.zeros((n, n)), ns)
+    assert abs(loss - L) <= 1e-13 * L and rel(dq0, gq) <= 1e-11
 
 
 def test_adjoint_slqg256_central_differences_8_directions():

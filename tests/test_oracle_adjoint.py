@@ -1,4 +1,4 @@
-"""The oracle's tangent-linear and adjoint SingleLayerQG ETDRK4 step (oracle/gf_adjoint.py):
+"""The oracle's tangent-linear and adjoint SingleLayerQG ETDRK4 and RK4 steps (oracle/gf_adjoint.py):
 its forward pass is the oracle's stepforward!, its gradients of the final kinetic energy with
 respect to q0 and the topography match central finite differences (eps = 1e-6) along seeded
 directions, and adjoint and tangent-linear satisfy the dot-product identity."""
@@ -18,8 +18,11 @@ def setup(n, stepper, ell=0.35, U=0.0, beta=0.0, nsteps=12):
     return p, AD.SLQGAdjoint(p), q0, eta, kw
 
 
-@pytest.mark.parametrize("stepper,ell,U,beta", [("ETDRK4", 0.35, 0.0, 0.0), ("ETDRK4", np.inf, 0.3, 2.0),
-                                                ("FilteredETDRK4", 0.35, 0.1, 1.0)])
+CASES = [("ETDRK4", 0.35, 0.0, 0.0), ("ETDRK4", np.inf, 0.3, 2.0), ("FilteredETDRK4", 0.35, 0.1, 1.0),
+         ("RK4", 0.35, 0.2, 1.0), ("FilteredRK4", np.inf, 0.0, 2.0)]
+
+
+@pytest.mark.parametrize("stepper,ell,U,beta", CASES)
 def test_adjoint_forward_is_stepforward(stepper, ell, U, beta):
     p, A, q0, eta, kw = setup(32, stepper, ell, U, beta)
     p.set_q(q0)
@@ -27,8 +30,7 @@ def test_adjoint_forward_is_stepforward(stepper, ell, U, beta):
     assert A.loss(q0, eta, 12) == pytest.approx(p.kinetic_energy(), rel=1e-14)
 
 
-@pytest.mark.parametrize("stepper,ell,U,beta", [("ETDRK4", 0.35, 0.0, 0.0), ("ETDRK4", np.inf, 0.3, 2.0),
-                                                ("FilteredETDRK4", 0.35, 0.1, 1.0)])
+@pytest.mark.parametrize("stepper,ell,U,beta", CASES)
 def test_gradient_matches_central_differences(stepper, ell, U, beta):
     """the SingleLayerQG 256^2 adjoint check in miniature: 8 seeded directions, eps = 1e-6, 1e-6 relative"""
     p, A, q0, eta, kw = setup(32, stepper, ell, U, beta)
@@ -43,8 +45,9 @@ def test_gradient_matches_central_differences(stepper, ell, U, beta):
         assert abs(fd - ad) <= 1e-6 * abs(ad)
 
 
-def test_dot_product_identity():
-    p, A, q0, eta, kw = setup(32, "ETDRK4", 0.35, 0.2, 1.0)
+@pytest.mark.parametrize("stepper", ["ETDRK4", "FilteredRK4"])
+def test_dot_product_identity(stepper):
+    p, A, q0, eta, kw = setup(32, stepper, 0.35, 0.2, 1.0)
     ns = 6
     rng = np.random.default_rng(3)
     u = A.initial_state(q0)
