@@ -8,8 +8,10 @@ quoted on.  A "step" is one FilteredRK4 time step (4 calcN! stages); --steps K a
 count these model steps.  `value` is FP32-fused grid-point*steps/s with the state resident in
 HBM, timed over exactly K steps run as stepforward! calls of 10 steps (an output interval: the
 state is looked at after every call, so the last step of each call computes every mode and
-the others only the modes a later step reads); single-step calls (every step observed) are
-timed beside it (`value_single_step_calls`).  The FP64-plain arm, its roofline and the
+the others only the modes a later step reads), each call one replay of the context's captured
+10-step CUDA graph; the per-kernel times behind the roofline come from the same calls run
+again with the library's per-launch events (no graphs; `ms_per_step_instrumented`);
+single-step calls (every step observed) are timed beside it (`value_single_step_calls`).  The FP64-plain arm, its roofline and the
 FP32-vs-FP64 error are reported beside it, and so are the other GPU workloads: SingleLayerQG
 512^2 ETDRK4 with stochastic forcing, MultiLayerQG 3 x 1024^2 ETDRK4, and the 1536-run
 TwoDNavierStokes ensemble (1024 x 64^2 + 384 x 128^2 + 128 x 256^2).  L2 is flushed (256 MiB
@@ -320,11 +322,13 @@ def time_arm(w, T, steps, warmup, flush, with_e2e, precision=None, graph=True, t
              call_steps=CALL_STEPS, tma=None):
     """Run one precision arm: `warmup` model steps, then exactly `steps` timed model steps as
     stepforward! calls of call_steps steps each (CUDA events on the legacy default stream,
-    which orders with the library's blocking stream; L2 flushed before every call) with the
-    library's per-kernel event timing on; then `steps` single-step calls (every step
-    observed, L2 flushed before each); then one call of `steps` steps replayed from captured
-    CUDA graphs of call_steps steps (one event pair); then optionally the end-to-end timing
-    through the host-buffer API (`steps` single-step calls).  Every timed leg starts from the
+    which orders with the library's blocking stream; L2 flushed before every call) -- each call
+    one replay of the context's captured call_steps-step graph, as a user's stepforward! runs;
+    then the same calls again with the library's per-launch events on (per-kernel times for
+    the roofline; no graphs); then `steps` single-step calls (every step observed, L2 flushed
+    before each), plain and with per-launch events; then one call of `steps` steps replayed
+    from captured CUDA graphs of call_steps steps (one event pair); then optionally the
+    end-to-end timing through the host-buffer API (`steps` single-step calls).  Every timed leg starts from the
     initial condition at t = 0 (the SingleLayerQG workload, nu = 0 and no filter, grows to the
     grid scale and overflows after ~220 steps in the reference algorithm too), so the state
     returned is the one after `steps` steps in every arm."""
@@ -347,9 +351,11 @@ def time_arm(w, T, steps, warmup, flush, with_e2e, precision=None, graph=True, t
     n2 = (C.c_int64 * 2)()
     nl = C.c_int64()
 
-    def timed_calls(calls):
+    def timed_calls(calls, profile):
+        """the calls, each timed with one event pair (L2 flushed before each); profile: with
+        the library's per-launch events (per-kernel times; no graphs)"""
         lib.gf_profile_read(ctx, ms2, n2, C.byref(nl))  # reset counters
-        lib.gf_profile_enable(ctx, 1)                  # (per-kernel events; no graphs)
+        lib.gf_profile_enable(ctx, 1 if profile else 0)
         ev = _events(len(calls))
         for i, nsteps in enumerate(calls):
             flush.zero_()
@@ -362,11 +368,17 @@ def time_arm(w, T, steps, warmup, flush, with_e2e, precision=None, graph=True, t
         lib.gf_profile_enable(ctx, 0)
         return ms, ms2[0] / max(n2[0], 1), ms2[1] / max(n2[1], 1), nl.value
 
+    plan = call_plan(steps, call_steps)
     set_initial_state(prob, w)
-    ms, mrow, mcol, launches = timed_calls(call_plan(steps, call_steps))
+    ms, _, _, launches = timed_calls(plan, False)         # the headline: stepforward! calls as a user runs them
     set_initial_state(prob, w)
-    mso, mrowo, mcolo, _ = timed_calls([1] * steps)
+    msi, mrow, mcol, _ = timed_calls(plan, True)          # the same calls with per-launch events
+    set_initial_state(prob, w)
+    mso, _, _, _ = timed_calls([1] * steps, False)
+    set_initial_state(prob, w)
+    _, mrowo, mcolo, _ = timed_calls([1] * steps, True)
     res = {"ms_per_step": ms, "ms_row": mrow, "ms_col": mcol, "launches": launches, "call_steps": call_steps,
+           "ms_per_step_instrumented": msi,
            "ms_per_step_observed": mso, "ms_row_observed": mrowo, "ms_col_observed": mcolo,
            "launch_shape": shape, "steps": steps}
     if graph:
@@ -745,7 +757,8 @@ def run_ours(args):
                    "parallelism": f"replicas x{world}", "steps_per_call": CALL_STEPS,
                    "steps_counted": "model time steps (4 FilteredRK4 stages each), timed as stepforward! "
                                     f"calls of {CALL_STEPS} steps",
-                   "ms_per_step_graph": msg, "launch_shape": r32["launch_shape"]},
+                   "ms_per_step_graph": msg, "ms_per_step_instrumented": r32["ms_per_step_instrumented"],
+                   "launch_shape": r32["launch_shape"]},
         "roofline": roofline(w, r32, 8, "twodns2048_fp32", peaks, peak_src),
         "roofline_step_two_sweep": step_roofline(w, ms, 4, peaks),
         "cpu_baseline": cpu,
