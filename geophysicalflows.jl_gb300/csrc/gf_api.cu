@@ -1942,7 +1942,7 @@ static void set_fp(gf_ctx* c, int Rr, int Rc, int C) {
 extern "C" int gf_set_field_parallel(gf_ctx* c, int32_t row_radix, int32_t col_radix, int32_t columns) {
   if (!c || row_radix < 0 || col_radix < 0 || columns < 0) return GF_ERR_ARG;
   if ((row_radix || col_radix) && !fp_ctx_ok(c))
-    return fail(c, GF_ERR_UNSUPPORTED, "field-parallel kernels: one layer without bottom drag, power-of-two lengths 32 ... 256");
+    return fail(c, GF_ERR_UNSUPPORTED, "field-parallel kernels: one layer without bottom drag, power-of-two lengths 32 ... 512");
   if (row_radix && !fp_radix_ok(c->g.nx, row_radix)) return fail(c, GF_ERR_ARG, "field-parallel row radix must be 2, 4 or 8");
   if (col_radix && (!fp_radix_ok(c->g.ny, col_radix) || !fp_cols_ok(c->g.ny, col_radix, columns ? columns : 1)))
     return fail(c, GF_ERR_ARG, "field-parallel column radix must be 2, 4 or 8, with 3 x columns x ny / radix <= 384");

@@ -1,4 +1,4 @@
-// Field-parallel small-grid step kernels (df64; lengths 32 ... 256 at radix 2, 4 and 8).
+// Field-parallel small-grid step kernels (df64; lengths 32 ... 256 at radix 2, 4 and 8; 512 at 4 and 8).
 #include "gf_fpar.cuh"
 
 namespace gf {

@@ -17,7 +17,7 @@
 // The arithmetic per element is that of the classic kernels (the same epilogue, products and
 // PV inversion functions); the transforms differ in their radix, so results agree to
 // rounding.  One layer without bottom drag (the column kernel holds the three fields of one
-// layer); lengths 32 ... 256.
+// layer); lengths 32 ... 512.
 #pragma once
 #include "gf_adjoint.cuh"
 #include "gf_kernels.cuh"
@@ -329,7 +329,7 @@ cudaError_t launch_adj_col_fp_nr(const Geom& g, const ModArgs& m, const AdjArgs&
   return cudaGetLastError();
 }
 
-// run-time length and radix -> instantiation (lengths 32 ... 256, radix 2, 4, 8)
+// run-time length and radix -> instantiation (lengths 32 ... 256 at radix 2, 4, 8; 512 at 4, 8)
 #define GF_FP_SWITCH(FN, N, R, ...)                                                     \
   switch (N * 16 + R) {                                                                 \
     case 32 * 16 + 2: return FN<T, 32, 2>(__VA_ARGS__);                                 \
@@ -344,6 +344,8 @@ cudaError_t launch_adj_col_fp_nr(const Geom& g, const ModArgs& m, const AdjArgs&
     case 256 * 16 + 2: return FN<T, 256, 2>(__VA_ARGS__);                               \
     case 256 * 16 + 4: return FN<T, 256, 4>(__VA_ARGS__);                               \
     case 256 * 16 + 8: return FN<T, 256, 8>(__VA_ARGS__);                               \
+    case 512 * 16 + 4: return FN<T, 512, 4>(__VA_ARGS__);                               \
+    case 512 * 16 + 8: return FN<T, 512, 8>(__VA_ARGS__);                               \
     default: return cudaErrorInvalidValue;                                              \
   }
 

@@ -192,14 +192,14 @@ template <class T> cudaError_t launch_ens_col(const EnsArgs&, cudaStream_t);
 template <class T> size_t ens_col_stride(int n);
 
 // field-parallel small-grid launchers (gf_fpar.cuh, gf_fp_<type>.cu), used by the dispatchers
-// when Geom::fpR / fpRc is set: one layer without bottom drag, power-of-two lengths 32 ... 256,
+// when Geom::fpR / fpRc is set: one layer without bottom drag, power-of-two lengths 32 ... 512,
 // radix 2, 4 or 8, blocks of 3 x (columns) x length / radix <= FP_MAXT threads
 constexpr int FP_MAXT = 384;
 // the radices a small-grid context starts with (gf_autotune may change them): rows 4, columns
 // 2 up to 128 points and 4 above (measured on TwoDNavierStokes 64^2 ... 256^2, FP32/FP64/df64)
 inline int fp_default_row_radix(int) { return 4; }
 inline int fp_default_col_radix(int ny) { return ny <= 128 ? 2 : 4; }
-inline bool fp_len_ok(int n) { return n == 32 || n == 64 || n == 128 || n == 256; }
+inline bool fp_len_ok(int n) { return n == 32 || n == 64 || n == 128 || n == 256 || n == 512; }
 inline bool fp_radix_ok(int n, int R) { return (R == 2 || R == 4 || R == 8) && 3 * (n / R) <= FP_MAXT; }
 inline bool fp_cols_ok(int n, int R, int C) { return C >= 1 && C <= 8 && 3 * C * (n / R) <= FP_MAXT; }
 template <class T> cudaError_t launch_row_fp(const Geom&, const ModArgs&, const Bufs&, cudaStream_t);

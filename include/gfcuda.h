@@ -317,9 +317,9 @@ int gf_set_tma_columns(gf_ctx* ctx, int32_t C);
 int gf_get_tma_columns(const gf_ctx* ctx, int32_t* C);
 
 /* Field-parallel small-grid kernels (no reference counterpart): for one layer without bottom
- * drag and power-of-two nx, ny in 32 ... 256, the row and column halves of each stage can run
+ * drag and power-of-two nx, ny in 32 ... 512, the row and column halves of each stage can run
  * with one thread group per field (the three inverse transforms, and the product transforms,
- * concurrently inside a block) at FFT radix 2, 4 or 8 -- the fast form when the grid has too
+ * concurrently inside a block) at FFT radix 2, 4 or 8 (512: 4 or 8) -- the fast form when the grid has too
  * few row pairs and columns to occupy the GPU (e.g. one 128^2 run).  row_radix / col_radix 0
  * select the classic kernel for that half; columns = kr columns per column block (3 x columns
  * x ny / col_radix <= 384 threads; 0 means 1).  A context whose row pairs, over all instances,

@@ -6,7 +6,7 @@ transforms differ in their radix, so states agree to rounding: FP32 1e-5, FP64 a
 1e-13 relative L2 after calls that mix unobserved steps (pruned columns) and observed ones.
 Covered: every radix and column count, TwoDNavierStokes, SingleLayerQG (beta, stochastic
 forcing, finite deformation radius, topography with U, PV-gradient products), SurfaceQG and
-BarotropicQGQL (three product fields), square and rectangular grids of 32 ... 256, a batch,
+BarotropicQGQL (three product fields), square and rectangular grids of 32 ... 512, a batch,
 the steppers' stage epilogues, calcN!, the adjoint's forward recompute, and the default
 selection rule."""
 import numpy as np
@@ -89,16 +89,16 @@ def test_field_parallel_equals_classic(case, T, prec):
         assert O.rel_l2(got, ref) <= tol(T), (case, fp, O.rel_l2(got, ref))
 
 
-@pytest.mark.parametrize("nx,ny", [(32, 32), (64, 128), (256, 64), (256, 256)])
+@pytest.mark.parametrize("nx,ny", [(32, 32), (64, 128), (256, 64), (256, 256), (512, 512)])
 @pytest.mark.parametrize("T,prec", [(np.float32, None), (np.float64, "DF64")])
 def test_field_parallel_sizes(nx, ny, T, prec):
     make, setup = CASES["slqg_forced"](nx, ny, T, prec, None, None)
     ref = run(make, setup, None, nsteps=(4, 1))
-    for fp in ((2, 2, 1), (4, 4, 2), (8, 8, 4)):
+    for fp in ((2, 2, 1), (4, 4, 2), (8, 8, 4), (4, 8, 1)):
         try:
             got = run(make, setup, fp, nsteps=(4, 1))
-        except ValueError:
-            assert 3 * fp[2] * ny // fp[1] > 384  # block too large: rejected
+        except ValueError:  # block too large: rejected
+            assert 3 * (nx // fp[0]) > 384 or 3 * fp[2] * (ny // fp[1]) > 384
             continue
         assert O.rel_l2(got, ref) <= tol(T), (nx, ny, fp)
 
@@ -188,11 +188,16 @@ def test_default_selection_and_rejection():
     q = TD.Problem("GPU", nx=64, T=np.float32, batch=8)   # 256 row pairs: classic
     assert q.field_parallel == (0, 0, 0)
     q.close()
-    big = TD.Problem("GPU", nx=512, T=np.float32)
+    big = TD.Problem("GPU", nx=512, T=np.float32)   # 256 row pairs: classic by default
     assert big.field_parallel == (0, 0, 0)
-    with pytest.raises(gfcuda.GFError):
-        big.field_parallel = (4, 4, 1)              # lengths above 256
+    with pytest.raises(ValueError):
+        big.field_parallel = (2, 4, 1)              # radix 2 at 512: 3 x 256 threads > 384
+    big.field_parallel = (4, 8, 1)
     big.close()
+    huge = TD.Problem("GPU", nx=1024, T=np.float32)
+    with pytest.raises(gfcuda.GFError):
+        huge.field_parallel = (4, 4, 1)             # lengths above 512
+    huge.close()
     m = ML.Problem(2, "GPU", nx=64, H=[0.3, 0.7], b=[-1.0, -1.4], T=np.float64)
     assert m.field_parallel == (0, 0, 0)
     with pytest.raises(gfcuda.GFError):
