@@ -481,7 +481,7 @@ def run_decaying128(cpu=True):
     return out
 
 
-def time_ensemble(steps, warmup, flush):
+def time_ensemble(steps, warmup, flush, tune=True):
     """The 1536-run ensemble: one batched Problem per size class (instance i of a class
     draws its forcing with seed + i), all stepped by gf_ensemble_step; each class runs on its
     own stream, concurrently.  `warmup` model steps, then exactly `steps` timed model steps
@@ -498,7 +498,8 @@ def time_ensemble(steps, warmup, flush):
         probs.append(gfcuda.TwoDNavierStokes.Problem(
             "GPU", nx=n, dt=e["dt"], nu=e["nu"], nnu=e["nnu"], stepper=e["stepper"], T=np.float32, batch=B,
             forcing=gfcuda.Forcing("stochastic", spectrum=spec, seed=1000 * n)))
-    shapes = [p.autotune(reps=3) for p in probs]  # FFT radix and tiles per size class
+    # FFT radix and tiles per size class (tune=False: the built-in block-shape rule)
+    shapes = [p.autotune(reps=3) for p in probs] if tune else None
     for p in probs:
         p.set_graph_steps(0)
     gfcuda.ensemble_step(probs, warmup)
@@ -852,7 +853,7 @@ def run_single(args):
     w, T, prec = SINGLE[args.single]
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     if w is ENSEMBLE:
-        r = time_ensemble(args.steps, args.warmup, flush)
+        r = time_ensemble(args.steps, args.warmup, flush, tune=not args.no_tune)
         r["pt_steps_per_s"] = r["points"] / (r["ms_per_step"] * 1e-3)
     elif w is ADJOINT256:
         r = time_adjoint(flush, T, reps=1)
