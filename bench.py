@@ -727,6 +727,7 @@ def run_ours(args):
         adj64 = time_adjoint(flush, np.float64)
     acc = accuracy_100_steps(w)
     acc1 = accuracy_100_steps(SLQG512)
+    acc2 = accuracy_100_steps(MLQG1024X3)
     dec128 = run_decaying128(cpu=is_rank0())
     ms, msg, msdf, ms64, e2e_s, e2e_df, e2e_64, mso = reduce_max(dist, [
         r32["ms_per_step"], r32["ms_per_step_graph"], rdf["ms_per_step"], r64["ms_per_step"],
@@ -808,6 +809,8 @@ def run_ours(args):
                        "ms_per_step_fp32": m32["ms_per_step"], "ms_per_step_graph_fp32": m32["ms_per_step_graph"],
                        "ms_per_step_df64": mdf["ms_per_step"],
                        "fp32_vs_df64_rel_l2": merr, "steps_compared": ks,
+                       "fp32_vs_fp64_rel_l2_100_steps": acc2["fp32_vs_fp64"],
+                       "df64_vs_fp64_rel_l2_100_steps": acc2["df64_vs_fp64"],
                        "roofline_fp32": roofline(MLQG1024X3, m32, 8, "mlqg1024x3_fp32", peaks, peak_src)},
         "ensemble1536": {"workload": "1536 TwoDNavierStokes runs: 1024 x 64^2 + 384 x 128^2 + 128 x 256^2, "
                                      "FilteredRK4 dt=0.01 nu=1e-4 (nnu=1), per-instance stochastic ring forcing "
