@@ -1,5 +1,5 @@
 // Adjoint (reverse mode) of the fused ETDRK4 / FilteredETDRK4 and RK4 / FilteredRK4 steps of
-// SingleLayerQG and TwoDNavierStokes (one layer, constant U): the transpose of the discrete
+// SingleLayerQG and TwoDNavierStokes (one layer, constant U or U(y)): the transpose of the discrete
 // step that gf_kernels.cuh computes, stage by stage in reverse, with the same two-kernel
 // structure (the stage combinations in adj_stage_combine).
 //
@@ -11,6 +11,10 @@
 //   abar = rfft^T(i kr Nbar), bbar = rfft^T(i l Nbar)                        [adj row kernel]
 //   ubar = abar qe, vbar = bbar qe, qbar = abar u + bbar v, etabar += qbar + U abar
 //   Xbar = irfft^T(qbar) + f (i l irfft^T(ubar) - i kr irfft^T(vbar))          [adj col kernel]
+// With U(y) (src/singlelayerqg.jl:395-432) the products are u' q, v q and C = u' Qx + v Qy
+// (u' = U + u, Qx = d(eta)/dx, Qy = d(eta)/dy - U_yy, no q + eta): cbar = rfft^T(-Nbar),
+// ubar += cbar Qx, vbar += cbar Qy, and the cotangents of Qx, Qy (cbar u', cbar v), summed over
+// every stage, give etabar = -d/dx(sum cbar u') - d/dy(sum cbar v) at the end of the sweep.
 // with rfft^T(Y) = sum over the half spectrum of Re(Y e^{i k x}) (the c2r path applied to
 // Y / w) and irfft^T(x) = w rfft(x) / (nx ny), w = 2 on interior kr columns, 1 on kr = 0 and
 // the Nyquist column.  The column kernel also runs the transposed stage combination:
@@ -110,6 +114,50 @@ __device__ __forceinline__ cplx<T> adj_stage_combine(const AdjArgs& a, size_t ti
   return a.head ? start(un) : czero<T>();
 }
 
+// The transposed products at column x of the packed row pair (j0, j0 + 1) from the cotangents
+// ab, bb (and cb) of the products A = u' qe, B = v qe (and C = u' Qx + v Qy) and the stored
+// forward fields (qe, u' = U + u, v): qbar = ab u' + bb v, ubar = ab qe (+ cb Qx),
+// vbar = bb qe (+ cb Qy); constant U: etabar += qbar + U ab (qe = q + eta and the -i kr U
+// eta_hat term); U(y): the cotangents of Qx and Qy (cb u', cb v) accumulated for the
+// topography gradient.  Each element is read and written by one thread.
+template <class T>
+__device__ __forceinline__ void adj_pair_products(const Geom& g, const AdjArgs& a, int j0, int x, int NX, cplx<T> ab,
+                                                  cplx<T> bb, cplx<T> cb, cplx<T>& qb_out, cplx<T>& ub_out,
+                                                  cplx<T>& vb_out) {
+  const T* ph = static_cast<const T*>(a.phys);
+  const size_t np = (size_t)g.ny * NX;
+  const size_t ia = (size_t)j0 * NX + x, ibb = ia + NX;
+  const cplx<T> qe = mk<T>(ph[ia], ph[ibb]);
+  const cplx<T> u = mk<T>(ph[np + ia], ph[np + ibb]);
+  const cplx<T> v = mk<T>(ph[2 * np + ia], ph[2 * np + ibb]);
+  const cplx<T> qb = mk<T>(ab.x * u.x + bb.x * v.x, ab.y * u.y + bb.y * v.y);
+  cplx<T> ub = mk<T>(ab.x * qe.x, ab.y * qe.y), vb = mk<T>(bb.x * qe.x, bb.y * qe.y);
+  if (a.hasC) {
+    const T* Qy1 = static_cast<const T*>(a.Qy1D);
+    const T* Qx2 = static_cast<const T*>(a.Qx2D);
+    const T* Qy2 = static_cast<const T*>(a.Qy2D);
+    cplx<T> Qx = czero<T>(), Qy = Qy1 ? mk<T>(Qy1[j0], Qy1[j0 + 1]) : czero<T>();
+    if (Qx2) Qx = mk<T>(Qx2[ia], Qx2[ibb]);
+    if (Qy2) Qy = Qy + mk<T>(Qy2[ia], Qy2[ibb]);
+    ub = ub + mk<T>(cb.x * Qx.x, cb.y * Qx.y);
+    vb = vb + mk<T>(cb.x * Qy.x, cb.y * Qy.y);
+    T* qxb = static_cast<T*>(a.qxb);
+    T* qyb = static_cast<T*>(a.qyb);
+    qxb[ia] = qxb[ia] + cb.x * u.x;
+    qxb[ibb] = qxb[ibb] + cb.y * u.y;
+    qyb[ia] = qyb[ia] + cb.x * v.x;
+    qyb[ibb] = qyb[ibb] + cb.y * v.y;
+  } else {
+    const T U = sel<T>(a.U, a.U_f, a.U_l);
+    T* etab = static_cast<T*>(a.etab);
+    etab[ia] = etab[ia] + (qb.x + U * ab.x);
+    etab[ibb] = etab[ibb] + (qb.y + U * ab.y);
+  }
+  qb_out = qb;
+  ub_out = ub;
+  vb_out = vb;
+}
+
 // Column kernel: y-direction FFT of the three adjoint products of stage a.stage (kr < kcut),
 // the transposed stage combination, and the y-direction inverse FFT of the next cotangent's
 // (i kr Nbar / w, i l Nbar / w) into Wb (all kr).  a.stage = 5: head only (start of a step
@@ -178,19 +226,22 @@ __global__ void __launch_bounds__(512, 1) adj_col_kernel(Geom g, ModArgs m, AdjA
   if (a.stage == 1 && !a.head) out_w = false;
   if (!out_w) return;
 
-  // 3) y-inverse FFT of (i kr Nbar / w, i l Nbar / w) into Wb (every kr column), both in lockstep
+  // 3) y-inverse FFT of (i kr Nbar / w, i l Nbar / w) -- and of -Nbar / w for the U(y)
+  // product -- into Wb (every kr column), in lockstep
   cplx<T>* Wb = static_cast<cplx<T>*>(a.Wb);
 #pragma unroll
   for (int i = 0; i < R; ++i) {
     const int j = t + i * TPF;
     F0[c * cs + swz<T>(j)] = (scale_out * krT) * mul_i(nb[i]);
     F1[c * cs + swz<T>(j)] = (scale_out * (T(lidx(g, j)) * dky)) * mul_i(nb[i]);
+    if (a.hasC) F2[c * cs + swz<T>(j)] = (-scale_out) * nb[i];
   }
   __syncthreads();
-  fft_smem_group<T, NY, R, +1, 2>(F0 + cf * cs, C * cs, tf, tw);
+  if (a.hasC) fft_smem_group<T, NY, R, +1, 3>(F0 + cf * cs, C * cs, tf, tw);
+  else fft_smem_group<T, NY, R, +1, 2>(F0 + cf * cs, C * cs, tf, tw);
   if (kin) {
-#pragma unroll
-    for (int f = 0; f < 2; ++f) {
+    const int nw = a.hasC ? 3 : 2;
+    for (int f = 0; f < nw; ++f) {
       cplx<T>* Wf = Wb + (size_t)f * g.ny * g.ldk + kr;
       const cplx<T>* Fe = F0 + (size_t)f * C * cs + c * cs;
 #pragma unroll
@@ -220,11 +271,8 @@ __global__ void __launch_bounds__(256, 1) adj_row_kernel(Geom g, AdjArgs a, Bufs
   const cplx<T>* tw = static_cast<const cplx<T>*>(b.twid);
   const cplx<T>* Wb = static_cast<const cplx<T>*>(a.Wb);
   cplx<T>* Pb = static_cast<cplx<T>*>(a.Pb);
-  const T* ph = static_cast<const T*>(a.phys);
-  T* etab = static_cast<T*>(a.etab);
-  const size_t np = (size_t)g.ny * NX;
-  const T U = sel<T>(a.U, a.U_f, a.U_l);
-  for (int f = 0; f < 2; ++f) {
+  const int nin = a.hasC ? 3 : 2;
+  for (int f = 0; f < nin; ++f) {
     const cplx<T>* Wa = Wb + (size_t)f * g.ny * g.ldk + (size_t)j0 * g.ldk;
 #pragma unroll
     for (int i = 0; i < R; ++i) {
@@ -233,22 +281,14 @@ __global__ void __launch_bounds__(256, 1) adj_row_kernel(Geom g, AdjArgs a, Bufs
     }
   }
   __syncthreads();
-  fft_smem_group<T, NX, R, +1, 2>(buf, PS, t, tw);
+  if (a.hasC) fft_smem_group<T, NX, R, +1, 3>(buf, PS, t, tw);
+  else fft_smem_group<T, NX, R, +1, 2>(buf, PS, t, tw);
 #pragma unroll
   for (int i = 0; i < R; ++i) {
     const int x = t + i * TPF;
     const int px = swz<T>(x);
-    const size_t ia = (size_t)j0 * NX + x, ibb = ia + NX;
-    const cplx<T> ab = buf[px], bb = buf[PS + px];
-    const cplx<T> qe = mk<T>(ph[ia], ph[ibb]);
-    const cplx<T> u = mk<T>(ph[np + ia], ph[np + ibb]);
-    const cplx<T> v = mk<T>(ph[2 * np + ia], ph[2 * np + ibb]);
-    const cplx<T> qb = mk<T>(ab.x * u.x + bb.x * v.x, ab.y * u.y + bb.y * v.y);
-    etab[ia] = etab[ia] + (qb.x + U * ab.x);
-    etab[ibb] = etab[ibb] + (qb.y + U * ab.y);
-    buf[px] = qb;
-    buf[PS + px] = mk<T>(ab.x * qe.x, ab.y * qe.y);
-    buf[2 * PS + px] = mk<T>(bb.x * qe.x, bb.y * qe.y);
+    adj_pair_products<T>(g, a, j0, x, NX, buf[px], buf[PS + px], a.hasC ? buf[2 * PS + px] : czero<T>(),
+                         buf[px], buf[PS + px], buf[2 * PS + px]);
   }
   __syncthreads();
   fft_smem_group<T, NX, R, -1, 3>(buf, PS, t, tw);

@@ -79,6 +79,8 @@ struct gf_ctx {
     void *ckpt = nullptr, *phys = nullptr, *ub = nullptr, *n1acc = nullptr, *xaacc = nullptr, *x1acc = nullptr;
     void *ubar_in = nullptr, *ubar_out = nullptr, *Wb = nullptr, *Pb = nullptr, *etab = nullptr;
     void *final_state = nullptr, *tmp = nullptr;
+    void *qxb = nullptr, *qyb = nullptr;  // U(y): cotangents of Qx, Qy (physical)
+    int nwb = 2;                        // cotangent fields in Wb (3 with the U(y) product)
     std::vector<double> ck_t;           // per slot
     std::vector<int64_t> ck_step;
     std::vector<int> split;             // binomial schedule: split[n * snaps + s]
@@ -2168,8 +2170,8 @@ extern "C" int gf_step_output(gf_ctx* c, int64_t nsteps, int32_t every, const in
 
 // ------------------------------------------------------------------------------- adjoint
 // Reverse-mode derivative of stepforward!(prob, nsteps) for TwoDNavierStokes and
-// SingleLayerQG (constant U) with ETDRK4 / FilteredETDRK4 or RK4 / FilteredRK4 (the kernels
-// are in gf_adjoint.cuh).
+// SingleLayerQG (constant U or U(y)) with ETDRK4 / FilteredETDRK4 or RK4 / FilteredRK4 (the
+// kernels are in gf_adjoint.cuh).
 // Checkpointing: the forward pass stores the state every `every` steps; the reverse pass
 // recomputes one segment at a time from its checkpoint with the fused forward kernels,
 // keeping the physical fields (q + eta, u, v) of all its stages, then runs the transposed
@@ -2183,7 +2185,7 @@ static int adj_check(gf_ctx* c) {
   if (c->kind != SK_ETDRK4 && c->kind != SK_RK4)
     return fail(c, GF_ERR_UNSUPPORTED, "the adjoint follows the ETDRK4 / FilteredETDRK4 and RK4 / FilteredRK4 stages");
   if (c->g.nb != 1) return fail(c, GF_ERR_UNSUPPORTED, "the adjoint runs one instance (batch = 1)");
-  if (c->m.U1D || c->m.hasC || c->m.linear) return fail(c, GF_ERR_UNSUPPORTED, "the adjoint supports a constant U");
+  if (c->m.linear) return fail(c, GF_ERR_UNSUPPORTED, "the adjoint covers the nonlinear step");
   return GF_OK;
 }
 
@@ -2251,18 +2253,20 @@ extern "C" int gf_adjoint_setup(gf_ctx* c, int64_t nsteps, int32_t checkpoint_ev
       adj_release(c);
       return fail(c, GF_ERR_CUDA, "adjoint events");
     }
+  a.nwb = c->m.hasC ? 3 : 2;
   if (!(a.ckpt = adj_alloc(c, a.snaps * spec)) || !(a.phys = adj_alloc(c, 2 * a.unit_phys)) ||
       !(a.ub = adj_alloc(c, spec)) || !(a.n1acc = adj_alloc(c, spec)) || !(a.xaacc = adj_alloc(c, spec)) ||
       !(a.x1acc = adj_alloc(c, spec)) || !(a.ubar_in = adj_alloc(c, spec)) || !(a.ubar_out = adj_alloc(c, spec)) ||
-      !(a.final_state = adj_alloc(c, spec)) || !(a.tmp = adj_alloc(c, spec)) || !(a.Wb = adj_alloc(c, 2 * wide)) ||
-      !(a.Pb = adj_alloc(c, 3 * wide)) || !(a.etab = adj_alloc(c, plane))) {
+      !(a.final_state = adj_alloc(c, spec)) || !(a.tmp = adj_alloc(c, spec)) || !(a.Wb = adj_alloc(c, a.nwb * wide)) ||
+      !(a.Pb = adj_alloc(c, 3 * wide)) || !(a.etab = adj_alloc(c, plane)) ||
+      (c->m.hasC && (!(a.qxb = adj_alloc(c, plane)) || !(a.qyb = adj_alloc(c, plane))))) {
     adj_release(c);
     return fail(c, GF_ERR_NOMEM, "adjoint buffers");
   }
   // unused padding columns of the accumulators stay zero
   for (void* p : {a.ub, a.n1acc, a.xaacc, a.x1acc, a.ubar_in, a.ubar_out, a.tmp})
     GF_CUDA(c, cudaMemsetAsync(p, 0, spec, c->stream));
-  GF_CUDA(c, cudaMemsetAsync(a.Wb, 0, 2 * wide, c->stream));
+  GF_CUDA(c, cudaMemsetAsync(a.Wb, 0, a.nwb * wide, c->stream));
   GF_CUDA(c, cudaMemsetAsync(a.Pb, 0, 3 * wide, c->stream));
   a.ck_t.assign(a.snaps, 0.0);
   a.ck_step.assign(a.snaps, 0);
@@ -2363,6 +2367,9 @@ static AdjArgs adj_args(gf_ctx* c) {
   a.L = (c->kind == SK_RK4 && c->hasL) ? c->Ltab : nullptr;
   a.dt = c->cfg.dt;
   split_hl(a.dt, &a.dt_f, &a.dt_l);
+  a.hasC = c->m.hasC;
+  a.Qy1D = c->m.Qy1D; a.Qx2D = c->m.Qx2D; a.Qy2D = c->m.Qy2D;
+  a.qxb = d.qxb; a.qyb = d.qyb;
   return a;
 }
 
@@ -2466,6 +2473,10 @@ static int adjoint_reverse(gf_ctx* c) {
   const Geom& g = c->g;
   const size_t spec = g.bs_spec * c->cb, plane = (size_t)g.ny * g.nx * c->rb;
   GF_CUDA(c, cudaMemsetAsync(d.etab, 0, plane, c->stream));
+  if (d.qxb) {
+    GF_CUDA(c, cudaMemsetAsync(d.qxb, 0, plane, c->stream));
+    GF_CUDA(c, cudaMemsetAsync(d.qyb, 0, plane, c->stream));
+  }
   AdjArgs a = adj_args(c);
   const Bufs b = Bufs{c->twid, nullptr, nullptr};
   // the transposed stages (stream d.ts) start after everything the context stream did so far
@@ -2484,6 +2495,15 @@ static int adjoint_reverse(gf_ctx* c) {
   // the context stream continues after the last transposed stage (ubar_out, etab)
   GF_CUDA(c, cudaEventRecord(d.ev_sync, d.ts));
   GF_CUDA(c, cudaStreamWaitEvent(c->stream, d.ev_sync, 0));
+  if (d.qxb) {  // U(y): Qx = d(eta)/dx, Qy = d(eta)/dy - U_yy, so etabar -= d(Qxbar)/dx + d(Qybar)/dy
+    const size_t pf = (size_t)g.ny * g.nx * c->rb;
+    char* ph = (char*)c->phys;
+    if (int r = fwd_transform(c, d.qxb, d.tmp, 0)) return r;
+    if (int r = inv_transform(c, d.tmp, SF_DX, 0, ph)) return r;
+    if (int r = fwd_transform(c, d.qyb, d.tmp, 0)) return r;
+    if (int r = inv_transform(c, d.tmp, SF_DY, 0, ph + pf)) return r;
+    GF_CUDA(c, DISPATCH(c, launch_sub2, (size_t)g.ny * g.nx, d.etab, ph, ph + pf, c->stream));
+  }
   GF_CUDA(c, cudaMemcpyAsync(c->sol, d.final_state, spec, cudaMemcpyDeviceToDevice, c->stream));
   c->t = d.t_end;
   c->step = d.step_end;

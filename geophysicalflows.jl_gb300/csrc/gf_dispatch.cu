@@ -202,6 +202,19 @@ cudaError_t launch_adj_spec(const Geom& g, const ModArgs& m, const void* in, voi
   return cudaGetLastError();
 }
 
+// out -= a + b (physical arrays of n elements)
+template <class T>
+__global__ void sub2_kernel(size_t n, T* out, const T* a, const T* b) {
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+    out[e] = out[e] - (a[e] + b[e]);
+}
+
+template <class T>
+cudaError_t launch_sub2(size_t n, void* out, const void* a, const void* b, cudaStream_t st) {
+  sub2_kernel<T><<<256, 256, 0, st>>>(n, static_cast<T*>(out), static_cast<const T*>(a), static_cast<const T*>(b));
+  return cudaGetLastError();
+}
+
 template <class T> __device__ __forceinline__ double to_double(T x) { return (double)x; }
 template <> __device__ __forceinline__ double to_double<df64>(df64 x) { return (double)x.hi + (double)x.lo; }
 
@@ -262,6 +275,7 @@ cudaError_t launch_flux(const Geom& g, const void* v, const void* uy, const void
   template cudaError_t launch_adj_row<T>(const Geom&, const AdjArgs&, const Bufs&, cudaStream_t);               \
   template cudaError_t launch_adj_col<T>(const Geom&, const ModArgs&, const AdjArgs&, const Bufs&, cudaStream_t); \
   template cudaError_t launch_adj_spec<T>(const Geom&, const ModArgs&, const void*, void*, int, cudaStream_t);      \
+  template cudaError_t launch_sub2<T>(size_t, void*, const void*, const void*, cudaStream_t);                     \
   template cudaError_t launch_flux<T>(const Geom&, const void*, const void*, const void*, const double*, double*,   \
                                       int, cudaStream_t);
 

@@ -179,11 +179,7 @@ __global__ void __launch_bounds__(FP_MAXT)
   const cplx<T>* tw = static_cast<const cplx<T>*>(b.twid);
   const cplx<T>* Wb = static_cast<const cplx<T>*>(a.Wb);
   cplx<T>* Pb = static_cast<cplx<T>*>(a.Pb);
-  const T* ph = static_cast<const T*>(a.phys);
-  T* etab = static_cast<T*>(a.etab);
-  const size_t np = (size_t)g.ny * NX;
-  const T U = sel<T>(a.U, a.U_f, a.U_l);
-  if (f < 2) {
+  if (f < (a.hasC ? 3 : 2)) {
     const cplx<T>* Wa = Wb + (size_t)f * g.ny * g.ldk + (size_t)j0 * g.ldk;
 #pragma unroll
     for (int i = 0; i < R; ++i) {
@@ -192,20 +188,11 @@ __global__ void __launch_bounds__(FP_MAXT)
     }
   }
   __syncthreads();
-  fft_smem<T, NX, R, +1>(mine, t, tw);  // group 2: a buffer that is overwritten below
+  fft_smem<T, NX, R, +1>(mine, t, tw);  // group 2 without the U(y) product: a buffer overwritten below
   for (int x = tid; x < NX; x += NT) {
     const int px = swz<T>(x);
-    const size_t ia = (size_t)j0 * NX + x, ibb = ia + NX;
-    const cplx<T> ab = buf[px], bb = buf[PS + px];
-    const cplx<T> qe = mk<T>(ph[ia], ph[ibb]);
-    const cplx<T> u = mk<T>(ph[np + ia], ph[np + ibb]);
-    const cplx<T> v = mk<T>(ph[2 * np + ia], ph[2 * np + ibb]);
-    const cplx<T> qb = mk<T>(ab.x * u.x + bb.x * v.x, ab.y * u.y + bb.y * v.y);
-    etab[ia] = etab[ia] + (qb.x + U * ab.x);
-    etab[ibb] = etab[ibb] + (qb.y + U * ab.y);
-    buf[px] = qb;
-    buf[PS + px] = mk<T>(ab.x * qe.x, ab.y * qe.y);
-    buf[2 * PS + px] = mk<T>(bb.x * qe.x, bb.y * qe.y);
+    adj_pair_products<T>(g, a, j0, x, NX, buf[px], buf[PS + px], a.hasC ? buf[2 * PS + px] : czero<T>(), buf[px],
+                         buf[PS + px], buf[2 * PS + px]);
   }
   __syncthreads();
   fft_smem<T, NX, R, -1>(mine, t, tw);
@@ -270,13 +257,14 @@ __global__ void __launch_bounds__(FP_MAXT)
     if (out_w) {
       F0[(size_t)c * cs + swz<T>(j)] = (scale_out * krT) * mul_i(nb);
       F0[(size_t)(C + c) * cs + swz<T>(j)] = (scale_out * (T(lidx(g, j)) * dky)) * mul_i(nb);
+      if (a.hasC) F0[(size_t)(2 * C + c) * cs + swz<T>(j)] = (-scale_out) * nb;  // the U(y) product
     }
   }
   if (!out_w) return;
   __syncthreads();
-  fft_smem<T, NY, R, +1>(F0 + (size_t)cf * cs, tf, tw);  // groups of the third field: not stored
+  fft_smem<T, NY, R, +1>(F0 + (size_t)cf * cs, tf, tw);  // the third field: stored with the U(y) product
   cplx<T>* Wb = static_cast<cplx<T>*>(a.Wb);
-  for (int e = tid; e < 2 * CN; e += NT) {
+  for (int e = tid; e < (a.hasC ? 3 : 2) * CN; e += NT) {
     const int f = e / CN, r = e - f * CN, c = r % C, j = r / C, kr = bx * C + c;
     if (kr < g.nkr) Wb[(size_t)f * g.ny * g.ldk + (size_t)j * g.ldk + kr] = F0[(size_t)(f * C + c) * cs + swz<T>(j)];
   }

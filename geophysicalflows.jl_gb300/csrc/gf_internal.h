@@ -161,6 +161,12 @@ struct AdjArgs {
   int rk4;
   const void* L;
   double dt; float dt_f, dt_l;
+  // U(y) (SingleLayerQG): the third product C = (U + u) Qx + v Qy, its cotangent field in Wb,
+  // the PV gradients (Qy1D [j], Qx2D / Qy2D [j][nx] or null) and the physical accumulators of
+  // the cotangents of Qx and Qy ([j][nx]) from which the topography gradient follows
+  int hasC;
+  const void *Qy1D, *Qx2D, *Qy2D;
+  void *qxb, *qyb;
 };
 
 // Generic transforms (updatevars!, set_*!, fwdtransform!/invtransform!).
@@ -238,6 +244,9 @@ template <class T> cudaError_t launch_adj_col(const Geom&, const ModArgs&, const
 // element-wise adjoint helpers: op 0 kinetic-energy gradient, op 1 rfft^T preparation (see gf_dispatch.cu)
 template <class T> cudaError_t launch_adj_spec(const Geom&, const ModArgs&, const void* in, void* out, int op,
                                                cudaStream_t);
+
+// out -= a + b over n physical elements (gf_dispatch.cu)
+template <class T> cudaError_t launch_sub2(size_t n, void* out, const void* a, const void* b, cudaStream_t);
 
 // MultiLayerQG fluxes: per-block partial sums (gf_dispatch.cu)
 template <class T> cudaError_t launch_flux(const Geom&, const void* v, const void* uy, const void* psi, const double* U,

@@ -335,7 +335,7 @@ int gf_get_field_parallel(const gf_ctx* ctx, int32_t* out);
  * ChainRulesCore.rrule on stepforward! (the reference has no derivative; its step is
  * src/singlelayerqg.jl:356-382 / src/twodnavierstokes.jl:253-294 under FourierFlows' ETDRK4
  * or RK4).
- * Supported: TwoDNavierStokes and SingleLayerQG with constant U, stepper ETDRK4,
+ * Supported: TwoDNavierStokes and SingleLayerQG (constant U or U(y)), stepper ETDRK4,
  * FilteredETDRK4, RK4 or FilteredRK4, batch = 1.  It is the exact transpose of the discrete step the library
  * computes (dealiasing, PV inversion, stage combinations), in the context's precision.
  * Checkpointing: see gf_adjoint_set_snapshots (binomial schedule over units of

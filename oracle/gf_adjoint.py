@@ -7,6 +7,8 @@ It differentiates the DISCRETE step of the restatement in gf_oracle.py exactly:
     psi_hat = f q_hat (f = -1/K^2 or -1/(K^2 + 1/l^2), src/singlelayerqg.jl:484-490),
     u_hat = -i l psi_hat, v_hat = i kr psi_hat, q,u,v = irfft2(.), qe = q + eta,
     N = -i kr rfft2(u qe) - i l rfft2(v qe) - i kr U eta_hat;
+    with U(y) (src/singlelayerqg.jl:395-432): u' = u + U, Qx = d(eta)/dx, Qy = d(eta)/dy - U_yy,
+    N = -rfft2(u' Qx) - rfft2(v Qy) - i kr rfft2(u' q) - i l rfft2(v q);
   * the FourierFlows ETDRK4 and RK4 stage sequences (restated in gf_oracle.TimeStepper.step),
     in which every calcN! dealiases its input array in place, so that later uses of that array
     see the dealiased values (RK4: RHS_s = N(X_s) + L X_s at X_s = M(X1 + c_s dt RHS_{s-1}),
@@ -45,13 +47,16 @@ def irfft2_T(x, grid):
 
 class SLQGAdjoint:
     """Tangent-linear and adjoint of an oracle SingleLayerQG problem stepped with ETDRK4,
-    FilteredETDRK4, RK4 or FilteredRK4 (constant U; additive forcing does not change the
-    derivative)."""
+    FilteredETDRK4, RK4 or FilteredRK4, with a constant U or U(y) (additive forcing does not
+    change the derivative)."""
 
     def __init__(self, prob):
-        if not prob.U_is_number:
-            raise NotImplementedError("the adjoint supports a constant U")
         ts = prob.timestepper
+        self.varying = not prob.U_is_number
+        if self.varying:
+            g = prob.grid
+            self.Uf = prob.U                                               # (ny, nx)
+            self.Qy0 = -O.irfft2(-g.l ** 2 * O.rfft2(self.Uf), g)          # -U_yy
         if ts.kind not in ("ETDRK4", "RK4"):
             raise NotImplementedError("the adjoint follows the ETDRK4 and RK4 stages")
         self.kind = ts.kind
@@ -71,9 +76,25 @@ class SLQGAdjoint:
         psih = f * X
         return O.irfft2(X, g), O.irfft2(-1j * g.l * psih, g), O.irfft2(1j * g.kr * psih, g)
 
+    def _dx(self, x):
+        return O.irfft2(1j * self.g.kr * O.rfft2(x), self.g)
+
+    def _dy(self, x):
+        return O.irfft2(1j * self.g.l * O.rfft2(x), self.g)
+
+    def _dT(self, x, k):
+        """transpose of x -> irfft2(i k rfft2(x)) (k = kr or l)"""
+        g = self.g
+        return rfft2_T(np.conj(1j * k) * irfft2_T(x, g), g)
+
     def N(self, X, eta):
         g = self.g
         q, u, v = self._fields(X)
+        if self.varying:
+            u = u + self.Uf
+            Qx, Qy = self._dx(eta), self.Qy0 + self._dy(eta)
+            return (-O.rfft2(u * Qx) - O.rfft2(v * Qy) - 1j * g.kr * O.rfft2(u * q)
+                    - 1j * g.l * O.rfft2(v * q))
         qe = q + eta
         return (-1j * g.kr * O.rfft2(u * qe) - 1j * g.l * O.rfft2(v * qe)
                 - 1j * g.kr * self.p.U * O.rfft2(eta))
@@ -82,6 +103,12 @@ class SLQGAdjoint:
         g = self.g
         q, u, v = self._fields(X)
         dq, du, dv = self._fields(dX)
+        if self.varying:
+            u = u + self.Uf
+            Qx, Qy = self._dx(eta), self.Qy0 + self._dy(eta)
+            dQx, dQy = self._dx(deta), self._dy(deta)
+            return (-O.rfft2(du * Qx + u * dQx) - O.rfft2(dv * Qy + v * dQy)
+                    - 1j * g.kr * O.rfft2(du * q + u * dq) - 1j * g.l * O.rfft2(dv * q + v * dq))
         qe, dqe = q + eta, dq + deta
         return (-1j * g.kr * O.rfft2(du * qe + u * dqe) - 1j * g.l * O.rfft2(dv * qe + v * dqe)
                 - 1j * g.kr * self.p.U * O.rfft2(deta))
@@ -90,6 +117,17 @@ class SLQGAdjoint:
         """(Xbar, etabar) = J^T Nbar at (X, eta)."""
         g = self.g
         q, u, v = self._fields(X)
+        if self.varying:
+            u = u + self.Uf
+            Qx, Qy = self._dx(eta), self.Qy0 + self._dy(eta)
+            abar = rfft2_T(1j * g.kr * Nbar, g)
+            bbar = rfft2_T(1j * g.l * Nbar, g)
+            cbar = rfft2_T(-Nbar, g)
+            qbar = abar * u + bbar * v
+            ub, vb = irfft2_T(abar * q + cbar * Qx, g), irfft2_T(bbar * q + cbar * Qy, g)
+            Xbar = irfft2_T(qbar, g) + self.f * (1j * g.l * ub - 1j * g.kr * vb)
+            etabar = self._dT(cbar * u, g.kr) + self._dT(cbar * v, g.l)
+            return Xbar, etabar
         qe = q + eta
         abar = rfft2_T(1j * g.kr * Nbar, g)
         bbar = rfft2_T(1j * g.l * Nbar, g)

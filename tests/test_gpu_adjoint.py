@@ -181,6 +181,29 @@ def test_classic_and_field_parallel_adjoint_kernels_agree(stepper):
     assert rel(g0, gq) <= 1e-11 and rel(e0, ge) <= 1e-11
 
 
+@pytest.mark.parametrize("stepper", ["ETDRK4", "FilteredRK4"])
+@pytest.mark.parametrize("classic", [False, True])
+def test_varying_U_gradient_matches_oracle(stepper, classic):
+    """SingleLayerQG with a zonal jet U(y) (the third product (U + u) Qx + v Qy and the
+    topography entering through Qx, Qy): gradients of the final kinetic energy with respect
+    to q0 and the topography against the oracle's discrete adjoint, with the field-parallel
+    (default at 64^2) and the classic adjoint kernels"""
+    n, ns = 64, 12
+    g = O.Grid(n)
+    Uy = 0.3 * np.cos(2 * g.y) + 0.1 * np.sin(g.y)
+    kw, q0, eta = slqg_case(n, stepper, U=Uy, beta=1.0, ell=0.35)
+    p = SL.Problem("GPU", T=np.float64, **kw)
+    if classic:
+        p.launch_shape = (8, 1, 8, 1)
+    SL.set_q(p, q0)
+    loss, dq0, deta = adjoint.grad(p, ns, checkpoint_every=5)
+    p.close()
+    L, gq, ge = AD.SLQGAdjoint(O.SingleLayerQG(**kw)).gradient(q0, eta, ns)
+    assert abs(loss - L) <= 1e-13 * L
+    assert rel(dq0, gq) <= 1e-11
+    assert rel(deta, ge) <= 1e-11
+
+
 def test_twodns_filtered_rk4_gradient():
     """TwoDNavierStokes with FilteredRK4 (the decaying run's stepper) and viscosity: the
     gradient of the final kinetic energy against the oracle's discrete adjoint"""

@@ -12,6 +12,8 @@ import gf_oracle as O
 def setup(n, stepper, ell=0.35, U=0.0, beta=0.0, nsteps=12):
     g = O.Grid(n)
     eta = AD.random_topography(g, 8, 0.1, 7)
+    if U == "y":   # a zonal jet U(y)
+        U = 0.3 * np.cos(2 * g.y) + 0.1 * np.sin(g.y)
     kw = dict(nx=n, deformation_radius=ell, eta=eta, dt=0.01, stepper=stepper, U=U, beta=beta)
     p = O.SingleLayerQG(**kw)
     q0 = O.peakedisotropicspectrum(g, 6, 0.5, seed=1234)
@@ -19,7 +21,8 @@ def setup(n, stepper, ell=0.35, U=0.0, beta=0.0, nsteps=12):
 
 
 CASES = [("ETDRK4", 0.35, 0.0, 0.0), ("ETDRK4", np.inf, 0.3, 2.0), ("FilteredETDRK4", 0.35, 0.1, 1.0),
-         ("RK4", 0.35, 0.2, 1.0), ("FilteredRK4", np.inf, 0.0, 2.0)]
+         ("RK4", 0.35, 0.2, 1.0), ("FilteredRK4", np.inf, 0.0, 2.0), ("ETDRK4", 0.35, "y", 1.0),
+         ("FilteredRK4", np.inf, "y", 0.0)]
 
 
 @pytest.mark.parametrize("stepper,ell,U,beta", CASES)
@@ -45,9 +48,9 @@ def test_gradient_matches_central_differences(stepper, ell, U, beta):
         assert abs(fd - ad) <= 1e-6 * abs(ad)
 
 
-@pytest.mark.parametrize("stepper", ["ETDRK4", "FilteredRK4"])
-def test_dot_product_identity(stepper):
-    p, A, q0, eta, kw = setup(32, stepper, 0.35, 0.2, 1.0)
+@pytest.mark.parametrize("stepper,U", [("ETDRK4", 0.2), ("FilteredRK4", 0.2), ("ETDRK4", "y")])
+def test_dot_product_identity(stepper, U):
+    p, A, q0, eta, kw = setup(32, stepper, 0.35, U, 1.0)
     ns = 6
     rng = np.random.default_rng(3)
     u = A.initial_state(q0)
