@@ -80,6 +80,7 @@ struct gf_ctx {
     void *ubar_in = nullptr, *ubar_out = nullptr, *Wb = nullptr, *Pb = nullptr, *etab = nullptr;
     void *final_state = nullptr, *tmp = nullptr;
     void *qxb = nullptr, *qyb = nullptr;  // U(y): cotangents of Qx, Qy (physical)
+    void* nbar = nullptr;               // several layers / bottom drag: the current stage's Nbar
     int nwb = 2;                        // cotangent fields in Wb (3 with the U(y) product)
     std::vector<double> ck_t;           // per slot
     std::vector<int64_t> ck_step;
@@ -2180,8 +2181,11 @@ extern "C" int gf_step_output(gf_ctx* c, int64_t nsteps, int32_t every, const in
 static int adj_check(gf_ctx* c) {
   const int mod = c->cfg.module;
   if (c->g.rtx || c->g.rty) return fail(c, GF_ERR_UNSUPPORTED, "the adjoint needs power-of-two nx, ny in [32, 2048]");
-  if (mod != GF_TWODNAVIERSTOKES && mod != GF_SINGLELAYERQG)
-    return fail(c, GF_ERR_UNSUPPORTED, "the adjoint covers TwoDNavierStokes and SingleLayerQG");
+  if (mod != GF_TWODNAVIERSTOKES && mod != GF_SINGLELAYERQG && mod != GF_MULTILAYERQG)
+    return fail(c, GF_ERR_UNSUPPORTED, "the adjoint covers TwoDNavierStokes, SingleLayerQG and MultiLayerQG");
+  if ((c->g.nl > 1 || c->m.drag) && (size_t)3 * c->g.nl * c->g.ny * c->cb > (size_t)SMEM_CAP)
+    return fail(c, GF_ERR_UNSUPPORTED, "the several-layer adjoint holds every layer of a column: 3 x nlayers x ny "
+                                       "complex values must fit in 200 KB of shared memory");
   if (c->kind != SK_ETDRK4 && c->kind != SK_RK4)
     return fail(c, GF_ERR_UNSUPPORTED, "the adjoint follows the ETDRK4 / FilteredETDRK4 and RK4 / FilteredRK4 stages");
   if (c->g.nb != 1) return fail(c, GF_ERR_UNSUPPORTED, "the adjoint runs one instance (batch = 1)");
@@ -2239,8 +2243,8 @@ extern "C" int gf_adjoint_setup(gf_ctx* c, int64_t nsteps, int32_t checkpoint_ev
   a.nseg = (int)((nsteps + a.every - 1) / a.every);
   a.snaps = a.nseg;  // one slot per unit boundary: a single forward pass, no recomputation of advances
   const size_t spec = g.bs_spec * c->cb, plane = (size_t)g.ny * g.nx * c->rb;
-  const size_t wide = (size_t)g.ny * g.ldk * c->cb;
-  a.unit_phys = (size_t)a.every * 4 * 3 * plane;
+  const size_t wide = (size_t)g.nl * g.ny * g.ldk * c->cb;  // one field, every layer
+  a.unit_phys = (size_t)a.every * 4 * 3 * g.nl * plane;
   // the second stream is non-blocking: it is ordered with the context stream by events only,
   // never implicitly with the legacy default stream
   if (cudaStreamCreateWithFlags(&a.ts, cudaStreamNonBlocking) != cudaSuccess) {
@@ -2259,7 +2263,9 @@ extern "C" int gf_adjoint_setup(gf_ctx* c, int64_t nsteps, int32_t checkpoint_ev
       !(a.x1acc = adj_alloc(c, spec)) || !(a.ubar_in = adj_alloc(c, spec)) || !(a.ubar_out = adj_alloc(c, spec)) ||
       !(a.final_state = adj_alloc(c, spec)) || !(a.tmp = adj_alloc(c, spec)) || !(a.Wb = adj_alloc(c, a.nwb * wide)) ||
       !(a.Pb = adj_alloc(c, 3 * wide)) || !(a.etab = adj_alloc(c, plane)) ||
-      (c->m.hasC && (!(a.qxb = adj_alloc(c, plane)) || !(a.qyb = adj_alloc(c, plane))))) {
+      (c->cfg.module == GF_SINGLELAYERQG && c->m.hasC &&
+       (!(a.qxb = adj_alloc(c, plane)) || !(a.qyb = adj_alloc(c, plane)))) ||
+      ((g.nl > 1 || c->m.drag) && !(a.nbar = adj_alloc(c, spec)))) {
     adj_release(c);
     return fail(c, GF_ERR_NOMEM, "adjoint buffers");
   }
@@ -2370,6 +2376,7 @@ static AdjArgs adj_args(gf_ctx* c) {
   a.hasC = c->m.hasC;
   a.Qy1D = c->m.Qy1D; a.Qx2D = c->m.Qx2D; a.Qy2D = c->m.Qy2D;
   a.qxb = d.qxb; a.qyb = d.qyb;
+  a.nbar = d.nbar;
   return a;
 }
 
@@ -2402,7 +2409,7 @@ static int adj_unit(gf_ctx* c, AdjArgs& a, int u) {
       const double ts = c->t + (stg == 1 ? 0.0 : stg == 4 ? dt : 0.5 * dt);
       StepArgs s = stage_args(c, stg, ts);
       s.clk = c->dclk;
-      c->row_phys = ph + ((size_t)i * 4 + stg - 1) * 3 * plane;
+      c->row_phys = ph + ((size_t)i * 4 + stg - 1) * 3 * g.nl * plane;
       const int r = launch_stage(c, s, 1, c->g.kcut < c->g.nkr);
       c->row_phys = nullptr;
       if (r) return r;
@@ -2419,7 +2426,7 @@ static int adj_unit(gf_ctx* c, AdjArgs& a, int u) {
     for (int r = 4; r >= 1; --r) {
       a.stage = r;
       a.head = (r == 1) && !(u == 0 && i == 0);
-      a.phys = ph + ((size_t)i * 4 + r - 1) * 3 * plane;
+      a.phys = ph + ((size_t)i * 4 + r - 1) * 3 * g.nl * plane;
       GF_CUDA(c, DISPATCH(c, launch_adj_row, g, a, b, d.ts));
       GF_CUDA(c, DISPATCH(c, launch_adj_col, g, c->m, a, b, d.ts));
       c->launches += 2;
@@ -2531,18 +2538,29 @@ extern "C" int gf_grad(gf_ctx* c, int loss_kind, void* dq0, void* deta, double* 
   if (loss_kind != GF_LOSS_KINETIC_ENERGY) return fail(c, GF_ERR_ARG, "unknown loss");
   auto& d = c->adj;
   if (!d.ready) return fail(c, GF_ERR_STATE, "call gf_adjoint_setup first");
-  if (deta && c->cfg.module != GF_SINGLELAYERQG) return fail(c, GF_ERR_ARG, "TwoDNavierStokes has no topography");
+  if (deta && c->cfg.module != GF_SINGLELAYERQG)
+    return fail(c, GF_ERR_ARG, "the topography gradient covers SingleLayerQG");
   if (int r = gf_adjoint_forward(c)) return r;
-  // loss: SingleLayerQG.kinetic_energy / TwoDNavierStokes.energy of the final state
+  // loss: SingleLayerQG.kinetic_energy / TwoDNavierStokes.energy / the total kinetic energy of
+  // MultiLayerQG.energies of the final state
+  const bool ml = c->cfg.module == GF_MULTILAYERQG;
+  LayerWeights hw{};
+  for (int L = 0; L < c->g.nl; ++L) hw.w[L] = (ml && c->g.nl > 1) ? c->Hl[L] / c->Hsum : 1.0;
   if (loss) {
-    const int32_t id = 0;
-    if (int r = gf_diagnostics(c, &id, 1, loss)) return r;
+    std::vector<int32_t> ids(ml ? c->g.nl : 1);
+    for (size_t q = 0; q < ids.size(); ++q) ids[q] = (int32_t)q;
+    std::vector<double> v(ids.size());
+    if (int r = gf_diagnostics(c, ids.data(), (int32_t)ids.size(), v.data())) return r;
+    *loss = 0;
+    for (double x : v) *loss += x;
   }
-  GF_CUDA(c, DISPATCH(c, launch_adj_spec, c->g, c->m, c->sol, d.ubar_in, 0, c->stream));
+  if (ml) GF_CUDA(c, DISPATCH(c, launch_adj_spec_ml, c->g, c->m, hw, c->sol, d.ubar_in, 0, c->stream));
+  else GF_CUDA(c, DISPATCH(c, launch_adj_spec, c->g, c->m, c->sol, d.ubar_in, 0, c->stream));
   if (int r = adjoint_reverse(c)) return r;
   if (dq0) {  // gradient with respect to q0 in set_q!(prob, q0): rfft^T of the dealiased cotangent
-    GF_CUDA(c, DISPATCH(c, launch_adj_spec, c->g, c->m, d.ubar_out, d.tmp, 1, c->stream));
-    const size_t pf = (size_t)c->g.ny * c->g.nx * c->rb;
+    if (ml) GF_CUDA(c, DISPATCH(c, launch_adj_spec_ml, c->g, c->m, hw, d.ubar_out, d.tmp, 1, c->stream));
+    else GF_CUDA(c, DISPATCH(c, launch_adj_spec, c->g, c->m, d.ubar_out, d.tmp, 1, c->stream));
+    const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->rb;
     void* ph = (char*)c->phys + 3 * pf;
     if (int r = inv_transform(c, d.tmp, SF_RAW, 0, ph)) return r;
     if (int r = copy_phys_out(c, dq0, ph, where)) return r;

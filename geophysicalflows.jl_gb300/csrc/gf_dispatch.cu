@@ -160,6 +160,18 @@ cudaError_t launch_adj_row(const Geom& g, const AdjArgs& a, const Bufs& b, cudaS
 
 template <class T>
 cudaError_t launch_adj_col(const Geom& g, const ModArgs& m, const AdjArgs& a, const Bufs& b, cudaStream_t st) {
+  if (g.nl > 1 || m.drag) {  // MultiLayerQG: every layer of a column in one block
+    switch (g.ny) {
+      case 32: return launch_adj_col_ml_n<T, 32>(g, m, a, b, st);
+      case 64: return launch_adj_col_ml_n<T, 64>(g, m, a, b, st);
+      case 128: return launch_adj_col_ml_n<T, 128>(g, m, a, b, st);
+      case 256: return launch_adj_col_ml_n<T, 256>(g, m, a, b, st);
+      case 512: return launch_adj_col_ml_n<T, 512>(g, m, a, b, st);
+      case 1024: return launch_adj_col_ml_n<T, 1024>(g, m, a, b, st);
+      case 2048: return launch_adj_col_ml_n<T, 2048>(g, m, a, b, st);
+      default: return cudaErrorInvalidValue;
+    }
+  }
   if (g.fpRc) return launch_adj_col_fp<T>(g, m, a, b, st);
   switch (g.ny) {
     GF_ADJ_COL_CASE(32) GF_ADJ_COL_CASE(64) GF_ADJ_COL_CASE(128) GF_ADJ_COL_CASE(256) GF_ADJ_COL_CASE(512)
@@ -199,6 +211,59 @@ __global__ void adj_spec_kernel(Geom g, ModArgs m, const cplx<T>* in, cplx<T>* o
 template <class T>
 cudaError_t launch_adj_spec(const Geom& g, const ModArgs& m, const void* in, void* out, int op, cudaStream_t st) {
   adj_spec_kernel<T><<<256, 256, 0, st>>>(g, m, static_cast<const cplx<T>*>(in), static_cast<cplx<T>*>(out), op);
+  return cudaGetLastError();
+}
+
+// MultiLayerQG (every layer at an element): op 0, the gradient of the total kinetic energy
+// sum_j H_j / sum(H) sum_full K^2 |psi_j|^2 / (2 (nx ny)^2), psi = S^-1 X:
+//   out = S^-T (H_j / sum(H) w K^2 psi_j / (nx ny)^2);
+// op 1: out = M in nx ny / w with the k = 0 mode zeroed (set_q! zeroes it), every layer.
+template <class T>
+__global__ void adj_spec_ml_kernel(Geom g, ModArgs m, LayerWeights hw, const cplx<T>* in, cplx<T>* out, int op) {
+  const size_t n = (size_t)g.ny * g.nkr, lstride = (size_t)g.ny * g.ldk;
+  const int nl = g.nl;
+  const T dky = sel<T>(g.dky, g.dky_f, g.dky_l), dkx = sel<T>(g.dkx, g.dkx_f, g.dkx_l);
+  const T ell2 = sel<T>(m.ell_inv2, m.ell_inv2_f, m.ell_inv2_l), inv_n = sel<T>(g.inv_nxny, g.inv_nxny_f, g.inv_nxny_l);
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const int kr = (int)(e % g.nkr), j = (int)(e / g.nkr);
+    const size_t ti = (size_t)j * g.ldk + kr;
+    const bool edge = (kr == 0) || (2 * kr == g.nx);
+    if (op == 1) {
+      const T nn = T((double)g.nx * (double)g.ny);
+      const bool z = !kept(g, kr, j) || (kr == 0 && j == 0);
+      for (int L = 0; L < nl; ++L)
+        out[L * lstride + ti] = z ? czero<T>() : ((edge ? T(1) : T(0.5)) * nn) * in[L * lstride + ti];
+      continue;
+    }
+    const T krT = T(kr) * dkx, lv = T(lidx(g, j)) * dky;
+    const T K2 = krT * krT + lv * lv;
+    cplx<T> X[MAXL], P[MAXL];
+    for (int L = 0; L < nl; ++L) X[L] = in[L * lstride + ti];
+    psi_all<T>(m, nl, K2, X, P, ti);
+    const T w = edge ? T(1) : T(2);
+    for (int L = 0; L < nl; ++L) P[L] = ((T(hw.w[L]) * w * K2) * inv_n * inv_n) * P[L];
+    if (m.psi_kind == PSI_EIGEN) {  // S^-T = Vinv^T diag(1/(lam - K^2)) V^T
+      for (int r = 0; r < nl; ++r) {
+        cplx<T> x = czero<T>();
+        if (K2 != T(0))
+          for (int q = 0; q < nl; ++q) {
+            cplx<T> sq = czero<T>();
+            for (int L = 0; L < nl; ++L) sq = sq + T(m.V[L * MAXL + q]) * P[L];
+            x = x + (T(m.Vinv[q * MAXL + r]) * (T(1) / (T(m.lam[q]) - K2))) * sq;
+          }
+        out[r * lstride + ti] = x;
+      }
+    } else {
+      const T f = psi_factor<T>(m.psi_kind, K2, ell2, m.mult, ti);
+      for (int L = 0; L < nl; ++L) out[L * lstride + ti] = f * P[L];
+    }
+  }
+}
+
+template <class T>
+cudaError_t launch_adj_spec_ml(const Geom& g, const ModArgs& m, const LayerWeights& hw, const void* in, void* out,
+                               int op, cudaStream_t st) {
+  adj_spec_ml_kernel<T><<<256, 256, 0, st>>>(g, m, hw, static_cast<const cplx<T>*>(in), static_cast<cplx<T>*>(out), op);
   return cudaGetLastError();
 }
 
@@ -276,6 +341,8 @@ cudaError_t launch_flux(const Geom& g, const void* v, const void* uy, const void
   template cudaError_t launch_adj_col<T>(const Geom&, const ModArgs&, const AdjArgs&, const Bufs&, cudaStream_t); \
   template cudaError_t launch_adj_spec<T>(const Geom&, const ModArgs&, const void*, void*, int, cudaStream_t);      \
   template cudaError_t launch_sub2<T>(size_t, void*, const void*, const void*, cudaStream_t);                     \
+  template cudaError_t launch_adj_spec_ml<T>(const Geom&, const ModArgs&, const LayerWeights&, const void*, void*, \
+                                             int, cudaStream_t);                                               \
   template cudaError_t launch_flux<T>(const Geom&, const void*, const void*, const void*, const double*, double*,   \
                                       int, cudaStream_t);
 

@@ -208,6 +208,24 @@ cudaError_t launch_adj_col_nr(const Geom& g, const ModArgs& m, const AdjArgs& a,
   return cudaGetLastError();
 }
 
+// the several-layer adjoint column kernel: every layer of C columns per block (C from the
+// shared-memory budget: 3 x nl x C columns)
+template <class T, int NN>
+cudaError_t launch_adj_col_ml_n(const Geom& g, const ModArgs& m, const AdjArgs& a, const Bufs& b, cudaStream_t st) {
+  cudaError_t err;
+  const size_t e = sizeof(cplx<T>);
+  constexpr int R = RADIX<T>;
+  auto smem = [&](int c) { return (size_t)3 * g.nl * c * col_stride<T>(NN, c) * e; };
+  const int C = pick_C(NN, R, g.nkr, smem, 1);
+  if (smem(C) > (size_t)SMEM_CAP) return cudaErrorInvalidConfiguration;
+  Geom g2 = g;
+  g2.cs = col_stride<T>(NN, C);
+  auto k = adj_col_ml_kernel<T, NN, R>;
+  if ((err = set_smem(k, smem(C))) != cudaSuccess) return err;
+  k<<<(g.nkr + C - 1) / C, C * (NN / R), smem(C), st>>>(g2, m, a, b, C);
+  return cudaGetLastError();
+}
+
 template <class T, int NN>
 cudaError_t launch_adj_row_n(const Geom& g, const AdjArgs& a, const Bufs& b, cudaStream_t st) {
   return launch_adj_row_nr<T, NN, RADIX<T>>(g, a, b, st);
@@ -238,6 +256,8 @@ cudaError_t launch_adj_col_n(const Geom& g, const ModArgs& m, const AdjArgs& a, 
   template cudaError_t launch_col_fwd_n<T, NN>(const Geom&, const Bufs&, int, void*, int, cudaStream_t);        \
   template cudaError_t launch_adj_row_n<T, NN>(const Geom&, const AdjArgs&, const Bufs&, cudaStream_t);         \
   template cudaError_t launch_adj_col_n<T, NN>(const Geom&, const ModArgs&, const AdjArgs&, const Bufs&,        \
-                                               cudaStream_t);
+                                               cudaStream_t);                                                  \
+  template cudaError_t launch_adj_col_ml_n<T, NN>(const Geom&, const ModArgs&, const AdjArgs&, const Bufs&,     \
+                                                  cudaStream_t);
 
 }  // namespace gf

@@ -167,6 +167,9 @@ struct AdjArgs {
   int hasC;
   const void *Qy1D, *Qx2D, *Qy2D;
   void *qxb, *qyb;
+  // several layers or bottom drag (MultiLayerQG): Nbar of the current stage of every layer,
+  // [layer][j][ldk], written by each column launch for the next (the drag term reads it)
+  void* nbar;
 };
 
 // Generic transforms (updatevars!, set_*!, fwdtransform!/invtransform!).
@@ -244,6 +247,11 @@ template <class T> cudaError_t launch_adj_col(const Geom&, const ModArgs&, const
 // element-wise adjoint helpers: op 0 kinetic-energy gradient, op 1 rfft^T preparation (see gf_dispatch.cu)
 template <class T> cudaError_t launch_adj_spec(const Geom&, const ModArgs&, const void* in, void* out, int op,
                                                cudaStream_t);
+
+// per-layer weights (H_j / sum H) of the MultiLayerQG kinetic-energy loss
+struct LayerWeights { double w[MAXL]; };
+template <class T> cudaError_t launch_adj_spec_ml(const Geom&, const ModArgs&, const LayerWeights&, const void* in,
+                                                  void* out, int op, cudaStream_t);
 
 // out -= a + b over n physical elements (gf_dispatch.cu)
 template <class T> cudaError_t launch_sub2(size_t n, void* out, const void* a, const void* b, cudaStream_t);

@@ -129,5 +129,7 @@ template <class T, int NN> cudaError_t launch_col_fwd_n(const Geom&, const Bufs&
 template <class T, int NN> cudaError_t launch_adj_row_n(const Geom&, const AdjArgs&, const Bufs&, cudaStream_t);
 template <class T, int NN> cudaError_t launch_adj_col_n(const Geom&, const ModArgs&, const AdjArgs&, const Bufs&,
                                                         cudaStream_t);
+template <class T, int NN>
+cudaError_t launch_adj_col_ml_n(const Geom&, const ModArgs&, const AdjArgs&, const Bufs&, cudaStream_t);
 
 }  // namespace gf

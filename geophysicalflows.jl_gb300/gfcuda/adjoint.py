@@ -5,7 +5,8 @@ ChainRulesCore.rrule on stepforward!), over libgfcuda's adjoint entry points.
     pullback = stepforward_with_pullback(prob, nsteps)           # rrule-style
     sol0_bar, eta_bar = pullback(sol_bar)
 
-TwoDNavierStokes and SingleLayerQG (constant U or U(y)) with ETDRK4, FilteredETDRK4, RK4 or FilteredRK4.  The
+TwoDNavierStokes, SingleLayerQG (constant U or U(y)) and MultiLayerQG with ETDRK4, FilteredETDRK4, RK4 or
+FilteredRK4.  The
 gradients are those of the discrete step the library computes, in the Problem's precision.
 """
 import ctypes as C
@@ -33,13 +34,14 @@ def info(prob):
 
 def grad(prob, nsteps=None, checkpoint_every=25, topography=None):
     """Step prob forward nsteps from its current state and return (loss, dq0, deta): the
-    final kinetic energy and its gradients with respect to the physical initial field (as
-    given to set_q!/set_zeta!) and to the topographic PV eta (SingleLayerQG; None for
-    TwoDNavierStokes unless topography=True is asked of it)."""
+    final kinetic energy (MultiLayerQG: the total of energies(prob)[0]) and its gradients with
+    respect to the physical initial field (as given to set_q!/set_zeta!; every layer) and to
+    the topographic PV eta (SingleLayerQG; None otherwise unless topography=True is asked)."""
     if nsteps is not None and getattr(prob, "_adj_steps", None) != int(nsteps):
         setup(prob, nsteps, checkpoint_every)
     g = prob.grid
-    dq0 = np.empty((g.ny, g.nx), dtype=prob.T)
+    nl = getattr(prob, "nlayers", 1)
+    dq0 = np.empty((nl, g.ny, g.nx) if prob.module == "MultiLayerQG" else (g.ny, g.nx), dtype=prob.T)
     want_eta = prob.module == "SingleLayerQG" if topography is None else topography
     deta = np.empty((g.ny, g.nx), dtype=prob.T) if want_eta else None
     loss = C.c_double()

@@ -279,7 +279,11 @@ class SLQGAdjoint:
         for n in range(nsteps - 1, -1, -1):
             ubar, eb = self.step_adj(us[n], eta, ubar)
             etabar += eb
-        return self.kinetic_energy(us[-1]), rfft2_T(self.mask * ubar, self.g), etabar
+        return self.kinetic_energy(us[-1]), self.initial_state_T(ubar), etabar
+
+    def initial_state_T(self, ubar):
+        """transpose of initial_state: the cotangent of q0"""
+        return rfft2_T(self.mask * ubar, self.g)
 
     def directional_derivative(self, q0, eta, nsteps, dq0, deta):
         """dL along (dq0, deta) from the tangent-linear model."""
@@ -288,6 +292,112 @@ class SLQGAdjoint:
             du = self.step_tlm(u, eta, du, deta)
             u = self.step(u, eta)[0]
         return float(np.sum(np.real(np.conj(self.kinetic_energy_grad(u)) * du)))
+
+
+class MLQGAdjoint(SLQGAdjoint):
+    """Tangent-linear and adjoint of an oracle MultiLayerQG problem (src/multilayerqg.jl:651-731,
+    the nonlinear calcN!) stepped with ETDRK4, FilteredETDRK4, RK4 or FilteredRK4, with respect
+    to the initial PV of every layer (the topography and the mean flow are parameters here).
+    Per layer j, with psi_hat = S^-1 q_hat (per wavenumber, src/multilayerqg.jl:495-509),
+    u'_j = irfft(-i l psi_hat_j) + U_j(y), v_j = irfft(i kr psi_hat_j), q_j = irfft(q_hat_j):
+      N_j = -rfft(u'_j Qx_j) - rfft(v_j Qy_j) - i kr rfft(u'_j q_j) - i l rfft(v_j q_j)
+            (+ mu K^2 psi_hat_n in the bottom layer),
+    and its transpose for Nbar: abar, bbar, cbar = rfft^T(i kr Nbar, i l Nbar, -Nbar),
+      ubar = abar q + cbar Qx, vbar = bbar q + cbar Qy, qbar = abar u' + bbar v,
+      psibar = i l irfft^T(ubar) - i kr irfft^T(vbar) (+ mu K^2 Nbar_n in the bottom layer),
+      Xbar = irfft^T(qbar) + S^-T psibar.
+    The loss is the total kinetic energy sum_j KE_j of MultiLayerQG.energies
+    (src/multilayerqg.jl:918-951)."""
+
+    def __init__(self, prob):
+        if prob.linear:
+            raise NotImplementedError("the adjoint covers the nonlinear step")
+        ts = prob.timestepper
+        if ts.kind not in ("ETDRK4", "RK4"):
+            raise NotImplementedError("the adjoint follows the ETDRK4 and RK4 stages")
+        self.varying = False
+        self.kind = ts.kind
+        self.L, self.dt = prob.L, prob.clock.dt
+        self.p, self.g = prob, prob.grid
+        g = self.g
+        self.n = prob.nlayers
+        self.mask = np.ones((g.ny, g.nkr))
+        O.dealias(self.mask, g)
+        self.filter = ts.filter if getattr(ts, "filtered", False) else None
+        if ts.kind == "ETDRK4":
+            self.c = dict(e=ts.expLdt, e2=ts.expLdt2, z=ts.zeta, a=ts.alpha, b=ts.beta, g=ts.gamma)
+        self.U = prob.Uy[:, :, None]
+        self.Qx, self.Qy = prob.Qx, prob.Qy
+        self.mu = prob.mu
+        self.Hw = np.asarray(prob.H, dtype=np.float64) / np.sum(prob.H) if self.n > 1 else np.ones(1)
+
+    def _psi(self, X):
+        if self.n == 1:
+            return -self.g.invKrsq * X
+        return np.einsum("yxij,jyx->iyx", self.p.Sinv, X)
+
+    def _psiT(self, P):
+        if self.n == 1:
+            return -self.g.invKrsq * P
+        return np.einsum("yxij,iyx->jyx", self.p.Sinv, P)
+
+    def _fields(self, X):
+        g = self.g
+        psih = self._psi(X)
+        return psih, O.irfft2(X, g), O.irfft2(-1j * g.l * psih, g), O.irfft2(1j * g.kr * psih, g)
+
+    def N(self, X, eta):
+        g = self.g
+        psih, q, u, v = self._fields(X)
+        u = u + self.U
+        N = (-O.rfft2(u * self.Qx) - O.rfft2(v * self.Qy) - 1j * g.kr * O.rfft2(u * q)
+             - 1j * g.l * O.rfft2(v * q))
+        N[-1] += self.mu * g.Krsq * psih[-1]
+        return N
+
+    def N_tlm(self, X, eta, dX, deta):
+        g = self.g
+        psih, q, u, v = self._fields(X)
+        dpsih, dq, du, dv = self._fields(dX)
+        u = u + self.U
+        dN = (-O.rfft2(du * self.Qx) - O.rfft2(dv * self.Qy) - 1j * g.kr * O.rfft2(du * q + u * dq)
+              - 1j * g.l * O.rfft2(dv * q + v * dq))
+        dN[-1] += self.mu * g.Krsq * dpsih[-1]
+        return dN
+
+    def N_adj(self, X, eta, Nbar):
+        g = self.g
+        psih, q, u, v = self._fields(X)
+        u = u + self.U
+        abar = rfft2_T(1j * g.kr * Nbar, g)
+        bbar = rfft2_T(1j * g.l * Nbar, g)
+        cbar = rfft2_T(-Nbar, g)
+        ub, vb = irfft2_T(abar * q + cbar * self.Qx, g), irfft2_T(bbar * q + cbar * self.Qy, g)
+        qbar = abar * u + bbar * v
+        psib = 1j * g.l * ub - 1j * g.kr * vb
+        psib[-1] += self.mu * g.Krsq * Nbar[-1]
+        return irfft2_T(qbar, g) + self._psiT(psib), np.zeros_like(eta)
+
+    def kinetic_energy(self, sol):
+        g = self.g
+        a = _w(g) * g.Krsq * np.abs(self._psi(sol)) ** 2
+        return float(np.sum(self.Hw[:, None, None] * a)) / (2 * (g.nx * g.ny) ** 2)
+
+    def kinetic_energy_grad(self, sol):
+        g = self.g
+        return self._psiT(self.Hw[:, None, None] * _w(g) * g.Krsq * self._psi(sol)) / (g.nx * g.ny) ** 2
+
+    def initial_state(self, q0):
+        """set_q! (src/multilayerqg.jl:842-870): rfft of every layer, the k = 0 mode zeroed,
+        dealiased by updatevars!"""
+        qh = O.rfft2(q0)
+        qh[..., 0, 0] = 0
+        return self.mask * qh
+
+    def initial_state_T(self, ubar):
+        ub = self.mask * ubar
+        ub[..., 0, 0] = 0
+        return rfft2_T(ub, self.g)
 
 
 def random_topography(grid, kmax, amp, seed):

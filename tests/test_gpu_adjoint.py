@@ -1,4 +1,5 @@
-"""GPU adjoint of the ETDRK4 and RK4 steps (gf_adjoint_* / gf_grad) against the oracle's discrete
+"""GPU adjoint of the ETDRK4 and RK4 steps of TwoDNavierStokes, SingleLayerQG (constant U and
+U(y)) and MultiLayerQG (gf_adjoint_* / gf_grad) against the oracle's discrete
 adjoint (oracle/gf_adjoint.py, itself pinned by finite differences and the tangent-linear
 dot-product identity), against central finite differences of the GPU forward model, and for
 checkpoint-interval invariance."""
@@ -11,7 +12,7 @@ import gf_oracle as O
 pytestmark = pytest.mark.gpu
 
 gfcuda = pytest.importorskip("gfcuda")
-from gfcuda import SingleLayerQG as SL, TwoDNavierStokes as TD, adjoint  # noqa: E402
+from gfcuda import MultiLayerQG as ML, SingleLayerQG as SL, TwoDNavierStokes as TD, adjoint  # noqa: E402
 from gfcuda import stepforward  # noqa: E402
 
 
@@ -271,3 +272,54 @@ def test_binomial_checkpointing_same_gradient_fewer_snapshots():
             ref = (loss, dq0, deta)
         else:
             assert loss == ref[0] and np.array_equal(dq0, ref[1]) and np.array_equal(deta, ref[2])
+
+
+def mlqg_case(n, nl, stepper):
+    g = O.Grid(n)
+    kw = dict(nx=n, f0=1.0, beta=5.0, H=[0.2, 0.3, 0.5], b=[-1.0, -1.2, -1.2 - 0.5 / 5.5], U=[1.0, 0.5, 0.0],
+              mu=0.05, dt=2.5e-3, stepper=stepper, eta=AD.random_topography(g, 6, 0.3, 9))
+    if nl == 2:
+        kw.update(H=[0.4, 0.6], b=[-1.0, -1.2], U=[0.5, 0.0])
+    q0 = 1e-2 * np.random.default_rng(1234).standard_normal((nl, n, n))
+    return kw, q0
+
+
+@pytest.mark.parametrize("nl,stepper", [(3, "ETDRK4"), (2, "FilteredRK4"), (3, "RK4")])
+def test_mlqg_gradient_matches_oracle_adjoint(nl, stepper):
+    """MultiLayerQG (PV inversion across layers, bottom drag, topographic and planetary PV
+    gradients, a mean flow per layer): the gradient of the total kinetic energy with respect
+    to the initial PV of every layer against the oracle's discrete adjoint"""
+    n, ns = 64, 10
+    kw, q0 = mlqg_case(n, nl, stepper)
+    p = ML.Problem(nl, "GPU", T=np.float64, **kw)
+    ML.set_q(p, q0)
+    loss, dq0, deta = adjoint.grad(p, ns, checkpoint_every=4)
+    assert deta is None and dq0.shape == (nl, n, n)
+    KE = ML.energies(p)[0]
+    p.close()
+    A = AD.MLQGAdjoint(O.MultiLayerQG(nl, **kw))
+    L, gq, _ = A.gradient(q0, np.zeros((n, n)), ns)
+    assert abs(loss - L) <= 1e-13 * L and abs(float(np.sum(KE)) - L) <= 1e-12 * L
+    assert rel(dq0, gq) <= 1e-11
+
+
+def test_mlqg_gradient_df64_and_checkpoint_invariance():
+    n, ns, nl = 64, 8, 3
+    kw, q0 = mlqg_case(n, nl, "ETDRK4")
+    A = AD.MLQGAdjoint(O.MultiLayerQG(nl, **kw))
+    L, gq, _ = A.gradient(q0, np.zeros((n, n)), ns)
+    ref = None
+    for every in (1, 3, 8):
+        p = ML.Problem(nl, "GPU", T=np.float64, **kw)
+        ML.set_q(p, q0)
+        loss, dq0, _ = adjoint.grad(p, ns, checkpoint_every=every)
+        p.close()
+        if ref is None:
+            ref = (loss, dq0)
+        else:
+            assert loss == ref[0] and np.array_equal(dq0, ref[1])
+    p = ML.Problem(nl, "GPU", T=np.float64, precision="DF64", **kw)
+    ML.set_q(p, q0)
+    loss, dq0, _ = adjoint.grad(p, ns, checkpoint_every=4)
+    p.close()
+    assert abs(loss - L) <= 1e-12 * L and rel(dq0, gq) <= 1e-10

@@ -69,3 +69,49 @@ def test_dot_product_identity(stepper, U):
     g = O.Grid(16)
     assert np.sum(np.real(np.conj(X) * O.rfft2(x))) == pytest.approx(np.sum(x * AD.rfft2_T(X, g)), rel=1e-12)
     assert np.sum(np.real(np.conj(X) * AD.irfft2_T(x, g))) == pytest.approx(np.sum(x * O.irfft2(X, g)), rel=1e-12)
+
+
+def ml_setup(stepper, n=32, nl=3):
+    g = O.Grid(n)
+    kw = dict(nx=n, f0=1.0, beta=5.0, H=[0.2, 0.3, 0.5], b=[-1.0, -1.2, -1.2 - 0.5 / 5.5][:nl], U=[1.0, 0.5, 0.0][:nl],
+              mu=0.05, dt=2.5e-3, stepper=stepper)
+    if nl == 2:
+        kw["H"] = [0.4, 0.6]
+    kw["eta"] = AD.random_topography(g, 6, 0.3, 9)
+    q0 = 1e-2 * np.random.default_rng(1234).standard_normal((nl, n, n))
+    p = O.MultiLayerQG(nl, **kw)
+    return p, AD.MLQGAdjoint(p), q0, kw
+
+
+@pytest.mark.parametrize("stepper,nl", [("ETDRK4", 3), ("FilteredRK4", 2), ("RK4", 3)])
+def test_mlqg_adjoint_forward_and_central_differences(stepper, nl):
+    p, A, q0, kw = ml_setup(stepper, nl=nl)
+    ns = 10
+    p.set_q(q0)
+    p.stepforward(ns)
+    KE = p.energies()[0]
+    eta0 = np.zeros((32, 32))
+    assert A.loss(q0, eta0, ns) == pytest.approx(float(np.sum(KE)), rel=1e-12)
+    _, gq, _ = A.gradient(q0, eta0, ns)
+    rng = np.random.default_rng(5)
+    for _ in range(4):
+        dq = rng.standard_normal(q0.shape)
+        eps = 1e-6
+        fd = (A.loss(q0 + eps * dq, eta0, ns) - A.loss(q0 - eps * dq, eta0, ns)) / (2 * eps)
+        ad = float(np.sum(gq * dq))
+        assert abs(fd - ad) <= 1e-6 * abs(ad)
+
+
+def test_mlqg_dot_product_identity():
+    p, A, q0, kw = ml_setup("ETDRK4")
+    rng = np.random.default_rng(2)
+    eta0 = np.zeros((32, 32))
+    u = A.initial_state(q0)
+    for _ in range(3):
+        u = A.step(u, eta0)[0]
+    du = A.initial_state(rng.standard_normal(q0.shape))
+    ubar = np.fft.rfft2(rng.standard_normal(q0.shape))
+    lhs = np.sum(np.real(np.conj(ubar) * A.step_tlm(u, eta0, du, eta0)))
+    xb, _ = A.step_adj(u, eta0, ubar)
+    rhs = np.sum(np.real(np.conj(xb) * du))
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
