@@ -2181,8 +2181,9 @@ extern "C" int gf_step_output(gf_ctx* c, int64_t nsteps, int32_t every, const in
 static int adj_check(gf_ctx* c) {
   const int mod = c->cfg.module;
   if (c->g.rtx || c->g.rty) return fail(c, GF_ERR_UNSUPPORTED, "the adjoint needs power-of-two nx, ny in [32, 2048]");
-  if (mod != GF_TWODNAVIERSTOKES && mod != GF_SINGLELAYERQG && mod != GF_MULTILAYERQG)
-    return fail(c, GF_ERR_UNSUPPORTED, "the adjoint covers TwoDNavierStokes, SingleLayerQG and MultiLayerQG");
+  if (mod != GF_TWODNAVIERSTOKES && mod != GF_SINGLELAYERQG && mod != GF_MULTILAYERQG && mod != GF_SURFACEQG)
+    return fail(c, GF_ERR_UNSUPPORTED,
+                "the adjoint covers TwoDNavierStokes, SingleLayerQG, MultiLayerQG and SurfaceQG");
   if ((c->g.nl > 1 || c->m.drag) && (size_t)3 * c->g.nl * c->g.ny * c->cb > (size_t)SMEM_CAP)
     return fail(c, GF_ERR_UNSUPPORTED, "the several-layer adjoint holds every layer of a column: 3 x nlayers x ny "
                                        "complex values must fit in 200 KB of shared memory");
@@ -2558,7 +2559,9 @@ extern "C" int gf_grad(gf_ctx* c, int loss_kind, void* dq0, void* deta, double* 
   else GF_CUDA(c, DISPATCH(c, launch_adj_spec, c->g, c->m, c->sol, d.ubar_in, 0, c->stream));
   if (int r = adjoint_reverse(c)) return r;
   if (dq0) {  // gradient with respect to q0 in set_q!(prob, q0): rfft^T of the dealiased cotangent
-    if (ml) GF_CUDA(c, DISPATCH(c, launch_adj_spec_ml, c->g, c->m, hw, d.ubar_out, d.tmp, 1, c->stream));
+    // (MultiLayerQG set_q! and SurfaceQG set_b! remove the k = 0 mode: so does its cotangent)
+    if (ml || c->cfg.module == GF_SURFACEQG)
+      GF_CUDA(c, DISPATCH(c, launch_adj_spec_ml, c->g, c->m, hw, d.ubar_out, d.tmp, 1, c->stream));
     else GF_CUDA(c, DISPATCH(c, launch_adj_spec, c->g, c->m, d.ubar_out, d.tmp, 1, c->stream));
     const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->rb;
     void* ph = (char*)c->phys + 3 * pf;

@@ -5,8 +5,8 @@ ChainRulesCore.rrule on stepforward!), over libgfcuda's adjoint entry points.
     pullback = stepforward_with_pullback(prob, nsteps)           # rrule-style
     sol0_bar, eta_bar = pullback(sol_bar)
 
-TwoDNavierStokes, SingleLayerQG (constant U or U(y)) and MultiLayerQG with ETDRK4, FilteredETDRK4, RK4 or
-FilteredRK4.  The
+TwoDNavierStokes, SingleLayerQG (constant U or U(y)), MultiLayerQG and SurfaceQG with ETDRK4, FilteredETDRK4,
+RK4 or FilteredRK4.  The
 gradients are those of the discrete step the library computes, in the Problem's precision.
 """
 import ctypes as C

@@ -335,8 +335,10 @@ int gf_get_field_parallel(const gf_ctx* ctx, int32_t* out);
  * ChainRulesCore.rrule on stepforward! (the reference has no derivative; its step is
  * src/singlelayerqg.jl:356-382 / src/twodnavierstokes.jl:253-294 under FourierFlows' ETDRK4
  * or RK4).
- * Supported: TwoDNavierStokes and SingleLayerQG (constant U or U(y)), stepper ETDRK4,
- * FilteredETDRK4, RK4 or FilteredRK4, batch = 1.  It is the exact transpose of the discrete step the library
+ * Supported: TwoDNavierStokes, SingleLayerQG (constant U or U(y)), MultiLayerQG (nonlinear)
+ * and SurfaceQG, stepper ETDRK4, FilteredETDRK4, RK4 or FilteredRK4, batch = 1.  The loss
+ * GF_LOSS_KINETIC_ENERGY is the module's kinetic energy (MultiLayerQG: summed over the layers);
+ * the topography gradient is SingleLayerQG's.  It is the exact transpose of the discrete step the library
  * computes (dealiasing, PV inversion, stage combinations), in the context's precision.
  * Checkpointing: see gf_adjoint_set_snapshots (binomial schedule over units of
  * checkpoint_every steps; each unit is recomputed once with its forward fields kept).
@@ -349,10 +351,12 @@ int gf_get_field_parallel(const gf_ctx* ctx, int32_t* out);
  *   state and clock are left at the forward pass's result.  Spectral arrays are taken as
  *   real vectors of (Re, Im) pairs over the stored half spectrum.
  * gf_grad: gf_adjoint_forward, the loss of the final state (loss_kind
- *   GF_LOSS_KINETIC_ENERGY: SingleLayerQG.kinetic_energy, src/singlelayerqg.jl:546-553, or
- *   TwoDNavierStokes.energy, src/twodnavierstokes.jl:374-380) into *loss, and its gradients
- *   with respect to the physical initial field q0 of set_q!/set_zeta! (dq0, [ny][nx]) and
- *   to eta (deta), either may be NULL. */
+ *   GF_LOSS_KINETIC_ENERGY: SingleLayerQG.kinetic_energy, src/singlelayerqg.jl:546-553,
+ *   TwoDNavierStokes.energy, src/twodnavierstokes.jl:374-380, the sum of MultiLayerQG's
+ *   per-layer kinetic energies, src/multilayerqg.jl:918-951, or SurfaceQG.kinetic_energy,
+ *   src/surfaceqg.jl:380-400) into *loss, and its gradients with respect to the physical
+ *   initial field q0 of set_q!/set_zeta!/set_b! (dq0, [nlayers][ny][nx]) and to eta (deta,
+ *   SingleLayerQG), either may be NULL. */
 enum { GF_LOSS_KINETIC_ENERGY = 0 };
 int gf_adjoint_setup(gf_ctx* ctx, int64_t nsteps, int32_t checkpoint_every);
 /* Binomial checkpointing (Griewank's schedule) over units of checkpoint_every steps: the

@@ -63,6 +63,7 @@ class SLQGAdjoint:
         self.L, self.dt = prob.L, prob.clock.dt
         self.p, self.g = prob, prob.grid
         g = self.g
+        self.U0 = 0.0 if self.varying else prob.U
         self.f = (-g.invKrsq if prob.ell is None else -1.0 / (g.Krsq + 1.0 / prob.ell ** 2))
         self.mask = np.ones((g.ny, g.nkr))
         O.dealias(self.mask, g)
@@ -97,7 +98,7 @@ class SLQGAdjoint:
                     - 1j * g.l * O.rfft2(v * q))
         qe = q + eta
         return (-1j * g.kr * O.rfft2(u * qe) - 1j * g.l * O.rfft2(v * qe)
-                - 1j * g.kr * self.p.U * O.rfft2(eta))
+                - 1j * g.kr * self.U0 * O.rfft2(eta))
 
     def N_tlm(self, X, eta, dX, deta):
         g = self.g
@@ -111,7 +112,7 @@ class SLQGAdjoint:
                     - 1j * g.kr * O.rfft2(du * q + u * dq) - 1j * g.l * O.rfft2(dv * q + v * dq))
         qe, dqe = q + eta, dq + deta
         return (-1j * g.kr * O.rfft2(du * qe + u * dqe) - 1j * g.l * O.rfft2(dv * qe + v * dqe)
-                - 1j * g.kr * self.p.U * O.rfft2(deta))
+                - 1j * g.kr * self.U0 * O.rfft2(deta))
 
     def N_adj(self, X, eta, Nbar):
         """(Xbar, etabar) = J^T Nbar at (X, eta)."""
@@ -132,7 +133,7 @@ class SLQGAdjoint:
         abar = rfft2_T(1j * g.kr * Nbar, g)
         bbar = rfft2_T(1j * g.l * Nbar, g)
         qbar = abar * u + bbar * v
-        etabar = qbar + self.p.U * abar
+        etabar = qbar + self.U0 * abar
         ub, vb = irfft2_T(abar * qe, g), irfft2_T(bbar * qe, g)
         Xbar = irfft2_T(qbar, g) + self.f * (1j * g.l * ub - 1j * g.kr * vb)
         return Xbar, etabar
@@ -292,6 +293,40 @@ class SLQGAdjoint:
             du = self.step_tlm(u, eta, du, deta)
             u = self.step(u, eta)[0]
         return float(np.sum(np.real(np.conj(self.kinetic_energy_grad(u)) * du)))
+
+
+class SQGAdjoint(SLQGAdjoint):
+    """Tangent-linear and adjoint of an oracle SurfaceQG problem (src/surfaceqg.jl:257-297):
+    the SingleLayerQG form with psi_hat = -psihfrombh b_hat (K^-1 coth(H K)), no topography and
+    no mean flow; the loss is SurfaceQG.kinetic_energy, the cotangent of b0 has no k = 0 mode
+    (set_b! removes it)."""
+
+    def __init__(self, prob):
+        ts = prob.timestepper
+        if ts.kind not in ("ETDRK4", "RK4"):
+            raise NotImplementedError("the adjoint follows the ETDRK4 and RK4 stages")
+        self.varying = False
+        self.kind = ts.kind
+        self.L, self.dt = prob.L, prob.clock.dt
+        self.p, self.g = prob, prob.grid
+        g = self.g
+        self.U0 = 0.0
+        self.f = -prob.psihfrombh
+        self.mask = np.ones((g.ny, g.nkr))
+        O.dealias(self.mask, g)
+        self.filter = ts.filter if getattr(ts, "filtered", False) else None
+        if ts.kind == "ETDRK4":
+            self.c = dict(e=ts.expLdt, e2=ts.expLdt2, z=ts.zeta, a=ts.alpha, b=ts.beta, g=ts.gamma)
+
+    def initial_state(self, b0):
+        bh = O.rfft2(b0)
+        bh[0, 0] = 0
+        return self.mask * bh
+
+    def initial_state_T(self, ubar):
+        ub = self.mask * ubar
+        ub[0, 0] = 0
+        return rfft2_T(ub, self.g)
 
 
 class MLQGAdjoint(SLQGAdjoint):

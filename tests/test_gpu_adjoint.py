@@ -323,3 +323,19 @@ def test_mlqg_gradient_df64_and_checkpoint_invariance():
     loss, dq0, _ = adjoint.grad(p, ns, checkpoint_every=4)
     p.close()
     assert abs(loss - L) <= 1e-12 * L and rel(dq0, gq) <= 1e-10
+
+
+@pytest.mark.parametrize("stepper,H", [("FilteredETDRK4", np.inf), ("RK4", 1.0)])
+def test_sqg_gradient_matches_oracle_adjoint(stepper, H):
+    from gfcuda import SurfaceQG as SQ
+    n, ns = 64, 10
+    g = O.Grid(n)
+    kw = dict(nx=n, H=H, nu=1e-4, nnu=1, dt=0.005, stepper=stepper)
+    b0 = O.peakedisotropicspectrum(g, 5, 0.5, seed=3)
+    p = SQ.Problem("GPU", T=np.float64, **kw)
+    SQ.set_b(p, b0)
+    loss, db0, deta = adjoint.grad(p, ns, checkpoint_every=4)
+    p.close()
+    assert deta is None
+    L, gb, _ = AD.SQGAdjoint(O.SurfaceQG(**kw)).gradient(b0, np.zeros((n, n)), ns)
+    assert abs(loss - L) <= 1e-13 * L and rel(db0, gb) <= 1e-11

@@ -115,3 +115,25 @@ def test_mlqg_dot_product_identity():
     xb, _ = A.step_adj(u, eta0, ubar)
     rhs = np.sum(np.real(np.conj(xb) * du))
     assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+
+
+@pytest.mark.parametrize("stepper,H", [("FilteredETDRK4", np.inf), ("RK4", 1.0)])
+def test_sqg_adjoint_forward_and_central_differences(stepper, H):
+    n, ns = 32, 10
+    g = O.Grid(n)
+    kw = dict(nx=n, H=H, nu=1e-4, nnu=1, dt=0.005, stepper=stepper)
+    p = O.SurfaceQG(**kw)
+    A = AD.SQGAdjoint(p)
+    b0 = O.peakedisotropicspectrum(g, 5, 0.5, seed=3)
+    p.set_b(b0)
+    p.stepforward(ns)
+    zero = np.zeros((n, n))
+    assert A.loss(b0, zero, ns) == pytest.approx(p.kinetic_energy(), rel=1e-12)
+    _, gb, _ = A.gradient(b0, zero, ns)
+    rng = np.random.default_rng(6)
+    for _ in range(4):
+        db = rng.standard_normal(b0.shape)
+        eps = 1e-6
+        fd = (A.loss(b0 + eps * db, zero, ns) - A.loss(b0 - eps * db, zero, ns)) / (2 * eps)
+        ad = float(np.sum(gb * db))
+        assert abs(fd - ad) <= 1e-6 * abs(ad)
