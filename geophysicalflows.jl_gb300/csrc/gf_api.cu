@@ -1896,14 +1896,14 @@ extern "C" int gf_fluxes(gf_ctx* c, double* lateral, double* vertical) {
 }
 
 // ------------------------------------------------------------------------------ autotune
-// Launch-shape autotuner: times the step kernels of this context at every candidate shape
+// Launch-shape autotuner: times the step of this context at every candidate shape
 // -- column kernel: FFT radix (FP32: 4, 8, 16; FP64/df64: 8) x columns per block C, the TMA
 // column stage, and on small grids the field-parallel kernel (radix 2, 4, 8 x C); row
 // kernel: radix x row pairs per block B (threads per row = length / radix) and the
-// field-parallel kernel (radix 2, 4, 8) -- with CUDA events around each launch, and keeps
-// the fastest.  The state, clock, AB3 history and
-// stochastic-forcing record are restored afterwards; captured graphs are dropped (they
-// are re-captured with the new shapes).  The profiling counters are reset.
+// field-parallel kernel (radix 2, 4, 8) -- by the GPU time of a graph-replayed step, and
+// keeps the fastest.  The state, clock, AB3 history and stochastic-forcing record are
+// restored afterwards; captured graphs are dropped (they are re-captured with the new
+// shapes).
 static int set_shape(gf_ctx* c, int Rr, int B, int Rc, int C, int tmaC = 0) {
   c->g.tuneRr = Rr; c->g.tuneB = B; c->g.tuneRc = Rc; c->g.tuneC = C; c->g.tmaC = tmaC;
   drop_graphs(c);
@@ -2011,18 +2011,34 @@ extern "C" int gf_autotune(gf_ctx* c, int32_t reps, int32_t* shape) {
     c->W_valid = false;
   };
   // average time of the row (which = 0) or column (1) kernel at the current shape
-  auto measure = [&](int which, double* ms) -> int {
+  // time of one unobserved step (the bulk of a stepforward! call) at the current shape: a few
+  // steps captured as one CUDA graph, as gf_step replays them, replayed twice and the second
+  // replay timed with events -- GPU time only (per-launch events around small kernels also
+  // count the host's launch gaps).  The column candidates are compared with the row shape
+  // fixed, then the row candidates with the chosen column shape.
+  auto measure = [&](int, double* ms) -> int {
     restore();
     if (int r = upload_clock(c)) return r;
-    c->profiling = true;
-    if (int r = one_step(c, false)) return r;  // warm-up (and kernel attributes)
-    double m2[2]; int64_t n2[2];
-    if (int r = gf_profile_read(c, m2, n2, nullptr)) return r;
-    for (int k = 0; k < reps; ++k)  // unobserved steps: the bulk of a stepforward! call
-      if (int r = one_step(c, false)) return r;
-    if (int r = gf_profile_read(c, m2, n2, nullptr)) return r;
+    c->profiling = false;
+    if (int r = one_step(c, false)) return r;  // warm-up (kernel attributes, W)
+    if (int r = ensure_W(c)) return r;
+    const int G = (c->kind == SK_AB3) ? 3 : std::max(reps, 2);
+    cudaGraphExec_t gx = nullptr;
+    if (int r = capture_steps(c, G, &gx, false)) return r;
+    cudaEvent_t e0 = take_event(c), e1 = take_event(c);
+    cudaError_t err = cudaGraphLaunch(gx, c->stream);
+    if (err == cudaSuccess) err = cudaEventRecord(e0, c->stream);
+    if (err == cudaSuccess) err = cudaGraphLaunch(gx, c->stream);
+    if (err == cudaSuccess) err = cudaEventRecord(e1, c->stream);
+    if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+    float t = 0;
+    if (err == cudaSuccess) err = cudaEventElapsedTime(&t, e0, e1);
+    cudaGraphExecDestroy(gx);
+    c->ev_free.push_back(e0);
+    c->ev_free.push_back(e1);
     c->profiling = prof0;
-    *ms = m2[which] / std::max<int64_t>(n2[which], 1);
+    if (err != cudaSuccess) return fail(c, GF_ERR_CUDA, std::string("autotune timing: ") + cudaGetErrorString(err));
+    *ms = t / G;
     return GF_OK;
   };
   const bool f32 = c->prec == GF_F32;

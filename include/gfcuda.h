@@ -288,9 +288,10 @@ int gf_step_callback(gf_ctx* ctx, int64_t nsteps, gf_forcing_fn fn, void* user);
 /* ---- launch-shape autotuner (no reference counterpart) ----------------------------------
  * gf_autotune times the step kernels of this context at every candidate launch shape --
  * column kernel: FFT radix (FP32: 4, 8, 16; otherwise 8) x kr columns per block; row kernel:
- * radix x row pairs per block (threads per row = length / radix) -- over `reps` steps each
- * (<= 0: 4) and keeps the fastest.  The state, clock, AB3 history and stochastic-forcing
- * record are restored; captured graphs are re-captured; the profiling counters are reset.
+ * radix x row pairs per block (threads per row = length / radix) -- by the GPU time of
+ * `reps` steps (<= 0: 4) replayed from a CUDA graph, and keeps the fastest.  The state,
+ * clock, AB3 history and stochastic-forcing record are restored; captured graphs are
+ * re-captured.
  * shape (may be NULL) receives {row radix, row pairs per block, column radix, columns per
  * block}; 0 entries mean the built-in block-shape rule.  The candidates are timed on the
  * steps inside a gf_step call (those that skip the aliased modes); FP32 one-layer problems
