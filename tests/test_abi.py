@@ -76,6 +76,16 @@ def test_null_arguments(lib):
     assert lib.gf_create(None, None, None) == -1
     assert lib.gf_step(None, 1) == -1
     assert lib.gf_destroy(None) == 0
+    # launch-shape, field-parallel, TMA, ensemble and adjoint entry points refuse a null context
+    out = (C.c_int32 * 4)()
+    assert lib.gf_set_field_parallel(None, 4, 4, 1) == -1
+    assert lib.gf_get_field_parallel(None, out) == -1
+    assert lib.gf_set_tma_columns(None, 2) == -1
+    assert lib.gf_set_ensemble_mode(None, 1) == -1
+    assert lib.gf_set_launch_shape(None, out) == -1
+    assert lib.gf_autotune(None, 2, out) == -1
+    assert lib.gf_adjoint_setup(None, 10, 5) == -1
+    assert lib.gf_grad(None, 0, None, None, None, 0) == -1
 
 
 def test_python_mirror_validates(lib):
