@@ -145,7 +145,7 @@ __device__ __forceinline__ void adj_pair_products(const Geom& g, const AdjArgs& 
     if (last && Qy2) Qy = Qy + mk<T>(Qy2[ia], Qy2[ibb]);
     ub = ub + mk<T>(cb.x * Qx.x, cb.y * Qx.y);
     vb = vb + mk<T>(cb.x * Qy.x, cb.y * Qy.y);
-    if (a.qxb) {  // SingleLayerQG U(y): the topography gradient
+    if (a.qxb && last) {  // the topography gradient (it enters the bottom layer's Qx, Qy)
       T* qxb = static_cast<T*>(a.qxb);
       T* qyb = static_cast<T*>(a.qyb);
       qxb[ia] = qxb[ia] + cb.x * u.x;

@@ -1025,8 +1025,9 @@ static int copy_phys_in(gf_ctx* c, void* dst, const void* src, int where) {
   GF_CUDA(c, cudaMemcpyAsync(dst, src, n * c->rb, kind, c->stream));
   return GF_OK;
 }
-static int copy_phys_out(gf_ctx* c, void* dst, const void* src, int where) {
-  const size_t n = (size_t)c->g.nl * c->g.ny * c->g.nx * c->g.nb;
+// nplanes: the number of [ny][nx] planes (0: every layer of every instance)
+static int copy_phys_out(gf_ctx* c, void* dst, const void* src, int where, int nplanes = 0) {
+  const size_t n = (size_t)(nplanes > 0 ? nplanes : c->g.nl * c->g.nb) * c->g.ny * c->g.nx;
   const cudaMemcpyKind kind = where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
   if (c->prec == GF_DF64) {
     if (int r = convert_launch(c, false, src, n, c->stage, n, 1, n)) return r;
@@ -2280,7 +2281,7 @@ extern "C" int gf_adjoint_setup(gf_ctx* c, int64_t nsteps, int32_t checkpoint_ev
       !(a.x1acc = adj_alloc(c, spec)) || !(a.ubar_in = adj_alloc(c, spec)) || !(a.ubar_out = adj_alloc(c, spec)) ||
       !(a.final_state = adj_alloc(c, spec)) || !(a.tmp = adj_alloc(c, spec)) || !(a.Wb = adj_alloc(c, a.nwb * wide)) ||
       !(a.Pb = adj_alloc(c, 3 * wide)) || !(a.etab = adj_alloc(c, plane)) ||
-      (c->cfg.module == GF_SINGLELAYERQG && c->m.hasC &&
+      (((c->cfg.module == GF_SINGLELAYERQG && c->m.hasC) || c->cfg.module == GF_MULTILAYERQG) &&
        (!(a.qxb = adj_alloc(c, plane)) || !(a.qyb = adj_alloc(c, plane)))) ||
       ((g.nl > 1 || c->m.drag) && !(a.nbar = adj_alloc(c, spec)))) {
     adj_release(c);
@@ -2519,13 +2520,20 @@ static int adjoint_reverse(gf_ctx* c) {
   // the context stream continues after the last transposed stage (ubar_out, etab)
   GF_CUDA(c, cudaEventRecord(d.ev_sync, d.ts));
   GF_CUDA(c, cudaStreamWaitEvent(c->stream, d.ev_sync, 0));
-  if (d.qxb) {  // U(y): Qx = d(eta)/dx, Qy = d(eta)/dy - U_yy, so etabar -= d(Qxbar)/dx + d(Qybar)/dy
+  if (d.qxb) {  // U(y), MultiLayerQG: Qx = d(eta)/dx + ..., Qy = ... + d(eta)/dy (bottom layer),
+                //   so etabar -= d(Qxbar)/dx + d(Qybar)/dy (one-layer transforms)
     const size_t pf = (size_t)g.ny * g.nx * c->rb;
     char* ph = (char*)c->phys;
-    if (int r = fwd_transform(c, d.qxb, d.tmp, 0)) return r;
-    if (int r = inv_transform(c, d.tmp, SF_DX, 0, ph)) return r;
-    if (int r = fwd_transform(c, d.qyb, d.tmp, 0)) return r;
-    if (int r = inv_transform(c, d.tmp, SF_DY, 0, ph + pf)) return r;
+    Geom g1 = full_geom(c);
+    g1.nl = 1;
+    g1.nb = 1;
+    const void* src[2] = {d.qxb, d.qyb};
+    for (int k = 0; k < 2; ++k) {
+      GF_CUDA(c, DISPATCH(c, launch_row_r2c, g1, bufs(c), 1, src[k], c->stream));
+      GF_CUDA(c, DISPATCH(c, launch_col_fwd, g1, bufs(c), 1, d.tmp, 0, c->stream));
+      GF_CUDA(c, DISPATCH(c, launch_col_inv, g1, c->m, d.tmp, (int)(k == 0 ? SF_DX : SF_DY), 0, bufs(c), c->stream));
+      GF_CUDA(c, DISPATCH(c, launch_row_c2r, g1, bufs(c), 1, ph + k * pf, c->stream));
+    }
     GF_CUDA(c, DISPATCH(c, launch_sub2, (size_t)g.ny * g.nx, d.etab, ph, ph + pf, c->stream));
   }
   GF_CUDA(c, cudaMemcpyAsync(c->sol, d.final_state, spec, cudaMemcpyDeviceToDevice, c->stream));
@@ -2539,13 +2547,14 @@ extern "C" int gf_adjoint_backward(gf_ctx* c, const void* sol_bar, void* sol0_ba
   if (!c || !sol_bar) return GF_ERR_ARG;
   auto& d = c->adj;
   if (!d.forward_done) return fail(c, GF_ERR_STATE, "run gf_adjoint_forward first");
-  if (eta_bar && c->cfg.module != GF_SINGLELAYERQG) return fail(c, GF_ERR_ARG, "TwoDNavierStokes has no topography");
+  if (eta_bar && c->cfg.module != GF_SINGLELAYERQG && c->cfg.module != GF_MULTILAYERQG)
+    return fail(c, GF_ERR_ARG, "the topography gradient covers SingleLayerQG and MultiLayerQG");
   if (int r = copy_spec_in(c, d.ubar_in, sol_bar, where)) return r;
   if (int r = adjoint_reverse(c)) return r;
   if (sol0_bar)
     if (int r = copy_spec_out(c, sol0_bar, d.ubar_out, where)) return r;
   if (eta_bar)
-    if (int r = copy_phys_out(c, eta_bar, d.etab, where)) return r;
+    if (int r = copy_phys_out(c, eta_bar, d.etab, where, 1)) return r;
   if (where == GF_HOST) GF_CUDA(c, cudaStreamSynchronize(c->stream));
   return GF_OK;
 }
@@ -2555,8 +2564,8 @@ extern "C" int gf_grad(gf_ctx* c, int loss_kind, void* dq0, void* deta, double* 
   if (loss_kind != GF_LOSS_KINETIC_ENERGY) return fail(c, GF_ERR_ARG, "unknown loss");
   auto& d = c->adj;
   if (!d.ready) return fail(c, GF_ERR_STATE, "call gf_adjoint_setup first");
-  if (deta && c->cfg.module != GF_SINGLELAYERQG)
-    return fail(c, GF_ERR_ARG, "the topography gradient covers SingleLayerQG");
+  if (deta && c->cfg.module != GF_SINGLELAYERQG && c->cfg.module != GF_MULTILAYERQG)
+    return fail(c, GF_ERR_ARG, "the topography gradient covers SingleLayerQG and MultiLayerQG");
   if (int r = gf_adjoint_forward(c)) return r;
   // loss: SingleLayerQG.kinetic_energy / TwoDNavierStokes.energy / the total kinetic energy of
   // MultiLayerQG.energies of the final state
@@ -2585,7 +2594,7 @@ extern "C" int gf_grad(gf_ctx* c, int loss_kind, void* dq0, void* deta, double* 
     if (int r = copy_phys_out(c, dq0, ph, where)) return r;
   }
   if (deta)
-    if (int r = copy_phys_out(c, deta, d.etab, where)) return r;
+    if (int r = copy_phys_out(c, deta, d.etab, where, 1)) return r;
   if (where == GF_HOST) GF_CUDA(c, cudaStreamSynchronize(c->stream));
   return GF_OK;
 }

@@ -36,13 +36,14 @@ def grad(prob, nsteps=None, checkpoint_every=25, topography=None):
     """Step prob forward nsteps from its current state and return (loss, dq0, deta): the
     final kinetic energy (MultiLayerQG: the total of energies(prob)[0]) and its gradients with
     respect to the physical initial field (as given to set_q!/set_zeta!; every layer) and to
-    the topographic PV eta (SingleLayerQG; None otherwise unless topography=True is asked)."""
+    the topography eta (SingleLayerQG, MultiLayerQG; None otherwise unless topography=True is
+    asked)."""
     if nsteps is not None and getattr(prob, "_adj_steps", None) != int(nsteps):
         setup(prob, nsteps, checkpoint_every)
     g = prob.grid
     nl = getattr(prob, "nlayers", 1)
     dq0 = np.empty((nl, g.ny, g.nx) if prob.module == "MultiLayerQG" else (g.ny, g.nx), dtype=prob.T)
-    want_eta = prob.module == "SingleLayerQG" if topography is None else topography
+    want_eta = prob.module in ("SingleLayerQG", "MultiLayerQG") if topography is None else topography
     deta = np.empty((g.ny, g.nx), dtype=prob.T) if want_eta else None
     loss = C.c_double()
     prob._c(prob._lib.gf_grad(prob._ctx, A.LOSS_KINETIC_ENERGY, dq0.ctypes.data,
@@ -52,7 +53,8 @@ def grad(prob, nsteps=None, checkpoint_every=25, topography=None):
 
 def stepforward_with_pullback(prob, nsteps, checkpoint_every=25):
     """stepforward!(prob, nsteps) keeping checkpoints; returns pullback(sol_bar) ->
-    (sol0_bar, eta_bar), the cotangents of the initial state and (SingleLayerQG) of eta."""
+    (sol0_bar, eta_bar), the cotangents of the initial state and (SingleLayerQG, MultiLayerQG)
+    of eta."""
     setup(prob, nsteps, checkpoint_every)
     prob._c(prob._lib.gf_adjoint_forward(prob._ctx))
 
@@ -60,7 +62,7 @@ def stepforward_with_pullback(prob, nsteps, checkpoint_every=25):
         g = prob.grid
         sb = np.ascontiguousarray(np.broadcast_to(sol_bar, prob.spec_shape), dtype=prob.CT)
         s0 = np.empty(prob.spec_shape, dtype=prob.CT)
-        eb = np.empty((g.ny, g.nx), dtype=prob.T) if prob.module == "SingleLayerQG" else None
+        eb = np.empty((g.ny, g.nx), dtype=prob.T) if prob.module in ("SingleLayerQG", "MultiLayerQG") else None
         prob._c(prob._lib.gf_adjoint_backward(prob._ctx, sb.ctypes.data, s0.ctypes.data,
                                               None if eb is None else eb.ctypes.data, A.HOST))
         return s0, eb

@@ -339,7 +339,7 @@ int gf_get_field_parallel(const gf_ctx* ctx, int32_t* out);
  * Supported: TwoDNavierStokes, SingleLayerQG (constant U or U(y)), MultiLayerQG (nonlinear)
  * and SurfaceQG, stepper ETDRK4, FilteredETDRK4, RK4 or FilteredRK4, batch = 1.  The loss
  * GF_LOSS_KINETIC_ENERGY is the module's kinetic energy (MultiLayerQG: summed over the layers);
- * the topography gradient is SingleLayerQG's.  It is the exact transpose of the discrete step the library
+ * the topography gradient is SingleLayerQG's and MultiLayerQG's.  It is the exact transpose of the discrete step the library
  * computes (dealiasing, PV inversion, stage combinations), in the context's precision.
  * Checkpointing: see gf_adjoint_set_snapshots (binomial schedule over units of
  * checkpoint_every steps; each unit is recomputed once with its forward fields kept).
@@ -356,8 +356,8 @@ int gf_get_field_parallel(const gf_ctx* ctx, int32_t* out);
  *   TwoDNavierStokes.energy, src/twodnavierstokes.jl:374-380, the sum of MultiLayerQG's
  *   per-layer kinetic energies, src/multilayerqg.jl:918-951, or SurfaceQG.kinetic_energy,
  *   src/surfaceqg.jl:380-400) into *loss, and its gradients with respect to the physical
- *   initial field q0 of set_q!/set_zeta!/set_b! (dq0, [nlayers][ny][nx]) and to eta (deta,
- *   SingleLayerQG), either may be NULL. */
+ *   initial field q0 of set_q!/set_zeta!/set_b! (dq0, [nlayers][ny][nx]) and to the
+ *   topography eta (deta, [ny][nx]: SingleLayerQG, MultiLayerQG), either may be NULL. */
 enum { GF_LOSS_KINETIC_ENERGY = 0 };
 int gf_adjoint_setup(gf_ctx* ctx, int64_t nsteps, int32_t checkpoint_every);
 /* Binomial checkpointing (Griewank's schedule) over units of checkpoint_every steps: the

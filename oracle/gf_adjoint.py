@@ -332,7 +332,8 @@ class SQGAdjoint(SLQGAdjoint):
 class MLQGAdjoint(SLQGAdjoint):
     """Tangent-linear and adjoint of an oracle MultiLayerQG problem (src/multilayerqg.jl:651-731,
     the nonlinear calcN!) stepped with ETDRK4, FilteredETDRK4, RK4 or FilteredRK4, with respect
-    to the initial PV of every layer (the topography and the mean flow are parameters here).
+    to the initial PV of every layer and to the topography eta (which enters through the bottom
+    layer's Qx = d(eta)/dx + ..., Qy = ... + d(eta)/dy; the mean flow is a parameter).
     Per layer j, with psi_hat = S^-1 q_hat (per wavenumber, src/multilayerqg.jl:495-509),
     u'_j = irfft(-i l psi_hat_j) + U_j(y), v_j = irfft(i kr psi_hat_j), q_j = irfft(q_hat_j):
       N_j = -rfft(u'_j Qx_j) - rfft(v_j Qy_j) - i kr rfft(u'_j q_j) - i l rfft(v_j q_j)
@@ -340,7 +341,8 @@ class MLQGAdjoint(SLQGAdjoint):
     and its transpose for Nbar: abar, bbar, cbar = rfft^T(i kr Nbar, i l Nbar, -Nbar),
       ubar = abar q + cbar Qx, vbar = bbar q + cbar Qy, qbar = abar u' + bbar v,
       psibar = i l irfft^T(ubar) - i kr irfft^T(vbar) (+ mu K^2 Nbar_n in the bottom layer),
-      Xbar = irfft^T(qbar) + S^-T psibar.
+      Xbar = irfft^T(qbar) + S^-T psibar,
+      etabar = -d/dx(cbar_n u'_n) - d/dy(cbar_n v_n) (transposes of the spectral derivatives).
     The loss is the total kinetic energy sum_j KE_j of MultiLayerQG.energies
     (src/multilayerqg.jl:918-951)."""
 
@@ -362,7 +364,10 @@ class MLQGAdjoint(SLQGAdjoint):
         if ts.kind == "ETDRK4":
             self.c = dict(e=ts.expLdt, e2=ts.expLdt2, z=ts.zeta, a=ts.alpha, b=ts.beta, g=ts.gamma)
         self.U = prob.Uy[:, :, None]
-        self.Qx, self.Qy = prob.Qx, prob.Qy
+        # the PV gradients without the topography's share (added back for a given eta)
+        self.Qx0, self.Qy0 = prob.Qx.copy(), prob.Qy.copy()
+        self.Qx0[-1] -= self._dx(prob.eta)
+        self.Qy0[-1] -= self._dy(prob.eta)
         self.mu = prob.mu
         self.Hw = np.asarray(prob.H, dtype=np.float64) / np.sum(prob.H) if self.n > 1 else np.ones(1)
 
@@ -381,11 +386,18 @@ class MLQGAdjoint(SLQGAdjoint):
         psih = self._psi(X)
         return psih, O.irfft2(X, g), O.irfft2(-1j * g.l * psih, g), O.irfft2(1j * g.kr * psih, g)
 
+    def _Q(self, eta):
+        Qx, Qy = self.Qx0.copy(), self.Qy0.copy()
+        Qx[-1] += self._dx(eta)
+        Qy[-1] += self._dy(eta)
+        return Qx, Qy
+
     def N(self, X, eta):
         g = self.g
         psih, q, u, v = self._fields(X)
         u = u + self.U
-        N = (-O.rfft2(u * self.Qx) - O.rfft2(v * self.Qy) - 1j * g.kr * O.rfft2(u * q)
+        Qx, Qy = self._Q(eta)
+        N = (-O.rfft2(u * Qx) - O.rfft2(v * Qy) - 1j * g.kr * O.rfft2(u * q)
              - 1j * g.l * O.rfft2(v * q))
         N[-1] += self.mu * g.Krsq * psih[-1]
         return N
@@ -395,8 +407,10 @@ class MLQGAdjoint(SLQGAdjoint):
         psih, q, u, v = self._fields(X)
         dpsih, dq, du, dv = self._fields(dX)
         u = u + self.U
-        dN = (-O.rfft2(du * self.Qx) - O.rfft2(dv * self.Qy) - 1j * g.kr * O.rfft2(du * q + u * dq)
+        Qx, Qy = self._Q(eta)
+        dN = (-O.rfft2(du * Qx) - O.rfft2(dv * Qy) - 1j * g.kr * O.rfft2(du * q + u * dq)
               - 1j * g.l * O.rfft2(dv * q + v * dq))
+        dN[-1] -= O.rfft2(u[-1] * self._dx(deta)) + O.rfft2(v[-1] * self._dy(deta))
         dN[-1] += self.mu * g.Krsq * dpsih[-1]
         return dN
 
@@ -407,11 +421,13 @@ class MLQGAdjoint(SLQGAdjoint):
         abar = rfft2_T(1j * g.kr * Nbar, g)
         bbar = rfft2_T(1j * g.l * Nbar, g)
         cbar = rfft2_T(-Nbar, g)
-        ub, vb = irfft2_T(abar * q + cbar * self.Qx, g), irfft2_T(bbar * q + cbar * self.Qy, g)
+        Qx, Qy = self._Q(eta)
+        ub, vb = irfft2_T(abar * q + cbar * Qx, g), irfft2_T(bbar * q + cbar * Qy, g)
         qbar = abar * u + bbar * v
         psib = 1j * g.l * ub - 1j * g.kr * vb
         psib[-1] += self.mu * g.Krsq * Nbar[-1]
-        return irfft2_T(qbar, g) + self._psiT(psib), np.zeros_like(eta)
+        etabar = self._dT(cbar[-1] * u[-1], g.kr) + self._dT(cbar[-1] * v[-1], g.l)
+        return irfft2_T(qbar, g) + self._psiT(psib), etabar
 
     def kinetic_energy(self, sol):
         g = self.g

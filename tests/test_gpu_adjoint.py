@@ -294,20 +294,20 @@ def test_mlqg_gradient_matches_oracle_adjoint(nl, stepper):
     p = ML.Problem(nl, "GPU", T=np.float64, **kw)
     ML.set_q(p, q0)
     loss, dq0, deta = adjoint.grad(p, ns, checkpoint_every=4)
-    assert deta is None and dq0.shape == (nl, n, n)
+    assert dq0.shape == (nl, n, n) and deta.shape == (n, n)
     KE = ML.energies(p)[0]
     p.close()
     A = AD.MLQGAdjoint(O.MultiLayerQG(nl, **kw))
-    L, gq, _ = A.gradient(q0, np.zeros((n, n)), ns)
+    L, gq, ge = A.gradient(q0, kw["eta"], ns)
     assert abs(loss - L) <= 1e-13 * L and abs(float(np.sum(KE)) - L) <= 1e-12 * L
-    assert rel(dq0, gq) <= 1e-11
+    assert rel(dq0, gq) <= 1e-11 and rel(deta, ge) <= 1e-11
 
 
 def test_mlqg_gradient_df64_and_checkpoint_invariance():
     n, ns, nl = 64, 8, 3
     kw, q0 = mlqg_case(n, nl, "ETDRK4")
     A = AD.MLQGAdjoint(O.MultiLayerQG(nl, **kw))
-    L, gq, _ = A.gradient(q0, np.zeros((n, n)), ns)
+    L, gq, _ = A.gradient(q0, kw["eta"], ns)
     ref = None
     for every in (1, 3, 8):
         p = ML.Problem(nl, "GPU", T=np.float64, **kw)

@@ -90,30 +90,33 @@ def test_mlqg_adjoint_forward_and_central_differences(stepper, nl):
     p.set_q(q0)
     p.stepforward(ns)
     KE = p.energies()[0]
-    eta0 = np.zeros((32, 32))
-    assert A.loss(q0, eta0, ns) == pytest.approx(float(np.sum(KE)), rel=1e-12)
-    _, gq, _ = A.gradient(q0, eta0, ns)
+    assert A.loss(q0, kw["eta"], ns) == pytest.approx(float(np.sum(KE)), rel=1e-12)
+    eta = kw["eta"]
+    _, gq, ge = A.gradient(q0, eta, ns)
     rng = np.random.default_rng(5)
-    for _ in range(4):
+    g = O.Grid(32)
+    for i in range(4):
         dq = rng.standard_normal(q0.shape)
+        de = AD.random_topography(g, 6, 0.3, 40 + i)
         eps = 1e-6
-        fd = (A.loss(q0 + eps * dq, eta0, ns) - A.loss(q0 - eps * dq, eta0, ns)) / (2 * eps)
-        ad = float(np.sum(gq * dq))
+        fd = (A.loss(q0 + eps * dq, eta + eps * de, ns) - A.loss(q0 - eps * dq, eta - eps * de, ns)) / (2 * eps)
+        ad = float(np.sum(gq * dq)) + float(np.sum(ge * de))
         assert abs(fd - ad) <= 1e-6 * abs(ad)
 
 
 def test_mlqg_dot_product_identity():
     p, A, q0, kw = ml_setup("ETDRK4")
     rng = np.random.default_rng(2)
-    eta0 = np.zeros((32, 32))
+    eta = kw["eta"]
     u = A.initial_state(q0)
     for _ in range(3):
-        u = A.step(u, eta0)[0]
+        u = A.step(u, eta)[0]
     du = A.initial_state(rng.standard_normal(q0.shape))
+    de = rng.standard_normal(eta.shape)
     ubar = np.fft.rfft2(rng.standard_normal(q0.shape))
-    lhs = np.sum(np.real(np.conj(ubar) * A.step_tlm(u, eta0, du, eta0)))
-    xb, _ = A.step_adj(u, eta0, ubar)
-    rhs = np.sum(np.real(np.conj(xb) * du))
+    lhs = np.sum(np.real(np.conj(ubar) * A.step_tlm(u, eta, du, de)))
+    xb, eb = A.step_adj(u, eta, ubar)
+    rhs = np.sum(np.real(np.conj(xb) * du)) + np.sum(eb * de)
     assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
 
 
