@@ -2053,7 +2053,7 @@ extern "C" int gf_autotune(gf_ctx* c, int32_t reps, int32_t* shape) {
   for (int ri = 0; ri < (f32 ? 3 : 1) && rc == GF_OK; ++ri) {
     const int R = radii[ri], TPF = g0.ny / R;
     if (!f32_radix_built(g0.ny, R) || TPF < 1) continue;
-    for (const int C : {1, 2, 3, 4, 5, 6, 8, 16}) {
+    for (const int C : {1, 2, 3, 4, 5, 6, 7, 8, 10, 12, 16}) {
       if (rc != GF_OK) break;
       const int cs = C > 1 ? g0.ny + std::max(unit / C, 1) : g0.ny;
       const size_t sm = col_stage_smem(g0.ny, C, cs, c->m, g0.nl, c->cb, C * TPF, c->prec == GF_DF64);
