@@ -64,6 +64,18 @@ __device__ __forceinline__ df64 operator+(df64 a, df64 b) {
   const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));  // TwoSum error
   return fast_two_sum(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
 }
+// The same sum without its final renormalisation: (s, e + a.lo + b.lo) is a double-word value
+// whose low word may exceed ulp(s)/2.  Sums, products and dot products below accept such a
+// pair (TwoSum and TwoProd of the high words stay exact whatever the low words are, and the
+// low words only enter FP32 sums), so an FFT butterfly level whose outputs feed only further
+// butterflies skips the renormalisation: 8 instead of 11 FP32 operations.  The added error
+// stays u |lo| = O(u^2 (|a| + |b|)), the order of the renormalised sum's normwise bound.
+__device__ __forceinline__ df64 add_unnorm(df64 a, df64 b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bb = __fsub_rn(s, a.hi);
+  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+  return df64(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
 __device__ __forceinline__ df64 operator-(df64 a) { return df64(-a.hi, -a.lo); }
 __device__ __forceinline__ df64 operator-(df64 a, df64 b) { return a + (-b); }
 __device__ __forceinline__ df64 operator*(df64 a, df64 b) {
@@ -100,6 +112,9 @@ template <class T> __device__ __forceinline__ cplx<T> operator*(T s, cplx<T> a) 
 // renormalisation.  About 19 FP32 operations instead of 25 for two double-word products and a
 // double-word sum; the error stays a few u^2 (|a b| + |c d|), u = 2^-24, as for that sequence
 // (the dropped a.lo b.lo terms are below u^2 |a b|).
+// NORM = false leaves the result unnormalised (add_unnorm above) for a caller that only feeds
+// it to further sums.
+template <bool NORM = true>
 __device__ __forceinline__ df64 dw_dot2(df64 a, df64 b, df64 c, df64 d) {
   const float p = __fmul_rn(a.hi, b.hi);
   const float ep = __fmaf_rn(a.hi, b.hi, -p);
@@ -110,11 +125,27 @@ __device__ __forceinline__ df64 dw_dot2(df64 a, df64 b, df64 c, df64 d) {
   const float es = __fadd_rn(__fsub_rn(p, __fsub_rn(s, bb)), __fsub_rn(q, bb));  // TwoSum error
   float lo = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, ep));
   lo = __fmaf_rn(c.hi, d.lo, __fmaf_rn(c.lo, d.hi, __fadd_rn(lo, eq)));
-  return fast_two_sum(s, __fadd_rn(lo, es));
+  if constexpr (NORM) return fast_two_sum(s, __fadd_rn(lo, es));
+  else return df64(s, __fadd_rn(lo, es));
 }
 // complex double-word product through dw_dot2 (real and imaginary parts)
 template <> __device__ __forceinline__ cplx<df64> operator*(cplx<df64> a, cplx<df64> b) {
   return mk<df64>(dw_dot2(a.x, b.x, -a.y, b.y), dw_dot2(a.x, b.y, a.y, b.x));
+}
+// Butterfly sums and twiddle products: renormalised (NORM) or, in df64, left unnormalised for
+// a consumer that is another butterfly level.  FP32 and FP64 ignore NORM.
+template <bool NORM, class T> __device__ __forceinline__ cplx<T> bf_add(cplx<T> a, cplx<T> b) {
+  if constexpr (!NORM && std::is_same<T, df64>::value) return mk<T>(add_unnorm(a.x, b.x), add_unnorm(a.y, b.y));
+  else return a + b;
+}
+template <bool NORM, class T> __device__ __forceinline__ cplx<T> bf_sub(cplx<T> a, cplx<T> b) {
+  if constexpr (!NORM && std::is_same<T, df64>::value) return mk<T>(add_unnorm(a.x, -b.x), add_unnorm(a.y, -b.y));
+  else return a - b;
+}
+template <bool NORM, class T> __device__ __forceinline__ cplx<T> tw_mul(cplx<T> a, cplx<T> w) {
+  if constexpr (!NORM && std::is_same<T, df64>::value)
+    return mk<T>(dw_dot2<false>(a.x, w.x, -a.y, w.y), dw_dot2<false>(a.x, w.y, a.y, w.x));
+  else return a * w;
 }
 template <class T> __device__ __forceinline__ cplx<T> conj(cplx<T> a) { return mk<T>(a.x, -a.y); }
 template <class T> __device__ __forceinline__ cplx<T> mul_i(cplx<T> a) { return mk<T>(-a.y, a.x); }   //  i*a
@@ -126,8 +157,9 @@ constexpr double kC1 = 0.92387953251128675612818318939678828682241662586364;  //
 constexpr double kS1 = 0.38268343236508977172845998403039886676134456248563;  // sin(pi/8)
 constexpr double kH = 0.70710678118654752440084436210484903928483593768847;   // sqrt(1/2)
 
-// x * exp(DIR * 2 pi i * m / 16) with DIR = -1 (forward) or +1 (inverse), 0 <= m < 8
-template <int m, int DIR, class T>
+// x * exp(DIR * 2 pi i * m / 16) with DIR = -1 (forward) or +1 (inverse), 0 <= m < 8.  NORM =
+// false: a df64 result may be left unnormalised (for a butterfly sum, see add_unnorm).
+template <int m, int DIR, class T, bool NORM = true>
 __device__ __forceinline__ cplx<T> rot16(cplx<T> a) {
   if constexpr (m == 0) {
     return a;
@@ -136,7 +168,13 @@ __device__ __forceinline__ cplx<T> rot16(cplx<T> a) {
   } else if constexpr (m == 2 || m == 6) {
     const T h = T(kH);
     // exp(-i pi/4) = h(1 - i); exp(-3 i pi/4) = h(-1 - i)
-    if constexpr (m == 2) {
+    if constexpr (std::is_same<T, df64>::value) {
+      // the sums unnormalised (the product's TwoProd of the high words is exact on any pair)
+      const df64 sp = add_unnorm(a.x, a.y), sm = add_unnorm(a.x, -a.y);
+      const df64 hp = h * sp, hm = h * sm;  // h (x + y), h (x - y)
+      if constexpr (m == 2) return DIR < 0 ? mk<T>(hp, -hm) : mk<T>(hm, hp);
+      else return DIR < 0 ? mk<T>(-hm, -hp) : mk<T>(-hp, hm);
+    } else if constexpr (m == 2) {
       return DIR < 0 ? mk<T>(h * (a.x + a.y), h * (a.y - a.x)) : mk<T>(h * (a.x - a.y), h * (a.y + a.x));
     } else {
       return DIR < 0 ? mk<T>(h * (a.y - a.x), -h * (a.x + a.y)) : mk<T>(-h * (a.x + a.y), h * (a.x - a.y));
@@ -147,8 +185,8 @@ __device__ __forceinline__ cplx<T> rot16(cplx<T> a) {
     constexpr double s = (m == 1 || m == 7) ? kS1 : kC1;
     const T cc = T(c), ss = T(s);
     if constexpr (std::is_same<T, df64>::value) {  // two-term double-word dot products
-      if constexpr (DIR < 0) return mk<T>(dw_dot2(a.x, cc, a.y, ss), dw_dot2(a.y, cc, -a.x, ss));
-      else return mk<T>(dw_dot2(a.x, cc, -a.y, ss), dw_dot2(a.y, cc, a.x, ss));
+      if constexpr (DIR < 0) return mk<T>(dw_dot2<NORM>(a.x, cc, a.y, ss), dw_dot2<NORM>(a.y, cc, -a.x, ss));
+      else return mk<T>(dw_dot2<NORM>(a.x, cc, -a.y, ss), dw_dot2<NORM>(a.y, cc, a.x, ss));
     } else {
       if constexpr (DIR < 0) return mk<T>(a.x * cc + a.y * ss, a.y * cc - a.x * ss);
       else return mk<T>(a.x * cc - a.y * ss, a.y * cc + a.x * ss);
@@ -157,26 +195,28 @@ __device__ __forceinline__ cplx<T> rot16(cplx<T> a) {
 }
 
 // In-register R-point DFT (R = 1,2,4,8,16), natural order in and out.
-template <int R, int DIR, class T>
+// In df64 only the top level (TOP) renormalises: the inner levels' sums and rotations feed
+// further butterflies and stay unnormalised (add_unnorm).
+template <int R, int DIR, class T, bool TOP = true>
 __device__ __forceinline__ void dft(cplx<T>* v) {
   if constexpr (R == 1) {
     return;
   } else if constexpr (R == 2) {
     cplx<T> a = v[0], b = v[1];
-    v[0] = a + b;
-    v[1] = a - b;
+    v[0] = bf_add<TOP>(a, b);
+    v[1] = bf_sub<TOP>(a, b);
   } else {
     constexpr int H = R / 2;
     cplx<T> e[H], o[H];
 #pragma unroll
     for (int i = 0; i < H; ++i) { e[i] = v[2 * i]; o[i] = v[2 * i + 1]; }
-    dft<H, DIR>(e);
-    dft<H, DIR>(o);
+    dft<H, DIR, T, false>(e);
+    dft<H, DIR, T, false>(o);
     auto step = [&](auto kk) {
       constexpr int k = decltype(kk)::value;
-      cplx<T> t = rot16<k * (16 / R), DIR>(o[k]);
-      v[k] = e[k] + t;
-      v[k + H] = e[k] - t;
+      cplx<T> t = rot16<k * (16 / R), DIR, T, false>(o[k]);
+      v[k] = bf_add<TOP>(e[k], t);
+      v[k + H] = bf_sub<TOP>(e[k], t);
     };
     // unrolled over k = 0..H-1 with k a compile-time constant
     [&]<int... ks>(std::integer_sequence<int, ks...>) {
@@ -245,7 +285,7 @@ __device__ __forceinline__ void fft_passes(cplx<T>* buf, int t, const cplx<T>* _
           }
         } else {
 #pragma unroll
-          for (int r = 1; r < Rp; ++r) v[b][r] = v[b][r] * twiddle<DIR>(tw, r * k * TWS);
+          for (int r = 1; r < Rp; ++r) v[b][r] = tw_mul<false>(v[b][r], twiddle<DIR>(tw, r * k * TWS));
         }
       }
       dft<Rp, DIR>(v[b]);
@@ -295,7 +335,7 @@ __device__ __forceinline__ void fft_pass_dyn(cplx<T>* buf, int stride, int t, co
 #pragma unroll
     for (int f = 0; f < NF; ++f)
 #pragma unroll
-      for (int r = 1; r < R; ++r) v[f][r] = v[f][r] * w[r];
+      for (int r = 1; r < R; ++r) v[f][r] = tw_mul<false>(v[f][r], w[r]);
   }
 #pragma unroll
   for (int f = 0; f < NF; ++f) dft<R, DIR>(v[f]);
@@ -345,7 +385,7 @@ __device__ __forceinline__ void fft_passes_multi(cplx<T>* buf, int stride, int t
 #pragma unroll
         for (int f = 0; f < NF; ++f)
 #pragma unroll
-          for (int r = 1; r < Rp; ++r) v[f][b][r] = v[f][b][r] * w[r];
+          for (int r = 1; r < Rp; ++r) v[f][b][r] = tw_mul<false>(v[f][b][r], w[r]);
       }
 #pragma unroll
       for (int f = 0; f < NF; ++f) dft<Rp, DIR>(v[f][b]);

@@ -48,7 +48,7 @@ __device__ __forceinline__ void rt_bfly(const cplx<T>* src, cplx<T>* dst, int j,
   if (Ns > 1) {
     const int ts = n / (Ns * P);
 #pragma unroll
-    for (int r = 1; r < P; ++r) v[r] = v[r] * twiddle<DIR>(tw, r * k * ts);
+    for (int r = 1; r < P; ++r) v[r] = tw_mul<false>(v[r], twiddle<DIR>(tw, r * k * ts));
   }
   if constexpr ((P & (P - 1)) == 0) dft<P, DIR>(v);
   else dft_direct<T, P, DIR>(v, tw, n);

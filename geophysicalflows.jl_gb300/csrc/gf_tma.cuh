@@ -134,7 +134,7 @@ __device__ __forceinline__ void tma_pass(cplx<T>* F, int fstride, int cs, int ti
 #pragma unroll
       for (int f = 0; f < NF; ++f)
 #pragma unroll
-        for (int r = 1; r < Rp; ++r) v[f][b][r] = v[f][b][r] * w[r];
+        for (int r = 1; r < Rp; ++r) v[f][b][r] = tw_mul<false>(v[f][b][r], w[r]);
     }
 #pragma unroll
     for (int f = 0; f < NF; ++f) dft<Rp, DIR>(v[f][b]);
