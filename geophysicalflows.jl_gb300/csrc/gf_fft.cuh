@@ -76,6 +76,12 @@ __device__ __forceinline__ df64 add_unnorm(df64 a, df64 b) {
   const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
   return df64(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
 }
+// the double-word product below without its renormalisation (for the same consumers)
+__device__ __forceinline__ df64 mul_unnorm(df64 a, df64 b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  const float e = __fmaf_rn(a.hi, b.hi, -p);  // TwoProd error
+  return df64(p, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e)));
+}
 __device__ __forceinline__ df64 operator-(df64 a) { return df64(-a.hi, -a.lo); }
 __device__ __forceinline__ df64 operator-(df64 a, df64 b) { return a + (-b); }
 __device__ __forceinline__ df64 operator*(df64 a, df64 b) {
@@ -147,6 +153,11 @@ template <bool NORM, class T> __device__ __forceinline__ cplx<T> tw_mul(cplx<T> 
     return mk<T>(dw_dot2<false>(a.x, w.x, -a.y, w.y), dw_dot2<false>(a.x, w.y, a.y, w.x));
   else return a * w;
 }
+// renormalises an unnormalised df64 complex value (identity for FP32 and FP64)
+template <class T> __device__ __forceinline__ cplx<T> renorm(cplx<T> a) {
+  if constexpr (std::is_same<T, df64>::value) return mk<T>(fast_two_sum(a.x.hi, a.x.lo), fast_two_sum(a.y.hi, a.y.lo));
+  else return a;
+}
 template <class T> __device__ __forceinline__ cplx<T> conj(cplx<T> a) { return mk<T>(a.x, -a.y); }
 template <class T> __device__ __forceinline__ cplx<T> mul_i(cplx<T> a) { return mk<T>(-a.y, a.x); }   //  i*a
 template <class T> __device__ __forceinline__ cplx<T> mul_mi(cplx<T> a) { return mk<T>(a.y, -a.x); }  // -i*a
@@ -171,7 +182,7 @@ __device__ __forceinline__ cplx<T> rot16(cplx<T> a) {
     if constexpr (std::is_same<T, df64>::value) {
       // the sums unnormalised (the product's TwoProd of the high words is exact on any pair)
       const df64 sp = add_unnorm(a.x, a.y), sm = add_unnorm(a.x, -a.y);
-      const df64 hp = h * sp, hm = h * sm;  // h (x + y), h (x - y)
+      const df64 hp = NORM ? h * sp : mul_unnorm(h, sp), hm = NORM ? h * sm : mul_unnorm(h, sm);  // h (x +- y)
       if constexpr (m == 2) return DIR < 0 ? mk<T>(hp, -hm) : mk<T>(hm, hp);
       else return DIR < 0 ? mk<T>(-hm, -hp) : mk<T>(-hp, hm);
     } else if constexpr (m == 2) {
@@ -288,7 +299,7 @@ __device__ __forceinline__ void fft_passes(cplx<T>* buf, int t, const cplx<T>* _
           for (int r = 1; r < Rp; ++r) v[b][r] = tw_mul<false>(v[b][r], twiddle<DIR>(tw, r * k * TWS));
         }
       }
-      dft<Rp, DIR>(v[b]);
+      dft<Rp, DIR, T, (Ns * Rp >= N)>(v[b]);  // df64: normalised only by the last pass
     }
     __syncthreads();
 #pragma unroll
@@ -310,9 +321,11 @@ template <int N, int R> __host__ __device__ constexpr int full_stride() { int s 
 // One full radix-R pass at a run-time stride Ns = R^p (2^lg): the same arithmetic as
 // fft_passes at that Ns, but one body serves every full pass (code size: the step kernels
 // are bound by instruction fetch when every pass is inlined separately).
+// In df64 the pass's outputs are renormalised only when it is the transform's last pass (last);
+// the next pass's twiddle products and butterflies accept unnormalised values.
 template <class T, int N, int R, int DIR, int NF>
 __device__ __forceinline__ void fft_pass_dyn(cplx<T>* buf, int stride, int t, const cplx<T>* __restrict__ tw,
-                                             int Ns, int lg) {
+                                             int Ns, int lg, bool last) {
   constexpr int TWR = TWN / R;  // TWS = TWN / (Ns R) = TWR >> lg
   cplx<T> v[NF][R];
 #pragma unroll
@@ -338,7 +351,15 @@ __device__ __forceinline__ void fft_pass_dyn(cplx<T>* buf, int stride, int t, co
       for (int r = 1; r < R; ++r) v[f][r] = tw_mul<false>(v[f][r], w[r]);
   }
 #pragma unroll
-  for (int f = 0; f < NF; ++f) dft<R, DIR>(v[f]);
+  for (int f = 0; f < NF; ++f) dft<R, DIR, T, false>(v[f]);
+  if constexpr (std::is_same<T, df64>::value) {
+    if (last) {
+#pragma unroll
+      for (int f = 0; f < NF; ++f)
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[f][r] = renorm(v[f][r]);
+    }
+  }
   __syncthreads();
   const int idxD = ((t >> lg) << lg) * R + k;
 #pragma unroll
@@ -388,7 +409,7 @@ __device__ __forceinline__ void fft_passes_multi(cplx<T>* buf, int stride, int t
           for (int r = 1; r < Rp; ++r) v[f][b][r] = tw_mul<false>(v[f][b][r], w[r]);
       }
 #pragma unroll
-      for (int f = 0; f < NF; ++f) dft<Rp, DIR>(v[f][b]);
+      for (int f = 0; f < NF; ++f) dft<Rp, DIR, T, (Ns * Rp >= N)>(v[f][b]);
     }
     __syncthreads();
 #pragma unroll
@@ -412,7 +433,7 @@ __device__ __forceinline__ void fft_smem_multi(cplx<T>* buf, int stride, int t, 
     int lg = 0;
 #pragma unroll 1
     for (int Ns = 1; Ns < full_stride<N, R>(); Ns *= R, lg += ilog2(R))
-      fft_pass_dyn<T, N, R, DIR, NF>(buf, stride, t, tw, Ns, lg);
+      fft_pass_dyn<T, N, R, DIR, NF>(buf, stride, t, tw, Ns, lg, Ns * R == N);
     fft_passes_multi<T, N, R, DIR, full_stride<N, R>(), NF>(buf, stride, t, tw);
   } else {
     fft_passes_multi<T, N, R, DIR, 1, NF>(buf, stride, t, tw);
@@ -434,7 +455,7 @@ __device__ __forceinline__ void fft_smem(cplx<T>* buf, int t, const cplx<T>* __r
   if constexpr (GF_FFT_LOOP && sizeof(T) == 8) {
     int lg = 0;
 #pragma unroll 1
-    for (int Ns = 1; Ns < full_stride<N, R>(); Ns *= R, lg += ilog2(R)) fft_pass_dyn<T, N, R, DIR, 1>(buf, 0, t, tw, Ns, lg);
+    for (int Ns = 1; Ns < full_stride<N, R>(); Ns *= R, lg += ilog2(R)) fft_pass_dyn<T, N, R, DIR, 1>(buf, 0, t, tw, Ns, lg, Ns * R == N);
     fft_passes<T, N, R, DIR, full_stride<N, R>()>(buf, t, tw);
   } else {
     fft_passes<T, N, R, DIR, 1>(buf, t, tw);

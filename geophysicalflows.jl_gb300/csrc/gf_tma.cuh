@@ -137,7 +137,7 @@ __device__ __forceinline__ void tma_pass(cplx<T>* F, int fstride, int cs, int ti
         for (int r = 1; r < Rp; ++r) v[f][b][r] = tw_mul<false>(v[f][b][r], w[r]);
     }
 #pragma unroll
-    for (int f = 0; f < NF; ++f) dft<Rp, DIR>(v[f][b]);
+    for (int f = 0; f < NF; ++f) dft<Rp, DIR, T, (Ns * Rp >= N)>(v[f][b]);  // df64: last pass normalises
   }
   __syncthreads();
 #pragma unroll
@@ -190,7 +190,7 @@ __device__ __forceinline__ void tma_passes_looped(cplx<T>* F, int fstride, int c
     int lg = ilog2(R);
 #pragma unroll 1
     for (int Ns = R; Ns < NL; Ns *= R, lg += ilog2(R))
-      fft_pass_dyn<T, N, R, DIR, NF>(F + (tid / TPF) * cs, fstride, tid % TPF, tw, Ns, lg);
+      fft_pass_dyn<T, N, R, DIR, NF>(F + (tid / TPF) * cs, fstride, tid % TPF, tw, Ns, lg, false);
     tma_pass<T, N, R, DIR, NF, C, NL, false, DSTD>(F, fstride, cs, tid, tw);
   }
 }
