@@ -467,6 +467,49 @@ static EncodeTiledFn encode_tiled() {
   return fn;
 }
 
+// Device address of the caller's host buffer [p, p + bytes) when the whole range lies in one
+// page-locked allocation that the current device addresses (cudaMallocHost, cudaHostAlloc,
+// cudaHostRegister): both ends are page-locked host memory with device addresses bytes - 1
+// apart, and the driver reports one buffer id for both (one allocation, hence contiguous).
+// The host transfers then run as one kernel pass that reads or writes the buffer over the
+// host link and re-pitches on the way, instead of a copy-engine transfer through the staging
+// buffer followed by a device pass.  Null for pageable memory, or when any check cannot be
+// made: the staged path is used.
+typedef CUresult (*PtrAttrFn)(void*, CUpointer_attribute, CUdeviceptr);
+static PtrAttrFn ptr_attr_fn() {
+  static PtrAttrFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PtrAttrFn>(p);
+  }
+  return fn;
+}
+static void* host_mapped(const void* p, size_t bytes) {
+  const PtrAttrFn fn = ptr_attr_fn();
+  if (!fn || !p || bytes == 0) return nullptr;
+  const char* a = static_cast<const char*>(p);
+  const char* z = a + (bytes - 1);
+  cudaPointerAttributes pa{}, pz{};
+  if (cudaPointerGetAttributes(&pa, a) != cudaSuccess || cudaPointerGetAttributes(&pz, z) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (pa.type != cudaMemoryTypeHost || pz.type != cudaMemoryTypeHost || !pa.devicePointer || !pz.devicePointer)
+    return nullptr;
+  if (static_cast<const char*>(pz.devicePointer) - static_cast<const char*>(pa.devicePointer) != (ptrdiff_t)(bytes - 1))
+    return nullptr;
+  unsigned long long ia = 0, iz = 0;
+  if (fn(&ia, CU_POINTER_ATTRIBUTE_BUFFER_ID, (CUdeviceptr)(uintptr_t)a) != CUDA_SUCCESS ||
+      fn(&iz, CU_POINTER_ATTRIBUTE_BUFFER_ID, (CUdeviceptr)(uintptr_t)z) != CUDA_SUCCESS || ia != iz)
+    return nullptr;
+  return pa.devicePointer;
+}
+
 // Tensor maps of the TMA column stage (one layer): P and W as 3-D arrays of 32-bit words
 // (x: the words of a row's complex elements; y: field * ny + j; z: instance), boxes of C
 // columns x min(ny, 256) rows for the two candidate column counts (2 and 4 columns of
@@ -974,20 +1017,23 @@ static int repack_launch(gf_ctx* c, const void* src, size_t ss, void* dst, size_
 }
 
 // caller spectral array (Julia layout, row stride nkr) -> internal array (row stride ldk).
-// Host arrays travel as one contiguous copy through the staging buffer and are re-pitched on
-// the device (a pitched host copy of thousands of short rows is several times slower).
+// Pageable host arrays travel as one contiguous copy through the staging buffer and are
+// re-pitched on the device (a pitched host copy of thousands of short rows is several times
+// slower); page-locked ones are read or written by the re-pitch kernel itself.
 static int copy_spec_in(gf_ctx* c, void* dst, const void* src, int where) {
   const Geom& g = c->g;
   const cudaMemcpyKind kind = where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   const size_t rows = (size_t)g.ny * g.nl * g.nb;
+  // page-locked host buffer: read by the re-pitch kernel directly (see host_mapped)
+  const void* hm = where == GF_HOST ? host_mapped(src, rows * g.nkr * (c->prec == GF_DF64 ? 16 : c->cb)) : nullptr;
   if (c->prec == GF_DF64) {
-    GF_CUDA(c, cudaMemcpyAsync(c->stage, src, (size_t)g.nkr * g.ny * g.nl * g.nb * 16, kind, c->stream));
-    if (int r = convert_launch(c, true, c->stage, 2 * (size_t)g.nkr, dst, 2 * (size_t)g.ldk,
+    if (!hm) GF_CUDA(c, cudaMemcpyAsync(c->stage, src, (size_t)g.nkr * g.ny * g.nl * g.nb * 16, kind, c->stream));
+    if (int r = convert_launch(c, true, hm ? hm : c->stage, 2 * (size_t)g.nkr, dst, 2 * (size_t)g.ldk,
                                (size_t)g.ny * g.nl * g.nb, 2 * (size_t)g.nkr)) return r;
   } else if (where == GF_HOST) {
     const size_t wpe = c->cb / 8;  // 8-byte words per complex element
-    GF_CUDA(c, cudaMemcpyAsync(c->stage, src, rows * g.nkr * c->cb, kind, c->stream));
-    if (int r = repack_launch(c, c->stage, wpe * g.nkr, dst, wpe * g.ldk, rows, wpe * g.nkr)) return r;
+    if (!hm) GF_CUDA(c, cudaMemcpyAsync(c->stage, src, rows * g.nkr * c->cb, kind, c->stream));
+    if (int r = repack_launch(c, hm ? hm : c->stage, wpe * g.nkr, dst, wpe * g.ldk, rows, wpe * g.nkr)) return r;
   } else {
     GF_CUDA(c, cudaMemcpy2DAsync(dst, g.ldk * c->cb, src, g.nkr * c->cb, g.nkr * c->cb, (size_t)g.ny * g.nl * g.nb,
                                  kind, c->stream));
@@ -999,14 +1045,16 @@ static int copy_spec_out(gf_ctx* c, void* dst, const void* src, int where) {
   const Geom& g = c->g;
   const cudaMemcpyKind kind = where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
   const size_t rows = (size_t)g.ny * g.nl * g.nb;
+  // page-locked host buffer: written by the re-pitch kernel directly (see host_mapped)
+  void* hm = where == GF_HOST ? host_mapped(dst, rows * g.nkr * (c->prec == GF_DF64 ? 16 : c->cb)) : nullptr;
   if (c->prec == GF_DF64) {
-    if (int r = convert_launch(c, false, src, 2 * (size_t)g.ldk, c->stage, 2 * (size_t)g.nkr,
+    if (int r = convert_launch(c, false, src, 2 * (size_t)g.ldk, hm ? hm : c->stage, 2 * (size_t)g.nkr,
                                (size_t)g.ny * g.nl * g.nb, 2 * (size_t)g.nkr)) return r;
-    GF_CUDA(c, cudaMemcpyAsync(dst, c->stage, (size_t)g.nkr * g.ny * g.nl * g.nb * 16, kind, c->stream));
+    if (!hm) GF_CUDA(c, cudaMemcpyAsync(dst, c->stage, (size_t)g.nkr * g.ny * g.nl * g.nb * 16, kind, c->stream));
   } else if (where == GF_HOST) {
     const size_t wpe = c->cb / 8;
-    if (int r = repack_launch(c, src, wpe * g.ldk, c->stage, wpe * g.nkr, rows, wpe * g.nkr)) return r;
-    GF_CUDA(c, cudaMemcpyAsync(dst, c->stage, rows * g.nkr * c->cb, kind, c->stream));
+    if (int r = repack_launch(c, src, wpe * g.ldk, hm ? hm : c->stage, wpe * g.nkr, rows, wpe * g.nkr)) return r;
+    if (!hm) GF_CUDA(c, cudaMemcpyAsync(dst, c->stage, rows * g.nkr * c->cb, kind, c->stream));
   } else {
     GF_CUDA(c, cudaMemcpy2DAsync(dst, g.nkr * c->cb, src, g.ldk * c->cb, g.nkr * c->cb, (size_t)g.ny * g.nl * g.nb,
                                  kind, c->stream));
