@@ -168,6 +168,12 @@ int gf_abi_version(void);
 int gf_get_dims(const gf_ctx* ctx, int32_t* nkr, int32_t* ny, int32_t* nlayers, int32_t* real_bytes);
 
 /* ---- state (prob.sol, prob.clock) ----------------------------------------------------- */
+/* prob.sol as a (ny, nkr) complex array per layer and instance (nkr fastest, Julia's memory
+ * order), in the context's arithmetic type (complex128 for GF_DF64).  where = GF_HOST: the call
+ * returns when the copy is complete, so the caller may reuse its buffer; a page-locked buffer
+ * (cudaMallocHost, cudaHostAlloc, cudaHostRegister; CUDA.jl's pinned arrays) lying in one
+ * allocation is read or written by the library's re-pitch kernel directly, a pageable one goes
+ * through a copy into a staging buffer.  where = GF_DEVICE: stream-ordered device copies. */
 int gf_set_state(gf_ctx* ctx, const void* sol, int where);
 int gf_get_state(gf_ctx* ctx, void* sol, int where);
 int gf_get_clock(const gf_ctx* ctx, double* t, int64_t* step);
