@@ -243,6 +243,51 @@ def ncu_traffic(kernel, workload):
     return ncu_figure(kernel, workload, "traffic_bytes_per_launch")
 
 
+def fft_flops_per_step(w, call_steps=CALL_STEPS):
+    """Flop of the transforms of one step of a one-layer 2-D workload, averaged over a call of
+    call_steps steps: 5 n log2(n) per complex length-n transform (the standard radix-2 count),
+    per stage five transforms per row pair (length nx) and five per column (length ny) -- the
+    kcut kept columns in the call's unobserved steps, all nkr in its last one."""
+    nx, ny = w["nx"], w["ny"]
+    nkr, kcut, _ = dealias_geometry(nx, ny)
+    fx, fy = 5 * nx * math.log2(nx), 5 * ny * math.log2(ny)
+    rows = 4 * 5 * (ny // 2) * fx
+    cols = (4 * 5 * fy) * ((call_steps - 1) * kcut + nkr) / call_steps
+    return rows + cols
+
+
+def fp64_gemm_peak_tflops(n=4096, reps=5):
+    """FP64 peak for the IEEE FP64 arm's compute roofline, measured here (MEASURED_PEAKS.json
+    holds no FP64 figure): cuBLAS DGEMM through torch.matmul in float64, n^3, best of `reps`
+    after one warm-up, CUDA events."""
+    import torch
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = math.inf
+    for _ in range(reps):
+        (e0, e1), = _events(1)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def fp64_compute_roofline(w, ms_per_step, peak_tflops):
+    """IEEE FP64 arm against the FP64 pipe: the transforms' flop per step (fft_flops_per_step)
+    over the step time, as a fraction of the measured DGEMM rate."""
+    fl = fft_flops_per_step(w)
+    ach = fl / (ms_per_step * 1e-3) / 1e12
+    return {"bound": "fp64", "flop_per_step": fl, "flop_model": "5 n log2 n per complex transform, "
+            "5 row and 5 column transforms per stage, kept columns in unobserved steps",
+            "achieved": ach, "peak": peak_tflops, "unit": "TFLOP/s", "frac": ach / peak_tflops,
+            "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 (torch.matmul float64), best of 5"}
+
+
 def compute_roofline(roof, workload):
     """Issue-rate roofline of a kernel whose arithmetic, not memory, bounds it (df64): the
     fraction of the SM's instruction-issue slots and of the FMA pipe's cycles it uses (ncu,
@@ -725,6 +770,7 @@ def run_ours(args):
         ens = time_ensemble(ks, args.warmup, flush)
         adj32 = time_adjoint(flush)
         adj64 = time_adjoint(flush, np.float64)
+    fp64_peak = fp64_gemm_peak_tflops()
     acc = accuracy_100_steps(w)
     acc1 = accuracy_100_steps(SLQG512)
     acc2 = accuracy_100_steps(MLQG1024X3)
@@ -783,6 +829,7 @@ def run_ours(args):
                        "rel_l2_vs_ieee_fp64": dferr},
         "fp64_ieee": {"value": v64, "ms_per_step": ms64, "e2e": {"value": whole_job(pts, world, e2e_64), "unit": UNIT},
                       "roofline": roofline(w, r64, 16, "twodns2048_fp64", peaks, peak_src),
+                      "compute_roofline": fp64_compute_roofline(w, ms64, fp64_peak),
                       "roofline_step_two_sweep": step_roofline(w, ms64, 8, peaks)},
         "fp32_over_fp64": value / vdf,
         "fp32_over_ieee_fp64": value / v64,

@@ -1,7 +1,8 @@
 """The benchmark's byte models (CPU only): the kept-mode geometry of the per-launch model
 agrees with the oracle's dealias mask, the two-sweep model gives the words per point of the
 reference model (2DNS FilteredRK4 64, SLQG ETDRK4 71, MLQG ETDRK4 79), and an unobserved
-launch moves fewer bytes than an observed one."""
+launch moves fewer bytes than an observed one; the transforms' flop model of the FP64 compute
+roofline."""
 import os
 import sys
 
@@ -43,3 +44,14 @@ def test_unobserved_launches_move_fewer_bytes(w, cb):
     r8, c8 = bench.launch_bytes(w, 8, True)
     r16, c16 = bench.launch_bytes(w, 16, True)
     assert r16 == pytest.approx(2 * r8) and c16 > c8
+
+
+def test_fft_flop_model():
+    # single-step calls: every column in every stage; 5 n log2 n per complex transform
+    w = bench.HEADLINE
+    f = 5 * 2048 * 11
+    assert bench.fft_flops_per_step(w, 1) == 4 * 5 * (1024 + 1025) * f
+    # calls of 10 steps: the kept 682 columns in 9 of them
+    assert bench.fft_flops_per_step(w, 10) == pytest.approx(4 * 5 * (1024 + (9 * 682 + 1025) / 10) * f)
+    r = bench.fp64_compute_roofline(w, 5.0, 1.0)
+    assert r["unit"] == "TFLOP/s" and r["frac"] == pytest.approx(r["achieved"])
