@@ -267,6 +267,13 @@ __global__ void from_df64_kernel(const df64* __restrict__ src, size_t ss, double
     }                                                                                \
   } while (0)
 
+// A pending non-sticky error of an earlier runtime call in the caller's thread (the caller's
+// own, or another library's -- a refused cudaHostRegister, say) would be read back by this
+// library's launch checks (cudaGetLastError after a launch) as if one of its launches had
+// failed; every entry point that launches work consumes it first.  Sticky errors (a lost
+// context) still surface through the calls that follow.
+static inline void clear_stale_error() { (void)cudaGetLastError(); }
+
 static int fail(gf_ctx* c, int code, const std::string& msg) {
   if (c) c->err = msg; else g_create_error = msg;
   return code;
@@ -473,8 +480,10 @@ static EncodeTiledFn encode_tiled() {
 // apart, and the driver reports one buffer id for both (one allocation, hence contiguous).
 // The host transfers then run as one kernel pass that reads or writes the buffer over the
 // host link and re-pitches on the way, instead of a copy-engine transfer through the staging
-// buffer followed by a device pass.  Null for pageable memory, or when any check cannot be
-// made: the staged path is used.
+// buffer followed by a device pass.  The driver must also report that the device may read the
+// range, and with write (the kernel stores into it) read and write it: a
+// cudaHostRegisterReadOnly range is only read directly.  Null for pageable memory, or when any
+// check cannot be made: the staged path is used.
 typedef CUresult (*PtrAttrFn)(void*, CUpointer_attribute, CUdeviceptr);
 static PtrAttrFn ptr_attr_fn() {
   static PtrAttrFn fn = nullptr;
@@ -489,7 +498,7 @@ static PtrAttrFn ptr_attr_fn() {
   }
   return fn;
 }
-static void* host_mapped(const void* p, size_t bytes) {
+static void* host_mapped(const void* p, size_t bytes, bool write) {
   const PtrAttrFn fn = ptr_attr_fn();
   if (!fn || !p || bytes == 0) return nullptr;
   const char* a = static_cast<const char*>(p);
@@ -506,6 +515,10 @@ static void* host_mapped(const void* p, size_t bytes) {
   unsigned long long ia = 0, iz = 0;
   if (fn(&ia, CU_POINTER_ATTRIBUTE_BUFFER_ID, (CUdeviceptr)(uintptr_t)a) != CUDA_SUCCESS ||
       fn(&iz, CU_POINTER_ATTRIBUTE_BUFFER_ID, (CUdeviceptr)(uintptr_t)z) != CUDA_SUCCESS || ia != iz)
+    return nullptr;
+  unsigned int acc = 0;  // the device's access to the range: read for gf_set_state, read-write for gf_get_state
+  if (fn(&acc, CU_POINTER_ATTRIBUTE_ACCESS_FLAGS, (CUdeviceptr)(uintptr_t)a) != CUDA_SUCCESS ||
+      (write ? acc != CU_POINTER_ATTRIBUTE_ACCESS_FLAG_READWRITE : !(acc & CU_POINTER_ATTRIBUTE_ACCESS_FLAG_READ)))
     return nullptr;
   return pa.devicePointer;
 }
@@ -909,6 +922,7 @@ static int build(gf_ctx* c, const gf_config* cfg) {
 
 extern "C" int gf_create(const gf_config* cfg, void* stream, gf_ctx** out) {
   if (!cfg || !out) return fail(nullptr, GF_ERR_ARG, "null argument");
+  clear_stale_error();
   *out = nullptr;
   const gf_config& k = *cfg;
   if (k.module < 0 || k.module > 4) return fail(nullptr, GF_ERR_ARG, "unknown module");
@@ -1025,7 +1039,7 @@ static int copy_spec_in(gf_ctx* c, void* dst, const void* src, int where) {
   const cudaMemcpyKind kind = where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   const size_t rows = (size_t)g.ny * g.nl * g.nb;
   // page-locked host buffer: read by the re-pitch kernel directly (see host_mapped)
-  const void* hm = where == GF_HOST ? host_mapped(src, rows * g.nkr * (c->prec == GF_DF64 ? 16 : c->cb)) : nullptr;
+  const void* hm = where == GF_HOST ? host_mapped(src, rows * g.nkr * (c->prec == GF_DF64 ? 16 : c->cb), false) : nullptr;
   if (c->prec == GF_DF64) {
     if (!hm) GF_CUDA(c, cudaMemcpyAsync(c->stage, src, (size_t)g.nkr * g.ny * g.nl * g.nb * 16, kind, c->stream));
     if (int r = convert_launch(c, true, hm ? hm : c->stage, 2 * (size_t)g.nkr, dst, 2 * (size_t)g.ldk,
@@ -1046,7 +1060,7 @@ static int copy_spec_out(gf_ctx* c, void* dst, const void* src, int where) {
   const cudaMemcpyKind kind = where == GF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
   const size_t rows = (size_t)g.ny * g.nl * g.nb;
   // page-locked host buffer: written by the re-pitch kernel directly (see host_mapped)
-  void* hm = where == GF_HOST ? host_mapped(dst, rows * g.nkr * (c->prec == GF_DF64 ? 16 : c->cb)) : nullptr;
+  void* hm = where == GF_HOST ? host_mapped(dst, rows * g.nkr * (c->prec == GF_DF64 ? 16 : c->cb), true) : nullptr;
   if (c->prec == GF_DF64) {
     if (int r = convert_launch(c, false, src, 2 * (size_t)g.ldk, hm ? hm : c->stage, 2 * (size_t)g.nkr,
                                (size_t)g.ny * g.nl * g.nb, 2 * (size_t)g.nkr)) return r;
@@ -1089,11 +1103,13 @@ static int copy_phys_out(gf_ctx* c, void* dst, const void* src, int where, int n
 
 extern "C" int gf_set_state(gf_ctx* c, const void* sol, int where) {
   if (!c || !sol) return GF_ERR_ARG;
+  clear_stale_error();
   c->W_valid = false;
   return copy_spec_in(c, c->sol, sol, where);
 }
 extern "C" int gf_get_state(gf_ctx* c, void* sol, int where) {
   if (!c || !sol) return GF_ERR_ARG;
+  clear_stale_error();
   return copy_spec_out(c, sol, c->sol, where);
 }
 extern "C" int gf_get_clock(const gf_ctx* c, double* t, int64_t* step) {
@@ -1109,6 +1125,7 @@ extern "C" int gf_set_clock(gf_ctx* c, double t, int64_t step) {
 }
 extern "C" int gf_synchronize(gf_ctx* c) {
   if (!c) return GF_ERR_ARG;
+  clear_stale_error();
   GF_CUDA(c, cudaStreamSynchronize(c->stream));
   int flag = 0;
   GF_CUDA(c, cudaMemcpy(&flag, c->derr, sizeof(int), cudaMemcpyDeviceToHost));
@@ -1144,6 +1161,7 @@ __global__ void zero_k0_kernel(char* sol, int cb, size_t bs, int nb) {
 
 extern "C" int gf_updatevars(gf_ctx* c) {
   if (!c) return GF_ERR_ARG;
+  clear_stale_error();
   const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->g.nb * c->rb;
   GF_CUDA(c, DISPATCH(c, launch_mask_inplace, c->g, c->sol, c->stream));
   c->W_valid = false;
@@ -1169,6 +1187,7 @@ extern "C" int gf_updatevars(gf_ctx* c) {
 
 extern "C" int gf_get_field(gf_ctx* c, int which, void* out, int where) {
   if (!c || !out) return GF_ERR_ARG;
+  clear_stale_error();
   const int maxf = c->cfg.module == GF_BAROTROPICQGQL ? 6 : 3;
   if (which < 0 || which > maxf) return fail(c, GF_ERR_ARG, "unknown field");
   const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->g.nb * c->rb;
@@ -1177,6 +1196,7 @@ extern "C" int gf_get_field(gf_ctx* c, int which, void* out, int where) {
 
 extern "C" int gf_fwdtransform(gf_ctx* c, void* fieldh, const void* field, int where) {
   if (!c || !fieldh || !field) return GF_ERR_ARG;
+  clear_stale_error();
   const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->g.nb * c->rb;
   void* ph = (char*)c->phys + 3 * pf;
   if (int r = copy_phys_in(c, ph, field, where)) return r;
@@ -1186,6 +1206,7 @@ extern "C" int gf_fwdtransform(gf_ctx* c, void* fieldh, const void* field, int w
 
 extern "C" int gf_invtransform(gf_ctx* c, void* field, const void* fieldh, int where) {
   if (!c || !fieldh || !field) return GF_ERR_ARG;
+  clear_stale_error();
   const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->g.nb * c->rb;
   if (int r = copy_spec_in(c, c->tmp_spec, fieldh, where)) return r;
   void* ph = (char*)c->phys + 3 * pf;
@@ -1261,6 +1282,7 @@ __global__ void peaked_zetah_kernel(Geom g, double k0, double E0, int allones, c
 extern "C" int gf_peakedisotropicspectrum(gf_ctx* c, double kpeak, double E0, const double* mask, int32_t allones,
                                           uint64_t seed, void* zeta, int where) {
   if (!c || !zeta) return GF_ERR_ARG;
+  clear_stale_error();
   if (c->g.nl != 1) return fail(c, GF_ERR_UNSUPPORTED, "peakedisotropicspectrum makes one 2-D field (nlayers = 1)");
   if (c->cfg.Lx != c->cfg.Ly) return fail(c, GF_ERR_ARG, "the domain is not square");  // src/utils.jl:30
   if (!(kpeak > 0) || !(E0 >= 0)) return fail(c, GF_ERR_ARG, "peakedisotropicspectrum: kpeak > 0 and E0 >= 0");
@@ -1305,6 +1327,7 @@ extern "C" int gf_get_filter(const gf_ctx* c, double* out) {
 
 extern "C" int gf_set_physical(gf_ctx* c, int which, const void* field, int where) {
   if (!c || !field) return GF_ERR_ARG;
+  clear_stale_error();
   const int mod = c->cfg.module;
   if (which != GF_FIELD_Q && !(which == GF_FIELD_PSI && mod == GF_MULTILAYERQG))
     return fail(c, GF_ERR_ARG, "set_physical supports q/zeta/b, and psi for MultiLayerQG");
@@ -1326,6 +1349,7 @@ extern "C" int gf_set_physical(gf_ctx* c, int which, const void* field, int wher
 
 extern "C" int gf_set_forcing(gf_ctx* c, const void* data, int where) {
   if (!c || !data) return GF_ERR_ARG;
+  clear_stale_error();
   const int fk = c->cfg.forcing_kind;
   if (fk == GF_FORCING_NONE) return fail(c, GF_ERR_STATE, "problem was created without forcing");
   if (fk == GF_FORCING_STATIC || fk == GF_FORCING_HARMONIC) return copy_spec_in(c, c->Fh, data, where);
@@ -1401,6 +1425,7 @@ extern "C" int gf_profile_enable(gf_ctx* c, int on) {
 
 extern "C" int gf_profile_read(gf_ctx* c, double* ms, int64_t* n, int64_t* launches) {
   if (!c) return GF_ERR_ARG;
+  clear_stale_error();
   GF_CUDA(c, cudaStreamSynchronize(c->stream));
   for (auto& u : c->ev_used) {
     float t = 0;
@@ -1528,6 +1553,7 @@ extern "C" int gf_set_graph_steps(gf_ctx* c, int32_t steps) {
 
 extern "C" int gf_step(gf_ctx* c, int64_t nsteps) {
   if (!c || nsteps < 0) return GF_ERR_ARG;
+  clear_stale_error();
   if (c->cfg.forcing_kind >= GF_FORCING_STOCHASTIC && !c->fspec) return fail(c, GF_ERR_STATE, "no forcing spectrum");
   // AB3 rotates three RHS buffers: a graph covers three steps so that it can be replayed
   const int G = c->graph_steps <= 0 ? 0 : (c->kind == SK_AB3 ? 3 : c->graph_steps);
@@ -1555,6 +1581,7 @@ extern "C" int gf_step(gf_ctx* c, int64_t nsteps) {
 // it and runs the stage; each stage waits for the host, so this is the slow, general path.
 extern "C" int gf_step_callback(gf_ctx* c, int64_t nsteps, gf_forcing_fn fn, void* user) {
   if (!c || nsteps < 0 || !fn) return GF_ERR_ARG;
+  clear_stale_error();
   if (c->cfg.forcing_kind != GF_FORCING_STATIC)
     return fail(c, GF_ERR_STATE, "gf_step_callback needs a context created with forcing_kind = GF_FORCING_STATIC");
   const Geom& g = c->g;
@@ -1711,6 +1738,7 @@ static int ensemble_capture(gf_ctx* const* ctxs, int32_t n, int G, int obs) {
 
 extern "C" int gf_ensemble_step(gf_ctx* const* ctxs, int32_t n, int64_t nsteps) {
   if (!ctxs || n <= 0 || nsteps < 0) return fail(nullptr, GF_ERR_ARG, "gf_ensemble_step: bad arguments");
+  clear_stale_error();
   for (int32_t i = 0; i < n; ++i) {
     if (!ctxs[i]) return fail(nullptr, GF_ERR_ARG, "gf_ensemble_step: null context");
     for (int32_t k = 0; k < i; ++k)
@@ -1768,6 +1796,7 @@ extern "C" int gf_get_batch(const gf_ctx* c, int32_t* nb) {
 
 extern "C" int gf_calcN(gf_ctx* c, void* N, void* sol, double t, int where) {
   if (!c || !N || !sol) return GF_ERR_ARG;
+  clear_stale_error();
   if (c->cfg.forcing_kind >= GF_FORCING_STOCHASTIC && !c->fspec) return fail(c, GF_ERR_STATE, "no forcing spectrum");
   if (int r = copy_spec_in(c, c->tmp_spec, sol, where)) return r;
   // first half of calcN! (dealias + inversion + inverse y-FFTs) on the caller's sol
@@ -1860,6 +1889,7 @@ static double diag_fscale(const gf_ctx* c) {
 
 extern "C" int gf_diagnostics(gf_ctx* c, const int32_t* which, int32_t nd, double* out) {
   if (!c || (nd > 0 && (!which || !out))) return GF_ERR_ARG;
+  clear_stale_error();
   uint32_t mask = 0;
   if (int r = diag_mask(c, which, nd, &mask)) return r;
   if (int r = diag_launch(c, mask, c->dout)) return r;
@@ -1875,6 +1905,7 @@ extern "C" int gf_diagnostics(gf_ctx* c, const int32_t* which, int32_t nd, doubl
 // per step; out[step][instance][nd].
 extern "C" int gf_step_diags(gf_ctx* c, int64_t nsteps, const int32_t* which, int32_t nd, double* out) {
   if (!c || nsteps < 0 || (nd > 0 && (!which || !out))) return GF_ERR_ARG;
+  clear_stale_error();
   if (nd == 0) return gf_step(c, nsteps);
   uint32_t mask = 0;
   if (int r = diag_mask(c, which, nd, &mask)) return r;
@@ -1910,6 +1941,7 @@ extern "C" int gf_step_diags(gf_ctx* c, int64_t nsteps, const int32_t* which, in
 // V = Lx Ly sum(H) (one layer: V = Lx Ly, no H factor), after updatevars!; FP64 sums.
 extern "C" int gf_fluxes(gf_ctx* c, double* lateral, double* vertical) {
   if (!c || !lateral) return GF_ERR_ARG;
+  clear_stale_error();
   if (c->cfg.module != GF_MULTILAYERQG) return fail(c, GF_ERR_ARG, "fluxes is a MultiLayerQG diagnostic");
   const Geom& g = c->g;
   const int nl = g.nl, NB = g.nb;
@@ -2028,6 +2060,7 @@ extern "C" int gf_get_launch_shape(const gf_ctx* c, int32_t* shape) {
 
 extern "C" int gf_autotune(gf_ctx* c, int32_t reps, int32_t* shape) {
   if (!c) return GF_ERR_ARG;
+  clear_stale_error();
   if (c->g.rtx || c->g.rty) {  // generic lengths: one launch shape, nothing to tune
     if (shape) for (int q = 0; q < 4; ++q) shape[q] = 0;
     return GF_OK;
@@ -2180,6 +2213,7 @@ extern "C" int gf_step_output(gf_ctx* c, int64_t nsteps, int32_t every, const in
   if (!c || nsteps < 0 || every < 1 || nd < 0 || nf < 0 || (nd > 0 && (!which_diag || !diag_out)) ||
       (nf > 0 && (!which_field || !field_out)))
     return GF_ERR_ARG;
+  clear_stale_error();
   uint32_t mask = 0;
   if (nd > 0)
     if (int r = diag_mask(c, which_diag, nd, &mask)) return r;
@@ -2297,6 +2331,7 @@ static int adj_schedule(gf_ctx* c) {
 
 extern "C" int gf_adjoint_setup(gf_ctx* c, int64_t nsteps, int32_t checkpoint_every) {
   if (!c || nsteps < 1 || checkpoint_every < 1) return GF_ERR_ARG;
+  clear_stale_error();
   if (int r = adj_check(c)) return r;
   if ((nsteps + checkpoint_every - 1) / checkpoint_every > 4096)
     return fail(c, GF_ERR_ARG, "more than 4096 recomputation units: raise checkpoint_every");
@@ -2403,6 +2438,7 @@ static int64_t adj_unit_steps(const gf_ctx* c, int u0, int n) {
 // first descent (the "spine"), so that the reverse sweep starts without recomputation.
 extern "C" int gf_adjoint_forward(gf_ctx* c) {
   if (!c) return GF_ERR_ARG;
+  clear_stale_error();
   auto& a = c->adj;
   if (!a.ready) return fail(c, GF_ERR_STATE, "call gf_adjoint_setup first");
   const size_t spec = c->g.bs_spec * c->cb;
@@ -2593,6 +2629,7 @@ static int adjoint_reverse(gf_ctx* c) {
 
 extern "C" int gf_adjoint_backward(gf_ctx* c, const void* sol_bar, void* sol0_bar, void* eta_bar, int where) {
   if (!c || !sol_bar) return GF_ERR_ARG;
+  clear_stale_error();
   auto& d = c->adj;
   if (!d.forward_done) return fail(c, GF_ERR_STATE, "run gf_adjoint_forward first");
   if (eta_bar && c->cfg.module != GF_SINGLELAYERQG && c->cfg.module != GF_MULTILAYERQG)
@@ -2609,6 +2646,7 @@ extern "C" int gf_adjoint_backward(gf_ctx* c, const void* sol_bar, void* sol0_ba
 
 extern "C" int gf_grad(gf_ctx* c, int loss_kind, void* dq0, void* deta, double* loss, int where) {
   if (!c) return GF_ERR_ARG;
+  clear_stale_error();
   if (loss_kind != GF_LOSS_KINETIC_ENERGY) return fail(c, GF_ERR_ARG, "unknown loss");
   auto& d = c->adj;
   if (!d.ready) return fail(c, GF_ERR_STATE, "call gf_adjoint_setup first");

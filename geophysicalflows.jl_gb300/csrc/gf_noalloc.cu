@@ -113,6 +113,9 @@ extern "C" int gf_rfft2_noalloc(const void* field, void* fieldh, int32_t nx, int
   g.dkx_f = 1.0f; g.dky_f = 1.0f; g.inv_nxny_f = (float)g.inv_nxny;
   cudaStream_t st = (cudaStream_t)stream;
   gf::Bufs b{precision == GF_F64 ? s->tw64 : s->tw32, nullptr, s->scratch};
+  // consume a pending non-sticky error of an earlier runtime call in this thread, which the
+  // launch checks below (cudaGetLastError) would otherwise report as theirs
+  (void)cudaGetLastError();
   if (precision == GF_F64) {
     e = gf::launch_row_r2c<double>(g, b, 1, field, st);
     if (e == cudaSuccess) e = gf::launch_col_fwd<double>(g, b, 1, fieldh, 0, st);
