@@ -3,7 +3,10 @@
  * Drop-in boundary for the hot path of GeophysicalFlows.jl v0.16.5 / FourierFlows.jl 0.10.5:
  * Problem construction, stepforward!, calcN!, updatevars!, set_*! and the Parseval-sum
  * diagnostics of TwoDNavierStokes, SingleLayerQG, MultiLayerQG and SurfaceQG.  Every call
- * returns GF_OK (0) or a negative gf_status; gf_last_error() gives the message.
+ * returns GF_OK (0) or a negative gf_status; gf_last_error() gives the message.  A call that
+ * launches GPU work first consumes a non-sticky CUDA runtime error that earlier calls of the
+ * caller's thread left pending (cudaGetLastError), so that it is not reported as the call's
+ * own; check your own runtime calls before calling into the library.
  *
  * Array conventions (identical to the reference's Julia arrays, column-major):
  *   spectral  (nkr, ny[, nlayers]) complex, nkr = nx/2 + 1, element (ik, j, L) at
