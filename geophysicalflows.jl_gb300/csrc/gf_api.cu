@@ -28,6 +28,7 @@ struct gf_ctx {
   int prec = GF_F32;
   size_t rb = 4, cb = 8;  // real / complex element bytes
   cudaStream_t stream = nullptr;
+  int dev = 0;  // the device current at gf_create; every call runs on it (DevGuard)
   Geom g{};
   ModArgs m{};
   int kind = SK_RK4, filtered = 0, hasL = 0, cplxL = 0, nstages = 4;
@@ -273,6 +274,23 @@ __global__ void from_df64_kernel(const df64* __restrict__ src, size_t ss, double
 // failed; every entry point that launches work consumes it first.  Sticky errors (a lost
 // context) still surface through the calls that follow.
 static inline void clear_stale_error() { (void)cudaGetLastError(); }
+
+// A context's buffers, stream and graphs live on the device that was current at gf_create.
+// Each entry point that works on a context makes that device current for the call and puts
+// the caller's current device back when it returns, so a caller that switched devices (a
+// CUDA.jl task on another GPU, say) does not launch this context's kernels on the wrong one.
+struct DevGuard {
+  int prev = -1;
+  explicit DevGuard(int dev) {
+    int cur = -1;
+    if (cudaGetDevice(&cur) == cudaSuccess && cur != dev && cudaSetDevice(dev) == cudaSuccess) prev = cur;
+  }
+  ~DevGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+  DevGuard(const DevGuard&) = delete;
+  DevGuard& operator=(const DevGuard&) = delete;
+};
 
 static int fail(gf_ctx* c, int code, const std::string& msg) {
   if (c) c->err = msg; else g_create_error = msg;
@@ -954,6 +972,10 @@ extern "C" int gf_create(const gf_config* cfg, void* stream, gf_ctx** out) {
   if (k.forcing_kind < 0 || k.forcing_kind > 4) return fail(nullptr, GF_ERR_ARG, "unknown forcing kind");
   if (k.batch < 0 || k.batch > 65535) return fail(nullptr, GF_ERR_ARG, "batch must be in [0, 65535]");
   gf_ctx* c = new gf_ctx();
+  if (cudaGetDevice(&c->dev) != cudaSuccess) {
+    delete c;
+    return fail(nullptr, GF_ERR_CUDA, "no current CUDA device");
+  }
   static std::atomic<uint64_t> next_uid{1};
   c->uid = next_uid++;
   c->cfg = k;
@@ -990,6 +1012,7 @@ static void adj_release(gf_ctx* c) {
 
 extern "C" int gf_destroy(gf_ctx* c) {
   if (!c) return GF_OK;
+  DevGuard dg_(c->dev);
   if (c->stream) cudaStreamSynchronize(c->stream); else cudaDeviceSynchronize();
   for (void* p : c->allocs) cudaFree(p);
   for (auto e : c->ev_free) cudaEventDestroy(e);
@@ -1103,12 +1126,14 @@ static int copy_phys_out(gf_ctx* c, void* dst, const void* src, int where, int n
 
 extern "C" int gf_set_state(gf_ctx* c, const void* sol, int where) {
   if (!c || !sol) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   clear_stale_error();
   c->W_valid = false;
   return copy_spec_in(c, c->sol, sol, where);
 }
 extern "C" int gf_get_state(gf_ctx* c, void* sol, int where) {
   if (!c || !sol) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   clear_stale_error();
   return copy_spec_out(c, sol, c->sol, where);
 }
@@ -1120,11 +1145,13 @@ extern "C" int gf_get_clock(const gf_ctx* c, double* t, int64_t* step) {
 }
 extern "C" int gf_set_clock(gf_ctx* c, double t, int64_t step) {
   if (!c) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   c->t = t; c->step = step;
   return upload_clock(c);
 }
 extern "C" int gf_synchronize(gf_ctx* c) {
   if (!c) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   clear_stale_error();
   GF_CUDA(c, cudaStreamSynchronize(c->stream));
   int flag = 0;
@@ -1161,6 +1188,7 @@ __global__ void zero_k0_kernel(char* sol, int cb, size_t bs, int nb) {
 
 extern "C" int gf_updatevars(gf_ctx* c) {
   if (!c) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   clear_stale_error();
   const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->g.nb * c->rb;
   GF_CUDA(c, DISPATCH(c, launch_mask_inplace, c->g, c->sol, c->stream));
@@ -1187,6 +1215,7 @@ extern "C" int gf_updatevars(gf_ctx* c) {
 
 extern "C" int gf_get_field(gf_ctx* c, int which, void* out, int where) {
   if (!c || !out) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   clear_stale_error();
   const int maxf = c->cfg.module == GF_BAROTROPICQGQL ? 6 : 3;
   if (which < 0 || which > maxf) return fail(c, GF_ERR_ARG, "unknown field");
@@ -1196,6 +1225,7 @@ extern "C" int gf_get_field(gf_ctx* c, int which, void* out, int where) {
 
 extern "C" int gf_fwdtransform(gf_ctx* c, void* fieldh, const void* field, int where) {
   if (!c || !fieldh || !field) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   clear_stale_error();
   const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->g.nb * c->rb;
   void* ph = (char*)c->phys + 3 * pf;
@@ -1206,6 +1236,7 @@ extern "C" int gf_fwdtransform(gf_ctx* c, void* fieldh, const void* field, int w
 
 extern "C" int gf_invtransform(gf_ctx* c, void* field, const void* fieldh, int where) {
   if (!c || !fieldh || !field) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   clear_stale_error();
   const size_t pf = (size_t)c->g.nl * c->g.ny * c->g.nx * c->g.nb * c->rb;
   if (int r = copy_spec_in(c, c->tmp_spec, fieldh, where)) return r;
@@ -1282,6 +1313,7 @@ __global__ void peaked_zetah_kernel(Geom g, double k0, double E0, int allones, c
 extern "C" int gf_peakedisotropicspectrum(gf_ctx* c, double kpeak, double E0, const double* mask, int32_t allones,
                                           uint64_t seed, void* zeta, int where) {
   if (!c || !zeta) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   clear_stale_error();
   if (c->g.nl != 1) return fail(c, GF_ERR_UNSUPPORTED, "peakedisotropicspectrum makes one 2-D field (nlayers = 1)");
   if (c->cfg.Lx != c->cfg.Ly) return fail(c, GF_ERR_ARG, "the domain is not square");  // src/utils.jl:30
@@ -1327,6 +1359,7 @@ extern "C" int gf_get_filter(const gf_ctx* c, double* out) {
 
 extern "C" int gf_set_physical(gf_ctx* c, int which, const void* field, int where) {
   if (!c || !field) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   clear_stale_error();
   const int mod = c->cfg.module;
   if (which != GF_FIELD_Q && !(which == GF_FIELD_PSI && mod == GF_MULTILAYERQG))
@@ -1349,6 +1382,7 @@ extern "C" int gf_set_physical(gf_ctx* c, int which, const void* field, int wher
 
 extern "C" int gf_set_forcing(gf_ctx* c, const void* data, int where) {
   if (!c || !data) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   clear_stale_error();
   const int fk = c->cfg.forcing_kind;
   if (fk == GF_FORCING_NONE) return fail(c, GF_ERR_STATE, "problem was created without forcing");
@@ -1425,6 +1459,7 @@ extern "C" int gf_profile_enable(gf_ctx* c, int on) {
 
 extern "C" int gf_profile_read(gf_ctx* c, double* ms, int64_t* n, int64_t* launches) {
   if (!c) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   clear_stale_error();
   GF_CUDA(c, cudaStreamSynchronize(c->stream));
   for (auto& u : c->ev_used) {
@@ -1546,6 +1581,7 @@ static int capture_steps(gf_ctx* c, int G, cudaGraphExec_t* out, bool last_obser
 
 extern "C" int gf_set_graph_steps(gf_ctx* c, int32_t steps) {
   if (!c || steps < 0) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   drop_graphs(c);
   c->graph_steps = steps;
   return GF_OK;
@@ -1553,6 +1589,7 @@ extern "C" int gf_set_graph_steps(gf_ctx* c, int32_t steps) {
 
 extern "C" int gf_step(gf_ctx* c, int64_t nsteps) {
   if (!c || nsteps < 0) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   clear_stale_error();
   if (c->cfg.forcing_kind >= GF_FORCING_STOCHASTIC && !c->fspec) return fail(c, GF_ERR_STATE, "no forcing spectrum");
   // AB3 rotates three RHS buffers: a graph covers three steps so that it can be replayed
@@ -1581,6 +1618,7 @@ extern "C" int gf_step(gf_ctx* c, int64_t nsteps) {
 // it and runs the stage; each stage waits for the host, so this is the slow, general path.
 extern "C" int gf_step_callback(gf_ctx* c, int64_t nsteps, gf_forcing_fn fn, void* user) {
   if (!c || nsteps < 0 || !fn) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   clear_stale_error();
   if (c->cfg.forcing_kind != GF_FORCING_STATIC)
     return fail(c, GF_ERR_STATE, "gf_step_callback needs a context created with forcing_kind = GF_FORCING_STATIC");
@@ -1677,6 +1715,7 @@ static int enqueue_ens_steps(gf_ctx* const* ctxs, int32_t n, int G, int obs) {
 
 extern "C" int gf_set_ensemble_mode(gf_ctx* c, int32_t mode) {
   if (!c || (mode != 0 && mode != 1)) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   c->ens_mode = mode;
   return GF_OK;
 }
@@ -1745,7 +1784,10 @@ extern "C" int gf_ensemble_step(gf_ctx* const* ctxs, int32_t n, int64_t nsteps) 
       if (ctxs[k] == ctxs[i]) return fail(nullptr, GF_ERR_ARG, "gf_ensemble_step: a context appears twice");
     if (ctxs[i]->cfg.forcing_kind >= GF_FORCING_STOCHASTIC && !ctxs[i]->fspec)
       return fail(ctxs[i], GF_ERR_STATE, "no forcing spectrum");
+    if (ctxs[i]->dev != ctxs[0]->dev)
+      return fail(nullptr, GF_ERR_ARG, "gf_ensemble_step: the contexts belong to different devices");
   }
+  DevGuard dg_(ctxs[0]->dev);
   int G = ctxs[0]->graph_steps;
   bool one_graph = n > 1 && G > 0;
   for (int32_t i = 0; i < n; ++i)
@@ -1796,6 +1838,7 @@ extern "C" int gf_get_batch(const gf_ctx* c, int32_t* nb) {
 
 extern "C" int gf_calcN(gf_ctx* c, void* N, void* sol, double t, int where) {
   if (!c || !N || !sol) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   clear_stale_error();
   if (c->cfg.forcing_kind >= GF_FORCING_STOCHASTIC && !c->fspec) return fail(c, GF_ERR_STATE, "no forcing spectrum");
   if (int r = copy_spec_in(c, c->tmp_spec, sol, where)) return r;
@@ -1889,6 +1932,7 @@ static double diag_fscale(const gf_ctx* c) {
 
 extern "C" int gf_diagnostics(gf_ctx* c, const int32_t* which, int32_t nd, double* out) {
   if (!c || (nd > 0 && (!which || !out))) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   clear_stale_error();
   uint32_t mask = 0;
   if (int r = diag_mask(c, which, nd, &mask)) return r;
@@ -1905,6 +1949,7 @@ extern "C" int gf_diagnostics(gf_ctx* c, const int32_t* which, int32_t nd, doubl
 // per step; out[step][instance][nd].
 extern "C" int gf_step_diags(gf_ctx* c, int64_t nsteps, const int32_t* which, int32_t nd, double* out) {
   if (!c || nsteps < 0 || (nd > 0 && (!which || !out))) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   clear_stale_error();
   if (nd == 0) return gf_step(c, nsteps);
   uint32_t mask = 0;
@@ -1941,6 +1986,7 @@ extern "C" int gf_step_diags(gf_ctx* c, int64_t nsteps, const int32_t* which, in
 // V = Lx Ly sum(H) (one layer: V = Lx Ly, no H factor), after updatevars!; FP64 sums.
 extern "C" int gf_fluxes(gf_ctx* c, double* lateral, double* vertical) {
   if (!c || !lateral) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   clear_stale_error();
   if (c->cfg.module != GF_MULTILAYERQG) return fail(c, GF_ERR_ARG, "fluxes is a MultiLayerQG diagnostic");
   const Geom& g = c->g;
@@ -1999,6 +2045,7 @@ static bool tma_eligible(const gf_ctx* c, int C) {
 
 extern "C" int gf_set_tma_columns(gf_ctx* c, int32_t C) {
   if (!c) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   if (C != 0 && !tma_eligible(c, C))
     return fail(c, GF_ERR_UNSUPPORTED, "no TMA column stage with this column count for this context");
   c->g.tmaC = C;
@@ -2025,6 +2072,7 @@ static void set_fp(gf_ctx* c, int Rr, int Rc, int C) {
 
 extern "C" int gf_set_field_parallel(gf_ctx* c, int32_t row_radix, int32_t col_radix, int32_t columns) {
   if (!c || row_radix < 0 || col_radix < 0 || columns < 0) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   if ((row_radix || col_radix) && !fp_ctx_ok(c))
     return fail(c, GF_ERR_UNSUPPORTED, "field-parallel kernels: one layer without bottom drag, power-of-two lengths 32 ... 512");
   if (row_radix && !fp_radix_ok(c->g.nx, row_radix)) return fail(c, GF_ERR_ARG, "field-parallel row radix must be 2, 4 or 8");
@@ -2042,6 +2090,7 @@ extern "C" int gf_get_field_parallel(const gf_ctx* c, int32_t* out) {
 
 extern "C" int gf_set_launch_shape(gf_ctx* c, const int32_t* shape) {
   if (!c || !shape) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   for (int k = 0; k < 4; ++k) if (shape[k] < 0) return fail(c, GF_ERR_ARG, "launch shape entries must be >= 0");
   const bool f32 = c->prec == GF_F32;
   for (int k : {0, 2}) {
@@ -2060,6 +2109,7 @@ extern "C" int gf_get_launch_shape(const gf_ctx* c, int32_t* shape) {
 
 extern "C" int gf_autotune(gf_ctx* c, int32_t reps, int32_t* shape) {
   if (!c) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   clear_stale_error();
   if (c->g.rtx || c->g.rty) {  // generic lengths: one launch shape, nothing to tune
     if (shape) for (int q = 0; q < 4; ++q) shape[q] = 0;
@@ -2213,6 +2263,7 @@ extern "C" int gf_step_output(gf_ctx* c, int64_t nsteps, int32_t every, const in
   if (!c || nsteps < 0 || every < 1 || nd < 0 || nf < 0 || (nd > 0 && (!which_diag || !diag_out)) ||
       (nf > 0 && (!which_field || !field_out)))
     return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   clear_stale_error();
   uint32_t mask = 0;
   if (nd > 0)
@@ -2331,6 +2382,7 @@ static int adj_schedule(gf_ctx* c) {
 
 extern "C" int gf_adjoint_setup(gf_ctx* c, int64_t nsteps, int32_t checkpoint_every) {
   if (!c || nsteps < 1 || checkpoint_every < 1) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   clear_stale_error();
   if (int r = adj_check(c)) return r;
   if ((nsteps + checkpoint_every - 1) / checkpoint_every > 4096)
@@ -2384,6 +2436,7 @@ extern "C" int gf_adjoint_setup(gf_ctx* c, int64_t nsteps, int32_t checkpoint_ev
 
 extern "C" int gf_adjoint_set_snapshots(gf_ctx* c, int32_t snapshots) {
   if (!c) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   auto& a = c->adj;
   if (!a.ready) return fail(c, GF_ERR_STATE, "call gf_adjoint_setup first");
   if (snapshots < 1) return fail(c, GF_ERR_ARG, "at least one snapshot (the initial state)");
@@ -2438,6 +2491,7 @@ static int64_t adj_unit_steps(const gf_ctx* c, int u0, int n) {
 // first descent (the "spine"), so that the reverse sweep starts without recomputation.
 extern "C" int gf_adjoint_forward(gf_ctx* c) {
   if (!c) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   clear_stale_error();
   auto& a = c->adj;
   if (!a.ready) return fail(c, GF_ERR_STATE, "call gf_adjoint_setup first");
@@ -2629,6 +2683,7 @@ static int adjoint_reverse(gf_ctx* c) {
 
 extern "C" int gf_adjoint_backward(gf_ctx* c, const void* sol_bar, void* sol0_bar, void* eta_bar, int where) {
   if (!c || !sol_bar) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   clear_stale_error();
   auto& d = c->adj;
   if (!d.forward_done) return fail(c, GF_ERR_STATE, "run gf_adjoint_forward first");
@@ -2646,6 +2701,7 @@ extern "C" int gf_adjoint_backward(gf_ctx* c, const void* sol_bar, void* sol0_ba
 
 extern "C" int gf_grad(gf_ctx* c, int loss_kind, void* dq0, void* deta, double* loss, int where) {
   if (!c) return GF_ERR_ARG;
+  DevGuard dg_(c->dev);
   clear_stale_error();
   if (loss_kind != GF_LOSS_KINETIC_ENERGY) return fail(c, GF_ERR_ARG, "unknown loss");
   auto& d = c->adj;

@@ -17,7 +17,8 @@
  *   `where` = GF_HOST (pageable or pinned host memory) or GF_DEVICE (device pointer on the
  *   context's GPU, e.g. from a CuArray).
  * One context = one problem on one stream; a context is not thread-safe, separate
- * contexts are independent.
+ * contexts are independent.  A context belongs to the device that was current at gf_create:
+ * every call on it runs there and gives the caller back its own current device on return.
  * Grid sizes: nx and ny even, at least 4, with no prime factor above 61 and at most 4096
  * (GF_F32) or 2048 (GF_F64, GF_DF64) -- the sizes FourierFlows' TwoDGrid accepts in practice,
  * e.g. the reference tests' 128 x 126, 64 x 66, 32 x 34 and 16 x 16 (FourierFlows also takes
