@@ -8,7 +8,7 @@ from .core import Diagnostic, Forcing, ensemble_step, stepforward, stepforward_o
 from . import TwoDNavierStokes, SingleLayerQG, MultiLayerQG, SurfaceQG, BarotropicQGQL
 from . import utils
 from . import adjoint
-from .utils import peakedisotropicspectrum
+from .utils import lambdipole, peakedisotropicspectrum
 
 __all__ = ["load", "GFError", "GFNotImplemented", "Diagnostic", "Forcing", "ensemble_step", "stepforward", "stepforward_output", "TwoDNavierStokes",
-           "SingleLayerQG", "MultiLayerQG", "SurfaceQG", "BarotropicQGQL", "utils", "adjoint", "peakedisotropicspectrum"]
+           "SingleLayerQG", "MultiLayerQG", "SurfaceQG", "BarotropicQGQL", "utils", "adjoint", "lambdipole", "peakedisotropicspectrum"]

@@ -38,6 +38,25 @@ def peakedisotropicspectrum(grid, kpeak, E0, mask=None, allones=False, seed=1234
     return out
 
 
+def lambdipole(U, R, grid, center=None):
+    """lambdipole(U, R, grid; center) (src/utils.jl:8-20): the vorticity of a Lamb dipole that
+    moves along x at speed U, radius R, centred by default at the means of the grid's x and y
+    coordinates.  Host-side set-up (SciPy's Bessel functions): J1(k r) (y - yc) / r scaled by
+    -2 U k / J0(k R) inside r < R, k R the first zero of J1, zero outside.  Shape (ny, nx)."""
+    from scipy.special import j0, j1
+    kR = 3.8317059702075123156  # first zero of J1
+    k = kR / R
+    amp = -2.0 * U * k / j0(kR)
+    xs, ys = np.asarray(grid.x, dtype=np.float64), np.asarray(grid.y, dtype=np.float64)
+    xc, yc = (xs.mean(), ys.mean()) if center is None else center
+    X, Y = np.meshgrid(xs, ys, indexing="xy")
+    r = np.hypot(X - xc, Y - yc)
+    inside = r < R
+    out = np.zeros_like(r)
+    out[inside] = amp * j1(k * r[inside]) * (Y[inside] - yc) / r[inside]
+    return out
+
+
 def parsevalsum(fh, grid):
     """FourierFlows.parsevalsum of a real field's half spectrum fh (ny, nkr): the sum over the
     full spectrum (interior kr columns counted twice, kr = 0 and, for even nx, the Nyquist

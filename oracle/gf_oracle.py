@@ -926,6 +926,22 @@ def peakedisotropicspectrum(grid, kpeak, E0, mask=None, allones=False, seed=1234
     return irfft2(-grid.Krsq * psih, grid)
 
 
+def lambdipole(U, R, grid, center=None):
+    """src/utils.jl:8-20: the Lamb dipole of strength U and radius R, centred at the means of
+    the grid coordinates (-dx/2, -dy/2 for the grid x = -Lx/2 + i dx): with k = j1 / R (j1 the
+    first zero of J1) and q0 = -2 U k / J0(k R), q = q0 J1(k r) (y - yc) / r inside r < R and
+    zero outside.  Returns (ny, nx)."""
+    from scipy.special import j0, j1
+    firstzero = 3.8317059702075123156
+    k = firstzero / R
+    q0 = -2 * U * k / j0(k * R)
+    x, y = grid.gridpoints()
+    xc, yc = (np.mean(grid.x), np.mean(grid.y)) if center is None else center
+    r = np.sqrt((x - xc) ** 2 + (y - yc) ** 2)
+    q = q0 * j1(k * r) * (y - yc) / r
+    return np.where(r >= R, 0.0, q)
+
+
 def ring_forcing_spectrum(grid, kf, dkf, eps):
     """Gaussian ring forcing spectrum normalised to inject energy at rate eps
     (examples/singlelayerqg_betaforced.jl:61-73)."""

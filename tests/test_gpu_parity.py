@@ -134,6 +134,52 @@ def test_twodns_energy_enstrophy_palinstrophy_gpu():
     assert isapprox(TD.palinstrophy(p), 126277 / 1458, RTOL_REF)
 
 
+_LAMB = {}
+
+
+def _lamb_oracle(L, n, dt, Ue, nt, nm):
+    """the oracle's Lamb-dipole run: the |zeta| centroids after each interval and the final zeta"""
+    key = (L, n, dt, Ue, nt, nm)
+    if key not in _LAMB:
+        r = O.TwoDNavierStokes(nx=n, Lx=L, nu=0.0, nnu=1, dt=dt, stepper="FilteredRK4")
+        r.set_zeta(O.lambdipole(Ue, L / 20, r.grid))
+        x, _ = r.grid.gridpoints()
+        xs = []
+        for _ in range(nm):
+            r.stepforward(nt)
+            r.updatevars()
+            a = np.abs(r.zeta)
+            xs.append(np.mean(a * x) / np.mean(a))
+        _LAMB[key] = (np.array(xs), r.zeta.copy())
+    return _LAMB[key]
+
+
+@pytest.mark.parametrize("T,precision,tol", [(np.float64, None, 1e-11), (np.float64, "DF64", 1e-11),
+                                             (np.float32, None, 1e-5)])
+def test_twodns_lambdipole_gpu(T, precision, tol):
+    """test/test_twodnavierstokes.jl:1-23 (runtests.jl:44: n = 256, dt = 1e-3) on the GPU: the
+    dipole from gfcuda.lambdipole (src/utils.jl:8-20) moves at Ue within rtol 1e-2, and the field
+    after the three intervals equals the oracle's run"""
+    L, n, dt, Ue = 2 * math.pi, 256, 1e-3, 1.0
+    nt, nm = round(L / Ue * 0.01 / dt), 3
+    p = TD.Problem("GPU", nx=n, Lx=L, nu=0.0, nnu=1, dt=dt, stepper="FilteredRK4", T=T, precision=precision)
+    TD.set_zeta(p, gfcuda.lambdipole(Ue, L / 20, p.grid))
+    x, _ = O.Grid(n).gridpoints()
+    xz, um = np.zeros(nm), np.zeros(nm)
+    for i in range(nm):
+        stepforward(p, nt)
+        TD.updatevars(p)
+        a = np.abs(np.asarray(p.vars.zeta, dtype=np.float64))
+        xz[i] = np.mean(a * x) / np.mean(a)
+        if i > 0:
+            um[i] = (xz[i] - xz[i - 1]) / ((nt - 1) * dt)
+    assert isapprox(Ue, np.mean(um[1:]), 1e-2)
+    xs_ref, z_ref = _lamb_oracle(L, n, dt, Ue, nt, nm)
+    assert np.max(np.abs(xz - xs_ref)) <= 100 * tol
+    assert rel(p.vars.zeta, z_ref) <= tol
+    p.close()
+
+
 def test_twodns_advection_manufactured_gpu():
     """test/test_twodnavierstokes.jl:221-257"""
     n, L, nu, dt = 128, 2 * np.pi, 1e-2, 0.0005

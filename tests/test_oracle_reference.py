@@ -53,6 +53,27 @@ def test_twodns_energy_enstrophy_palinstrophy():
     assert isapprox(p.palinstrophy(), 126277 / 1458, RTOL)
 
 
+def test_twodns_lambdipole():
+    """test/test_twodnavierstokes.jl:1-23 (n = 256, dt = 1e-3, runtests.jl:44): a Lamb dipole of
+    speed Ue = 1 and radius L/20 (src/utils.jl:8-20), FilteredRK4, nu = 0; the |zeta|-weighted
+    centroid moves at Ue within rtol_lambdipole = 1e-2 over three intervals of round(0.01 L /
+    Ue / dt) steps, the speed taken as the centroid shift over (nt - 1) dt as in the reference."""
+    L, n, dt, Ue = 2 * math.pi, 256, 1e-3, 1.0
+    nt, nm = round(L / Ue * 0.01 / dt), 3
+    r = O.TwoDNavierStokes(nx=n, Lx=L, nu=0.0, nnu=1, dt=dt, stepper="FilteredRK4")
+    r.set_zeta(O.lambdipole(Ue, L / 20, r.grid))
+    x, _ = r.grid.gridpoints()
+    xz, um = np.zeros(nm), np.zeros(nm)
+    for i in range(nm):
+        r.stepforward(nt)
+        r.updatevars()
+        a = np.abs(r.zeta)
+        xz[i] = np.mean(a * x) / np.mean(a)
+        if i > 0:
+            um[i] = (xz[i] - xz[i - 1]) / ((nt - 1) * dt)
+    assert isapprox(Ue, np.mean(um[1:]), rtol=1e-2)
+
+
 def test_twodns_advection_manufactured():
     """test/test_twodnavierstokes.jl:221-257 (ForwardEuler dt=5e-4, 2000 steps, rtol 1e-13)"""
     n, L, nu, nnu, dt = 128, 2 * np.pi, 1e-2, 1, 0.0005
