@@ -250,3 +250,51 @@ def test_batched_generic_size_equals_single_runs():
         assert rel(sb[i], r.sol) <= TOL64
         p.close()
     pb.close()
+
+
+@pytest.mark.parametrize("T,precision,tol", [(np.float64, None, 1e-12), (np.float64, "DF64", 1e-12),
+                                             (np.float32, None, 1e-5)])
+def test_mlqg_topographic_pv_largescale_gradient_gpu(T, precision, tol):
+    """test/test_multilayerqg.jl:709-753 set-up on the GPU (32 x 34, two layers, bumps plus a
+    large-scale topographic PV gradient, no dealiasing): the library's Qx, Qy enter calcN!, which
+    matches the oracle's (whose Qx, Qy equal the analytic fields, test_oracle_reference.py), and
+    so do 20 ForwardEuler steps"""
+    nx, ny, L = 32, 34, 2 * np.pi
+    g = O.Grid(nx, L, ny, L)
+    x, y = g.gridpoints()
+    f0, H, b, U = 1.0, [0.2, 0.8], [-1.0, -1.2], [1.0, 0.0]
+    eta = f0 * 0.1 * np.cos(x) * np.cos(y) / H[1]
+    kw = dict(nx=nx, ny=ny, Lx=L, Ly=L, f0=f0, H=H, b=b, U=U, beta=0.0, eta=eta,
+              topographic_pv_gradient=(f0 / H[1] * 1e-2, f0 / H[1] * 1e-1), dt=0.001, stepper="ForwardEuler",
+              aliased_fraction=0)
+    p = ML.Problem(2, "GPU", T=T, precision=precision, **kw)
+    r = O.MultiLayerQG(2, **kw)
+    rng = np.random.default_rng(3)
+    q0 = 0.1 * rng.standard_normal((2, ny, nx))
+    sol = np.stack([np.fft.rfft2(q) for q in q0])
+    N_gpu, _ = p.calcN(sol, 0.0)
+    N_ref = np.zeros_like(sol)
+    r.calcN(N_ref, sol.copy(), 0.0)
+    assert rel(N_gpu, N_ref) <= tol
+    ML.set_q(p, q0)
+    r.set_q(q0)
+    stepforward(p, 20)
+    r.stepforward(20)
+    assert rel(p.sol, r.sol) <= tol
+    p.close()
+
+
+@pytest.mark.parametrize("precision", [None, "DF64"])
+def test_mlqg_energy_single_layer_gpu(precision):
+    """test/test_multilayerqg.jl:538-559 on the GPU: one layer, 64 x 64 on [0, 2 pi) x [0, 3 pi),
+    energies = 29/9 at rtol 1e-13"""
+    nx, Lx, ny, Ly = 64, 2 * np.pi, 64, 3 * np.pi
+    p = ML.Problem(1, "GPU", nx=nx, ny=ny, Lx=Lx, Ly=Ly, U=np.zeros(ny), stepper="ForwardEuler", dt=0.001,
+                   precision=precision)
+    x, y = O.Grid(nx, Lx, ny, Ly).gridpoints()
+    k0, l0 = 2 * np.pi / Lx, 2 * np.pi / Ly
+    q0 = (-((2 * k0) ** 2 + (2 * l0) ** 2) * np.sin(2 * k0 * x) * np.cos(2 * l0 * y)
+          - (k0 ** 2 + (3 * l0) ** 2) * 2 * np.sin(k0 * x) * np.cos(3 * l0 * y))
+    ML.set_q(p, q0)
+    assert isapprox(ML.energies(p), 29 / 9, 1e-13)
+    p.close()

@@ -346,6 +346,42 @@ def test_mlqg_fluxes(nlayers):
         assert abs(lat[2]) < 1e-12 and abs(ver[1]) < 1e-12
 
 
+def test_mlqg_topographic_pv_largescale_gradient():
+    """test/test_multilayerqg.jl:709-753: with bumps h0 cos(k0 x) cos(l0 y) and a large-scale
+    topographic PV gradient f0/H2 (0.01, 0.1), the bottom layer's Qx and Qy equal the analytic
+    fields (32 x 34 grid, no dealiasing)"""
+    nx, ny, L = 32, 34, 2 * math.pi
+    g = O.Grid(nx, L, ny, L)
+    x, y = g.gridpoints()
+    k0, l0 = 2 * math.pi / L, 2 * math.pi / L
+    f0, H, b, U = 1.0, [0.2, 0.8], [-1.0, -1.2], [1.0, 0.0]
+    h0, sx, sy = 0.1, 1e-2, 1e-1
+    eta = f0 * h0 * np.cos(k0 * x) * np.cos(l0 * y) / H[1]
+    p = O.MultiLayerQG(2, nx=nx, ny=ny, Lx=L, Ly=L, f0=f0, H=H, b=b, U=U, beta=0.0, eta=eta,
+                       topographic_pv_gradient=(f0 / H[1] * sx, f0 / H[1] * sy), dt=0.001,
+                       stepper="ForwardEuler", aliased_fraction=0)
+    gp = b[0] - b[1]
+    F1 = f0 ** 2 / (H[1] * gp)
+    Q2x = f0 * (sx - h0 * k0 * np.sin(k0 * x) * np.cos(l0 * y)) / H[1]
+    Q2y = f0 * (sy - h0 * l0 * np.cos(k0 * x) * np.sin(l0 * y)) / H[1] + F1 * (-U[0] + U[1])
+    assert isapprox(p.Qx[1], Q2x, rtol=RTOL)
+    assert isapprox(p.Qy[1], Q2y, rtol=RTOL)
+
+
+def test_mlqg_energy_single_layer():
+    """test/test_multilayerqg.jl:538-559: one layer, 64 x 64 on [0, 2 pi) x [0, 3 pi), energies
+    of the known streamfunction = 29/9"""
+    nx, Lx, ny, Ly = 64, 2 * math.pi, 64, 3 * math.pi
+    g = O.Grid(nx, Lx, ny, Ly)
+    x, y = g.gridpoints()
+    k0, l0 = 2 * math.pi / Lx, 2 * math.pi / Ly
+    q0 = (-((2 * k0) ** 2 + (2 * l0) ** 2) * np.sin(2 * k0 * x) * np.cos(2 * l0 * y)
+          - (k0 ** 2 + (3 * l0) ** 2) * 2 * np.sin(k0 * x) * np.cos(3 * l0 * y))
+    p = O.MultiLayerQG(1, nx=nx, ny=ny, Lx=Lx, Ly=Ly, U=np.zeros(ny), stepper="ForwardEuler", dt=0.001)
+    p.set_q(q0[None])
+    assert isapprox(p.energies(), 29 / 9, rtol=RTOL)
+
+
 def test_mlqg_fluxes_single_layer():
     """test/test_multilayerqg.jl:630-655"""
     nx, ny = 128, 126
