@@ -108,3 +108,48 @@ def test_filter_parameters_are_used():
         assert np.max(np.abs(f - O.makefilter(g, order=6.0, innerK=0.5, outerK=0.9))) <= 1e-14
     finally:
         lib.gf_destroy(ctx)
+
+
+@pytest.mark.parametrize("T", [np.float32, np.float64])
+@pytest.mark.parametrize("kind", ["TwoDNavierStokes", "SingleLayerQG", "SurfaceQG", "BarotropicQGQL", "MLQG1", "MLQG2"])
+def test_problemtype(kind, T):
+    """test_*_problemtype (test/test_twodnavierstokes.jl:319-325, test_singlelayerqg.jl,
+    test_surfaceqg.jl, test_barotropicqgql.jl, test_multilayerqg.jl:790-801; runtests.jl runs them
+    with Float32): the state is complex of the problem's real type, the grid points and the
+    physical fields real of it; MultiLayerQG arrays keep a layer axis for one layer as well"""
+    CT = np.complex64 if T == np.float32 else np.complex128
+    mod = {"TwoDNavierStokes": TD, "SingleLayerQG": SL, "SurfaceQG": SQ}.get(kind)
+    if mod is not None:
+        p = mod.Problem("GPU", nx=32, T=T)
+    elif kind == "BarotropicQGQL":
+        p = QL.Problem("GPU", nx=32, T=T)
+    else:
+        p = ML.Problem(int(kind[-1]), "GPU", nx=32, T=T)
+    try:
+        assert p.sol.dtype == CT
+        assert p.grid.x.dtype == T and p.grid.y.dtype == T
+        p.updatevars()
+        assert p.vars.u.dtype == T
+        nd = 3 if kind.startswith("MLQG") else 2
+        assert p.sol.ndim == nd and p.vars.u.ndim == nd
+    finally:
+        p.close()
+
+
+def test_mlqg_params_constructor_U_floats_or_vectors():
+    """test/test_multilayerqg.jl:760-788: U given per layer as floats or as (ny, nlayers) vectors
+    defines the same problem -- the same mean flow and, on the GPU, the same calcN!"""
+    nx, ny, L = 32, 34, 2 * np.pi
+    kw = dict(nx=nx, ny=ny, Lx=L, f0=1.0, H=[0.2, 0.8], b=[-1.0, -1.2])
+    Uvec = np.zeros((ny, 2))
+    Uvec[:, 0], Uvec[:, 1] = 0.1, 0.05
+    pv = ML.Problem(2, "GPU", U=Uvec, **kw)
+    pf = ML.Problem(2, "GPU", U=np.array([0.1, 0.05]), **kw)
+    try:
+        np.testing.assert_array_equal(pv.Uy, pf.Uy)
+        rng = np.random.default_rng(4)
+        sol = np.stack([np.fft.rfft2(0.1 * rng.standard_normal((ny, nx))) for _ in range(2)])
+        np.testing.assert_array_equal(pv.calcN(sol, 0.0)[0], pf.calcN(sol, 0.0)[0])
+    finally:
+        pv.close()
+        pf.close()
