@@ -153,3 +153,23 @@ def test_mlqg_params_constructor_U_floats_or_vectors():
     finally:
         pv.close()
         pf.close()
+
+
+@pytest.mark.parametrize("n", [16, 32])
+@pytest.mark.parametrize("precision", [None, "DF64"])
+def test_sqg_noforcing(n, precision):
+    """test/test_surfaceqg.jl:127-145 (n = 16): calcN! of a zero state is the forcing alone --
+    zero without forcing, and the static forcing 2 at every mode (aliased ones included) with
+    it; at the reference's 16 points (generic-length kernels) and at 32 (compiled-in)"""
+    from gfcuda import Forcing
+    pu = SQ.Problem("GPU", nx=n, stepper="ForwardEuler", precision=precision)
+    shape = pu.spec_shape
+    pf = SQ.Problem("GPU", nx=n, stepper="ForwardEuler", precision=precision,
+                    forcing=Forcing("static", Fh=2 * np.ones(shape, dtype=np.complex128)))
+    try:
+        zero = np.zeros(shape, dtype=np.complex128)
+        np.testing.assert_array_equal(pu.calcN(zero, 0.0)[0], np.zeros(shape))
+        np.testing.assert_array_equal(pf.calcN(zero, 0.0)[0], 2 * np.ones(shape))
+    finally:
+        pu.close()
+        pf.close()
