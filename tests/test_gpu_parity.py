@@ -511,3 +511,22 @@ def test_mlqg_fluxes_gpu(nlayers, prec):
     else:
         for a, c in zip(got, ref):
             assert np.allclose(a, c, rtol=1e-12, atol=1e-14 * np.max(np.abs(c)))
+
+
+@pytest.mark.parametrize("ell", [np.inf, 1.23])
+@pytest.mark.parametrize("T,precision,tol", [(np.float64, None, 1e-12), (np.float64, "DF64", 1e-12),
+                                             (np.float32, None, 1e-6)])
+def test_slqg_streamfunctionfrompv_gpu(ell, T, precision, tol):
+    """test/test_singlelayerqg.jl:490-510 on the GPU: set_q! with the PV of a known streamfunction,
+    barotropic and equivalent-barotropic (deformation radius 1.23); the device's psi is that
+    streamfunction"""
+    nx = 64
+    p = SL.Problem("GPU", nx=nx, deformation_radius=ell, T=T, precision=precision)
+    x, y = O.Grid(nx).gridpoints()
+    k0 = l0 = 1.0
+    psi = np.sin(2 * k0 * x) * np.cos(3 * l0 * y)
+    extra = 0.0 if np.isinf(ell) else 1 / ell ** 2
+    SL.set_q(p, -((2 * k0) ** 2 + (3 * l0) ** 2 + extra) * psi)
+    SL.updatevars(p)
+    assert rel(p.vars.psi, psi) <= tol
+    p.close()
