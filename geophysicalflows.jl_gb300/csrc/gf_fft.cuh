@@ -65,11 +65,13 @@ __device__ __forceinline__ df64 operator+(df64 a, df64 b) {
   return fast_two_sum(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
 }
 // The same sum without its final renormalisation: (s, e + a.lo + b.lo) is a double-word value
-// whose low word may exceed ulp(s)/2.  Sums, products and dot products below accept such a
-// pair (TwoSum and TwoProd of the high words stay exact whatever the low words are, and the
-// low words only enter FP32 sums), so an FFT butterfly level whose outputs feed only further
-// butterflies skips the renormalisation: 8 instead of 11 FP32 operations.  The added error
-// stays u |lo| = O(u^2 (|a| + |b|)), the order of the renormalised sum's normwise bound.
+// whose low word may exceed ulp(s)/2.  The sums, products and dot products of this file accept
+// such a pair (TwoSum and TwoProd of the high words stay exact whatever the low words are, and
+// the low words only enter FP32 sums), so an FFT butterfly level whose outputs feed only
+// further butterflies skips the renormalisation: 8 instead of 11 FP32 operations.  The added
+// error stays u |lo| = O(u^2 (|a| + |b|)), the order of the renormalised sum's normwise bound.
+// The division takes normalised operands only (its first quotient is that of the high words);
+// unnormalised pairs never leave a transform, whose last pass renormalises.
 __device__ __forceinline__ df64 add_unnorm(df64 a, df64 b) {
   const float s = __fadd_rn(a.hi, b.hi);
   const float bb = __fsub_rn(s, a.hi);
