@@ -478,17 +478,20 @@ extern "C" const char* gf_last_error(const gf_ctx* c) { return c ? c->err.c_str(
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-static EncodeTiledFn encode_tiled() {
-  static EncodeTiledFn fn = nullptr;
-  static bool tried = false;
-  if (!tried) {
-    tried = true;
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q{};
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<EncodeTiledFn>(p);
+// A driver entry point by name, resolved once per process (the static's initialisation is
+// thread-safe); null if the driver does not provide it.
+static void* driver_entry(const char* name) {
+  void* p = nullptr;
+  cudaDriverEntryPointQueryResult q{};
+  if (cudaGetDriverEntryPointByVersion(name, &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess) {
+    cudaGetLastError();
+    return nullptr;
   }
+  return p;
+}
+static EncodeTiledFn encode_tiled() {
+  static const EncodeTiledFn fn = reinterpret_cast<EncodeTiledFn>(driver_entry("cuTensorMapEncodeTiled"));
   return fn;
 }
 
@@ -504,16 +507,7 @@ static EncodeTiledFn encode_tiled() {
 // check cannot be made: the staged path is used.
 typedef CUresult (*PtrAttrFn)(void*, CUpointer_attribute, CUdeviceptr);
 static PtrAttrFn ptr_attr_fn() {
-  static PtrAttrFn fn = nullptr;
-  static bool tried = false;
-  if (!tried) {
-    tried = true;
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q{};
-    if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PtrAttrFn>(p);
-  }
+  static const PtrAttrFn fn = reinterpret_cast<PtrAttrFn>(driver_entry("cuPointerGetAttribute"));
   return fn;
 }
 static void* host_mapped(const void* p, size_t bytes, bool write) {
